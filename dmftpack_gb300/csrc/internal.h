@@ -1,0 +1,78 @@
+// internal.h -- host-side context of libdmftgpu shared by the translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "dmftgpu.h"
+
+struct dmftgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    long long launches = 0;
+    struct Buf {
+        void *p = nullptr;
+        size_t bytes = 0;
+    };
+    std::map<std::string, Buf> bufs;  // grow-only named device workspaces
+    int *d_status = nullptr;          // device status word (max of kernel-reported codes)
+    bool timing = false;              // record CUDA events around the named hot kernels
+    std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
+};
+
+// event pair around one launch of `name` when ctx->timing is on (no-op otherwise)
+struct DgTimer {
+    dmftgpu_ctx *ctx;
+    cudaEvent_t b = nullptr, e = nullptr;
+    const char *name;
+    DgTimer(dmftgpu_ctx *c, const char *n) : ctx(c), name(n) {
+        if (ctx->timing) {
+            cudaEventCreate(&b);
+            cudaEventCreate(&e);
+            cudaEventRecord(b, ctx->stream);
+        }
+    }
+    ~DgTimer() {
+        if (ctx->timing) {
+            cudaEventRecord(e, ctx->stream);
+            ctx->events[name].push_back({b, e});
+        }
+    }
+};
+
+int dg_set_cuda_error(dmftgpu_ctx *ctx, cudaError_t e, const char *what);
+int dg_fail(dmftgpu_ctx *ctx, int code, const char *msg);
+// device workspace `name` of at least `bytes` (contents undefined); nullptr + error text on failure
+void *dg_buf(dmftgpu_ctx *ctx, const char *name, size_t bytes);
+// checks the last launch, counts it
+int dg_launched(dmftgpu_ctx *ctx, const char *what);
+// zero the status word, read it back (synchronising the stream)
+int dg_status_reset(dmftgpu_ctx *ctx);
+int dg_status_read(dmftgpu_ctx *ctx, int *code);
+
+// stage a caller array on the device: returns the caller's pointer if it is already a device pointer
+// (flags & DMFTGPU_DEVICE_PTRS), else copies `bytes` into workspace `name`.
+const void *dg_in(dmftgpu_ctx *ctx, const void *p, size_t bytes, int flags, const char *name, int *st);
+// output staging: device pointer to write into, and the copy-back afterwards
+void *dg_out(dmftgpu_ctx *ctx, void *p, size_t bytes, int flags, const char *name, int *st);
+int dg_out_done(dmftgpu_ctx *ctx, void *host, const void *dev, size_t bytes, int flags);
+
+// internal device-to-device entry points (all pointers device, enqueue only)
+int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double2 *fw, int green,
+                   double2 *mom);
+
+#define DG_LAUNCH(ctx, what)                     \
+    do {                                         \
+        int s_ = dg_launched((ctx), (what));     \
+        if (s_) return s_;                       \
+    } while (0)
+#define DG_TRY(expr)          \
+    do {                      \
+        int s_ = (expr);      \
+        if (s_) return s_;    \
+    } while (0)

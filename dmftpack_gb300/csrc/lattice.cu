@@ -1,0 +1,589 @@
+// lattice.cu -- the lattice stage of the DMFT iteration on the device:
+//   H(k) from t(R)                       (Construct_Hk_Sk, src/ConstructModelHamiltonian.cpp:66-77)
+//   G_loc(iw), GwHF(iw), NumMatrix       (GreenFtn_w, src/GreenFtn.cpp:142-422)
+//   N(mu), dN/dmu                        (GiwToNele, src/GreenFtn.cpp:513-635, trace form)
+//   the chemical-potential search        (GreenFtn_w_adjust_mu, src/GreenFtn.cpp:66-139)
+//
+// The hot kernel is k_gloc<N,W,MODE>: one CTA owns FPB Matsubara frequencies and sweeps every k point;
+// inside, lane groups of W lanes each invert one N x N matrix (iw+mu) I - H(k) - Sigma(iw) held one
+// column per lane (warp_gj_inverse) and add the correlated block of G, of G0 = U (iw+mu-e)^-1 U^H and the
+// trace terms of N(mu) into per-group shared-memory accumulators.  The k sum is therefore a fixed-order
+// in-CTA reduction: no atomics in global memory, no partial buffers, bit-reproducible results.
+// Orbitals are permuted so that the correlated (Hartree) orbitals lead; matrices whose dimension is not
+// an instantiated N are padded with an identity block (which leaves the leading block's inverse intact).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "gloc.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------------
+// H(k)
+// ---------------------------------------------------------------------------------------------------
+// hk[k][e] = sum_R T[R][e] exp(-i (kx ax Rx + ky ay Ry + kz az Rz)), e = i + j n (column-major element)
+constexpr int HK_KB = 4;     // k points per CTA
+constexpr int HK_RB = 32;    // R vectors per smem tile
+constexpr int HK_EB = 64;    // elements per CTA (threads = HK_KB * HK_EB)
+
+__global__ void __launch_bounds__(HK_KB *HK_EB) k_hk(int nk, int nR, int ne, int kx, int ky, int kz,
+                                                       const int *__restrict__ R, const double2 *__restrict__ T,
+                                                       double2 *__restrict__ hk) {
+    __shared__ double2 ph[HK_KB][HK_RB];
+    __shared__ double2 tt[HK_RB][HK_EB];
+    const int kl = threadIdx.x / HK_EB, el = threadIdx.x % HK_EB;
+    const int k = blockIdx.x * HK_KB + kl, e = blockIdx.y * HK_EB + el;
+    // k mesh (src/TB.cpp:196-207), ax = ay = az = pi
+    const double ax = DG_PI;
+    double2 acc = cmk(0, 0);
+    for (int r0 = 0; r0 < nR; r0 += HK_RB) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < HK_KB * HK_RB; t += blockDim.x) {
+            int kk = t / HK_RB, rr = t % HK_RB, kg = blockIdx.x * HK_KB + kk;
+            double2 v = cmk(0, 0);
+            if (kg < nk && r0 + rr < nR) {
+                const int kpxy = kx * ky;
+                const double delx = 2. * DG_PI / (ax * double(kx)), dely = 2. * DG_PI / (ax * double(ky)),
+                             delz = 2. * DG_PI / (ax * double(kz));
+                double k0 = -DG_PI / ax + delx / 2. + (kg % kx) * delx;
+                double k1 = -DG_PI / ax + dely / 2. + ((kg % kpxy) / kx) * dely;
+                double k2 = -DG_PI / ax + delz / 2. + (kg / kpxy) * delz;
+                const int *Rv = R + 3 * (r0 + rr);
+                double ang = (k0 * ax * Rv[0]) + (k1 * ax * Rv[1]) + (k2 * ax * Rv[2]);
+                double s, c;
+                sincos(ang, &s, &c);
+                v = cmk(c, -s);
+            }
+            ph[kk][rr] = v;
+        }
+        for (int t = threadIdx.x; t < HK_RB * HK_EB; t += blockDim.x) {
+            int rr = t / HK_EB, ee = t % HK_EB, eg = blockIdx.y * HK_EB + ee;
+            tt[rr][ee] = (r0 + rr < nR && eg < ne) ? T[(size_t)(r0 + rr) * ne + eg] : cmk(0, 0);
+        }
+        __syncthreads();
+        const int rmax = min(HK_RB, nR - r0);
+        for (int rr = 0; rr < rmax; rr++) acc = cfma(tt[rr][el], ph[kl][rr], acc);
+    }
+    if (k < nk && e < ne) hk[(size_t)k * ne + e] = acc;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// per-pass preparation
+// ---------------------------------------------------------------------------------------------------
+// H'(k) = H(k)[perm][perm] so that the correlated orbitals come first
+__global__ void k_permute(int nk, int n, const int *__restrict__ perm, const double2 *__restrict__ H,
+                          double2 *__restrict__ Hp) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long tot = (long long)nk * n * n;
+    if (t >= tot) return;
+    int e = (int)(t % ((long long)n * n));
+    long long k = t / ((long long)n * n);
+    int i = e % n, j = e / n;
+    Hp[t] = H[k * n * n + perm[i] + (size_t)perm[j] * n];
+}
+
+// Sigma(iw_n) for n < 2 N_freq: data below N_freq, moment tail above (src/GreenFtn.cpp:224-240 and the
+// valenceHAMILTONIAN macro :13-31); `mask` keeps only within-cluster blocks (GiwToNele's placement).
+__global__ void k_sigall(int Nf, int D, int nh, int mask, double beta, const double2 *__restrict__ S,
+                         const double2 *__restrict__ mom, double2 *__restrict__ sig) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long DD = (long long)D * D;
+    if (t >= 2LL * Nf * DD) return;
+    int n = (int)(t / DD), e = (int)(t % DD);
+    int a = e % D, b = e / D;
+    double2 v;
+    if (mask && (a / nh != b / nh)) v = cmk(0, 0);
+    else if (n < Nf) v = S[(size_t)n * DD + e];
+    else {
+        // m0 + m1/iw + m2/iw^2 + m3/iw^3 with iw = i w: 1/iw = -i/w, 1/iw^2 = -1/w^2, 1/iw^3 = i/w^3
+        double w = DG_PI * (2. * n + 1.) / beta;
+        double2 m0 = mom[e], m1 = mom[DD + e], m2 = mom[2 * DD + e], m3 = mom[3 * DD + e];
+        double2 i1 = cmk(0, -1.0 / w), i2 = cmk(-1.0 / (w * w), 0), i3 = cmk(0, 1.0 / (w * w * w));
+        v = cadd(cadd(m0, cmul(m1, i1)), cadd(cmul(m2, i2), cmul(m3, i3)));
+    }
+    sig[t] = v;
+}
+
+// static eigen-decomposition of H(k) + S_inf on the correlated block (src/GreenFtn.cpp:197-215)
+// outputs eps[k][n], UP[k][l][a] = U(a,l) for a < D (correlated rows of the eigenvectors)
+__global__ void k_static_eig(int nk, int n, int D, int nh, int mask, const double2 *__restrict__ H,
+                             const double2 *__restrict__ m0, double2 *work, int *iwork, double *eps,
+                             double2 *UP, int *status) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    size_t nn = (size_t)n * n;
+    double2 *A0 = work + (size_t)k * 3 * nn, *A = A0 + nn, *U = A + nn;
+    const double2 *Hk = H + (size_t)k * nn;
+    for (size_t q = 0; q < nn; q++) A0[q] = Hk[q];
+    for (int b = 0; b < D; b++)
+        for (int a = 0; a < D; a++)
+            if (!mask || a / nh == b / nh) DG_AT(A0, n, a, b) = cadd(DG_AT(A0, n, a, b), m0[a + b * D]);
+    int st = thread_heig(n, A0, A, U, eps + (size_t)k * n, iwork + (size_t)k * n);
+    if (st) dg_flag(status, DG_NONCONV);
+    for (int l = 0; l < n; l++)
+        for (int a = 0; a < D; a++) UP[((size_t)k * n + l) * D + a] = DG_AT(U, n, a, l);
+}
+
+// Fermi parts: occ_k = P U f U^H P (with the +-100 cut-offs of src/GreenFtn.cpp:314-316) for NumMatrix,
+// and sum_l f, beta f (1-f) for N(mu) (src/GreenFtn.cpp:616-620, no cut-off there)
+__global__ void k_fermi(int nk, int n, int D, double beta, double mu, const double *__restrict__ eps,
+                        const double2 *__restrict__ UP, double2 *occ, double *fs) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double fsum = 0, dfsum = 0;
+    for (int l = 0; l < n; l++) {
+        double e = eps[(size_t)k * n + l];
+        double f = 1. / (1 + exp(beta * (e - mu)));
+        fsum += f;
+        dfsum += beta * f * (1 - f);
+    }
+    fs[2 * k] = fsum;
+    fs[2 * k + 1] = dfsum;
+    if (!occ) return;
+    for (int b = 0; b < D; b++)
+        for (int a = 0; a < D; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < n; l++) {
+                double x = beta * (eps[(size_t)k * n + l] - mu);
+                double f = x > 100.0 ? 0.0 : (x < -100.0 ? 1.0 : 1. / (1. + exp(x)));
+                const double2 *u = UP + ((size_t)k * n + l) * D;
+                s = cadd(s, cscale(cmulc(u[a], u[b]), f));
+            }
+            occ[(size_t)k * D * D + a + b * D] = s;
+        }
+}
+
+// single CTA: G_loc, GwHF, NumMatrix (src/GreenFtn.cpp:298-354, 371-383)
+__global__ void k_gloc_finalize(int Nf, int nk, int D, int ncl, int nh, double beta, const double2 *blk,
+                                const double2 *blk0, const double2 *occ, double2 *gw, double2 *gwhf,
+                                double2 *nummat) {
+    const int DD = D * D;
+    for (long long t = threadIdx.x; t < (long long)Nf * DD; t += blockDim.x) {
+        int e = (int)(t % DD);
+        int a = e % D, b = e / D;
+        bool same = (a / nh == b / nh);
+        gw[t] = same ? cscale(blk[t], 1.0 / nk) : cmk(0, 0);
+        if (gwhf) gwhf[t] = same ? cscale(blk0[t], 1.0 / nk) : cmk(0, 0);
+    }
+    // the reference divides by knum_mpiGlobal with x /= knum; use the same division
+    for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+        int a = e % D, b = e / D;
+        int et = b + a * D;
+        double2 s = cmk(0, 0), s0 = cmk(0, 0), o = cmk(0, 0);
+        for (int f = 0; f < 2 * Nf; f++) {
+            s = cadd(s, cadd(blk[(size_t)f * DD + e], cconj(blk[(size_t)f * DD + et])));
+            s0 = cadd(s0, cadd(blk0[(size_t)f * DD + e], cconj(blk0[(size_t)f * DD + et])));
+        }
+        for (int k = 0; k < nk; k++) o = cadd(o, occ[(size_t)k * DD + e]);
+        s = cmk(s.x / beta, s.y / beta);
+        s0 = cmk(s0.x / beta, s0.y / beta);
+        if (a == b) {
+            s.x += 0.5 * nk;
+            s0.x += 0.5 * nk;
+        }
+        s = cadd(s, o);
+        s = cmk(s.x / nk, s.y / nk);
+        s0 = cmk(s0.x / nk, s0.y / nk);
+        nummat[e] = csub(s, s0);
+    }
+    (void)ncl;
+}
+
+// single CTA: N(mu) = (2/beta sum tr + sum f)/nk and dN/dmu
+__global__ void k_nele_finalize(int nf2, int nk, double beta, const double *tr, const double *dtr, const double *fs,
+                                int deriv, double *out) {
+    __shared__ double red[4][256];
+    double a = 0, b = 0, c = 0, d = 0;
+    for (int f = threadIdx.x; f < nf2; f += blockDim.x) {
+        a += tr[f];
+        if (deriv) b += dtr[f];
+    }
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        c += fs[2 * k];
+        d += fs[2 * k + 1];
+    }
+    red[0][threadIdx.x] = a;
+    red[1][threadIdx.x] = b;
+    red[2][threadIdx.x] = c;
+    red[3][threadIdx.x] = d;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 4; q++) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = (red[0][0] * 2. / beta + red[2][0]) / nk;
+        out[1] = (red[1][0] * 2. / beta + red[3][0]) / nk;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------------------
+using dg::GlocArgs;
+using dg::GlocKernel;
+using dg::M_BLOCK;
+using dg::M_DERIV;
+using dg::M_TRACE;
+
+struct Inst {
+    int N, W;
+    GlocKernel (*get)(int);
+};
+const Inst kInst[] = {
+    {1, 1, dg::gloc_kernel_1},    {2, 2, dg::gloc_kernel_2},    {3, 4, dg::gloc_kernel_3},
+    {4, 4, dg::gloc_kernel_4},    {6, 8, dg::gloc_kernel_6},    {8, 8, dg::gloc_kernel_8},
+    {12, 16, dg::gloc_kernel_12}, {16, 16, dg::gloc_kernel_16}, {28, 32, dg::gloc_kernel_28},
+};
+
+const Inst *pick_inst(int n) {
+    for (const auto &x : kInst)
+        if (x.N >= n) return &x;
+    return nullptr;
+}
+
+// Everything a lattice pass needs, prepared once per (H, Sigma, placement) and reused by every
+// N(mu) evaluation of the mu search.
+struct Prepared {
+    int n, nk, Nf, D, ncl, nh, mask;
+    double beta;
+    const double2 *H;  // permuted
+    double2 *sig, *mom, *UP;
+    double *eps;
+};
+
+int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P) {
+    P.n = L->n;
+    P.nk = L->nk;
+    P.Nf = L->nfreq;
+    P.ncl = L->ncl;
+    P.nh = L->nh;
+    P.D = L->ncl * L->nh;
+    P.mask = mask;
+    P.beta = L->beta;
+    const int n = P.n, nk = P.nk, D = P.D, Nf = P.Nf;
+    if (n < 1 || nk < 1 || Nf < 1 || D < 1 || D > n || !pick_inst(n))
+        return dg_fail(ctx, DMFTGPU_BADARG, "lattice: unsupported sizes (need 1 <= ncl*nh <= n <= 28)");
+    cudaStream_t s = ctx->stream;
+    // orbital permutation: Hartree orbitals first, the rest in their order
+    std::vector<int> perm;
+    bool identity = true;
+    if (L->hartr) {
+        std::vector<char> used(n, 0);
+        for (int i = 0; i < D; i++) {
+            int h = L->hartr[i];
+            if (h < 0 || h >= n || used[h]) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: bad HartrIndex");
+            used[h] = 1;
+            perm.push_back(h);
+            if (h != i) identity = false;
+        }
+        for (int i = 0; i < n; i++)
+            if (!used[i]) perm.push_back(i);
+    }
+    if (identity) P.H = dH;
+    else {
+        int *dperm = (int *)dg_buf(ctx, "lat.perm", n * sizeof(int));
+        double2 *Hp = (double2 *)dg_buf(ctx, "lat.Hperm", (size_t)nk * n * n * sizeof(double2));
+        if (!dperm || !Hp) return DMFTGPU_NOMEM;
+        DG_CUDA(cudaMemcpyAsync(dperm, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
+        long long tot = (long long)nk * n * n;
+        k_permute<<<dg_ceil_div(tot, 256), 256, 0, s>>>(nk, n, dperm, dH, Hp);
+        DG_LAUNCH(ctx, "k_permute");
+        P.H = Hp;
+    }
+    P.mom = (double2 *)dg_buf(ctx, "lat.mom", 4 * (size_t)D * D * sizeof(double2));
+    P.sig = (double2 *)dg_buf(ctx, "lat.sig", 2 * (size_t)Nf * D * D * sizeof(double2));
+    P.eps = (double *)dg_buf(ctx, "lat.eps", (size_t)nk * n * sizeof(double));
+    P.UP = (double2 *)dg_buf(ctx, "lat.UP", (size_t)nk * n * D * sizeof(double2));
+    double2 *work = (double2 *)dg_buf(ctx, "lat.eigwork", (size_t)nk * 3 * n * n * sizeof(double2));
+    int *iwork = (int *)dg_buf(ctx, "lat.eigiwork", (size_t)nk * n * sizeof(int));
+    if (!P.mom || !P.sig || !P.eps || !P.UP || !work || !iwork) return DMFTGPU_NOMEM;
+    DG_TRY(dg_moments_dev(ctx, D, Nf, P.beta, dS, 0, P.mom));
+    long long tot = 2LL * Nf * D * D;
+    k_sigall<<<dg_ceil_div(tot, 256), 256, 0, s>>>(Nf, D, P.nh, mask, P.beta, dS, P.mom, P.sig);
+    DG_LAUNCH(ctx, "k_sigall");
+    k_static_eig<<<dg_ceil_div(nk, 64), 64, 0, s>>>(nk, n, D, P.nh, mask, P.H, P.mom, work, iwork, P.eps, P.UP,
+                                                    ctx->d_status);
+    DG_LAUNCH(ctx, "k_static_eig");
+    return DMFTGPU_OK;
+}
+
+int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
+             double *tr, double *dtr) {
+    const Inst *in = pick_inst(P.n);
+    GlocKernel kern = in->get(mode);
+    const int NG = 128 / in->W, DD = P.D * P.D;
+    int fpb = 4;
+    auto smem_for = [&](int f) {
+        size_t s = (size_t)NG * f * DD * 2 + (size_t)NG * in->N * P.D + (size_t)NG * f;
+        if (mode & M_DERIV) s += (size_t)NG * in->N * in->N;
+        return s * sizeof(double2);
+    };
+    while (fpb > 1 && smem_for(fpb) > 160 * 1024) fpb--;
+    size_t smem = smem_for(fpb);
+    if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GlocArgs g;
+    g.H = P.H;
+    g.sig = P.sig;
+    g.eps = P.eps;
+    g.UP = P.UP;
+    g.n = P.n;
+    g.nk = P.nk;
+    g.nf2 = 2 * P.Nf;
+    g.D = P.D;
+    g.fpb = fpb;
+    g.wgrid = wgrid;
+    g.beta = P.beta;
+    g.mu = mu;
+    g.blk = blk;
+    g.blk0 = blk0;
+    g.tr = tr;
+    g.dtr = dtr;
+    g.status = ctx->d_status;
+    {
+        DgTimer tm(ctx, "k_gloc");
+        kern<<<dg_ceil_div(g.nf2, fpb), 128, smem, ctx->stream>>>(g);
+    }
+    DG_LAUNCH(ctx, "k_gloc");
+    return DMFTGPU_OK;
+}
+
+// one N(mu) evaluation on a prepared lattice; result (N, dN/dmu) in device out[2]
+int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *dout) {
+    const int nf2 = 2 * P.Nf;
+    double *tr = (double *)dg_buf(ctx, "nele.tr", nf2 * sizeof(double));
+    double *dtr = (double *)dg_buf(ctx, "nele.dtr", nf2 * sizeof(double));
+    double *fs = (double *)dg_buf(ctx, "nele.fs", 2 * (size_t)P.nk * sizeof(double));
+    if (!tr || !dtr || !fs) return DMFTGPU_NOMEM;
+    DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+    k_fermi<<<dg_ceil_div(P.nk, 128), 128, 0, ctx->stream>>>(P.nk, P.n, P.D, P.beta, mu, P.eps, P.UP, nullptr, fs);
+    DG_LAUNCH(ctx, "k_fermi");
+    k_nele_finalize<<<1, 256, 0, ctx->stream>>>(nf2, P.nk, P.beta, tr, dtr, fs, deriv ? 1 : 0, dout);
+    DG_LAUNCH(ctx, "k_nele_finalize");
+    return DMFTGPU_OK;
+}
+
+int nele_host(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *N, double *dN) {
+    double *dout = (double *)dg_buf(ctx, "nele.out", 2 * sizeof(double));
+    if (!dout) return DMFTGPU_NOMEM;
+    DG_TRY(nele_pass(ctx, P, mu, deriv, dout));
+    double h[2];
+    DG_CUDA(cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    *N = h[0];
+    if (dN) *dN = h[1];
+    return DMFTGPU_OK;
+}
+
+int check_lat(const dmftgpu_lattice *L) {
+    if (!L || L->n < 1 || L->nk < 1 || L->nfreq < 1 || L->ncl < 1 || L->nh < 1 || !(L->beta > 0))
+        return DMFTGPU_BADARG;
+    return DMFTGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double *hr, int kx, int ky, int kz,
+               double *hk, int flags) {
+    if (!ctx || n < 1 || nnz < 0 || !rindex || !hr || !hk || kx < 1 || ky < 1 || kz < 1) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    // group the read_HR rows by lattice vector into a dense [N_R][n*n] table (duplicates add up, as the
+    // reference's += does)
+    std::map<std::array<int, 3>, int> rid;
+    std::vector<std::array<int, 3>> Rl;
+    for (int e = 0; e < nnz; e++) {
+        const int *r = rindex + 5 * e;
+        if (r[3] < 0 || r[3] >= n || r[4] < 0 || r[4] >= n) return dg_fail(ctx, DMFTGPU_BADARG, "hk: orbital index");
+        std::array<int, 3> key = {r[0], r[1], r[2]};
+        if (!rid.count(key)) {
+            rid[key] = (int)Rl.size();
+            Rl.push_back(key);
+        }
+    }
+    const int nR = std::max(1, (int)Rl.size()), ne = n * n, nk = kx * ky * kz;
+    std::vector<double2> T((size_t)nR * ne, make_double2(0, 0));
+    std::vector<int> Rv(3 * (size_t)nR, 0);
+    for (size_t i = 0; i < Rl.size(); i++)
+        for (int d = 0; d < 3; d++) Rv[3 * i + d] = Rl[i][d];
+    for (int e = 0; e < nnz; e++) {
+        const int *r = rindex + 5 * e;
+        int q = rid[{r[0], r[1], r[2]}];
+        double2 &t = T[(size_t)q * ne + r[3] + (size_t)r[4] * n];
+        t.x += hr[2 * e];
+        t.y += hr[2 * e + 1];
+    }
+    int *dR = (int *)dg_buf(ctx, "hk.R", Rv.size() * sizeof(int));
+    double2 *dT = (double2 *)dg_buf(ctx, "hk.T", T.size() * sizeof(double2));
+    if (!dR || !dT) return DMFTGPU_NOMEM;
+    DG_CUDA(cudaMemcpyAsync(dR, Rv.data(), Rv.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    DG_CUDA(cudaMemcpyAsync(dT, T.data(), T.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    int st;
+    double2 *dH = (double2 *)dg_out(ctx, hk, (size_t)nk * ne * sizeof(double2), flags, "io.hk", &st);
+    if (st) return st;
+    dim3 grid(dg_ceil_div(nk, HK_KB), dg_ceil_div(ne, HK_EB));
+    k_hk<<<grid, HK_KB * HK_EB, 0, ctx->stream>>>(nk, (int)Rl.size(), ne, kx, ky, kz, dR, dT, dH);
+    DG_LAUNCH(ctx, "k_hk");
+    DG_TRY(dg_out_done(ctx, hk, dH, (size_t)nk * ne * sizeof(double2), flags));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return DMFTGPU_OK;
+}
+
+int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                       double *gw, double *gwhf, double *nummat, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !gw || !nummat) return DMFTGPU_BADARG;
+    if (flags & DMFTGPU_MIXED) return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w: mixed precision not built yet");
+    cudaSetDevice(ctx->device);
+    const int D = L->ncl * L->nh, Nf = L->nfreq;
+    const size_t DD = (size_t)D * D;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, Nf * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    double2 *dG = (double2 *)dg_out(ctx, gw, Nf * DD * sizeof(double2), flags, "io.gw", &st);
+    if (st) return st;
+    double2 *dG0 = gwhf ? (double2 *)dg_out(ctx, gwhf, Nf * DD * sizeof(double2), flags, "io.gwhf", &st) : nullptr;
+    if (st) return st;
+    double2 *dN = (double2 *)dg_out(ctx, nummat, DD * sizeof(double2), flags, "io.nummat", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
+    double2 *blk = (double2 *)dg_buf(ctx, "gloc.blk", 2 * Nf * DD * sizeof(double2));
+    double2 *blk0 = (double2 *)dg_buf(ctx, "gloc.blk0", 2 * Nf * DD * sizeof(double2));
+    double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
+    double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
+    if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
+    DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
+    DG_LAUNCH(ctx, "k_fermi");
+    k_gloc_finalize<<<1, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->ncl, L->nh, L->beta, blk, blk0, occ, dG, dG0, dN);
+    DG_LAUNCH(ctx, "k_gloc_finalize");
+    DG_TRY(dg_out_done(ctx, gw, dG, Nf * DD * sizeof(double2), flags));
+    if (gwhf) DG_TRY(dg_out_done(ctx, gwhf, dG0, Nf * DD * sizeof(double2), flags));
+    DG_TRY(dg_out_done(ctx, nummat, dN, DD * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                 double *nele, double *dnele, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !nele) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t DD = (size_t)L->ncl * L->nh * L->ncl * L->nh;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, L->nfreq * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 1, P));
+    DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    if (!std::isfinite(*nele)) return DMFTGPU_NAN;
+    return code;
+}
+
+int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                      double dmu, double n_target, double *mu_out, int *n_eval, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !mu_out) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t DD = (size_t)L->ncl * L->nh * L->ncl * L->nh;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, L->nfreq * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 1, P));
+    int evals = 0;
+    auto N = [&](double m, double *out, double *dout) {
+        evals++;
+        return nele_host(ctx, P, m, dout != nullptr, out, dout);
+    };
+    const double goal = n_target;
+    if (flags & DMFTGPU_NEWTON) {
+        // safeguarded Newton: keep a bracket [lo, hi] with N(lo) < goal < N(hi) once found
+        double lo = -1e300, hi = 1e300, Nv, dN;
+        for (int it = 0; it < 100; it++) {
+            DG_TRY(N(mu, &Nv, &dN));
+            if (!std::isfinite(Nv)) return DMFTGPU_NAN;
+            double r = Nv - goal;
+            if (r < 0) lo = std::max(lo, mu);
+            else hi = std::min(hi, mu);
+            if (std::fabs(r) <= 1e-11 * std::max(1.0, std::fabs(goal))) {
+                *mu_out = mu;
+                if (n_eval) *n_eval = evals;
+                return DMFTGPU_OK;
+            }
+            double step = (dN > 0) ? -r / dN : (r < 0 ? std::fabs(dmu) : -std::fabs(dmu));
+            double next = mu + step;
+            if (!(next > lo && next < hi)) {
+                if (lo > -1e299 && hi < 1e299) next = 0.5 * (lo + hi);
+                else next = mu + (r < 0 ? std::fabs(dmu) : -std::fabs(dmu));
+            }
+            if (std::fabs(next - mu) < 1e-15 * std::max(1.0, std::fabs(mu))) {
+                *mu_out = next;
+                if (n_eval) *n_eval = evals;
+                return DMFTGPU_OK;
+            }
+            mu = next;
+        }
+        *mu_out = mu;
+        if (n_eval) *n_eval = evals;
+        return DMFTGPU_NONCONVERGED;
+    }
+    // the reference's bracket expansion + bisection (src/GreenFtn.cpp:81-121)
+    double Nele[2] = {-1, -1};
+    DG_TRY(N(mu, &Nele[0], nullptr));
+    if (!std::isfinite(Nele[0])) return DMFTGPU_NAN;
+    double muUB = 0, muLB = 0, mu_next;
+    int nearAns = 0;
+    if (Nele[0] > goal) mu -= (dmu - dmu);
+    else if (Nele[0] < goal) mu -= (dmu + dmu);
+    int guard = 0;
+    while ((Nele[0] != goal) && std::abs(dmu) > 1e-5) {
+        if (++guard > 10000) return DMFTGPU_NONCONVERGED;
+        mu += dmu;
+        Nele[1] = Nele[0];
+        DG_TRY(N(mu, &Nele[0], nullptr));
+        if (nearAns == 0) {
+            if (Nele[0] < goal) {
+                muLB = mu;
+                if (Nele[1] > goal && Nele[1] > 0) nearAns = 1;
+                else dmu = std::fabs(dmu);
+            }
+            if (Nele[0] > goal) {
+                muUB = mu;
+                if (Nele[1] < goal && Nele[1] > 0) nearAns = 1;
+                else dmu = -1 * std::fabs(dmu);
+            }
+            if (Nele[0] == goal) break;
+            if (!(std::abs(mu) < 600)) return DMFTGPU_NONCONVERGED;
+        } else {
+            if (Nele[0] > goal) muUB = mu;
+            else if (Nele[0] < goal) muLB = mu;
+            mu_next = (muUB + muLB) / 2.;
+            dmu = mu_next - mu;
+        }
+    }
+    *mu_out = mu;
+    if (n_eval) *n_eval = evals;
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+}  // extern "C"

@@ -1,0 +1,327 @@
+// moments.cu -- getAsymto_moments (src/FourierTransform.cpp:184-465) on the device.
+//
+// The reference fits F(iw) ~ m0 + m1/iw + m2/(iw)^2 + m3/(iw)^3 by least squares on every suffix window
+// [w, N_freq) of the Matsubara axis, with (K^T K)^-1 K^T G per window.  K has two non-zeros per row, so
+// K^T G and K^T K are suffix sums of four (resp. six) weighted series: the device forms those sums with one
+// backward scan per series (O(N_freq) instead of the reference's O(N_freq^2)), inverts each 4x4 K^T K with
+// partial pivoting, and then reproduces the reference's window averaging (2Nv+1 windows, Nv = N_freq/20),
+// the variance of the trace of each moment, the positivity gates on the averaged moments, the first-minimum
+// window choice (sequential argmin started at the last window) and the final Hermitisation.
+#include "linalg.cuh"
+
+namespace {
+
+struct MomArgs {
+    int D, Nf, R, C, Nv, ncol;
+    double beta;
+    int green;
+    const double2 *fw;  // [Nf][D][D]
+    double2 *S;         // [D*D][ncol][R]  suffix sums K^T G
+    double *KS;         // [6][R]          suffix sums for K^T K
+    double *kinv;       // [R][16]
+    double2 *mt;        // [D*D][R][ncol]  fitted moments per window ("momentstest")
+    double *tr;         // [ncol][R]
+    double2 *avg;       // [ncol][C][D*D]
+    double *var;        // [ncol][C]
+    int *ok;            // [C]
+    double2 *work;      // [C][8][D*D]
+    int *iwork;         // [C][2*D]
+    double2 *mom;       // [4][D][D]
+    int *status;
+};
+
+__device__ __forceinline__ double zof(int wn, double beta) { return (2 * wn + 1) * DG_PI / beta; }
+
+// one thread per (element ab, column c): backward scan of the weighted series
+__global__ void k_mom_suffix(MomArgs g) {
+    const int DD = g.D * g.D;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < DD * g.ncol) {
+        int ab = t / g.ncol, c = t % g.ncol;
+        int a = ab / g.D, b = ab % g.D;  // momentstest index alp*Dim + bet
+        double2 s = cmk(0, 0);
+        for (int wn = g.Nf - 1; wn >= 0; wn--) {
+            double z = zof(wn, g.beta);
+            double2 fab = g.fw[(size_t)wn * DD + a + b * g.D], fba = g.fw[(size_t)wn * DD + b + a * g.D];
+            double2 re = cmk((fab.x + fba.x) / 2, (fab.y - fba.y) / 2);        // (F_ab + conj F_ba)/2
+            double2 im = cmk((fab.y + fba.y) * 0.5, -(fab.x - fba.x) * 0.5);  // (F_ab - conj F_ba)/(2i)
+            double2 term;
+            if (!g.green) {
+                if (c == 0) term = re;
+                else if (c == 1) term = cscale(im, -1. / pow(z, 1));
+                else if (c == 2) term = cscale(re, -1. / pow(z, 2));
+                else term = cscale(im, 1. / pow(z, 3));
+            } else {
+                if (c == 0) term = cscale(re, -1. / pow(z, 2));
+                else {
+                    if (a == b) im.x += 1.0 / z;
+                    term = cscale(im, 1. / pow(z, 3));
+                }
+            }
+            s = cadd(s, term);
+            if (wn < g.R) g.S[((size_t)ab * g.ncol + c) * g.R + wn] = s;
+        }
+    } else if (t < DD * g.ncol + 6) {
+        int q = t - DD * g.ncol;
+        double s = 0;
+        for (int wn = g.Nf - 1; wn >= 0; wn--) {
+            double z = zof(wn, g.beta);
+            double v;
+            if (q == 0) v = 1.0;
+            else if (q == 1) v = (-1. / pow(z, 2)) * (1.0);        // K(.,0) K(.,2) on Re rows
+            else if (q == 2) v = (-1. / pow(z, 2)) * (-1. / pow(z, 2));
+            else if (q == 3) v = (-1. / pow(z, 1)) * (-1. / pow(z, 1));
+            else if (q == 4) v = (-1. / pow(z, 1)) * (1. / pow(z, 3));
+            else v = (1. / pow(z, 3)) * (1. / pow(z, 3));
+            s += v;
+            if (wn < g.R) g.KS[(size_t)q * g.R + wn] = s;
+        }
+    }
+}
+
+// one thread per window: (K^T K)^-1
+__global__ void k_mom_kinv(MomArgs g) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= g.R) return;
+    double2 K[16];
+    int perm[4];
+    for (int i = 0; i < 16; i++) K[i] = cmk(0, 0);
+    const int n = g.ncol;
+    if (!g.green) {
+        K[0 + 0 * 4] = cmk(g.KS[0 * g.R + w], 0);
+        K[0 + 2 * 4] = K[2 + 0 * 4] = cmk(g.KS[1 * g.R + w], 0);
+        K[2 + 2 * 4] = cmk(g.KS[2 * g.R + w], 0);
+        K[1 + 1 * 4] = cmk(g.KS[3 * g.R + w], 0);
+        K[1 + 3 * 4] = K[3 + 1 * 4] = cmk(g.KS[4 * g.R + w], 0);
+        K[3 + 3 * 4] = cmk(g.KS[5 * g.R + w], 0);
+    } else {
+        K[0 + 0 * 2] = cmk(g.KS[2 * g.R + w], 0);
+        K[1 + 1 * 2] = cmk(g.KS[5 * g.R + w], 0);
+    }
+    if (thread_gj_inverse(n, K, perm)) dg_flag(g.status, DG_SINGULAR);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) g.kinv[(size_t)w * 16 + i + j * n] = K[i + j * n].x;
+}
+
+// one thread per (window, element): m_i = sum_c inv(i,c) (K^T G)_c, and the trace contributions
+__global__ void k_mom_solve(MomArgs g) {
+    const int DD = g.D * g.D;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.R * DD) return;
+    int w = (int)(t / DD), ab = (int)(t % DD);
+    const int n = g.ncol;
+    const double *ki = g.kinv + (size_t)w * 16;
+    for (int i = 0; i < n; i++) {
+        double2 m = cmk(0, 0);
+        for (int c = 0; c < n; c++) m = cadd(m, cscale(g.S[((size_t)ab * n + c) * g.R + w], ki[i + c * n]));
+        g.mt[((size_t)ab * g.R + w) * n + i] = m;
+    }
+}
+
+__global__ void k_mom_trace(MomArgs g) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.R * g.ncol) return;
+    int w = t / g.ncol, i = t % g.ncol;
+    double s = 0;
+    for (int a = 0; a < g.D; a++) s += g.mt[((size_t)(a * g.D + a) * g.R + w) * g.ncol + i].x;
+    g.tr[(size_t)i * g.R + w] = s;
+}
+
+// one thread per (centre, element, moment): window averages; one per (centre, moment): variance
+__global__ void k_mom_avg(MomArgs g) {
+    const int DD = g.D * g.D;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long navg = (long long)g.C * DD * g.ncol;
+    if (t < navg) {
+        int i = (int)(t % g.ncol);
+        long long r = t / g.ncol;
+        int ab = (int)(r % DD), ci = (int)(r / DD);
+        int a = ab / g.D, b = ab % g.D;
+        double2 s = cmk(0, 0);
+        for (int iw = ci; iw <= ci + 2 * g.Nv; iw++) s = cadd(s, g.mt[((size_t)ab * g.R + iw) * g.ncol + i]);
+        // Eigen MatrixXcd(a,b) with ab = a*Dim + b; stored column-major
+        g.avg[((size_t)i * g.C + ci) * DD + a + b * g.D] = cmk(s.x / (2 * g.Nv + 1), s.y / (2 * g.Nv + 1));
+    } else if (t < navg + (long long)g.C * g.ncol) {
+        long long u = t - navg;
+        int i = (int)(u % g.ncol), ci = (int)(u / g.ncol);
+        const double *tr = g.tr + (size_t)i * g.R + ci;
+        int L = 2 * g.Nv + 1;
+        double mean = 0;
+        for (int j = 0; j < L; j++) mean += tr[j];
+        mean /= L;
+        double ss = 0;
+        for (int j = 0; j < L; j++) ss += (tr[j] - mean) * (tr[j] - mean);
+        g.var[(size_t)i * g.C + ci] = sqrt(ss / L);
+    }
+}
+
+// one thread per centre: the positivity gates of the window search
+__global__ void k_mom_gate(MomArgs g) {
+    int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= g.C) return;
+    const int D = g.D, DD = D * D;
+    double2 *W = g.work + (size_t)ci * 8 * DD;
+    double2 *A = W, *U = W + DD, *T1 = W + 2 * DD, *T2 = W + 3 * DD, *T3 = W + 4 * DD, *X = W + 5 * DD;
+    int *ord = g.iwork + (size_t)ci * 2 * D, *perm = ord + D;
+    double *ev = (double *)(W + 6 * DD);  // D doubles fit in DD complex slots
+    int okv = 0;
+    if (!g.green) {
+        const double2 *m1 = g.avg + ((size_t)1 * g.C + ci) * DD;
+        const double2 *m2 = g.avg + ((size_t)2 * g.C + ci) * DD;
+        const double2 *m3 = g.avg + ((size_t)3 * g.C + ci) * DD;
+        thread_heig(D, m1, A, U, ev, ord);
+        double a = ev[0];
+        if (a > 0) {
+            // V_inv = (U sqrt(ev) U^H)^-1
+            for (int j = 0; j < D; j++)
+                for (int i = 0; i < D; i++) {
+                    double2 s = cmk(0, 0);
+                    for (int l = 0; l < D; l++) s = cfma(cscale(DG_AT(U, D, i, l), sqrt(ev[l])), cconj(DG_AT(U, D, j, l)), s);
+                    DG_AT(T1, D, i, j) = s;
+                }
+            thread_gj_inverse(D, T1, perm);                   // T1 = V_inv
+            thread_matmul(D, T1, m2, T2);                     // V_inv m2
+            thread_matmul(D, T2, T1, T3);                     // T3 = V_inv m2 V_inv
+            thread_matmul(D, T1, m3, T2);                     // V_inv m3
+            thread_matmul(D, T2, T1, X);                      // X = V_inv m3 V_inv
+            thread_matmul(D, T3, T3, T2);                     // T2 = (V_inv m2 V_inv)^2
+            for (int k = 0; k < DD; k++) X[k] = csub(X[k], T2[k]);
+            thread_heig(D, X, A, nullptr, ev, ord);
+            double b = ev[0];
+            okv = (a > 0 && b > 0);
+        }
+    } else {
+        const double2 *m0 = g.avg + ((size_t)0 * g.C + ci) * DD;
+        const double2 *m1 = g.avg + ((size_t)1 * g.C + ci) * DD;
+        thread_matmul(D, m0, m0, T1);
+        for (int k = 0; k < DD; k++) X[k] = csub(m1[k], T1[k]);
+        thread_heig(D, X, A, nullptr, ev, ord);
+        okv = (ev[0] > 1);
+    }
+    g.ok[ci] = okv;
+}
+
+// single block: window choice per moment and the final averaged, Hermitised moments
+__global__ void k_mom_final(MomArgs g) {
+    __shared__ int win[4];
+    const int D = g.D, DD = D * D;
+    if (threadIdx.x < g.ncol) {
+        int m = threadIdx.x;
+        const double *var = g.var + (size_t)m * g.C;
+        int minPos = g.C - 1;
+        for (int i = 0; i < g.C; i++)
+            if (g.ok[i] && var[i] < var[minPos]) minPos = i;
+        win[m] = minPos;  // centre = minPos + Nv, window iw in [minPos, minPos + 2 Nv]
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 4 * DD; t += blockDim.x) {
+        int mom = t / DD, e = t % DD;
+        int a = e % D, b = e / D;  // column-major element (a, b)
+        double2 val = cmk(0, 0);
+        int src = g.green ? mom - 2 : mom;
+        if (src >= 0) {
+            int w0 = win[src];
+            double2 s = cmk(0, 0);
+            for (int w = w0; w <= w0 + 2 * g.Nv; w++) {
+                double2 x = g.mt[((size_t)(a * D + b) * g.R + w) * g.ncol + src];
+                double2 y = g.mt[((size_t)(b * D + a) * g.R + w) * g.ncol + src];
+                s = cadd(s, cscale(cadd(x, cconj(y)), 0.5));
+            }
+            val = cmk(s.x / (2 * g.Nv + 1), s.y / (2 * g.Nv + 1));
+        } else if (mom == 1) {
+            val = cmk(a == b ? 1.0 : 0.0, 0.0);
+        }
+        g.mom[(size_t)mom * DD + a + b * D] = val;
+    }
+    __syncthreads();
+    // (m + m^H)/2
+    for (int t = threadIdx.x; t < 4 * DD; t += blockDim.x) {
+        int mom = t / DD, e = t % DD;
+        int a = e % D, b = e / D;
+        if (a > b) continue;
+        double2 x = g.mom[(size_t)mom * DD + a + b * D], y = g.mom[(size_t)mom * DD + b + a * D];
+        double2 h = cscale(cadd(x, cconj(y)), 0.5);
+        g.mom[(size_t)mom * DD + a + b * D] = h;
+        g.mom[(size_t)mom * DD + b + a * D] = cconj(h);
+    }
+}
+
+}  // namespace
+
+int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double2 *fw, int green,
+                   double2 *mom) {
+    MomArgs g;
+    g.D = dim;
+    g.Nf = nfreq;
+    g.green = green ? 1 : 0;
+    g.ncol = green ? 2 : 4;
+    g.R = green ? nfreq - 1 : nfreq - 3;
+    g.Nv = nfreq / 20;
+    if (g.Nv == 0) g.Nv = 1;
+    g.C = g.R - 2 * g.Nv;
+    g.beta = beta;
+    if (dim < 1 || g.R < 1 || g.C < 1) return dg_fail(ctx, DMFTGPU_BADARG, "moments: N_freq too small");
+    const size_t DD = (size_t)dim * dim;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    size_t oS = carve(DD * g.ncol * g.R * sizeof(double2)), oKS = carve(6 * g.R * sizeof(double)),
+           oKi = carve((size_t)g.R * 16 * sizeof(double)), oMt = carve(DD * g.R * g.ncol * sizeof(double2)),
+           oTr = carve((size_t)g.ncol * g.R * sizeof(double)), oAvg = carve((size_t)g.ncol * g.C * DD * sizeof(double2)),
+           oVar = carve((size_t)g.ncol * g.C * sizeof(double)), oOk = carve((size_t)g.C * sizeof(int)),
+           oW = carve((size_t)g.C * 8 * DD * sizeof(double2)), oIw = carve((size_t)g.C * 2 * dim * sizeof(int));
+    char *base = (char *)dg_buf(ctx, "moments.work", off);
+    if (!base) return DMFTGPU_NOMEM;
+    g.fw = fw;
+    g.S = (double2 *)(base + oS);
+    g.KS = (double *)(base + oKS);
+    g.kinv = (double *)(base + oKi);
+    g.mt = (double2 *)(base + oMt);
+    g.tr = (double *)(base + oTr);
+    g.avg = (double2 *)(base + oAvg);
+    g.var = (double *)(base + oVar);
+    g.ok = (int *)(base + oOk);
+    g.work = (double2 *)(base + oW);
+    g.iwork = (int *)(base + oIw);
+    g.mom = mom;
+    g.status = ctx->d_status;
+    cudaStream_t s = ctx->stream;
+    int nthr = (int)(DD * g.ncol + 6);
+    k_mom_suffix<<<dg_ceil_div(nthr, 64), 64, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_suffix");
+    k_mom_kinv<<<dg_ceil_div(g.R, 128), 128, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_kinv");
+    k_mom_solve<<<dg_ceil_div((long long)g.R * DD, 256), 256, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_solve");
+    k_mom_trace<<<dg_ceil_div(g.R * g.ncol, 256), 256, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_trace");
+    long long navg = (long long)g.C * DD * g.ncol + (long long)g.C * g.ncol;
+    k_mom_avg<<<dg_ceil_div(navg, 256), 256, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_avg");
+    k_mom_gate<<<dg_ceil_div(g.C, 64), 64, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_gate");
+    k_mom_final<<<1, 256, 0, s>>>(g);
+    DG_LAUNCH(ctx, "k_mom_final");
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_moments(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double *fw, int green_asym,
+                               double *mom, int flags) {
+    if (!ctx || !fw || !mom || dim < 1 || nfreq < 1) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    int st;
+    size_t DD = (size_t)dim * dim;
+    const double2 *dfw = (const double2 *)dg_in(ctx, fw, nfreq * DD * sizeof(double2), flags, "io.fw", &st);
+    if (st) return st;
+    double2 *dmom = (double2 *)dg_out(ctx, mom, 4 * DD * sizeof(double2), flags, "io.mom", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_moments_dev(ctx, dim, nfreq, beta, dfw, green_asym, dmom));
+    DG_TRY(dg_out_done(ctx, mom, dmom, 4 * DD * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code ? code : DMFTGPU_OK;
+}

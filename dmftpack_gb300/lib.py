@@ -1,0 +1,294 @@
+"""ctypes binding of libdmftgpu.so and the Python mirror of the reference's call surface for the hot path.
+
+Function names follow DMFTpack (GreenFtn_w, GreenFtn_w_adjust_mu, GiwToNele, Construct_hyb_delta,
+getAsymto_moments, Construct_Hk_Sk ...).  The reference's globals (beta, N_freq, HartrIndex, ...) are
+passed explicitly through :class:`Lattice`.
+
+Arrays are ordinary ``(count, i, j)`` complex stacks: numpy arrays (host; the library copies them to the
+device and back) or CUDA ``torch`` tensors (device; the call is enqueued on torch's current stream).  The
+library itself stores matrices column-major like Eigen; this module does the transposition.
+
+There is no CPU fallback: if libdmftgpu.so is missing or no CUDA device is present, calls raise.
+"""
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
+STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
+                6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
+DEVICE_PTRS, MIXED, NEWTON = 0x1, 0x2, 0x4
+
+# every symbol include/dmftgpu.h declares
+EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
+           "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
+           "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta"]
+
+
+class DmftGpuError(RuntimeError):
+    def __init__(self, what, code, detail=""):
+        super().__init__("%s failed: %s%s" % (what, STATUS_NAMES.get(code, code), (" (%s)" % detail) if detail else ""))
+        self.code = code
+
+
+class _Lat(C.Structure):
+    _fields_ = [("n", C.c_int), ("nk", C.c_int), ("nfreq", C.c_int), ("beta", C.c_double),
+                ("ncl", C.c_int), ("nh", C.c_int), ("hartr", _ip)]
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(require_built=True):
+    """Load libdmftgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if require_built:
+            raise RuntimeError("libdmftgpu.so is not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        _build.build()
+    lib = C.CDLL(path)
+    P = C.POINTER
+    lib.dmftgpu_create.argtypes = [P(_vp), C.c_int]
+    lib.dmftgpu_destroy.argtypes = [_vp]
+    lib.dmftgpu_set_stream.argtypes = [_vp, _vp]
+    lib.dmftgpu_get_stream.argtypes = [_vp]
+    lib.dmftgpu_get_stream.restype = _vp
+    lib.dmftgpu_synchronize.argtypes = [_vp]
+    lib.dmftgpu_last_error.argtypes = [_vp]
+    lib.dmftgpu_last_error.restype = C.c_char_p
+    lib.dmftgpu_launch_count.argtypes = [_vp]
+    lib.dmftgpu_launch_count.restype = C.c_longlong
+    lib.dmftgpu_timing.argtypes = [_vp, C.c_int]
+    lib.dmftgpu_kernel_time.argtypes = [_vp, C.c_char_p, _dp, _ip]
+    lib.dmftgpu_kmesh.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
+    lib.dmftgpu_hk.argtypes = [_vp, C.c_int, C.c_int, _ip, _dp, C.c_int, C.c_int, C.c_int, _vp, C.c_int]
+    lib.dmftgpu_moments.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, C.c_int, _vp, C.c_int]
+    lib.dmftgpu_greenftn_w.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
+    lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
+    lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
+                                      _vp, C.c_int]
+    _lib = lib
+    return lib
+
+
+@dataclass
+class Lattice:
+    """The reference's lattice globals (NBAND, knum, N_freq, beta, NumCluster, NumHartrOrbit_per_cluster,
+    HartrIndex)."""
+    n: int
+    nk: int
+    nfreq: int
+    beta: float
+    ncl: int = 1
+    nh: int = 1
+    hartr: object = None
+
+    @property
+    def D(self):
+        return self.ncl * self.nh
+
+    def _c(self):
+        h = None
+        if self.hartr is not None:
+            h = np.ascontiguousarray(self.hartr, dtype=np.int32)
+        s = _Lat(self.n, self.nk, self.nfreq, float(self.beta), self.ncl, self.nh,
+                 h.ctypes.data_as(_ip) if h is not None else None)
+        s._keep = h
+        return s
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class _Arr:
+    """A (count, i, j) complex stack converted to the library's column-major layout."""
+
+    def __init__(self, x, device):
+        self.device = device
+        if device:
+            import torch
+            t = x.to(torch.complex128).transpose(-1, -2).contiguous()
+            self.obj = t
+            self.ptr = t.data_ptr()
+        else:
+            a = np.ascontiguousarray(np.swapaxes(np.asarray(x, dtype=np.complex128), -1, -2))
+            self.obj = a
+            self.ptr = a.ctypes.data
+
+    @staticmethod
+    def empty(shape, device, like=None):
+        if device:
+            import torch
+            t = torch.empty(shape[:-2] + (shape[-1], shape[-2]), dtype=torch.complex128, device=like.device)
+            o = _Arr.__new__(_Arr)
+            o.device, o.obj, o.ptr = True, t, t.data_ptr()
+            return o
+        a = np.empty(shape[:-2] + (shape[-1], shape[-2]), np.complex128)
+        o = _Arr.__new__(_Arr)
+        o.device, o.obj, o.ptr = False, a, a.ctypes.data
+        return o
+
+    def result(self):
+        if self.device:
+            return self.obj.transpose(-1, -2)
+        return np.ascontiguousarray(np.swapaxes(self.obj, -1, -2))
+
+
+class Context:
+    """One libdmftgpu context (CUDA device, stream, device workspaces)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = _vp()
+        st = self.lib.dmftgpu_create(C.byref(h), device)
+        if st != OK:
+            raise DmftGpuError("dmftgpu_create", st)
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dmftgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, what, st, allowed=(OK,)):
+        if st not in allowed:
+            raise DmftGpuError(what, st, self.lib.dmftgpu_last_error(self.h).decode(errors="replace"))
+        return st
+
+    def launches(self):
+        return int(self.lib.dmftgpu_launch_count(self.h))
+
+    def timing(self, enable=True):
+        self._check("dmftgpu_timing", self.lib.dmftgpu_timing(self.h, int(bool(enable))))
+
+    def kernel_time(self, name):
+        """(total ms, launches) of kernel `name` since timing(True)."""
+        ms, cnt = C.c_double(), C.c_int()
+        self._check("dmftgpu_kernel_time", self.lib.dmftgpu_kernel_time(self.h, name.encode(), C.byref(ms),
+                                                                           C.byref(cnt)))
+        return ms.value, cnt.value
+
+    def synchronize(self):
+        self._check("dmftgpu_synchronize", self.lib.dmftgpu_synchronize(self.h))
+
+    def _flags(self, device, extra=0):
+        if device:
+            import torch
+            self.lib.dmftgpu_set_stream(self.h, _vp(torch.cuda.current_stream().cuda_stream))
+            return DEVICE_PTRS | extra
+        return extra
+
+    # ------------------------------------------------------------------ lattice stage
+    def Construct_Hk(self, n, rindex, hr, kgrid, device_out=None):
+        """H(k) on the TightBinding mesh (Construct_Hk_Sk's Fourier sum); kgrid = (kx, ky, kz).
+        Returns (nk, n, n): numpy, or a CUDA tensor when device_out is a torch device."""
+        rindex = np.ascontiguousarray(rindex, np.int32)
+        hr = np.ascontiguousarray(hr, np.complex128)
+        kx, ky, kz = kgrid
+        nk = kx * ky * kz
+        dev = device_out is not None
+        if dev:
+            import torch
+            out = torch.empty((nk, n, n), dtype=torch.complex128, device=device_out)
+            ptr = out.data_ptr()
+        else:
+            out = np.empty((nk, n, n), np.complex128)
+            ptr = out.ctypes.data
+        st = self.lib.dmftgpu_hk(self.h, n, rindex.shape[0], rindex.ctypes.data_as(_ip),
+                                 hr.view(np.float64).ctypes.data_as(_dp), kx, ky, kz, _vp(ptr), self._flags(dev))
+        self._check("dmftgpu_hk", st)
+        # stored column-major per k: reinterpret
+        return out.transpose(-1, -2) if dev else np.ascontiguousarray(np.swapaxes(out, -1, -2))
+
+    def getAsymto_moments(self, fw, beta, greenFtnAsym=False):
+        dev = _is_torch(fw)
+        a = _Arr(fw, dev)
+        nf, dim = a.obj.shape[0], a.obj.shape[1]
+        out = _Arr.empty((4, dim, dim), dev, like=a.obj)
+        st = self.lib.dmftgpu_moments(self.h, dim, nf, float(beta), _vp(a.ptr), int(bool(greenFtnAsym)),
+                                      _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_moments", st)
+        return out.result()
+
+    def GreenFtn_w(self, lat, H_k, SelfE_w, mu, mixed=False, with_gwhf=True):
+        """GreenFtn_w: returns (Gw[nfreq,D,D], GwHF[nfreq,D,D] or None, NumMatrix[D,D])."""
+        dev = _is_torch(H_k)
+        h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
+        D = lat.D
+        gw = _Arr.empty((lat.nfreq, D, D), dev, like=h.obj)
+        g0 = _Arr.empty((lat.nfreq, D, D), dev, like=h.obj) if with_gwhf else None
+        nm = _Arr.empty((D, D), dev, like=h.obj)
+        L = lat._c()
+        st = self.lib.dmftgpu_greenftn_w(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(gw.ptr),
+                                         _vp(g0.ptr) if g0 else None, _vp(nm.ptr),
+                                         self._flags(dev, MIXED if mixed else 0))
+        self._check("dmftgpu_greenftn_w", st)
+        return gw.result(), (g0.result() if g0 else None), nm.result()
+
+    def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False):
+        dev = _is_torch(H_k)
+        h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
+        N, dN = C.c_double(), C.c_double()
+        L = lat._c()
+        st = self.lib.dmftgpu_nele(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), C.byref(N),
+                                   C.byref(dN) if deriv else None, self._flags(dev, MIXED if mixed else 0))
+        self._check("dmftgpu_nele", st)
+        return (N.value, dN.value) if deriv else N.value
+
+    def GreenFtn_w_adjust_mu(self, lat, H_k, SelfE_w, mu, dmu, n_target, newton=False, mixed=False):
+        """Returns (mu, number of N(mu) passes)."""
+        dev = _is_torch(H_k)
+        h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
+        out, ne = C.c_double(), C.c_int()
+        L = lat._c()
+        fl = (NEWTON if newton else 0) | (MIXED if mixed else 0)
+        st = self.lib.dmftgpu_adjust_mu(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), float(dmu),
+                                        float(n_target), C.byref(out), C.byref(ne), self._flags(dev, fl))
+        self._check("dmftgpu_adjust_mu", st)
+        return out.value, ne.value
+
+    def Construct_hyb_delta(self, impurityOrbit, SelfE_w, Gw, mu, beta, impurity_site_Hamiltonian):
+        dev = _is_torch(Gw)
+        orb = np.ascontiguousarray(impurityOrbit, np.int32)
+        s, g = _Arr(SelfE_w, dev), _Arr(Gw, dev)
+        hi = _Arr(impurity_site_Hamiltonian[None] if not dev else impurity_site_Hamiltonian.unsqueeze(0), dev)
+        nf, D = s.obj.shape[0], s.obj.shape[1]
+        dim = orb.shape[0]
+        out = _Arr.empty((nf, dim, dim), dev, like=s.obj)
+        st = self.lib.dmftgpu_hyb_delta(self.h, dim, orb.ctypes.data_as(_ip), nf, float(beta), D, _vp(s.ptr),
+                                        _vp(g.ptr), _vp(hi.ptr), float(mu), _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_hyb_delta", st)
+        return out.result()
+
+
+def kmesh(kx, ky, kz):
+    out = np.empty((kx * ky * kz, 3))
+    st = load().dmftgpu_kmesh(kx, ky, kz, out.ctypes.data_as(_dp))
+    if st != OK:
+        raise DmftGpuError("dmftgpu_kmesh", st)
+    return out

@@ -1,0 +1,127 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Each builder returns a :class:`Workload`: the tight-binding table in read_HR form (rindex, hr), the k grid,
+beta, N_freq, N_tau, the correlated-space layout and an initial self-energy SelfE_w[N_freq, D, D].
+All randomness comes from numpy's PCG64 with a fixed seed per workload.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PI = 3.1415926535897932384626
+
+
+@dataclass
+class Workload:
+    name: str
+    n: int
+    rindex: np.ndarray
+    hr: np.ndarray
+    kgrid: tuple
+    beta: float
+    nfreq: int
+    ntau: int
+    ncl: int
+    nh: int
+    sigma: np.ndarray
+    n_electrons: float
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nk(self):
+        return self.kgrid[0] * self.kgrid[1] * self.kgrid[2]
+
+    @property
+    def D(self):
+        return self.ncl * self.nh
+
+    def wn(self):
+        return PI * (2 * np.arange(self.nfreq) + 1) / self.beta
+
+
+def _hermitian_hoppings(n, rvecs, draw, onsite):
+    """t(R) for every R in rvecs with t(-R) = t(R)^H; draw(R) -> n x n complex for one of each +-R pair."""
+    rows, vals = [], []
+    seen = {}
+    for R in rvecs:
+        R = tuple(int(x) for x in R)
+        if R in seen:
+            continue
+        mR = tuple(-x for x in R)
+        if R == (0, 0, 0):
+            t = draw(R)
+            t = (t + t.conj().T) / 2 + np.diag(onsite)
+            seen[R] = t
+        else:
+            t = draw(R)
+            seen[R] = t
+            seen[mR] = t.conj().T
+    for R, t in seen.items():
+        for i in range(n):
+            for j in range(n):
+                if t[i, j] != 0:
+                    rows.append((R[0], R[1], R[2], i, j))
+                    vals.append(t[i, j])
+    return np.asarray(rows, np.int32), np.asarray(vals, np.complex128)
+
+
+def hubbard_2d(kx=64, ky=64, beta=50.0, nfreq=2048, ntau=None, U=2.0, t=1.0, tp=-0.25):
+    """Single-band Hubbard model on the square lattice, 2 spin-orbitals (Norbital of Atom = 2):
+    H(k) = -2t(cos kx + cos ky) - 4t' cos kx cos ky, Sigma(iw) = U^2/(4 iw), half filling (N = 1)."""
+    rows, vals = [], []
+    for s in range(2):
+        for R in [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0)]:
+            rows.append(R + (s, s))
+            vals.append(-t)
+        for R in [(1, 1, 0), (1, -1, 0), (-1, 1, 0), (-1, -1, 0)]:
+            rows.append(R + (s, s))
+            vals.append(-tp)
+    wn = PI * (2 * np.arange(nfreq) + 1) / beta
+    sigma = np.zeros((nfreq, 2, 2), np.complex128)
+    for s in range(2):
+        sigma[:, s, s] = U * U / (4 * 1j * wn)
+    return Workload("hubbard2d", 2, np.asarray(rows, np.int32), np.asarray(vals, np.complex128), (kx, ky, 1), beta,
+                    nfreq, ntau if ntau else 4 * nfreq, 1, 2, sigma, 1.0, {"U": U})
+
+
+def t2g_p(k=24, beta=40.0, nfreq=4096, ntau=None, seed=20250102, rmax=2):
+    """3 t2g (on-site 0 eV) + 9 O-p (on-site -3 eV) orbitals, 12 x 12 complex Hermitian H(k) with seeded
+    hoppings t(R) ~ N(0,1)/|R|^2 (complex) for |R_i| <= 2 (125 R vectors); Sigma is a diagonal 3 x 3 block
+    on the d orbitals with Im Sigma = -0.5/(w_n + 1)."""
+    n = 12
+    rng = np.random.default_rng(seed)
+    rvecs = [(a, b, c) for a in range(-rmax, rmax + 1) for b in range(-rmax, rmax + 1) for c in range(-rmax, rmax + 1)]
+
+    def draw(R):
+        r2 = max(1, R[0] ** 2 + R[1] ** 2 + R[2] ** 2)
+        return (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))) / np.sqrt(2) / r2
+
+    onsite = np.array([0.0] * 3 + [-3.0] * 9)
+    rows, vals = _hermitian_hoppings(n, rvecs, draw, onsite)
+    wn = PI * (2 * np.arange(nfreq) + 1) / beta
+    sigma = np.zeros((nfreq, 3, 3), np.complex128)
+    for d in range(3):
+        sigma[:, d, d] = -0.5j / (wn + 1.0)
+    return Workload("t2g_p", n, rows, vals, (k, k, k), beta, nfreq, ntau if ntau else 2 * nfreq, 1, 3, sigma, 8.0)
+
+
+def dp28(k=32, beta=40.0, nfreq=4096, ntau=8192, seed=20250105, rmax=4, U=4.0, J=0.7):
+    """d+p model of dimension 28 (5 d x 2 spins correlated + 18 ligand spin-orbitals), seeded t(R) over
+    |R_i| <= 4 (729 R vectors) with 1/|R|^2 decay; Sigma is a diagonal 10 x 10 block.  Kanamori U=4, J=0.7,
+    U' = U - 2J."""
+    n = 28
+    rng = np.random.default_rng(seed)
+    rvecs = [(a, b, c) for a in range(-rmax, rmax + 1) for b in range(-rmax, rmax + 1) for c in range(-rmax, rmax + 1)]
+
+    def draw(R):
+        r2 = max(1, R[0] ** 2 + R[1] ** 2 + R[2] ** 2)
+        return (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))) / np.sqrt(2) / (2 * r2)
+
+    onsite = np.array([0.0] * 10 + [-3.0] * 18)
+    rows, vals = _hermitian_hoppings(n, rvecs, draw, onsite)
+    wn = PI * (2 * np.arange(nfreq) + 1) / beta
+    sigma = np.zeros((nfreq, 10, 10), np.complex128)
+    for d in range(10):
+        sigma[:, d, d] = -0.5j / (wn + 1.0)
+    return Workload("dp28", n, rows, vals, (k, k, k), beta, nfreq, ntau, 1, 10, sigma, 20.0,
+                    {"U": U, "J": J, "Up": U - 2 * J})

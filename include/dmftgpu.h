@@ -1,0 +1,112 @@
+/*
+ * dmftgpu.h -- C ABI of libdmftgpu, the GB300 (sm_103a) implementation of DMFTpack's DMFT
+ * self-consistency hot path.  Plain pointers, sizes and an opaque context; no C++ or torch types.
+ *
+ * Data conventions (identical to the reference's in-memory Eigen data, so a shim can pass .data()):
+ *   - complex numbers are interleaved doubles (re, im)  == std::complex<double> / Eigen::MatrixXcd;
+ *   - matrices are column-major (element (i,j) at [i + j*rows]) == Eigen's default storage;
+ *   - a std::vector<Eigen::MatrixXcd> of equal-size matrices becomes one contiguous stack;
+ *   - index tables are row-major int32 ([row][col]).
+ * Array arguments are host pointers unless DMFTGPU_DEVICE_PTRS is set in `flags`, in which case every
+ * array argument (except the small int index tables, which are always host) is a device pointer and the
+ * call only enqueues work on the context's stream.  Scalar outputs (nele, mu_out, counters) are always
+ * host pointers.  Every entry point returns a DMFTGPU_* status; nothing aborts the process.
+ *
+ * Each entry point names the reference function (path within the DMFTpack repository, file:line) that it
+ * replaces.  The globals the reference reads (beta, N_freq, N_tau, knum, NBAND, HartrIndex, ...) become
+ * explicit arguments.
+ */
+#ifndef DMFTGPU_H
+#define DMFTGPU_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    DMFTGPU_OK = 0,
+    DMFTGPU_SINGULAR = 1,     /* a zero pivot (the reference would produce inf/nan silently) */
+    DMFTGPU_NONCONVERGED = 2, /* iteration cap reached (mu search, Jacobi, SCGF2 loop) */
+    DMFTGPU_NAN = 3,          /* NaN/Inf in a result the reference asserts finite */
+    DMFTGPU_BADARG = 4,
+    DMFTGPU_CAUSALITY = 5,    /* an eigenvalue of Im G or Im Delta has the wrong sign (reference: assert) */
+    DMFTGPU_HERMITICITY = 6,  /* G(tau) or Sigma(tau) not Hermitian (reference: assert) */
+    DMFTGPU_CUDA_ERROR = 7,
+    DMFTGPU_NOMEM = 8
+};
+
+#define DMFTGPU_DEVICE_PTRS 0x1 /* array arguments live in device memory */
+#define DMFTGPU_MIXED 0x2       /* FP32 factorisation + double-float (FP32-pair) refinement */
+#define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
+
+typedef struct dmftgpu_ctx dmftgpu_ctx;
+
+/* The reference's lattice globals: NBAND (n), knum (nk), N_freq (nfreq), beta, NumCluster (ncl),
+ * NumHartrOrbit_per_cluster (nh) and HartrIndex[ncl*nh] (src/tight_common.cpp:28-114, src/TB.h:7-35).
+ * hartr is a host pointer; NULL means HartrIndex[i] = i (the layout downfolding_ftn leaves behind,
+ * src/downfolding.cpp:69-79). */
+typedef struct {
+    int n;
+    int nk;
+    int nfreq;
+    double beta;
+    int ncl;
+    int nh;
+    const int *hartr;
+} dmftgpu_lattice;
+
+int dmftgpu_version(void);
+/* Context: one CUDA device, one stream, grow-only device workspaces. */
+int dmftgpu_create(dmftgpu_ctx **ctx, int device);
+int dmftgpu_destroy(dmftgpu_ctx *ctx);
+int dmftgpu_set_stream(dmftgpu_ctx *ctx, void *cuda_stream);
+void *dmftgpu_get_stream(dmftgpu_ctx *ctx);
+int dmftgpu_synchronize(dmftgpu_ctx *ctx);
+const char *dmftgpu_last_error(dmftgpu_ctx *ctx);
+/* Number of kernels this context has launched so far (for launch accounting in benchmarks). */
+long long dmftgpu_launch_count(dmftgpu_ctx *ctx);
+/* Kernel timing for benchmarks: while enabled, CUDA events on the context's stream bracket every launch of
+ * the hot kernels ("k_gloc", ...); dmftgpu_kernel_time sums their durations since the last enable.
+ * No counterpart in the reference (which prints clock() estimates, src/GreenFtn.cpp:306-307). */
+int dmftgpu_timing(dmftgpu_ctx *ctx, int enable);
+int dmftgpu_kernel_time(dmftgpu_ctx *ctx, const char *kernel, double *ms, int *count);
+
+/* k mesh of TightBinding (src/TB.cpp:196-207): kmesh[nk][3], nk = kx*ky*kz, host output. */
+int dmftgpu_kmesh(int kx, int ky, int kz, double *kmesh);
+
+/* H(k) = sum_R t(R) exp(-i k.a R) (Construct_Hk_Sk, src/ConstructModelHamiltonian.cpp:66-77) on the
+ * TightBinding k mesh.  rindex[nnz][5] = (Rx, Ry, Rz, i0, j0) and hr[nnz] complex are read_HR's H_Rindex
+ * and H_RMatrix (src/read_TB_parm.cpp:6-76).  Output hk[nk][n][n]. */
+int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double *hr, int kx, int ky, int kz,
+               double *hk, int flags);
+
+/* getAsymto_moments (src/FourierTransform.cpp:184-465): fw[nfreq][dim][dim] -> mom[4][dim][dim]
+ * (m0 + m1/iw + m2/(iw)^2 + m3/(iw)^3), green_asym selects the m0=0, m1=I variant (:337-457). */
+int dmftgpu_moments(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double *fw, int green_asym,
+                    double *mom, int flags);
+
+/* GreenFtn_w (src/GreenFtn.cpp:142-422, declared src/TB.h:59-61): hk[nk][n][n] = H_k_inModelSpace,
+ * sigma[nfreq][D][D] = SelfE_w (D = ncl*nh), mu.  Outputs gw[nfreq][D][D] (Gw), gwhf[nfreq][D][D]
+ * (GwHF, may be NULL) and nummat[D][D] (the global NumMatrix). */
+int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma,
+                       double mu, double *gw, double *gwhf, double *nummat, int flags);
+
+/* GiwToNele (src/GreenFtn.cpp:513-635) in trace form; dnele (may be NULL) = dN/dmu. */
+int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
+                 double *nele, double *dnele, int flags);
+
+/* GreenFtn_w_adjust_mu (src/GreenFtn.cpp:66-139, declared src/TB.h:58): the reference's bracket +
+ * bisection to |dmu| <= 1e-5, or with DMFTGPU_NEWTON a safeguarded Newton iteration to |N-n_target| <=
+ * 1e-11 using dN/dmu from the same pass.  *mu_out = mu; *n_eval = number of N(mu) passes. */
+int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma,
+                      double mu, double dmu, double n_target, double *mu_out, int *n_eval, int flags);
+
+/* Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119, declared src/TB.h:45-47):
+ * delta[nfreq][dim][dim] = (iw+mu) I - himp[orb] - sigma[orb] - (gw[orb])^-1, orb[dim] indexes D. */
+int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, double beta, int D,
+                      const double *sigma, const double *gw, const double *himp, double mu, double *delta,
+                      int flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,305 @@
+"""ctypes binding of the CPU FP64 oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
+reference arm, always as the checker or the timed CPU baseline, never by the product package.
+
+Parity status: unpinned against the reference program (see dmft_oracle.cpp's header).
+
+All arrays are numpy complex128 stacks of column-major matrices: a numpy array of shape (count, n, n)
+whose element [c, j, i] is matrix c's entry (i, j) -- i.e. the Fortran-ordered matrices stacked in C order.
+Use :func:`to_cm` / :func:`from_cm` to convert from/to ordinary (count, i, j) arrays.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Lattice(C.Structure):
+    _fields_ = [("n", C.c_int), ("nk", C.c_int), ("nfreq", C.c_int), ("beta", C.c_double),
+                ("ncl", C.c_int), ("nh", C.c_int), ("hartr", _ip)]
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+                os.path.join(_HERE, "dmft_oracle.cpp")):
+            build()
+        _lib = C.CDLL(_LIB_PATH)
+        _lib.orc_nele.argtypes = [C.POINTER(Lattice), _dp, _dp, C.c_double, _dp, _dp, C.c_int]
+        _lib.orc_greenftn_w.argtypes = [C.POINTER(Lattice), _dp, _dp, C.c_double, _dp, _dp, _dp, C.c_int]
+        _lib.orc_adjust_mu.argtypes = [C.POINTER(Lattice), _dp, _dp, C.c_double, C.c_double, C.c_double,
+                                       _dp, _ip, C.c_int]
+        _lib.orc_w2tau_single.argtypes = [C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_double, _dp]
+        _lib.orc_hyb_delta.argtypes = [C.c_int, _ip, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, C.c_double,
+                                       _dp]
+        _lib.orc_dyson.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp]
+        _lib.orc_ipt.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp,
+                                 C.c_int, _ip, _dp, _dp, _dp, _dp]
+        _lib.orc_moments.argtypes = [C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp]
+        _lib.orc_w2tau.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _ip]
+        _lib.orc_fourier.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp, _dp, _ip]
+        _lib.orc_tau2w.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp]
+        _lib.orc_sigma2_tau.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, _ip, _dp, _dp, _dp, _ip]
+        _lib.orc_fock.argtypes = [C.c_int, C.c_int, _ip, _dp, _dp, _dp]
+        _lib.orc_estimate_asymto.argtypes = [C.c_int, C.c_int, C.c_double, _dp, C.c_int]
+        _lib.orc_occ.argtypes = [C.c_int, C.c_int, C.c_double, _dp, _dp]
+        _lib.orc_gen_uijkl.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _ip, _dp]
+        _lib.orc_hk.argtypes = [C.c_int, C.c_int, _ip, _dp, C.c_int, _dp, _dp, C.c_int]
+        _lib.orc_kmesh.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
+        _lib.orc_kmesh.restype = None
+        _lib.orc_fock.restype = None
+        _lib.orc_estimate_asymto.restype = None
+        _lib.orc_hermitian_eig.argtypes = [C.c_int, _dp, _dp, _dp]
+        _lib.orc_inverse.argtypes = [C.c_int, _dp, _dp]
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def to_cm(a):
+    """(count, i, j) complex -> column-major stack (count, j, i), contiguous complex128."""
+    a = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2))
+
+
+def from_cm(a):
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2))
+
+
+def _lat(n, nk, nfreq, beta, ncl, nh, hartr):
+    h = np.ascontiguousarray(hartr, dtype=np.int32)
+    L = Lattice(n, nk, nfreq, beta, ncl, nh, _i(h))
+    L._keep = h
+    return L
+
+
+def _check(st, what, allowed=(0,)):
+    if st not in allowed:
+        raise RuntimeError(f"oracle {what} returned status {st}")
+    return st
+
+
+def kmesh(kx, ky, kz):
+    out = np.zeros((kx * ky * kz, 3))
+    lib().orc_kmesh(kx, ky, kz, _d(out))
+    return out
+
+
+def hk(n, rindex, hr, km, nthreads=1):
+    """rindex: (nnz,5) int (Rx,Ry,Rz,i0,j0); hr: (nnz,) complex; returns (nk, n, n) H(k) (i,j order)."""
+    rindex = np.ascontiguousarray(rindex, dtype=np.int32)
+    hr = np.ascontiguousarray(hr, dtype=np.complex128)
+    km = np.ascontiguousarray(km, dtype=np.float64)
+    out = np.zeros((km.shape[0], n, n), np.complex128)
+    _check(lib().orc_hk(n, rindex.shape[0], _i(rindex), _d(hr.view(np.float64)), km.shape[0], _d(km),
+                        _d(out.view(np.float64)), nthreads), "hk")
+    return from_cm(out)
+
+
+def hermitian_eig(a):
+    a = np.asarray(a, np.complex128)
+    n = a.shape[0]
+    w = np.zeros(n)
+    v = np.zeros((n, n), np.complex128)
+    am = to_cm(a)
+    st = lib().orc_hermitian_eig(n, _d(am.view(np.float64)), _d(w), _d(v.view(np.float64)))
+    return w, from_cm(v), st
+
+
+def inverse(a):
+    a = np.asarray(a, np.complex128)
+    n = a.shape[0]
+    out = np.zeros((n, n), np.complex128)
+    st = lib().orc_inverse(n, _d(to_cm(a).view(np.float64)), _d(out.view(np.float64)))
+    return from_cm(out), st
+
+
+def moments(fw, beta, green_asym=False):
+    fw = to_cm(fw)
+    nf, dim = fw.shape[0], fw.shape[1]
+    out = np.zeros((4, dim, dim), np.complex128)
+    _check(lib().orc_moments(dim, nf, beta, _d(fw.view(np.float64)), int(green_asym), _d(out.view(np.float64))),
+           "moments")
+    return from_cm(out)
+
+
+def greenftn_w(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1):
+    """GreenFtn_w: hk_ (nk,n,n), sigma (nfreq,D,D); returns (Gw, GwHF, NumMatrix)."""
+    hk_c = to_cm(hk_)
+    s_c = to_cm(sigma)
+    nk, n = hk_c.shape[0], hk_c.shape[1]
+    nf, D = s_c.shape[0], ncl * nh
+    if hartr is None:
+        hartr = np.arange(D)
+    L = _lat(n, nk, nf, beta, ncl, nh, hartr)
+    gw = np.zeros((nf, D, D), np.complex128)
+    gwhf = np.zeros_like(gw)
+    num = np.zeros((D, D), np.complex128)
+    _check(lib().orc_greenftn_w(C.byref(L), _d(hk_c.view(np.float64)), _d(s_c.view(np.float64)), mu,
+                                _d(gw.view(np.float64)), _d(gwhf.view(np.float64)), _d(num.view(np.float64)),
+                                nthreads), "greenftn_w")
+    return from_cm(gw), from_cm(gwhf), from_cm(num)
+
+
+def nele(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1, deriv=False):
+    hk_c = to_cm(hk_)
+    s_c = to_cm(sigma)
+    nk, n = hk_c.shape[0], hk_c.shape[1]
+    nf, D = s_c.shape[0], ncl * nh
+    if hartr is None:
+        hartr = np.arange(D)
+    L = _lat(n, nk, nf, beta, ncl, nh, hartr)
+    N = C.c_double()
+    dN = C.c_double()
+    _check(lib().orc_nele(C.byref(L), _d(hk_c.view(np.float64)), _d(s_c.view(np.float64)), mu, C.byref(N),
+                          C.byref(dN) if deriv else None, nthreads), "nele")
+    return (N.value, dN.value) if deriv else N.value
+
+
+def adjust_mu(hk_, sigma, mu, beta, ncl, nh, n_target, dmu=1.0, hartr=None, nthreads=1):
+    hk_c = to_cm(hk_)
+    s_c = to_cm(sigma)
+    nk, n = hk_c.shape[0], hk_c.shape[1]
+    nf, D = s_c.shape[0], ncl * nh
+    if hartr is None:
+        hartr = np.arange(D)
+    L = _lat(n, nk, nf, beta, ncl, nh, hartr)
+    out = C.c_double()
+    ne = C.c_int()
+    _check(lib().orc_adjust_mu(C.byref(L), _d(hk_c.view(np.float64)), _d(s_c.view(np.float64)), mu, dmu,
+                               n_target, C.byref(out), C.byref(ne), nthreads), "adjust_mu")
+    return out.value, ne.value
+
+
+def hyb_delta(orb, sigma, gw, himp, mu, beta):
+    orb = np.ascontiguousarray(orb, np.int32)
+    s_c, g_c, h_c = to_cm(sigma), to_cm(gw), to_cm(himp[None])[0]
+    nf, D = s_c.shape[0], s_c.shape[1]
+    dim = orb.shape[0]
+    out = np.zeros((nf, dim, dim), np.complex128)
+    _check(lib().orc_hyb_delta(dim, _i(orb), nf, beta, D, _d(s_c.view(np.float64)), _d(g_c.view(np.float64)),
+                               _d(h_c.view(np.float64)), mu, _d(out.view(np.float64))), "hyb_delta")
+    return from_cm(out)
+
+
+def w2tau(fw, mom, beta, ntau):
+    f_c, m_c = to_cm(fw), to_cm(mom)
+    nf, dim = f_c.shape[0], f_c.shape[1]
+    out = np.zeros((ntau + 1, dim, dim), np.complex128)
+    fix = C.c_int()
+    _check(lib().orc_w2tau(dim, nf, ntau, beta, _d(f_c.view(np.float64)), _d(m_c.view(np.float64)),
+                           _d(out.view(np.float64)), C.byref(fix)), "w2tau")
+    return from_cm(out), fix.value
+
+
+def fourier(fw, beta, ntau, green_asym=False, m1=None):
+    f_c = to_cm(fw)
+    nf, dim = f_c.shape[0], f_c.shape[1]
+    out = np.zeros((ntau + 1, dim, dim), np.complex128)
+    fix = C.c_int()
+    m1p = None
+    if m1 is not None:
+        m1c = to_cm(np.asarray(m1)[None])[0]
+        m1p = _d(m1c.view(np.float64))
+    _check(lib().orc_fourier(dim, nf, ntau, beta, _d(f_c.view(np.float64)), int(green_asym), m1p,
+                             _d(out.view(np.float64)), C.byref(fix)), "fourier")
+    return from_cm(out), fix.value
+
+
+def tau2w(ft, beta, nfreq):
+    t_c = to_cm(ft)
+    ntau, dim = t_c.shape[0] - 1, t_c.shape[1]
+    out = np.zeros((nfreq, dim, dim), np.complex128)
+    st = lib().orc_tau2w(dim, nfreq, ntau, beta, _d(t_c.view(np.float64)), _d(out.view(np.float64)))
+    return from_cm(out), st
+
+
+def sigma2_tau(gt, uidx, ut, beta):
+    g_c = to_cm(gt)
+    ntau, dim = g_c.shape[0] - 1, g_c.shape[1]
+    uidx = np.ascontiguousarray(uidx, np.int32)
+    ut = np.ascontiguousarray(ut, np.complex128)
+    out = np.zeros((ntau + 1, dim, dim), np.complex128)
+    fix = C.c_int()
+    st = lib().orc_sigma2_tau(dim, ntau, beta, uidx.shape[0], _i(uidx), _d(ut.view(np.float64)),
+                              _d(g_c.view(np.float64)), _d(out.view(np.float64)), C.byref(fix))
+    return from_cm(out), fix.value, st
+
+
+def fock(occ, uidx, ut):
+    dim = occ.shape[0]
+    uidx = np.ascontiguousarray(uidx, np.int32)
+    ut = np.ascontiguousarray(ut, np.complex128)
+    out = np.zeros((dim, dim), np.complex128)
+    lib().orc_fock(dim, uidx.shape[0], _i(uidx), _d(ut.view(np.float64)), _d(to_cm(occ[None])[0].view(np.float64)),
+                   _d(out.view(np.float64)))
+    return from_cm(out)
+
+
+def dyson(himp, delta, fk, s2, mu, beta):
+    d_c, s_c = to_cm(delta), to_cm(s2)
+    nf, dim = d_c.shape[0], d_c.shape[1]
+    out = np.zeros((nf, dim, dim), np.complex128)
+    st = lib().orc_dyson(dim, nf, beta, mu, _d(to_cm(himp[None])[0].view(np.float64)), _d(d_c.view(np.float64)),
+                         _d(to_cm(fk[None])[0].view(np.float64)), _d(s_c.view(np.float64)),
+                         _d(out.view(np.float64)))
+    return from_cm(out), st
+
+
+def estimate_asymto(f, nfreq, beta, order):
+    """f: (nfreq+3, dim, dim) stack; returns a copy with slot nfreq+order-1 written."""
+    f_c = to_cm(f)
+    dim = f_c.shape[1]
+    lib().orc_estimate_asymto(dim, nfreq, beta, _d(f_c.view(np.float64)), order)
+    return from_cm(f_c)
+
+
+def occ(gw, beta):
+    g_c = to_cm(gw)
+    nf, dim = g_c.shape[0], g_c.shape[1]
+    out = np.zeros((dim, dim), np.complex128)
+    _check(lib().orc_occ(dim, nf, beta, _d(g_c.view(np.float64)), _d(out.view(np.float64))), "occ")
+    return from_cm(out[None])[0]
+
+
+def gen_uijkl(nso, U, Up, J, density_density=False):
+    cap = nso ** 4
+    uidx = np.zeros((cap, 4), np.int32)
+    ut = np.zeros(cap, np.complex128)
+    cnt = lib().orc_gen_uijkl(nso, U, Up, J, int(density_density), cap, _i(uidx), _d(ut.view(np.float64)))
+    return uidx[:cnt].copy(), ut[:cnt].copy()
+
+
+def ipt(himp, delta, nummat, uidx, ut, U, mu, beta, ntau):
+    d_c = to_cm(delta)
+    nf, dim = d_c.shape[0], d_c.shape[1]
+    uidx = np.ascontiguousarray(uidx, np.int32)
+    ut = np.ascontiguousarray(ut, np.complex128)
+    se = np.zeros((nf + 5, dim, dim), np.complex128)
+    gi = np.zeros((nf + 5, dim, dim), np.complex128)
+    nm = np.zeros((dim, dim), np.complex128)
+    st = lib().orc_ipt(dim, nf, ntau, beta, U, mu, _d(to_cm(himp[None])[0].view(np.float64)),
+                       _d(d_c.view(np.float64)), _d(to_cm(nummat[None])[0].view(np.float64)), uidx.shape[0],
+                       _i(uidx), _d(ut.view(np.float64)), _d(se.view(np.float64)), _d(gi.view(np.float64)),
+                       _d(nm.view(np.float64)))
+    return from_cm(se), from_cm(gi), from_cm(nm[None])[0], st

@@ -1,0 +1,47 @@
+"""CPU tests of the C ABI boundary: the library builds, loads and exports every symbol the header declares.
+No compute call is made (there is no GPU here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    hdr = open(os.path.join(ROOT, "include", "dmftgpu.h")).read()
+    return sorted(set(re.findall(r"\b(dmftgpu_[a-z0-9_]+)\s*\(", hdr)))
+
+
+def test_header_declares_the_python_export_list():
+    from dmftpack_gb300 import lib
+    assert sorted(lib.EXPORTS) == _declared()
+
+
+def test_library_exports_every_declared_symbol():
+    from dmftpack_gb300 import build
+    path = build.build()
+    so = ctypes.CDLL(path)
+    missing = [s for s in _declared() if not hasattr(so, s)]
+    assert not missing, missing
+
+
+def test_kmesh_is_host_only_and_matches_oracle(orc):
+    from dmftpack_gb300 import lib
+    import numpy as np
+    assert np.array_equal(lib.kmesh(5, 4, 3), orc.kmesh(5, 4, 3))
+
+
+def test_hwr_round_trip_and_reference_example():
+    from dmftpack_gb300 import hwr, models
+    wl = models.t2g_p(k=2, nfreq=8)
+    text = hwr.write_hr([12], wl.rindex, wl.hr)
+    norb, r2, h2 = hwr.read_hr(text)
+    assert norb == [12]
+    assert (r2 == wl.rindex).all() and (h2 == wl.hr).all()
+    ex = "/root/reference/example/Hubb_model/primitive_Cell_ipt/Hk.HWR"
+    if os.path.exists(ex):  # only in the build container
+        norb, r, h = hwr.read_hr(ex, num_atoms=1)
+        assert norb == [2] and r.shape == (8, 5) and np.allclose(h, -0.25)

@@ -1,0 +1,139 @@
+"""GPU parity of the lattice stage (H(k), G_loc, N(mu), mu search, Delta, moments) against the FP64 oracle.
+Every call goes through the C ABI (libdmftgpu.so via ctypes)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from dmftpack_gb300 import lib, models
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10   # relative, plain FP64 path vs FP64 oracle
+
+
+def _setup(orc, wl):
+    km = orc.kmesh(*wl.kgrid)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, km)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, wl.ncl, wl.nh)
+    return H, lat
+
+
+def test_hk_matches_oracle(ctx, orc):
+    wl = models.t2g_p(k=5, nfreq=16)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    Hg = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid)
+    assert rel_err(Hg, H) < 1e-13
+    import torch
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=torch.device("cuda:0"))
+    assert rel_err(Hd.cpu().numpy(), H) < 1e-13
+
+
+@pytest.mark.parametrize("green", [False, True])
+def test_moments_match_oracle(ctx, orc, green):
+    wl = models.t2g_p(k=2, nfreq=200, beta=20.0)
+    F = wl.sigma if not green else np.linalg.inv(1j * wl.wn()[:, None, None] * np.eye(3)[None]
+                                                   - 0.3 * np.eye(3)[None] - wl.sigma)
+    m_o = orc.moments(F, wl.beta, green_asym=green)
+    m_g = ctx.getAsymto_moments(F, wl.beta, greenFtnAsym=green)
+    for i in range(4):
+        assert np.abs(m_g[i] - m_o[i]).max() <= 1e-9 * max(1.0, np.abs(m_o[i]).max()), i
+
+
+CASES = {
+    "t2g_p": lambda: models.t2g_p(k=4, nfreq=40, beta=12.0),
+    "hubbard": lambda: models.hubbard_2d(kx=8, ky=8, nfreq=48, beta=10.0),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_greenftn_w_matches_oracle(ctx, orc, case):
+    wl = CASES[case]()
+    H, lat = _setup(orc, wl)
+    mu = 0.25
+    gw, gwhf, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, wl.ncl, wl.nh)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, wl.sigma, mu)
+    assert rel_err(g_gw, gw) < TOL
+    assert rel_err(g_gwhf, gwhf) < TOL
+    assert rel_err(g_num, num) < TOL
+
+
+def test_greenftn_w_device_pointers(ctx, orc):
+    import torch
+    wl = CASES["t2g_p"]()
+    H, lat = _setup(orc, wl)
+    gw, gwhf, num = orc.greenftn_w(H, wl.sigma, 0.1, wl.beta, wl.ncl, wl.nh)
+    dev = torch.device("cuda:0")
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, torch.from_numpy(H).to(dev), torch.from_numpy(wl.sigma).to(dev), 0.1)
+    torch.cuda.synchronize()
+    assert rel_err(g_gw.cpu().numpy(), gw) < TOL
+    assert rel_err(g_num.cpu().numpy(), num) < TOL
+
+
+@pytest.mark.parametrize("n,D,hartr", [(5, 2, [3, 1]), (7, 3, None), (3, 1, [2])])
+def test_greenftn_w_padding_and_hartree_index(ctx, orc, n, D, hartr):
+    """Odd sizes (identity padding to the next instantiated N) and a HartrIndex that is not the identity."""
+    rng = np.random.default_rng(n * 10 + D)
+    nk, nf, beta = 27, 32, 8.0
+    A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (A + np.conj(np.swapaxes(A, 1, 2))) / 2
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = np.zeros((nf, D, D), complex)
+    for d in range(D):
+        S[:, d, d] = 0.2 - 0.7j / (wn + 0.5)
+    h = np.arange(D) if hartr is None else np.array(hartr)
+    lat = lib.Lattice(n, nk, nf, beta, 1, D, hartr=h)
+    gw, gwhf, num = orc.greenftn_w(H, S, -0.3, beta, 1, D, hartr=h)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, -0.3)
+    assert rel_err(g_gw, gw) < TOL and rel_err(g_gwhf, gwhf) < TOL and rel_err(g_num, num) < TOL
+
+
+def test_two_clusters(ctx, orc):
+    rng = np.random.default_rng(11)
+    n, nk, nf, beta, ncl, nh = 8, 16, 32, 6.0, 2, 2
+    A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (A + np.conj(np.swapaxes(A, 1, 2))) / 2
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = np.zeros((nf, 4, 4), complex)
+    for d in range(4):
+        S[:, d, d] = -0.3j / (wn + 1)
+    lat = lib.Lattice(n, nk, nf, beta, ncl, nh)
+    gw, gwhf, num = orc.greenftn_w(H, S, 0.0, beta, ncl, nh)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, 0.0)
+    assert rel_err(g_gw, gw) < TOL and rel_err(g_num, num) < TOL
+    N = orc.nele(H, S, 0.0, beta, ncl, nh)
+    assert abs(ctx.GiwToNele(lat, H, S, 0.0) - N) < 1e-11 * abs(N)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_nele_matches_oracle(ctx, orc, case):
+    wl = CASES[case]()
+    H, lat = _setup(orc, wl)
+    for mu in (-0.5, 0.25):
+        N, dN = orc.nele(H, wl.sigma, mu, wl.beta, wl.ncl, wl.nh, deriv=True)
+        gN, gdN = ctx.GiwToNele(lat, H, wl.sigma, mu, deriv=True)
+        assert abs(gN - N) < 1e-11 * max(1, abs(N))
+        assert abs(gdN - dN) < 1e-9 * abs(dN)
+
+
+def test_adjust_mu_bisection_matches_oracle_and_newton_converges(ctx, orc):
+    wl = CASES["t2g_p"]()
+    H, lat = _setup(orc, wl)
+    target = 7.3
+    mu_o, ne_o = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, wl.ncl, wl.nh, target)
+    mu_g, ne_g = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, target)
+    assert ne_g == ne_o and abs(mu_g - mu_o) <= 1e-12
+    mu_n, ne_n = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, target, newton=True)
+    assert abs(mu_n - mu_o) < 2e-5
+    assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, wl.ncl, wl.nh) - target) < 1e-9
+    assert ne_n < ne_o
+
+
+def test_hyb_delta_matches_oracle(ctx, orc):
+    wl = CASES["t2g_p"]()
+    H, lat = _setup(orc, wl)
+    gw, _, _ = orc.greenftn_w(H, wl.sigma, 0.2, wl.beta, wl.ncl, wl.nh)
+    himp = H.mean(0)[:3, :3]
+    orb = [0, 1, 2]
+    d_o = orc.hyb_delta(orb, wl.sigma, gw, himp, 0.2, wl.beta)
+    d_g = ctx.Construct_hyb_delta(orb, wl.sigma, gw, 0.2, wl.beta, himp)
+    assert rel_err(d_g, d_o) < TOL

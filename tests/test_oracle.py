@@ -1,0 +1,158 @@
+"""CPU tests of the FP64 oracle: primitives against numpy/LAPACK, the lattice functions against an
+independent literal numpy restatement (tests/ref_numpy.py), and analytic known answers."""
+import numpy as np
+import pytest
+
+import ref_numpy as R
+from conftest import rel_err
+from dmftpack_gb300 import models
+
+
+def _herm(rng, n):
+    a = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    return a + a.conj().T
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 12, 28])
+def test_inverse_matches_lapack(orc, n):
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    x, st = orc.inverse(a)
+    assert st == 0
+    assert rel_err(x, np.linalg.inv(a)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 10, 20])
+def test_hermitian_eig_matches_lapack(orc, n):
+    rng = np.random.default_rng(100 + n)
+    h = _herm(rng, n)
+    w, v, st = orc.hermitian_eig(h)
+    assert st == 0
+    assert np.allclose(w, np.linalg.eigvalsh(h), rtol=0, atol=1e-12 * np.abs(w).max())
+    assert np.allclose(v @ np.diag(w) @ v.conj().T, h, atol=1e-12 * np.abs(h).max())
+
+
+def test_hermitian_eig_reads_lower_triangle(orc):
+    rng = np.random.default_rng(7)
+    h = _herm(rng, 5)
+    junk = np.triu(rng.normal(size=(5, 5)) * 10, 1)  # garbage in the strict upper triangle
+    w, _, _ = orc.hermitian_eig(np.tril(h) + junk)
+    assert np.allclose(w, np.linalg.eigvalsh(h), atol=1e-12)
+
+
+def test_kmesh_and_hk(orc):
+    wl = models.t2g_p(k=3, nfreq=32)
+    km = orc.kmesh(*wl.kgrid)
+    assert np.abs(km - R.kmesh(*wl.kgrid)).max() == 0.0
+    H = orc.hk(wl.n, wl.rindex, wl.hr, km)
+    assert rel_err(H, R.hk(wl.n, wl.rindex, wl.hr, km)) < 1e-14
+    assert np.abs(H - np.conj(np.swapaxes(H, 1, 2))).max() < 1e-12  # t(-R) = t(R)^H
+
+
+def test_hubbard_dispersion(orc):
+    wl = models.hubbard_2d(kx=8, ky=8, nfreq=16)
+    km = orc.kmesh(*wl.kgrid)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, km)
+    kxs, kys = np.pi * km[:, 0], np.pi * km[:, 1]
+    e = -2 * (np.cos(kxs) + np.cos(kys)) + np.cos(kxs) * np.cos(kys)
+    assert np.abs(H[:, 0, 0] - e).max() < 1e-13 and np.abs(H[:, 0, 1]).max() == 0
+
+
+def _small_t2g(nfreq=48):
+    wl = models.t2g_p(k=3, nfreq=nfreq, beta=10.0)
+    return wl
+
+
+def test_greenftn_w_matches_numpy(orc):
+    wl = _small_t2g()
+    km = orc.kmesh(*wl.kgrid)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, km)
+    mom = orc.moments(wl.sigma, wl.beta)
+    gw, gwhf, num = orc.greenftn_w(H, wl.sigma, 0.3, wl.beta, wl.ncl, wl.nh)
+    gw2, gwhf2, num2 = R.greenftn_w(H, wl.sigma, mom, 0.3, wl.beta, np.arange(wl.D), wl.ncl, wl.nh)
+    assert rel_err(gw, gw2) < 1e-12
+    assert rel_err(gwhf, gwhf2) < 1e-12
+    assert rel_err(num, num2) < 1e-12
+
+
+def test_nele_trace_form_matches_eigenvalue_form(orc):
+    """GiwToNele literally (numpy eigvals of H+Sigma) == the oracle's trace identity."""
+    wl = _small_t2g()
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    mom = orc.moments(wl.sigma, wl.beta)
+    for mu in (-1.0, 0.3):
+        N = orc.nele(H, wl.sigma, mu, wl.beta, wl.ncl, wl.nh)
+        N2 = R.nele_eig(H, wl.sigma, mom, mu, wl.beta, np.arange(wl.D), wl.ncl, wl.nh)
+        assert abs(N - N2) < 1e-11 * max(1, abs(N2))
+
+
+def test_dnele_matches_finite_difference(orc):
+    wl = _small_t2g()
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    N, dN = orc.nele(H, wl.sigma, 0.1, wl.beta, wl.ncl, wl.nh, deriv=True)
+    h = 1e-6
+    fd = (orc.nele(H, wl.sigma, 0.1 + h, wl.beta, wl.ncl, wl.nh)
+          - orc.nele(H, wl.sigma, 0.1 - h, wl.beta, wl.ncl, wl.nh)) / (2 * h)
+    assert abs(dN - fd) < 1e-6 * abs(fd)
+
+
+def test_free_electron_known_answers(orc):
+    """Sigma = 0, diagonal H(k): G_loc = (1/Nk) sum_k 1/(iw+mu-e_k)."""
+    wl = models.hubbard_2d(kx=6, ky=6, nfreq=40, beta=8.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    sigma = np.zeros_like(wl.sigma)
+    gw, gwhf, num = orc.greenftn_w(H, sigma, 0.2, wl.beta, 1, 2)
+    iw = 1j * np.pi * (2 * np.arange(40) + 1) / wl.beta
+    ek = H[:, 0, 0].real
+    exact = (1.0 / (iw[:, None] + 0.2 - ek[None, :])).mean(1)
+    assert np.abs(gw[:, 0, 0] - exact).max() < 1e-13
+    assert np.abs(gwhf[:, 0, 0] - exact).max() < 1e-13
+    # with Sigma = 0, NumMatrix is the Fermi sum
+    f = 1 / (1 + np.exp(wl.beta * (ek - 0.2)))
+    assert abs(num[0, 0].real - f.mean()) < 1e-12
+
+
+def test_moments_recover_laurent_series(orc):
+    rng = np.random.default_rng(3)
+    beta, nf = 20.0, 400
+    iw = 1j * np.pi * (2 * np.arange(nf) + 1) / beta
+    m = [_herm(rng, 3) * 0.1 for _ in range(4)]
+    m[1] = m[1] @ m[1] + np.eye(3)   # positive definite m1
+    F = m[0][None] + m[1][None] / iw[:, None, None] + m[2][None] / iw[:, None, None] ** 2 + m[3][None] / iw[:, None, None] ** 3
+    mom = orc.moments(F, beta)
+    for i in range(4):
+        assert np.abs(mom[i] - m[i]).max() < 1e-7 * max(1, np.abs(m[i]).max())
+
+
+def test_fourier_round_trip_two_pole(orc):
+    """iw -> tau -> iw on a two-pole G: the tail-corrected transform and the exact piecewise-linear inverse."""
+    beta, nf, ntau = 10.0, 256, 2048
+    iw = 1j * np.pi * (2 * np.arange(nf) + 1) / beta
+    e = np.array([-0.7, 0.4])
+    G = np.zeros((nf, 2, 2), complex)
+    for i in range(2):
+        G[:, i, i] = 1.0 / (iw - e[i])
+    gt, fix = orc.fourier(G, beta, ntau, green_asym=True)
+    tau = np.arange(ntau + 1) * beta / ntau
+    exact = -np.exp(-np.outer(tau, e)) / (1 + np.exp(-beta * e))
+    assert np.abs(gt[:, 0, 0] - exact[:, 0]).max() < 1e-6
+    assert np.abs(gt[0, 0, 0] + gt[-1, 0, 0] + 1) < 1e-6   # G(0+) + G(beta-) = -1
+    gw, st = orc.tau2w(gt, beta, 64)
+    assert np.abs(gw[:, 1, 1] - G[:64, 1, 1]).max() < 1e-4
+
+
+def test_sigma2_vanishes_without_interaction(orc):
+    beta, ntau = 5.0, 64
+    tau = np.arange(ntau + 1) * beta / ntau
+    gt = np.zeros((ntau + 1, 2, 2), complex)
+    gt[:, 0, 0] = gt[:, 1, 1] = -0.5
+    uidx, ut = orc.gen_uijkl(2, 0.0, 0.0, 0.0, density_density=True)
+    st, fix, status = orc.sigma2_tau(gt, uidx, ut * 0, beta)
+    assert np.all(np.abs(st[1:-1]) <= 1e-10)
+
+
+def test_gen_uijkl_counts(orc):
+    uidx, ut = orc.gen_uijkl(10, 4.0, 2.6, 0.7)
+    assert len(ut) == 180
+    uidx, ut = orc.gen_uijkl(2, 2.0, 2.0, 0.0, density_density=True)
+    assert len(ut) == 4
