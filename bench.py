@@ -189,16 +189,17 @@ def run_ours(args, rank, world, local_rank):
     lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, wl.ncl, wl.nh)
     L = lat._c()
     mixed = args.precision == "mixed"
-    flags = lib.DEVICE_PTRS | (lib.MIXED if mixed else 0)
+    explicit = args.algo == "explicit"
+    flags = lib.DEVICE_PTRS | (lib.MIXED if mixed else 0) | (lib.EXPLICIT if explicit else 0)
     stream = torch.cuda.current_stream(dev)
     ctx.lib.dmftgpu_set_stream(ctx.h, lib._vp(stream.cuda_stream))
     import ctypes as C
     mu = 0.0
 
-    def step_dev():
+    def step_dev(fl=flags):
         st = ctx.lib.dmftgpu_greenftn_w(ctx.h, C.byref(L), lib._vp(Hcm.data_ptr()), lib._vp(Scm.data_ptr()), mu,
                                         lib._vp(gw.data_ptr()), lib._vp(g0.data_ptr()), lib._vp(nm.data_ptr()),
-                                        flags)
+                                        fl)
         ctx._check("dmftgpu_greenftn_w", st)
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.float32, device=dev)  # 1 GiB > L2
@@ -226,7 +227,8 @@ def run_ours(args, rank, world, local_rank):
         times.append(s.elapsed_time(e) / 1e3)
     torch.cuda.synchronize()
     launches = ctx.launches() - launches0
-    k_ms, k_cnt = ctx.kernel_time("k_gloc")
+    kname = "k_gloc" if explicit else "k_schur"
+    k_ms, k_cnt = ctx.kernel_time(kname)
     ctx.timing(False)
     clk = clocks.stop()
     t_total = sum(times)
@@ -247,7 +249,7 @@ def run_ours(args, rank, world, local_rank):
     def step_host():
         st = ctx.lib.dmftgpu_greenftn_w(ctx.h, C.byref(L), lib._vp(Hh.ctypes.data), lib._vp(Sh.ctypes.data), mu,
                                         lib._vp(gw_h.ctypes.data), lib._vp(g0_h.ctypes.data),
-                                        lib._vp(nm_h.ctypes.data), (lib.MIXED if mixed else 0))
+                                        lib._vp(nm_h.ctypes.data), flags & ~lib.DEVICE_PTRS)
         ctx._check("dmftgpu_greenftn_w", st)
 
     step_host()
@@ -260,10 +262,28 @@ def run_ours(args, rank, world, local_rank):
     h2d = Hh.nbytes + Sh.nbytes
     d2h = gw_h.nbytes + g0_h.nbytes + nm_h.nbytes
 
+    # side measurement: the other algorithm on the same inputs (one timed step)
+    variants = {}
+    if not args.no_variants:
+        other = flags ^ lib.EXPLICIT
+        step_dev(other)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        step_dev(other)
+        e.record(stream)
+        e.synchronize()
+        t_o = s.elapsed_time(e) / 1e3
+        variants["explicit" if not explicit else "schur"] = {"value": inv_per_step / t_o, "unit": UNIT,
+                                                              "ms_per_step": t_o * 1e3}
     if rank != 0:
         return
-    # roofline of the dominant kernel: 8 n^3 real flops per (k, iw) inversion (zgetrf+zgetri convention)
-    flops = 8.0 * wl.n ** 3 * inv_per_step
+    # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
+    #   explicit: 8 n^3 real flops per (k, iw) inversion (zgetrf+zgetri convention)
+    #   schur:    8 m D^2 (Schur sum over the m = n - D ligand poles) + 2 x 8 D^3 (G and G0 blocks)
+    m_ = wl.n - wl.D
+    per_unit = 8.0 * wl.n ** 3 if explicit else 8.0 * m_ * wl.D ** 2 + 16.0 * wl.D ** 3
+    flops = per_unit * inv_per_step
     k_avg = (k_ms / 1e3) / max(k_cnt, 1)
     achieved = flops / k_avg / 1e12
     peak = fp64_peak_tflops(torch, dev)
@@ -272,13 +292,14 @@ def run_ours(args, rank, world, local_rank):
            "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64-refine",
            "data": "synthetic (seeded t(R), Sigma = -0.5i/(w_n+1) on the 3 d orbitals)",
-           "config": dict(describe(wl), precision=args.precision, l2="1 GiB buffer written between timed steps",
-                          replicas=world),
+           "config": dict(describe(wl), precision=args.precision, algorithm=args.algo,
+                          l2="1 GiB buffer written between timed steps", replicas=world),
+           "variants": variants,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "fp64" if not mixed else "fp32", "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                        "kernel": "k_gloc", "kernel_ms_avg": k_avg * 1e3,
+                        "kernel": kname, "kernel_ms_avg": k_avg * 1e3, "flops_per_unit": per_unit,
                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 is not in "
                                        "MEASURED_PEAKS.json)",
                         "flops_per_launch": flops},
@@ -295,6 +316,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--algo", default="schur", choices=["schur", "explicit"],
+                    help="schur: exact correlated-block form (default); explicit: full n x n inversion per (k, iw)")
+    ap.add_argument("--no-variants", action="store_true", help="skip the side measurement of the other algorithm")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -33,13 +33,12 @@ __host__ __device__ __forceinline__ double2 cfms(double2 a, double2 b, double2 a
     return cmk(fma(-a.x, b.x, fma(a.y, b.y, acc.x)), fma(-a.x, b.y, fma(-a.y, b.x, acc.y)));
 }
 __host__ __device__ __forceinline__ double cabs2(double2 a) { return fma(a.x, a.x, a.y * a.y); }
+// 1/a = conj(a)/|a|^2 with a single division (FP64 division is a multi-instruction sequence on this GPU).
+// |a| stays within 1e-150..1e150 for every caller (shifted Matsubara frequencies, pivots of well-scaled
+// matrices); a zero pivot gives inf/nan, as the reference's division would.
 __host__ __device__ __forceinline__ double2 crcp(double2 a) {
-    // 1/a with one scaling step (a is never 0 when called on a pivot that passed the singularity check)
-    double s = fmax(fabs(a.x), fabs(a.y));
-    if (s == 0.0) return cmk(1.0 / a.x, 0.0);  // propagates inf/nan like the reference's division
-    double ar = a.x / s, ai = a.y / s;
-    double d = fma(ar, ar, ai * ai);
-    return cmk(ar / (d * s), -ai / (d * s));
+    const double r = 1.0 / fma(a.x, a.x, a.y * a.y);
+    return cmk(a.x * r, -a.y * r);
 }
 __host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) { return cmul(a, crcp(b)); }
 __host__ __device__ __forceinline__ double2 cexpi(double ang) {  // exp(i ang)

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "gloc.cuh"
+#include "schur.cuh"
 
 namespace {
 
@@ -89,9 +90,13 @@ __global__ void k_permute(int nk, int n, const int *__restrict__ perm, const dou
 // Sigma(iw_n) for n < 2 N_freq: data below N_freq, moment tail above (src/GreenFtn.cpp:224-240 and the
 // valenceHAMILTONIAN macro :13-31); `mask` keeps only within-cluster blocks (GiwToNele's placement).
 __global__ void k_sigall(int Nf, int D, int nh, int mask, double beta, const double2 *__restrict__ S,
-                         const double2 *__restrict__ mom, double2 *__restrict__ sig) {
+                         const double2 *__restrict__ mom, double2 *__restrict__ sig, double2 *__restrict__ m0eff) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long DD = (long long)D * D;
+    if (t < DD) {
+        int a = (int)(t % D), b = (int)(t / D);
+        m0eff[t] = (mask && (a / nh != b / nh)) ? cmk(0, 0) : mom[t];
+    }
     if (t >= 2LL * Nf * DD) return;
     int n = (int)(t / DD), e = (int)(t % DD);
     int a = e % D, b = e / D;
@@ -128,6 +133,28 @@ __global__ void k_static_eig(int nk, int n, int D, int nh, int mask, const doubl
         for (int a = 0; a < D; a++) UP[((size_t)k * n + l) * D + a] = DG_AT(U, n, a, l);
 }
 
+// per-k data of the Schur form: H_QQ = V diag(e) V^H, b_l = H_PQ V(:,l)   (Q = orbitals D..n-1)
+__global__ void k_schur_prep(int nk, int n, int D, const double2 *__restrict__ H, double2 *work, int *iwork,
+                             double *epsQ, double2 *B, int *status) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    const int m = n - D;
+    if (m == 0) return;
+    const size_t mm = (size_t)m * m;
+    double2 *A0 = work + (size_t)k * 3 * mm, *A = A0 + mm, *V = A + mm;
+    const double2 *Hk = H + (size_t)k * n * n;
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < m; i++) DG_AT(A0, m, i, j) = Hk[(D + i) + (size_t)(D + j) * n];
+    int st = thread_heig(m, A0, A, V, epsQ + (size_t)k * m, iwork + (size_t)k * m);
+    if (st) dg_flag(status, DG_NONCONV);
+    for (int l = 0; l < m; l++)
+        for (int a = 0; a < D; a++) {
+            double2 s = cmk(0, 0);
+            for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(V, m, j, l), s);
+            B[((size_t)k * m + l) * D + a] = s;
+        }
+}
+
 // Fermi parts: occ_k = P U f U^H P (with the +-100 cut-offs of src/GreenFtn.cpp:314-316) for NumMatrix,
 // and sum_l f, beta f (1-f) for N(mu) (src/GreenFtn.cpp:616-620, no cut-off there)
 __global__ void k_fermi(int nk, int n, int D, double beta, double mu, const double *__restrict__ eps,
@@ -157,40 +184,56 @@ __global__ void k_fermi(int nk, int n, int D, double beta, double mu, const doub
         }
 }
 
-// single CTA: G_loc, GwHF, NumMatrix (src/GreenFtn.cpp:298-354, 371-383)
-__global__ void k_gloc_finalize(int Nf, int nk, int D, int ncl, int nh, double beta, const double2 *blk,
-                                const double2 *blk0, const double2 *occ, double2 *gw, double2 *gwhf,
-                                double2 *nummat) {
-    const int DD = D * D;
-    for (long long t = threadIdx.x; t < (long long)Nf * DD; t += blockDim.x) {
-        int e = (int)(t % DD);
-        int a = e % D, b = e / D;
-        bool same = (a / nh == b / nh);
-        gw[t] = same ? cscale(blk[t], 1.0 / nk) : cmk(0, 0);
-        if (gwhf) gwhf[t] = same ? cscale(blk0[t], 1.0 / nk) : cmk(0, 0);
+// G_loc, GwHF (src/GreenFtn.cpp:298-305, 371-383): scale the per-frequency k sums, keep within-cluster blocks
+__global__ void k_gloc_scale(int Nf, int nk, int D, int nh, const double2 *blk, const double2 *blk0, double2 *gw,
+                             double2 *gwhf) {
+    const long long DD = (long long)D * D;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)Nf * DD) return;
+    int e = (int)(t % DD);
+    int a = e % D, b = e / D;
+    bool same = (a / nh == b / nh);
+    gw[t] = same ? cmk(blk[t].x / nk, blk[t].y / nk) : cmk(0, 0);
+    if (gwhf) gwhf[t] = same ? cmk(blk0[t].x / nk, blk0[t].y / nk) : cmk(0, 0);
+}
+
+// NumMatrix (src/GreenFtn.cpp:283-290, 322-354): one CTA per element, fixed-order tree reductions over the
+// 2 N_freq frequency sums and the N_k Fermi terms
+__global__ void k_nummat(int Nf, int nk, int D, double beta, const double2 *blk, const double2 *blk0,
+                         const double2 *occ, double2 *nummat) {
+    __shared__ double2 r0[256], r1[256], r2[256];
+    const int DD = D * D, e = blockIdx.x;
+    const int a = e % D, b = e / D, et = b + a * D;
+    double2 s = cmk(0, 0), s0 = cmk(0, 0), o = cmk(0, 0);
+    for (int f = threadIdx.x; f < 2 * Nf; f += blockDim.x) {
+        s = cadd(s, cadd(blk[(size_t)f * DD + e], cconj(blk[(size_t)f * DD + et])));
+        s0 = cadd(s0, cadd(blk0[(size_t)f * DD + e], cconj(blk0[(size_t)f * DD + et])));
     }
-    // the reference divides by knum_mpiGlobal with x /= knum; use the same division
-    for (int e = threadIdx.x; e < DD; e += blockDim.x) {
-        int a = e % D, b = e / D;
-        int et = b + a * D;
-        double2 s = cmk(0, 0), s0 = cmk(0, 0), o = cmk(0, 0);
-        for (int f = 0; f < 2 * Nf; f++) {
-            s = cadd(s, cadd(blk[(size_t)f * DD + e], cconj(blk[(size_t)f * DD + et])));
-            s0 = cadd(s0, cadd(blk0[(size_t)f * DD + e], cconj(blk0[(size_t)f * DD + et])));
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) o = cadd(o, occ[(size_t)k * DD + e]);
+    r0[threadIdx.x] = s;
+    r1[threadIdx.x] = s0;
+    r2[threadIdx.x] = o;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            r0[threadIdx.x] = cadd(r0[threadIdx.x], r0[threadIdx.x + h]);
+            r1[threadIdx.x] = cadd(r1[threadIdx.x], r1[threadIdx.x + h]);
+            r2[threadIdx.x] = cadd(r2[threadIdx.x], r2[threadIdx.x + h]);
         }
-        for (int k = 0; k < nk; k++) o = cadd(o, occ[(size_t)k * DD + e]);
-        s = cmk(s.x / beta, s.y / beta);
-        s0 = cmk(s0.x / beta, s0.y / beta);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        s = cmk(r0[0].x / beta, r0[0].y / beta);
+        s0 = cmk(r1[0].x / beta, r1[0].y / beta);
         if (a == b) {
             s.x += 0.5 * nk;
             s0.x += 0.5 * nk;
         }
-        s = cadd(s, o);
+        s = cadd(s, r2[0]);
         s = cmk(s.x / nk, s.y / nk);
         s0 = cmk(s0.x / nk, s0.y / nk);
         nummat[e] = csub(s, s0);
     }
-    (void)ncl;
 }
 
 // single CTA: N(mu) = (2/beta sum tr + sum f)/nk and dN/dmu
@@ -247,14 +290,33 @@ const Inst *pick_inst(int n) {
     return nullptr;
 }
 
+using dg::SchurArgs;
+using dg::SchurKernel;
+
+struct SInst {
+    int DP, W;
+    SchurKernel (*get)(int);
+};
+const SInst kSInst[] = {
+    {1, 1, dg::schur_kernel_1},    {2, 2, dg::schur_kernel_2},    {3, 4, dg::schur_kernel_3},
+    {4, 4, dg::schur_kernel_4},    {6, 8, dg::schur_kernel_6},    {8, 8, dg::schur_kernel_8},
+    {10, 16, dg::schur_kernel_10}, {12, 16, dg::schur_kernel_12}, {16, 16, dg::schur_kernel_16},
+    {20, 32, dg::schur_kernel_20},
+};
+const SInst *pick_schur(int D) {
+    for (const auto &x : kSInst)
+        if (x.DP >= D) return &x;
+    return nullptr;
+}
+
 // Everything a lattice pass needs, prepared once per (H, Sigma, placement) and reused by every
 // N(mu) evaluation of the mu search.
 struct Prepared {
     int n, nk, Nf, D, ncl, nh, mask;
     double beta;
     const double2 *H;  // permuted
-    double2 *sig, *mom, *UP;
-    double *eps;
+    double2 *sig, *mom, *UP, *m0, *B;
+    double *eps, *epsQ;
 };
 
 int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P) {
@@ -267,8 +329,8 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     P.mask = mask;
     P.beta = L->beta;
     const int n = P.n, nk = P.nk, D = P.D, Nf = P.Nf;
-    if (n < 1 || nk < 1 || Nf < 1 || D < 1 || D > n || !pick_inst(n))
-        return dg_fail(ctx, DMFTGPU_BADARG, "lattice: unsupported sizes (need 1 <= ncl*nh <= n <= 28)");
+    if (n < 1 || nk < 1 || Nf < 1 || D < 1 || D > n || !pick_schur(D))
+        return dg_fail(ctx, DMFTGPU_BADARG, "lattice: unsupported sizes (need 1 <= ncl*nh <= min(n, 20))");
     cudaStream_t s = ctx->stream;
     // orbital permutation: Hartree orbitals first, the rest in their order
     std::vector<int> perm;
@@ -300,22 +362,34 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     P.sig = (double2 *)dg_buf(ctx, "lat.sig", 2 * (size_t)Nf * D * D * sizeof(double2));
     P.eps = (double *)dg_buf(ctx, "lat.eps", (size_t)nk * n * sizeof(double));
     P.UP = (double2 *)dg_buf(ctx, "lat.UP", (size_t)nk * n * D * sizeof(double2));
+    P.m0 = (double2 *)dg_buf(ctx, "lat.m0", (size_t)D * D * sizeof(double2));
+    const int m = n - D;
+    P.epsQ = (double *)dg_buf(ctx, "lat.epsQ", (size_t)nk * (m + 1) * sizeof(double));
+    P.B = (double2 *)dg_buf(ctx, "lat.B", (size_t)nk * (m + 1) * D * sizeof(double2));
+    double2 *qwork = (double2 *)dg_buf(ctx, "lat.qwork", (size_t)nk * 3 * (m * m + 1) * sizeof(double2));
+    int *qiwork = (int *)dg_buf(ctx, "lat.qiwork", (size_t)nk * (m + 1) * sizeof(int));
+    if (!P.m0 || !P.epsQ || !P.B || !qwork || !qiwork) return DMFTGPU_NOMEM;
     double2 *work = (double2 *)dg_buf(ctx, "lat.eigwork", (size_t)nk * 3 * n * n * sizeof(double2));
     int *iwork = (int *)dg_buf(ctx, "lat.eigiwork", (size_t)nk * n * sizeof(int));
     if (!P.mom || !P.sig || !P.eps || !P.UP || !work || !iwork) return DMFTGPU_NOMEM;
     DG_TRY(dg_moments_dev(ctx, D, Nf, P.beta, dS, 0, P.mom));
     long long tot = 2LL * Nf * D * D;
-    k_sigall<<<dg_ceil_div(tot, 256), 256, 0, s>>>(Nf, D, P.nh, mask, P.beta, dS, P.mom, P.sig);
+    k_sigall<<<dg_ceil_div(tot, 256), 256, 0, s>>>(Nf, D, P.nh, mask, P.beta, dS, P.mom, P.sig, P.m0);
     DG_LAUNCH(ctx, "k_sigall");
     k_static_eig<<<dg_ceil_div(nk, 64), 64, 0, s>>>(nk, n, D, P.nh, mask, P.H, P.mom, work, iwork, P.eps, P.UP,
                                                     ctx->d_status);
     DG_LAUNCH(ctx, "k_static_eig");
+    if (m > 0) {
+        k_schur_prep<<<dg_ceil_div(nk, 64), 64, 0, s>>>(nk, n, D, P.H, qwork, qiwork, P.epsQ, P.B, ctx->d_status);
+        DG_LAUNCH(ctx, "k_schur_prep");
+    }
     return DMFTGPU_OK;
 }
 
 int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
              double *tr, double *dtr) {
     const Inst *in = pick_inst(P.n);
+    if (!in) return dg_fail(ctx, DMFTGPU_BADARG, "explicit inversion: n > 28 not instantiated");
     GlocKernel kern = in->get(mode);
     const int NG = 128 / in->W, DD = P.D * P.D;
     int fpb = 4;
@@ -354,14 +428,55 @@ int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid
     return DMFTGPU_OK;
 }
 
+
+// the Schur-form pass (default); mode: dg::S_BLOCK (GreenFtn_w) or S_TRACE[|S_DERIV] (N(mu))
+int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
+              double *tr, double *dtr) {
+    const SInst *in = pick_schur(P.D);
+    SchurKernel kern = in->get(mode);
+    const int m = P.n - P.D;
+    int fpb = 8;
+    while (fpb > 1 && dg::schur_smem(in->DP, in->W, mode, fpb, P.D, m) > 160 * 1024) fpb--;
+    size_t smem = dg::schur_smem(in->DP, in->W, mode, fpb, P.D, m);
+    if (smem > 220 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SchurArgs g;
+    g.H = P.H;
+    g.B = P.B;
+    g.epsQ = P.epsQ;
+    g.sig = P.sig;
+    g.m0 = P.m0;
+    g.n = P.n;
+    g.m = m;
+    g.nk = P.nk;
+    g.nf2 = 2 * P.Nf;
+    g.D = P.D;
+    g.fpb = fpb;
+    g.wgrid = wgrid;
+    g.beta = P.beta;
+    g.mu = mu;
+    g.blk = blk;
+    g.blk0 = blk0;
+    g.tr = tr;
+    g.dtr = dtr;
+    g.status = ctx->d_status;
+    {
+        DgTimer tm(ctx, "k_schur");
+        kern<<<dg_ceil_div(g.nf2, fpb), 128, smem, ctx->stream>>>(g);
+    }
+    DG_LAUNCH(ctx, "k_schur");
+    return DMFTGPU_OK;
+}
+
 // one N(mu) evaluation on a prepared lattice; result (N, dN/dmu) in device out[2]
-int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *dout) {
+int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *dout, bool explicit_inv) {
     const int nf2 = 2 * P.Nf;
     double *tr = (double *)dg_buf(ctx, "nele.tr", nf2 * sizeof(double));
     double *dtr = (double *)dg_buf(ctx, "nele.dtr", nf2 * sizeof(double));
     double *fs = (double *)dg_buf(ctx, "nele.fs", 2 * (size_t)P.nk * sizeof(double));
     if (!tr || !dtr || !fs) return DMFTGPU_NOMEM;
-    DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+    if (explicit_inv) DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+    else DG_TRY(run_schur(ctx, P, deriv ? (dg::S_TRACE | dg::S_DERIV) : dg::S_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
     k_fermi<<<dg_ceil_div(P.nk, 128), 128, 0, ctx->stream>>>(P.nk, P.n, P.D, P.beta, mu, P.eps, P.UP, nullptr, fs);
     DG_LAUNCH(ctx, "k_fermi");
     k_nele_finalize<<<1, 256, 0, ctx->stream>>>(nf2, P.nk, P.beta, tr, dtr, fs, deriv ? 1 : 0, dout);
@@ -369,10 +484,10 @@ int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double
     return DMFTGPU_OK;
 }
 
-int nele_host(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *N, double *dN) {
+int nele_host(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *N, double *dN, bool explicit_inv) {
     double *dout = (double *)dg_buf(ctx, "nele.out", 2 * sizeof(double));
     if (!dout) return DMFTGPU_NOMEM;
-    DG_TRY(nele_pass(ctx, P, mu, deriv, dout));
+    DG_TRY(nele_pass(ctx, P, mu, deriv, dout, explicit_inv));
     double h[2];
     DG_CUDA(cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     DG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -462,11 +577,14 @@ int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double 
     double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
     double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
     if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
-    DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    if (flags & DMFTGPU_EXPLICIT) DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
     k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
     DG_LAUNCH(ctx, "k_fermi");
-    k_gloc_finalize<<<1, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->ncl, L->nh, L->beta, blk, blk0, occ, dG, dG0, dN);
-    DG_LAUNCH(ctx, "k_gloc_finalize");
+    k_gloc_scale<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, ctx->stream>>>(Nf, L->nk, D, L->nh, blk, blk0, dG, dG0);
+    DG_LAUNCH(ctx, "k_gloc_scale");
+    k_nummat<<<(int)DD, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->beta, blk, blk0, occ, dN);
+    DG_LAUNCH(ctx, "k_nummat");
     DG_TRY(dg_out_done(ctx, gw, dG, Nf * DD * sizeof(double2), flags));
     if (gwhf) DG_TRY(dg_out_done(ctx, gwhf, dG0, Nf * DD * sizeof(double2), flags));
     DG_TRY(dg_out_done(ctx, nummat, dN, DD * sizeof(double2), flags));
@@ -488,7 +606,7 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, c
     DG_TRY(dg_status_reset(ctx));
     Prepared P;
     DG_TRY(prepare(ctx, L, dH, dS, 1, P));
-    DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele));
+    DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele, (flags & DMFTGPU_EXPLICIT) != 0));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     if (!std::isfinite(*nele)) return DMFTGPU_NAN;
@@ -511,7 +629,7 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
     int evals = 0;
     auto N = [&](double m, double *out, double *dout) {
         evals++;
-        return nele_host(ctx, P, m, dout != nullptr, out, dout);
+        return nele_host(ctx, P, m, dout != nullptr, out, dout, (flags & DMFTGPU_EXPLICIT) != 0);
     };
     const double goal = n_target;
     if (flags & DMFTGPU_NEWTON) {

@@ -32,49 +32,65 @@ struct MomArgs {
 
 __device__ __forceinline__ double zof(int wn, double beta) { return (2 * wn + 1) * DG_PI / beta; }
 
-// one thread per (element ab, column c): backward scan of the weighted series
+// weighted series term q of element ab at frequency wn (q < ncol: K^T G columns; q >= ncol: K^T K sums)
+__device__ __forceinline__ double2 mom_term(const MomArgs &g, int series, int wn) {
+    const int DD = g.D * g.D;
+    const double z = zof(wn, g.beta), z2 = z * z, z3 = z2 * z;
+    if (series < DD * g.ncol) {
+        const int ab = series / g.ncol, c = series % g.ncol;
+        const int a = ab / g.D, b = ab % g.D;  // momentstest index alp*Dim + bet
+        const double2 fab = g.fw[(size_t)wn * DD + a + b * g.D], fba = g.fw[(size_t)wn * DD + b + a * g.D];
+        const double2 re = cmk((fab.x + fba.x) / 2, (fab.y - fba.y) / 2);        // (F_ab + conj F_ba)/2
+        double2 im = cmk((fab.y + fba.y) * 0.5, -(fab.x - fba.x) * 0.5);        // (F_ab - conj F_ba)/(2i)
+        if (!g.green) {
+            if (c == 0) return re;
+            if (c == 1) return cscale(im, -1. / z);
+            if (c == 2) return cscale(re, -1. / z2);
+            return cscale(im, 1. / z3);
+        }
+        if (c == 0) return cscale(re, -1. / z2);
+        if (a == b) im.x += 1.0 / z;
+        return cscale(im, 1. / z3);
+    }
+    const int q = series - DD * g.ncol;
+    double v;
+    if (q == 0) v = 1.0;
+    else if (q == 1) v = -1. / z2;                  // K(.,0) K(.,2) on Re rows
+    else if (q == 2) v = (-1. / z2) * (-1. / z2);
+    else if (q == 3) v = (-1. / z) * (-1. / z);
+    else if (q == 4) v = (-1. / z) * (1. / z3);
+    else v = (1. / z3) * (1. / z3);
+    return cmk(v, 0.0);
+}
+
+// one warp per series: suffix sums S(w) = sum_{wn >= w} term(wn), lanes own contiguous chunks
 __global__ void k_mom_suffix(MomArgs g) {
     const int DD = g.D * g.D;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < DD * g.ncol) {
-        int ab = t / g.ncol, c = t % g.ncol;
-        int a = ab / g.D, b = ab % g.D;  // momentstest index alp*Dim + bet
-        double2 s = cmk(0, 0);
-        for (int wn = g.Nf - 1; wn >= 0; wn--) {
-            double z = zof(wn, g.beta);
-            double2 fab = g.fw[(size_t)wn * DD + a + b * g.D], fba = g.fw[(size_t)wn * DD + b + a * g.D];
-            double2 re = cmk((fab.x + fba.x) / 2, (fab.y - fba.y) / 2);        // (F_ab + conj F_ba)/2
-            double2 im = cmk((fab.y + fba.y) * 0.5, -(fab.x - fba.x) * 0.5);  // (F_ab - conj F_ba)/(2i)
-            double2 term;
-            if (!g.green) {
-                if (c == 0) term = re;
-                else if (c == 1) term = cscale(im, -1. / pow(z, 1));
-                else if (c == 2) term = cscale(re, -1. / pow(z, 2));
-                else term = cscale(im, 1. / pow(z, 3));
+    const int nseries = DD * g.ncol + 6;
+    const int series = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (series >= nseries) return;  // warp-uniform
+    const int chunk = (g.Nf + 31) / 32;
+    const int lo = min(g.Nf, lane * chunk), hi = min(g.Nf, lo + chunk);
+    double2 part = cmk(0, 0);
+    for (int wn = hi - 1; wn >= lo; wn--) part = cadd(part, mom_term(g, series, wn));
+    // carry = sum of the chunks of all higher lanes (inclusive suffix scan, then shift)
+    double2 incl = part;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        double2 v = shfl2(incl, min(31, lane + off), 32);
+        if (lane + off < 32) incl = cadd(incl, v);
+    }
+    double2 run = csub(incl, part);
+    for (int wn = hi - 1; wn >= lo; wn--) {
+        run = cadd(run, mom_term(g, series, wn));
+        if (wn < g.R) {
+            if (series < DD * g.ncol) {
+                const int ab = series / g.ncol, c = series % g.ncol;
+                g.S[((size_t)ab * g.ncol + c) * g.R + wn] = run;
             } else {
-                if (c == 0) term = cscale(re, -1. / pow(z, 2));
-                else {
-                    if (a == b) im.x += 1.0 / z;
-                    term = cscale(im, 1. / pow(z, 3));
-                }
+                g.KS[(size_t)(series - DD * g.ncol) * g.R + wn] = run.x;
             }
-            s = cadd(s, term);
-            if (wn < g.R) g.S[((size_t)ab * g.ncol + c) * g.R + wn] = s;
-        }
-    } else if (t < DD * g.ncol + 6) {
-        int q = t - DD * g.ncol;
-        double s = 0;
-        for (int wn = g.Nf - 1; wn >= 0; wn--) {
-            double z = zof(wn, g.beta);
-            double v;
-            if (q == 0) v = 1.0;
-            else if (q == 1) v = (-1. / pow(z, 2)) * (1.0);        // K(.,0) K(.,2) on Re rows
-            else if (q == 2) v = (-1. / pow(z, 2)) * (-1. / pow(z, 2));
-            else if (q == 3) v = (-1. / pow(z, 1)) * (-1. / pow(z, 1));
-            else if (q == 4) v = (-1. / pow(z, 1)) * (1. / pow(z, 3));
-            else v = (1. / pow(z, 3)) * (1. / pow(z, 3));
-            s += v;
-            if (wn < g.R) g.KS[(size_t)q * g.R + wn] = s;
         }
     }
 }
@@ -289,8 +305,8 @@ int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const doub
     g.mom = mom;
     g.status = ctx->d_status;
     cudaStream_t s = ctx->stream;
-    int nthr = (int)(DD * g.ncol + 6);
-    k_mom_suffix<<<dg_ceil_div(nthr, 64), 64, 0, s>>>(g);
+    int nseries = (int)(DD * g.ncol + 6);
+    k_mom_suffix<<<dg_ceil_div(nseries, 4), 128, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_suffix");
     k_mom_kinv<<<dg_ceil_div(g.R, 128), 128, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_kinv");

@@ -25,7 +25,7 @@ _vp = C.c_void_p
 OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
 STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
                 6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
-DEVICE_PTRS, MIXED, NEWTON = 0x1, 0x2, 0x4
+DEVICE_PTRS, MIXED, NEWTON, EXPLICIT = 0x1, 0x2, 0x4, 0x8
 
 # every symbol include/dmftgpu.h declares
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
@@ -235,8 +235,10 @@ class Context:
         self._check("dmftgpu_moments", st)
         return out.result()
 
-    def GreenFtn_w(self, lat, H_k, SelfE_w, mu, mixed=False, with_gwhf=True):
-        """GreenFtn_w: returns (Gw[nfreq,D,D], GwHF[nfreq,D,D] or None, NumMatrix[D,D])."""
+    def GreenFtn_w(self, lat, H_k, SelfE_w, mu, mixed=False, with_gwhf=True, explicit=False):
+        """GreenFtn_w: returns (Gw[nfreq,D,D], GwHF[nfreq,D,D] or None, NumMatrix[D,D]).
+        explicit=True inverts every (k, iw) matrix in full as the reference does; the default computes the
+        same correlated block through its exact Schur complement."""
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         D = lat.D
@@ -246,27 +248,28 @@ class Context:
         L = lat._c()
         st = self.lib.dmftgpu_greenftn_w(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(gw.ptr),
                                          _vp(g0.ptr) if g0 else None, _vp(nm.ptr),
-                                         self._flags(dev, MIXED if mixed else 0))
+                                         self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)))
         self._check("dmftgpu_greenftn_w", st)
         return gw.result(), (g0.result() if g0 else None), nm.result()
 
-    def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False):
+    def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False):
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         N, dN = C.c_double(), C.c_double()
         L = lat._c()
         st = self.lib.dmftgpu_nele(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), C.byref(N),
-                                   C.byref(dN) if deriv else None, self._flags(dev, MIXED if mixed else 0))
+                                   C.byref(dN) if deriv else None,
+                                   self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)))
         self._check("dmftgpu_nele", st)
         return (N.value, dN.value) if deriv else N.value
 
-    def GreenFtn_w_adjust_mu(self, lat, H_k, SelfE_w, mu, dmu, n_target, newton=False, mixed=False):
+    def GreenFtn_w_adjust_mu(self, lat, H_k, SelfE_w, mu, dmu, n_target, newton=False, mixed=False, explicit=False):
         """Returns (mu, number of N(mu) passes)."""
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         out, ne = C.c_double(), C.c_int()
         L = lat._c()
-        fl = (NEWTON if newton else 0) | (MIXED if mixed else 0)
+        fl = (NEWTON if newton else 0) | (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)
         st = self.lib.dmftgpu_adjust_mu(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), float(dmu),
                                         float(n_target), C.byref(out), C.byref(ne), self._flags(dev, fl))
         self._check("dmftgpu_adjust_mu", st)

@@ -37,6 +37,8 @@ enum {
 #define DMFTGPU_DEVICE_PTRS 0x1 /* array arguments live in device memory */
 #define DMFTGPU_MIXED 0x2       /* FP32 factorisation + double-float (FP32-pair) refinement */
 #define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
+#define DMFTGPU_EXPLICIT 0x8    /* lattice sums by explicit n x n inversion of every (k, iw) matrix, as the
+                                   reference does (default: the exact correlated-block Schur form) */
 
 typedef struct dmftgpu_ctx dmftgpu_ctx;
 

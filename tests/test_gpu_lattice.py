@@ -45,13 +45,14 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("explicit", [False, True])
 @pytest.mark.parametrize("case", list(CASES))
-def test_greenftn_w_matches_oracle(ctx, orc, case):
+def test_greenftn_w_matches_oracle(ctx, orc, case, explicit):
     wl = CASES[case]()
     H, lat = _setup(orc, wl)
     mu = 0.25
     gw, gwhf, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, wl.ncl, wl.nh)
-    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, wl.sigma, mu)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, wl.sigma, mu, explicit=explicit)
     assert rel_err(g_gw, gw) < TOL
     assert rel_err(g_gwhf, gwhf) < TOL
     assert rel_err(g_num, num) < TOL
@@ -69,8 +70,9 @@ def test_greenftn_w_device_pointers(ctx, orc):
     assert rel_err(g_num.cpu().numpy(), num) < TOL
 
 
-@pytest.mark.parametrize("n,D,hartr", [(5, 2, [3, 1]), (7, 3, None), (3, 1, [2])])
-def test_greenftn_w_padding_and_hartree_index(ctx, orc, n, D, hartr):
+@pytest.mark.parametrize("explicit", [False, True])
+@pytest.mark.parametrize("n,D,hartr", [(5, 2, [3, 1]), (7, 3, None), (3, 1, [2]), (16, 5, None), (9, 9, None)])
+def test_greenftn_w_padding_and_hartree_index(ctx, orc, n, D, hartr, explicit):
     """Odd sizes (identity padding to the next instantiated N) and a HartrIndex that is not the identity."""
     rng = np.random.default_rng(n * 10 + D)
     nk, nf, beta = 27, 32, 8.0
@@ -83,7 +85,26 @@ def test_greenftn_w_padding_and_hartree_index(ctx, orc, n, D, hartr):
     h = np.arange(D) if hartr is None else np.array(hartr)
     lat = lib.Lattice(n, nk, nf, beta, 1, D, hartr=h)
     gw, gwhf, num = orc.greenftn_w(H, S, -0.3, beta, 1, D, hartr=h)
-    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, -0.3)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, -0.3, explicit=explicit)
+    assert rel_err(g_gw, gw) < TOL and rel_err(g_gwhf, gwhf) < TOL and rel_err(g_num, num) < TOL
+    N, dN = orc.nele(H, S, -0.3, beta, 1, D, hartr=h, deriv=True)
+    gN, gdN = ctx.GiwToNele(lat, H, S, -0.3, deriv=True, explicit=explicit)
+    assert abs(gN - N) < 1e-11 * max(1, abs(N)) and abs(gdN - dN) < 1e-9 * abs(dN)
+
+
+def test_large_orbital_count_schur_only(ctx, orc):
+    """n = 56 with a 20-orbital correlated block (beyond the explicit kernels' register budget)."""
+    rng = np.random.default_rng(5)
+    n, D, nk, nf, beta = 56, 20, 8, 24, 5.0
+    A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (A + np.conj(np.swapaxes(A, 1, 2))) / 4
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = np.zeros((nf, D, D), complex)
+    for d in range(D):
+        S[:, d, d] = -0.4j / (wn + 0.7)
+    lat = lib.Lattice(n, nk, nf, beta, 1, D)
+    gw, gwhf, num = orc.greenftn_w(H, S, 0.1, beta, 1, D)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, 0.1)
     assert rel_err(g_gw, gw) < TOL and rel_err(g_gwhf, gwhf) < TOL and rel_err(g_num, num) < TOL
 
 
@@ -98,19 +119,21 @@ def test_two_clusters(ctx, orc):
         S[:, d, d] = -0.3j / (wn + 1)
     lat = lib.Lattice(n, nk, nf, beta, ncl, nh)
     gw, gwhf, num = orc.greenftn_w(H, S, 0.0, beta, ncl, nh)
-    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, 0.0)
-    assert rel_err(g_gw, gw) < TOL and rel_err(g_num, num) < TOL
-    N = orc.nele(H, S, 0.0, beta, ncl, nh)
-    assert abs(ctx.GiwToNele(lat, H, S, 0.0) - N) < 1e-11 * abs(N)
+    for explicit in (False, True):
+        g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, 0.0, explicit=explicit)
+        assert rel_err(g_gw, gw) < TOL and rel_err(g_num, num) < TOL
+        N = orc.nele(H, S, 0.0, beta, ncl, nh)
+        assert abs(ctx.GiwToNele(lat, H, S, 0.0, explicit=explicit) - N) < 1e-11 * abs(N)
 
 
+@pytest.mark.parametrize("explicit", [False, True])
 @pytest.mark.parametrize("case", list(CASES))
-def test_nele_matches_oracle(ctx, orc, case):
+def test_nele_matches_oracle(ctx, orc, case, explicit):
     wl = CASES[case]()
     H, lat = _setup(orc, wl)
     for mu in (-0.5, 0.25):
         N, dN = orc.nele(H, wl.sigma, mu, wl.beta, wl.ncl, wl.nh, deriv=True)
-        gN, gdN = ctx.GiwToNele(lat, H, wl.sigma, mu, deriv=True)
+        gN, gdN = ctx.GiwToNele(lat, H, wl.sigma, mu, deriv=True, explicit=explicit)
         assert abs(gN - N) < 1e-11 * max(1, abs(N))
         assert abs(gdN - dN) < 1e-9 * abs(dN)
 
@@ -122,6 +145,8 @@ def test_adjust_mu_bisection_matches_oracle_and_newton_converges(ctx, orc):
     mu_o, ne_o = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, wl.ncl, wl.nh, target)
     mu_g, ne_g = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, target)
     assert ne_g == ne_o and abs(mu_g - mu_o) <= 1e-12
+    mu_x, ne_x = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, target, explicit=True)
+    assert ne_x == ne_o and abs(mu_x - mu_o) <= 1e-12
     mu_n, ne_n = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, target, newton=True)
     assert abs(mu_n - mu_o) < 2e-5
     assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, wl.ncl, wl.nh) - target) < 1e-9
