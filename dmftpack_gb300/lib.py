@@ -31,7 +31,8 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT = 0x1, 0x2, 0x4, 0x8
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta"]
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_hyb_delta_noalloc"]
 
 
 class DmftGpuError(RuntimeError):
@@ -84,6 +85,8 @@ def load(require_built=True):
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
                                       _vp, C.c_int]
+    lib.dmftgpu_hyb_delta_noalloc.argtypes = [C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
+                                              C.c_double, _vp, _vp]
     _lib = lib
     return lib
 

@@ -108,6 +108,17 @@ int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, doub
                       const double *sigma, const double *gw, const double *himp, double mu, double *delta,
                       int flags);
 
+/* No counterpart in the reference.  Construct_hyb_delta for callers that cannot allocate device memory
+ * (a driver whose HBM belongs to a pool allocator, or one that must not stall the device with a
+ * non-stream-ordered cudaMalloc): no context, no allocation, every array argument a DEVICE pointer except
+ * orb (host, dim <= 32); work is enqueued on cuda_stream, which is then synchronised to return the status.
+ * Scratch is a static device array of 2^19 complex numbers (8 MiB) per GPU that loads the library, so
+ * nfreq*dim*dim must not exceed 524288 (else DMFTGPU_BADARG).  The first call on a device resolves the
+ * array's device address and should precede any stream capture; calls that overlap on the GPU share the
+ * array and race. */
+int dmftgpu_hyb_delta_noalloc(int dim, const int *orb, int nfreq, double beta, int D, const double *sigma,
+                              const double *gw, const double *himp, double mu, double *delta, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
