@@ -1,9 +1,20 @@
-// impurity.cu -- impurity-side kernels: the hybridisation function (Construct_hyb_delta).
-#include "linalg.cuh"
+// impurity.cu -- impurity-side kernels of the DMFT iteration:
+//   Construct_hyb_delta                  (src/Construct_hyb_delta.cpp:47-119)
+//   FourierTransform_ / _tau (iw -> tau)  (src/FourierTransform.cpp:16-178) with the two-pole tail
+//   FT_t_to_w (tau -> iw)                 (src/FourierTransform.cpp:521-561)
+//   getStimp (second-order Sigma(tau))    (src/SCGF2_fullLoop.cpp:603-690)
+//   getFockOperator, getGwimp, getoccMat, estimate_asymto  (src/SCGF2_fullLoop.cpp:539-597, 736-787)
+// Matsubara phases are taken from an exact table of exp(-i pi q / N_tau), q = (2n+1) j mod 2 N_tau, instead
+// of exp(-i w tau) of a rounded product (the reference's phase error grows to ~1e-12 at w tau ~ 1e4).
+#include <vector>
+
+#include "impurity.h"
 
 namespace {
 
-// one thread per Matsubara frequency (src/Construct_hyb_delta.cpp:98-113)
+// ---------------------------------------------------------------------------------------------------
+// Construct_hyb_delta: one thread per Matsubara frequency (src/Construct_hyb_delta.cpp:98-113)
+// ---------------------------------------------------------------------------------------------------
 __global__ void k_hyb_delta(int dim, int nfreq, int D, double beta, double mu, const int *__restrict__ orb,
                             const double2 *__restrict__ S, const double2 *__restrict__ G,
                             const double2 *__restrict__ Himp, double2 *work, int *iwork, double2 *delta,
@@ -29,11 +40,702 @@ __global__ void k_hyb_delta(int dim, int nfreq, int D, double beta, double mu, c
     }
 }
 
+// ---------------------------------------------------------------------------------------------------
+// FourierTransform_tau: the tau-independent tail data (src/FourierTransform.cpp:22-44, 66-83)
+// ---------------------------------------------------------------------------------------------------
+// T layout (complex slots, d x d each): V, H, H2, UH, UH2, then eH, eH2 (d doubles each, in a slot)
+struct TailPtrs {
+    double2 *V, *H, *H2, *UH, *UH2;
+    double *eH, *eH2;
+};
+__device__ TailPtrs tail_ptrs(double2 *T, int d) {
+    const size_t dd = (size_t)d * d;
+    TailPtrs p;
+    p.V = T;
+    p.H = T + dd;
+    p.H2 = T + 2 * dd;
+    p.UH = T + 3 * dd;
+    p.UH2 = T + 4 * dd;
+    p.eH = (double *)(T + 5 * dd);
+    p.eH2 = (double *)(T + 6 * dd);
+    return p;
+}
+
+// single thread: V = sqrt(m1); M2' = V^-H (2 m2) V^-1, M3' likewise; H = M2'/2 + sqrt(M3'/2 - M2'^2/4)
+// (or M2'/2 if that is not positive), H2 = M2' - H; eigen-decompositions of H and H2
+__global__ void k_tail_setup(int d, const double2 *mom, double2 *T, double2 *w, int *iw, int *status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const size_t dd = (size_t)d * d;
+    TailPtrs p = tail_ptrs(T, d);
+    const double2 *m1 = mom + dd, *m2 = mom + 2 * dd, *m3 = mom + 3 * dd;
+    double2 *A = w, *U = w + dd, *X = w + 2 * dd, *Vi = w + 3 * dd, *Vai = w + 4 * dd, *M2 = w + 5 * dd,
+            *M3 = w + 6 * dd, *t1 = w + 7 * dd;
+    double *ev = (double *)(w + 8 * dd);
+    int *ord = iw, *perm = iw + d;
+    if (thread_heig(d, m1, A, U, ev, ord)) dg_flag(status, DG_NONCONV);
+    if (ev[0] > 0) {
+        // V = U sqrt(ev) U^H
+        for (int j = 0; j < d; j++)
+            for (int i = 0; i < d; i++) {
+                double2 s = cmk(0, 0);
+                for (int l = 0; l < d; l++) s = cfma(cscale(DG_AT(U, d, i, l), sqrt(ev[l])), cconj(DG_AT(U, d, j, l)), s);
+                DG_AT(p.V, d, i, j) = s;
+            }
+        for (size_t q = 0; q < dd; q++) Vi[q] = p.V[q];
+        thread_gj_inverse(d, Vi, perm);
+        for (int j = 0; j < d; j++)
+            for (int i = 0; i < d; i++) DG_AT(Vai, d, i, j) = cconj(DG_AT(p.V, d, j, i));
+        thread_gj_inverse(d, Vai, perm);
+        for (size_t q = 0; q < dd; q++) X[q] = cscale(m2[q], 2.0);
+        thread_matmul(d, Vai, X, t1);
+        thread_matmul(d, t1, Vi, M2);
+        for (size_t q = 0; q < dd; q++) X[q] = cscale(m3[q], 2.0);
+        thread_matmul(d, Vai, X, t1);
+        thread_matmul(d, t1, Vi, M3);
+        thread_matmul(d, M2, M2, t1);
+        for (size_t q = 0; q < dd; q++) X[q] = csub(cscale(M3[q], 0.5), cscale(t1[q], 0.25));
+        thread_heig(d, X, A, U, ev, ord);
+        if (ev[0] > 0) {
+            for (int j = 0; j < d; j++)
+                for (int i = 0; i < d; i++) {
+                    double2 s = cmk(0, 0);
+                    for (int l = 0; l < d; l++) s = cfma(cscale(DG_AT(U, d, i, l), sqrt(ev[l])), cconj(DG_AT(U, d, j, l)), s);
+                    DG_AT(p.H, d, i, j) = cadd(cscale(DG_AT(M2, d, i, j), 0.5), s);
+                }
+        } else {
+            for (size_t q = 0; q < dd; q++) p.H[q] = cscale(M2[q], 0.5);
+        }
+        for (size_t q = 0; q < dd; q++) p.H2[q] = csub(M2[q], p.H[q]);
+    } else {
+        for (size_t q = 0; q < dd; q++) p.V[q] = p.H[q] = p.H2[q] = cmk(0, 0);
+    }
+    thread_heig(d, p.H, A, p.UH, p.eH, ord);
+    thread_heig(d, p.H2, A, p.UH2, p.eH2, ord);
+}
+
+// one thread per frequency: Dw_i = F_i - V^H [(iw - H)^-1 + (iw - H2)^-1] V / 2  (:55-60; the inverses
+// through the eigen-decompositions of H and H2)
+__global__ void k_ft_subtract(int d, int nfreq, double beta, const double2 *F, const double2 *T, double2 *Dw,
+                              double2 *work) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nfreq) return;
+    const size_t dd = (size_t)d * d;
+    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
+    const double w = (DG_PI / beta) + i * ((2 * DG_PI) / beta);
+    double2 *R = work + (size_t)i * 2 * dd, *Q = R + dd;
+    // R = UH diag(1/(iw - eH)) UH^H + UH2 diag(1/(iw - eH2)) UH2^H
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) {
+                s = cfma(cmul(DG_AT(p.UH, d, a, l), crcp(cmk(-p.eH[l], w))), cconj(DG_AT(p.UH, d, b, l)), s);
+                s = cfma(cmul(DG_AT(p.UH2, d, a, l), crcp(cmk(-p.eH2[l], w))), cconj(DG_AT(p.UH2, d, b, l)), s);
+            }
+            DG_AT(R, d, a, b) = s;
+        }
+    // Q = R V ; tail = V^H Q / 2
+    thread_matmul(d, R, p.V, Q);
+    const double2 *Fi = F + (size_t)i * dd;
+    double2 *Di = Dw + (size_t)i * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(Q, d, l, b), s);
+            DG_AT(Di, d, a, b) = csub(DG_AT(Fi, d, a, b), cscale(s, 0.5));
+        }
+}
+
+// exact phase table: ph[q] = exp(-i pi q / ntau), q in [0, 2 ntau)
+__global__ void k_phase_table(int ntau, double2 *ph) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * ntau) return;
+    double s, c;
+    sincospi(-(double)q / ntau, &s, &c);
+    ph[q] = cmk(c, s);
+}
+
+// S(tau_j) = sum_i Dw_i exp(-i w_i tau_j), w_i tau_j = pi (2i+1) j / ntau.  Block: TJ tau points x all
+// elements, frequencies staged through shared memory.
+constexpr int FT_TJ = 64;
+constexpr int FT_IB = 32;
+__global__ void __launch_bounds__(FT_TJ) k_ft_sum(int dd, int nfreq, int ntau, const double2 *__restrict__ Dw,
+                                                   const double2 *__restrict__ ph, double2 *__restrict__ S) {
+    extern __shared__ double2 sd[];  // [FT_IB][16]
+    const int j = blockIdx.x * FT_TJ + threadIdx.x;
+    const int e0 = blockIdx.y * 16, ne = min(16, dd - e0);
+    double2 acc[16];
+#pragma unroll
+    for (int e = 0; e < 16; e++) acc[e] = cmk(0, 0);
+    const long long twoN = 2LL * ntau;
+    const int jj = min(j, ntau);
+    const double2 r = ph[(2LL * jj) % twoN];  // exp(-i 2 pi j / ntau): frequency step
+    for (int i0 = 0; i0 < nfreq; i0 += FT_IB) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < FT_IB * ne; t += blockDim.x) {
+            int ii = t / ne, e = t % ne;
+            sd[ii * 16 + e] = (i0 + ii < nfreq) ? Dw[(size_t)(i0 + ii) * dd + e0 + e] : cmk(0, 0);
+        }
+        __syncthreads();
+        if (j <= ntau) {
+            const int imax = min(FT_IB, nfreq - i0);
+            double2 p = ph[((long long)(2 * i0 + 1) * jj) % twoN];  // exact at the chunk start
+            for (int ii = 0; ii < imax; ii++) {
+#pragma unroll
+                for (int e = 0; e < 16; e++)
+                    if (e < ne) acc[e] = cfma(sd[ii * 16 + e], p, acc[e]);
+                p = cmul(p, r);
+            }
+        }
+    }
+    if (j <= ntau)
+        for (int e = 0; e < ne; e++) S[(size_t)j * dd + e0 + e] = acc[e];
+}
+
+// one thread per tau: (S + S^H)/beta + V^H G0_H V/2 + V^H G0_H2 V/2, symmetrised (:62-90); minimum eigenvalue
+__global__ void k_ft_finish(int d, int ntau, double beta, const double2 *T, const double2 *S, double2 *out,
+                            double *mineig, double2 *work, int *iwork) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > ntau) return;
+    const size_t dd = (size_t)d * d;
+    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
+    const double tau = j * beta / ntau;
+    double2 *A = work + (size_t)j * 4 * dd, *B = A + dd, *C = B + dd, *E = C + dd;
+    const double2 *Sj = S + (size_t)j * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 v = cadd(DG_AT(Sj, d, a, b), cconj(DG_AT(Sj, d, b, a)));
+            DG_AT(A, d, a, b) = cscale(v, 1.0 / beta);
+        }
+    // G0 tail terms: M = UH diag(g) UH^H + UH2 diag(g2) UH2^H, g = -1/(exp(e tau) + exp(e (tau - beta)))
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) {
+                double g1 = -1.0 / (exp(p.eH[l] * tau) + exp(p.eH[l] * (tau - beta)));
+                double g2 = -1.0 / (exp(p.eH2[l] * tau) + exp(p.eH2[l] * (tau - beta)));
+                s = cfma(cscale(DG_AT(p.UH, d, a, l), g1), cconj(DG_AT(p.UH, d, b, l)), s);
+                s = cfma(cscale(DG_AT(p.UH2, d, a, l), g2), cconj(DG_AT(p.UH2, d, b, l)), s);
+            }
+            DG_AT(B, d, a, b) = s;
+        }
+    thread_matmul(d, B, p.V, C);  // C = M V
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(C, d, l, b), s);
+            DG_AT(A, d, a, b) = cadd(DG_AT(A, d, a, b), cscale(s, 0.5));
+        }
+    double2 *O = out + (size_t)j * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++)
+            DG_AT(O, d, a, b) = cscale(cadd(DG_AT(A, d, a, b), cconj(DG_AT(A, d, b, a))), 0.5);
+    thread_heig(d, O, B, nullptr, (double *)E, iwork + (size_t)j * d);
+    mineig[j] = ((double *)E)[0];
+}
+
+// one thread per tau: minimum eigenvalue of M[t] (lower triangle), used by the fix-up scan
+__global__ void k_mineig(int d, int nt1, const double2 *M, double *mineig, double2 *work, int *iwork) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt1) return;
+    const size_t dd = (size_t)d * d;
+    double2 *A = work + (size_t)t * 2 * dd;
+    thread_heig(d, M + (size_t)t * dd, A, nullptr, (double *)(A + dd), iwork + (size_t)t * d);
+    mineig[t] = ((double *)(A + dd))[0];
+}
+
+// single thread: the sequential positivity fix-up (src/FourierTransform.cpp:145-175,
+// src/SCGF2_fullLoop.cpp:657-688); eigenvalues of untouched points come precomputed in mineig
+__global__ void k_fixup_scan(int d, int ntau, double beta, double2 *M, const double *mineig, double2 *work,
+                             int *iwork, int *nfix) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const size_t dd = (size_t)d * d;
+    double2 *A = work, *X = work + dd;
+    double *ev = (double *)(work + 2 * dd);
+    int fixed = 0;
+    for (int t = 0; t < ntau + 1; t++) {
+        const double tau = t * beta / ntau;
+        const double mineigval = mineig[t];
+        double m11 = mineigval;
+        bool touched = false;
+        double2 *Mt = M + (size_t)t * dd;
+        if (mineigval >= 0 && (t != 0 && t != ntau)) {
+            touched = true;
+            for (int t1 = t + 1; t1 < ntau + 1; t1++) {
+                const double tau1 = t1 * beta / ntau, tprev = (t - 1) * beta / ntau;
+                const double2 *M1 = M + (size_t)t1 * dd, *M0 = M + (size_t)(t - 1) * dd;
+                for (size_t q = 0; q < dd; q++) {
+                    double2 v = csub(M1[q], M0[q]);
+                    v = cmk(v.x / (tau1 - tprev) * (tau - tprev) + M0[q].x, v.y / (tau1 - tprev) * (tau - tprev) + M0[q].y);
+                    Mt[q] = v;
+                }
+                thread_heig(d, Mt, A, nullptr, ev, iwork);
+                m11 = ev[0];
+                if (m11 < 0) break;
+            }
+        }
+        if (m11 >= 0) {
+            touched = true;
+            for (int b = 0; b < d; b++)
+                for (int a = 0; a < d; a++) DG_AT(Mt, d, a, b) = cmk(a == b ? -1e-10 : 0.0, 0.0);
+        }
+        if (touched) fixed++;
+    }
+    (void)X;
+    *nfix = fixed;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// FT_t_to_w (src/FourierTransform.cpp:521-561): one thread per (frequency, element)
+// ---------------------------------------------------------------------------------------------------
+__global__ void k_tau2w(int dd, int nfreq, int ntau, double beta, const double2 *__restrict__ Ft,
+                        const double2 *__restrict__ ph, double2 *__restrict__ W) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nfreq * dd) return;
+    const int n = (int)(t / dd), e = (int)(t % dd);
+    const double wn = (2 * n + 1) * DG_PI / beta, dt = beta / ntau;
+    const int twoN = 2 * ntau;
+    const double2 iwn = cmk(0.0, wn);
+    const double2 inv_iw = crcp(iwn);
+    const double inv_w2 = 1.0 / (wn * wn);
+    double2 acc = cmk(0, 0);
+    double2 e0 = cmk(1.0, 0.0);  // exp(i w tau_0), tau_0 = 0
+    const int step = (int)((2LL * n + 1) % twoN);
+    int q = 0;
+    for (int s = 0; s < ntau; s++) {
+        const double tau0 = s * dt, tau1 = (s + 1) * dt;
+        q += step;
+        if (q >= twoN) q -= twoN;
+        const double2 e1 = cconj(ph[q]);  // exp(+i pi (2n+1)(s+1)/ntau)
+        const double2 pI = csub(e1, e0);
+        const double2 pI2 = csub(cscale(e1, tau1), cscale(e0, tau0));
+        const double2 ca = cadd(cscale(pI, inv_w2), cmul(pI2, inv_iw));
+        const double2 cb = cmul(pI, inv_iw);
+        const double2 f0 = Ft[(size_t)s * dd + e], f1 = Ft[(size_t)(s + 1) * dd + e];
+        const double2 at = cscale(csub(f1, f0), 1.0 / (tau1 - tau0));
+        const double2 bt = cadd(cscale(at, -tau0), f0);
+        acc = cfma(at, ca, acc);
+        acc = cfma(bt, cb, acc);
+        e0 = e1;
+    }
+    W[t] = acc;
+}
+
+// causality check of FT_t_to_w (:551-558) and getGwimp (:564-568): max eig of (W - W^H)/(2i)
+__global__ void k_causal(int d, int nfreq, const double2 *W, double2 *work, int *iwork, int strict, int *status) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nfreq) return;
+    const size_t dd = (size_t)d * d;
+    double2 *A = work + (size_t)n * 3 * dd, *B = A + dd;
+    const double2 *Wn = W + (size_t)n * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 v = csub(DG_AT(Wn, d, a, b), cconj(DG_AT(Wn, d, b, a)));  // (W - W^H)
+            DG_AT(A, d, a, b) = cmk(v.y / 2, -v.x / 2);                        // / (2i)
+        }
+    double *ev = (double *)(B + dd);
+    thread_heig(d, A, B, nullptr, ev, iwork + (size_t)n * d);
+    const double mx = ev[d - 1];
+    if (strict ? !(mx < 0) : (mx > 0)) dg_flag(status, DG_CAUSAL);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// getStimp (src/SCGF2_fullLoop.cpp:603-653): one block per tau point, one thread per output (i, j);
+// the U list is pre-sorted on the host by its first index (idx1 role) and by its last index (idx2 role)
+// ---------------------------------------------------------------------------------------------------
+__global__ void k_sigma2(int d, int ntau, const int *__restrict__ byI, const int *__restrict__ byIoff,
+                         const int *__restrict__ byJ, const int *__restrict__ byJoff, const int *__restrict__ uidx,
+                         const double2 *__restrict__ ut, const double2 *__restrict__ G, double2 *__restrict__ S,
+                         int *status) {
+    extern __shared__ double2 sg[];  // G(tau) [dd], G(beta - tau) [dd]
+    const int t = blockIdx.x;
+    const size_t dd = (size_t)d * d;
+    for (int q = threadIdx.x; q < (int)dd; q += blockDim.x) {
+        sg[q] = G[(size_t)t * dd + q];
+        sg[dd + q] = G[(size_t)(ntau - t) * dd + q];
+    }
+    __syncthreads();
+    const double2 *Gt = sg, *Gm = sg + dd;
+    for (int o = threadIdx.x; o < (int)dd; o += blockDim.x) {
+        const int i = o % d, j = o / d;
+        double2 acc = cmk(0, 0);
+        for (int a1 = byIoff[i]; a1 < byIoff[i + 1]; a1++) {
+            const int x1 = byI[a1];
+            const int qq = uidx[4 * x1 + 1], m = uidx[4 * x1 + 2], k = uidx[4 * x1 + 3];
+            const double2 u1 = ut[x1];
+            for (int a2 = byJoff[j]; a2 < byJoff[j + 1]; a2++) {
+                const int x2 = byJ[a2];
+                const int l = uidx[4 * x2], n = uidx[4 * x2 + 1], p = uidx[4 * x2 + 2];
+                const double2 u12 = cmul(u1, ut[x2]);
+                const double2 mg = cneg(DG_AT(Gm, d, p, qq));
+                // (-1) G_kl G_mn (-G'_pq) U1 U2 + G_kn G_ml (-G'_pq) U1 U2
+                const double2 bub = cmul(cmul(DG_AT(Gt, d, k, l), DG_AT(Gt, d, m, n)), mg);
+                const double2 exc = cmul(cmul(DG_AT(Gt, d, k, n), DG_AT(Gt, d, m, l)), mg);
+                acc = cadd(acc, cmul(csub(exc, bub), u12));
+            }
+        }
+        S[(size_t)t * dd + o] = acc;
+    }
+    __syncthreads();
+    // Hermiticity asserts of the reference (:641-651): ||(G - G^H)/2i|| > 1e-10, ||(S - S^H)/2i|| > 1e-5
+    if (threadIdx.x == 0) {
+        double ng = 0, ns = 0;
+        for (int b = 0; b < d; b++)
+            for (int a = 0; a < d; a++) {
+                double2 vg = csub(DG_AT(Gt, d, a, b), cconj(DG_AT(Gt, d, b, a)));
+                double2 vs = csub(S[(size_t)t * dd + a + b * d], cconj(S[(size_t)t * dd + b + a * d]));
+                ng += cabs2(vg) / 4;
+                ns += cabs2(vs) / 4;
+            }
+        if (sqrt(ng) > 1e-10 || sqrt(ns) > 1e-5) dg_flag(status, DG_HERMIT);
+    }
+}
+
+// getFockOperator (:583-597), single thread
+__global__ void k_fock(int d, int nu, const int *uidx, const double2 *ut, const double2 *occ, double2 *fock) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int q = 0; q < d * d; q++) fock[q] = cmk(0, 0);
+    for (int x = 0; x < nu; x++) {
+        const int a = uidx[4 * x], b = uidx[4 * x + 1], c = uidx[4 * x + 2], dd_ = uidx[4 * x + 3];
+        DG_AT(fock, d, b, dd_) = cadd(DG_AT(fock, d, b, dd_), cmul(ut[x], DG_AT(occ, d, c, a)));
+        DG_AT(fock, d, b, c) = csub(DG_AT(fock, d, b, c), cmul(ut[x], DG_AT(occ, d, dd_, a)));
+    }
+}
+
+// getGwimp (:551-570): one thread per frequency
+__global__ void k_dyson(int d, int nfreq, double beta, double mu, const double2 *himp, const double2 *delta,
+                        const double2 *fock, const double2 *s2, double2 *gw, int *iwork, int *status) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nfreq) return;
+    const size_t dd = (size_t)d * d;
+    const double wn = (DG_PI * (2. * n + 1.)) / beta;
+    double2 *G = gw + (size_t)n * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 v = (a == b) ? cmk(mu, wn) : cmk(0, 0);
+            v = csub(v, DG_AT(himp, d, a, b));
+            v = csub(v, delta[(size_t)n * dd + a + b * d]);
+            v = csub(v, DG_AT(fock, d, a, b));
+            v = csub(v, s2[(size_t)n * dd + a + b * d]);
+            DG_AT(G, d, a, b) = v;
+        }
+    if (thread_gj_inverse(d, G, iwork + (size_t)n * d)) dg_flag(status, DG_SINGULAR);
+}
+
+// estimate_asymto (:736-787), single thread; F holds nfreq+3 matrices
+__global__ void k_estimate_asymto(int d, int Nf, double beta, double2 *F, int order) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const size_t dd = (size_t)d * d;
+    auto wn = [&](int i) { return (2 * (Nf - 3 + i) + 1) * DG_PI / beta; };
+    double w0, w1, w2;
+    int p = (order == 1) ? 2 : (order == 2 ? 4 : 6);
+    w0 = 1. / pow(wn(0), p);
+    w1 = 1. / pow(wn(1), p);
+    w2 = 1. / pow(wn(2), p);
+    const double wsum = w0 + w1 + w2;
+    double2 *dst = F + (size_t)(Nf + order - 1) * dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 acc = cmk(0, 0);
+            for (int w = 0; w < 3; w++) {
+                const double2 *T = F + (size_t)(Nf - 3 + w) * dd;
+                double2 tab = DG_AT(T, d, a, b), tba = DG_AT(T, d, b, a);
+                double2 v;
+                if (order == 1) {
+                    v = cscale(csub(cconj(tba), tab), 0.5);   // (t^H - t)/2
+                    v = cmul(v, crcp(cmk(0, wn(w))));          // / (i w)
+                } else if (order == 2) {
+                    v = cscale(cadd(tab, cconj(tba)), 0.5);
+                    v = cscale(v, -1.0 / pow(wn(w), 2));
+                } else {
+                    const double2 *F0 = F + (size_t)Nf * dd;
+                    const double2 ir = crcp(cmk(0, wn(w)));
+                    double2 xab = csub(tab, cmul(DG_AT(F0, d, a, b), ir));
+                    double2 xba = csub(tba, cmul(DG_AT(F0, d, b, a), ir));
+                    v = cscale(csub(cconj(xba), xab), 0.5);
+                    v = cscale(cmul(cmk(0, 1), v), 1.0 / pow(wn(w), 3));
+                }
+                acc = cadd(acc, v);
+            }
+            DG_AT(dst, d, a, b) = cscale(acc, 1.0 / wsum);
+        }
+}
+
+// Kajueter-Kotliar interpolation of the IPT self-energy on (0,0), (1,1) (:1033-1046)
+__global__ void k_ipt_kk(int nfreq, double a0, double a1, double b0, double b1, double c0, double c1, double2 *s2) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nfreq) return;
+    double2 *S = s2 + (size_t)n * 4;
+    double2 x0 = S[0], x1 = S[3];
+    S[0] = cdiv(cscale(x0, a0), csub(cmk(c0, 0), cscale(x0, b0)));
+    S[3] = cdiv(cscale(x1, a1), csub(cmk(c1, 0), cscale(x1, b1)));
+}
+
 }  // namespace
 
-extern "C" int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, double beta, int D,
-                                 const double *sigma, const double *gw, const double *himp, double mu, double *delta,
-                                 int flags) {
+// ===================================================================================================
+// device-level building blocks (all pointers device; enqueue only)
+// ===================================================================================================
+int dg_phase_table(dmftgpu_ctx *ctx, int ntau, double2 **ph) {
+    *ph = (double2 *)dg_buf(ctx, "imp.phase", 2 * (size_t)ntau * sizeof(double2));
+    if (!*ph) return DMFTGPU_NOMEM;
+    k_phase_table<<<dg_ceil_div(2 * ntau, 256), 256, 0, ctx->stream>>>(ntau, *ph);
+    DG_LAUNCH(ctx, "k_phase_table");
+    return DMFTGPU_OK;
+}
+
+int dg_fixup_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, double2 *M, const double *mineig) {
+    double2 *w = (double2 *)dg_buf(ctx, "imp.fixwork", 4 * (size_t)d * d * sizeof(double2) + 64);
+    int *iw = (int *)dg_buf(ctx, "imp.fixiwork", (size_t)(d + 1) * sizeof(int));
+    int *nfix = (int *)dg_buf(ctx, "imp.nfix", sizeof(int));
+    if (!w || !iw || !nfix) return DMFTGPU_NOMEM;
+    k_fixup_scan<<<1, 1, 0, ctx->stream>>>(d, ntau, beta, M, mineig, w, iw, nfix);
+    DG_LAUNCH(ctx, "k_fixup_scan");
+    return DMFTGPU_OK;
+}
+
+int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *fw, const double2 *mom,
+                 double2 *ft) {
+    const size_t dd = (size_t)d * d;
+    cudaStream_t s = ctx->stream;
+    double2 *T = (double2 *)dg_buf(ctx, "imp.tail", 8 * dd * sizeof(double2));
+    double2 *tw = (double2 *)dg_buf(ctx, "imp.tailwork", 10 * dd * sizeof(double2));
+    int *tiw = (int *)dg_buf(ctx, "imp.tailiwork", 2 * (size_t)d * sizeof(int));
+    double2 *Dw = (double2 *)dg_buf(ctx, "imp.Dw", (size_t)nfreq * dd * sizeof(double2));
+    double2 *sw = (double2 *)dg_buf(ctx, "imp.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
+    double2 *S = (double2 *)dg_buf(ctx, "imp.Ssum", (size_t)(ntau + 1) * dd * sizeof(double2));
+    double2 *fw2 = (double2 *)dg_buf(ctx, "imp.finwork", (size_t)(ntau + 1) * 4 * dd * sizeof(double2));
+    int *fiw = (int *)dg_buf(ctx, "imp.finiwork", (size_t)(ntau + 1) * d * sizeof(int));
+    double *mineig = (double *)dg_buf(ctx, "imp.mineig", (size_t)(ntau + 1) * sizeof(double));
+    if (!T || !tw || !tiw || !Dw || !sw || !S || !fw2 || !fiw || !mineig) return DMFTGPU_NOMEM;
+    double2 *ph;
+    DG_TRY(dg_phase_table(ctx, ntau, &ph));
+    k_tail_setup<<<1, 1, 0, s>>>(d, mom, T, tw, tiw, ctx->d_status);
+    DG_LAUNCH(ctx, "k_tail_setup");
+    k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, fw, T, Dw, sw);
+    DG_LAUNCH(ctx, "k_ft_subtract");
+    dim3 grid(dg_ceil_div(ntau + 1, FT_TJ), dg_ceil_div((int)dd, 16));
+    {
+        DgTimer tm(ctx, "k_ft_sum");
+        k_ft_sum<<<grid, FT_TJ, FT_IB * 16 * sizeof(double2), s>>>((int)dd, nfreq, ntau, Dw, ph, S);
+    }
+    DG_LAUNCH(ctx, "k_ft_sum");
+    k_ft_finish<<<dg_ceil_div(ntau + 1, 64), 64, 0, s>>>(d, ntau, beta, T, S, ft, mineig, fw2, fiw);
+    DG_LAUNCH(ctx, "k_ft_finish");
+    return dg_fixup_dev(ctx, d, ntau, beta, ft, mineig);
+}
+
+int dg_fourier_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *fw, int green,
+                   const double2 *m1, double2 *ft) {
+    const size_t dd = (size_t)d * d;
+    double2 *mom = (double2 *)dg_buf(ctx, "imp.mom", 4 * dd * sizeof(double2));
+    if (!mom) return DMFTGPU_NOMEM;
+    DG_TRY(dg_moments_dev(ctx, d, nfreq, beta, fw, green, mom));
+    if (m1) {
+        DG_CUDA(cudaMemsetAsync(mom, 0, dd * sizeof(double2), ctx->stream));
+        DG_CUDA(cudaMemcpyAsync(mom + dd, m1, dd * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    return dg_w2tau_dev(ctx, d, nfreq, ntau, beta, fw, mom, ft);
+}
+
+int dg_tau2w_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *ft, double2 *fw,
+                 bool check) {
+    const size_t dd = (size_t)d * d;
+    double2 *ph;
+    DG_TRY(dg_phase_table(ctx, ntau, &ph));
+    {
+        DgTimer tm(ctx, "k_tau2w");
+        k_tau2w<<<dg_ceil_div((long long)nfreq * dd, 128), 128, 0, ctx->stream>>>((int)dd, nfreq, ntau, beta, ft, ph, fw);
+    }
+    DG_LAUNCH(ctx, "k_tau2w");
+    if (check) {
+        double2 *w = (double2 *)dg_buf(ctx, "imp.causwork", (size_t)nfreq * 3 * dd * sizeof(double2));
+        int *iw = (int *)dg_buf(ctx, "imp.causiwork", (size_t)nfreq * d * sizeof(int));
+        if (!w || !iw) return DMFTGPU_NOMEM;
+        k_causal<<<dg_ceil_div(nfreq, 64), 64, 0, ctx->stream>>>(d, nfreq, fw, w, iw, 0, ctx->d_status);
+        DG_LAUNCH(ctx, "k_causal");
+    }
+    return DMFTGPU_OK;
+}
+
+int dg_sigma2_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, const DgUList &U, const double2 *gt, double2 *st) {
+    const size_t dd = (size_t)d * d;
+    {
+        DgTimer tm(ctx, "k_sigma2");
+        k_sigma2<<<ntau + 1, 128, 2 * dd * sizeof(double2), ctx->stream>>>(d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff,
+                                                                           U.uidx, U.ut, gt, st, ctx->d_status);
+    }
+    DG_LAUNCH(ctx, "k_sigma2");
+    double2 *w = (double2 *)dg_buf(ctx, "imp.s2work", (size_t)(ntau + 1) * 2 * dd * sizeof(double2) + 64);
+    int *iw = (int *)dg_buf(ctx, "imp.s2iwork", (size_t)(ntau + 1) * d * sizeof(int));
+    double *mineig = (double *)dg_buf(ctx, "imp.s2mineig", (size_t)(ntau + 1) * sizeof(double));
+    if (!w || !iw || !mineig) return DMFTGPU_NOMEM;
+    k_mineig<<<dg_ceil_div(ntau + 1, 64), 64, 0, ctx->stream>>>(d, ntau + 1, st, mineig, w, iw);
+    DG_LAUNCH(ctx, "k_mineig");
+    return dg_fixup_dev(ctx, d, ntau, beta, st, mineig);
+}
+
+int dg_fock_dev(dmftgpu_ctx *ctx, int d, const DgUList &U, const double2 *occ, double2 *fock) {
+    k_fock<<<1, 1, 0, ctx->stream>>>(d, U.nu, U.uidx, U.ut, occ, fock);
+    DG_LAUNCH(ctx, "k_fock");
+    return DMFTGPU_OK;
+}
+
+int dg_dyson_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, double mu, const double2 *himp,
+                 const double2 *delta, const double2 *fock, const double2 *s2, double2 *gw, bool check) {
+    const size_t dd = (size_t)d * d;
+    int *iw = (int *)dg_buf(ctx, "imp.dysiwork", (size_t)nfreq * d * sizeof(int));
+    if (!iw) return DMFTGPU_NOMEM;
+    k_dyson<<<dg_ceil_div(nfreq, 64), 64, 0, ctx->stream>>>(d, nfreq, beta, mu, himp, delta, fock, s2, gw, iw,
+                                                            ctx->d_status);
+    DG_LAUNCH(ctx, "k_dyson");
+    if (check) {
+        double2 *w = (double2 *)dg_buf(ctx, "imp.causwork", (size_t)nfreq * 3 * dd * sizeof(double2));
+        int *iw2 = (int *)dg_buf(ctx, "imp.causiwork", (size_t)nfreq * d * sizeof(int));
+        if (!w || !iw2) return DMFTGPU_NOMEM;
+        k_causal<<<dg_ceil_div(nfreq, 64), 64, 0, ctx->stream>>>(d, nfreq, gw, w, iw2, 1, ctx->d_status);
+        DG_LAUNCH(ctx, "k_causal");
+    }
+    return DMFTGPU_OK;
+}
+
+int dg_estimate_asymto_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, double2 *f, int order) {
+    k_estimate_asymto<<<1, 1, 0, ctx->stream>>>(d, nfreq, beta, f, order);
+    DG_LAUNCH(ctx, "k_estimate_asymto");
+    return DMFTGPU_OK;
+}
+
+// getoccMat: n = -G(tau = beta) with the m0 = 0, m1 = I green tail (src/SCGF2_fullLoop.cpp:539-549)
+__global__ void k_occ_finish(int d, int nfreq, double beta, const double2 *T, const double2 *Dw, double2 *occ,
+                             double2 *work) {
+    // single block: S(beta) = sum_i Dw_i exp(-i w_i beta) = -sum_i Dw_i (exp(-i pi (2i+1)) = -1)
+    __shared__ double2 red[256];
+    const size_t dd = (size_t)d * d;
+    for (size_t e = 0; e < dd; e++) {
+        double2 s = cmk(0, 0);
+        for (int i = threadIdx.x; i < nfreq; i += blockDim.x) s = csub(s, Dw[(size_t)i * dd + e]);
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if (threadIdx.x < h) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + h]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) work[e] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
+    const double tau = beta;
+    double2 *A = work + dd, *B = A + dd, *C = B + dd;
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++)
+            DG_AT(A, d, a, b) = cscale(cadd(work[a + b * d], cconj(work[b + a * d])), 1.0 / beta);
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) {
+                double g1 = -1.0 / (exp(p.eH[l] * tau) + exp(p.eH[l] * (tau - beta)));
+                double g2 = -1.0 / (exp(p.eH2[l] * tau) + exp(p.eH2[l] * (tau - beta)));
+                s = cfma(cscale(DG_AT(p.UH, d, a, l), g1), cconj(DG_AT(p.UH, d, b, l)), s);
+                s = cfma(cscale(DG_AT(p.UH2, d, a, l), g2), cconj(DG_AT(p.UH2, d, b, l)), s);
+            }
+            DG_AT(B, d, a, b) = s;
+        }
+    thread_matmul(d, B, p.V, C);
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) {
+            double2 s = cmk(0, 0);
+            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(C, d, l, b), s);
+            DG_AT(A, d, a, b) = cadd(DG_AT(A, d, a, b), cscale(s, 0.5));
+        }
+    for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++) DG_AT(occ, d, a, b) = cscale(cadd(DG_AT(A, d, a, b), cconj(DG_AT(A, d, b, a))), -0.5);
+}
+
+__global__ void k_set_identity_slot(int d, double2 *m1) {
+    int q = threadIdx.x + blockIdx.x * blockDim.x;
+    if (q < d * d) m1[q] = cmk((q % d) == (q / d) ? 1.0 : 0.0, 0.0);
+}
+
+int dg_occ_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *occ) {
+    const size_t dd = (size_t)d * d;
+    cudaStream_t s = ctx->stream;
+    double2 *mom = (double2 *)dg_buf(ctx, "occ.mom", 4 * dd * sizeof(double2));
+    double2 *T = (double2 *)dg_buf(ctx, "occ.tail", 8 * dd * sizeof(double2));
+    double2 *tw = (double2 *)dg_buf(ctx, "occ.tailwork", 10 * dd * sizeof(double2));
+    int *tiw = (int *)dg_buf(ctx, "occ.tailiwork", 2 * (size_t)d * sizeof(int));
+    double2 *Dw = (double2 *)dg_buf(ctx, "occ.Dw", (size_t)nfreq * dd * sizeof(double2));
+    double2 *sw = (double2 *)dg_buf(ctx, "occ.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
+    double2 *fw = (double2 *)dg_buf(ctx, "occ.finwork", 4 * dd * sizeof(double2));
+    if (!mom || !T || !tw || !tiw || !Dw || !sw || !fw) return DMFTGPU_NOMEM;
+    DG_TRY(dg_moments_dev(ctx, d, nfreq, beta, gw, 1, mom));
+    k_set_identity_slot<<<dg_ceil_div((int)dd, 64), 64, 0, s>>>(d, mom + dd);  // m1 = I (m0 = 0 already)
+    DG_LAUNCH(ctx, "k_set_identity_slot");
+    k_tail_setup<<<1, 1, 0, s>>>(d, mom, T, tw, tiw, ctx->d_status);
+    DG_LAUNCH(ctx, "k_tail_setup");
+    k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, gw, T, Dw, sw);
+    DG_LAUNCH(ctx, "k_ft_subtract");
+    k_occ_finish<<<1, 256, 0, s>>>(d, nfreq, beta, T, Dw, occ, fw);
+    DG_LAUNCH(ctx, "k_occ_finish");
+    return DMFTGPU_OK;
+}
+
+int dg_ipt_kk_dev(dmftgpu_ctx *ctx, int nfreq, const double *a, const double *b, const double *c, double2 *s2) {
+    k_ipt_kk<<<dg_ceil_div(nfreq, 128), 128, 0, ctx->stream>>>(nfreq, a[0], a[1], b[0], b[1], c[0], c[1], s2);
+    DG_LAUNCH(ctx, "k_ipt_kk");
+    return DMFTGPU_OK;
+}
+
+// U list on the device with the two index orders getStimp's output-stationary kernel needs
+int dg_ulist(dmftgpu_ctx *ctx, int d, int nu, const int *uidx, const double *ut, DgUList &U) {
+    for (int x = 0; x < nu; x++)
+        for (int q = 0; q < 4; q++)
+            if (uidx[4 * x + q] < 0 || uidx[4 * x + q] >= d) return dg_fail(ctx, DMFTGPU_BADARG, "U list index");
+    std::vector<int> byI, byJ, offI(d + 1, 0), offJ(d + 1, 0);
+    for (int i = 0; i < d; i++) {
+        offI[i] = (int)byI.size();
+        for (int x = 0; x < nu; x++)
+            if (uidx[4 * x] == i) byI.push_back(x);
+    }
+    offI[d] = (int)byI.size();
+    for (int j = 0; j < d; j++) {
+        offJ[j] = (int)byJ.size();
+        for (int x = 0; x < nu; x++)
+            if (uidx[4 * x + 3] == j) byJ.push_back(x);
+    }
+    offJ[d] = (int)byJ.size();
+    const size_t nb = (size_t)std::max(nu, 1);
+    int *dI = (int *)dg_buf(ctx, "u.byI", nb * sizeof(int)), *dJ = (int *)dg_buf(ctx, "u.byJ", nb * sizeof(int));
+    int *dOI = (int *)dg_buf(ctx, "u.offI", (d + 1) * sizeof(int)), *dOJ = (int *)dg_buf(ctx, "u.offJ", (d + 1) * sizeof(int));
+    int *dU = (int *)dg_buf(ctx, "u.idx", nb * 4 * sizeof(int));
+    double2 *dT = (double2 *)dg_buf(ctx, "u.val", nb * sizeof(double2));
+    if (!dI || !dJ || !dOI || !dOJ || !dU || !dT) return DMFTGPU_NOMEM;
+    cudaStream_t s = ctx->stream;
+    if (nu > 0) {
+        DG_CUDA(cudaMemcpyAsync(dI, byI.data(), nu * sizeof(int), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(dJ, byJ.data(), nu * sizeof(int), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(dU, uidx, (size_t)nu * 4 * sizeof(int), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(dT, ut, (size_t)nu * sizeof(double2), cudaMemcpyHostToDevice, s));
+    }
+    DG_CUDA(cudaMemcpyAsync(dOI, offI.data(), (d + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    DG_CUDA(cudaMemcpyAsync(dOJ, offJ.data(), (d + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    DG_CUDA(cudaStreamSynchronize(s));  // host vectors go out of scope
+    U.nu = nu;
+    U.byI = dI;
+    U.byJ = dJ;
+    U.byIoff = dOI;
+    U.byJoff = dOJ;
+    U.uidx = dU;
+    U.ut = dT;
+    return DMFTGPU_OK;
+}
+
+// ===================================================================================================
+// C ABI
+// ===================================================================================================
+extern "C" {
+
+int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, double beta, int D, const double *sigma,
+                      const double *gw, const double *himp, double mu, double *delta, int flags) {
     if (!ctx || dim < 1 || !orb || nfreq < 1 || D < 1 || !sigma || !gw || !himp || !delta || !(beta > 0))
         return DMFTGPU_BADARG;
     for (int i = 0; i < dim; i++)
@@ -63,3 +765,138 @@ extern "C" int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int 
     DG_TRY(dg_status_read(ctx, &code));
     return code;
 }
+
+int dmftgpu_fourier_w2tau(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, const double *fw,
+                          const double *mom, int green_asym, const double *m1, double *ft, int flags) {
+    if (!ctx || dim < 1 || nfreq < 1 || ntau < 1 || !fw || !ft || !(beta > 0)) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    const double2 *dF = (const double2 *)dg_in(ctx, fw, nfreq * dd * sizeof(double2), flags, "io.ft_fw", &st);
+    if (st) return st;
+    const double2 *dM = mom ? (const double2 *)dg_in(ctx, mom, 4 * dd * sizeof(double2), flags, "io.ft_mom", &st) : nullptr;
+    if (st) return st;
+    const double2 *dM1 = m1 ? (const double2 *)dg_in(ctx, m1, dd * sizeof(double2), flags, "io.ft_m1", &st) : nullptr;
+    if (st) return st;
+    double2 *dT = (double2 *)dg_out(ctx, ft, (ntau + 1) * dd * sizeof(double2), flags, "io.ft_out", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    if (dM) DG_TRY(dg_w2tau_dev(ctx, dim, nfreq, ntau, beta, dF, dM, dT));
+    else DG_TRY(dg_fourier_dev(ctx, dim, nfreq, ntau, beta, dF, green_asym, dM1, dT));
+    DG_TRY(dg_out_done(ctx, ft, dT, (ntau + 1) * dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_fourier_tau2w(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, const double *ft, double *fw,
+                          int flags) {
+    if (!ctx || dim < 1 || nfreq < 1 || ntau < 1 || !fw || !ft || !(beta > 0)) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    const double2 *dT = (const double2 *)dg_in(ctx, ft, (ntau + 1) * dd * sizeof(double2), flags, "io.t2w_ft", &st);
+    if (st) return st;
+    double2 *dW = (double2 *)dg_out(ctx, fw, nfreq * dd * sizeof(double2), flags, "io.t2w_fw", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_tau2w_dev(ctx, dim, nfreq, ntau, beta, dT, dW, true));
+    DG_TRY(dg_out_done(ctx, fw, dW, nfreq * dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_sigma2_tau(dmftgpu_ctx *ctx, int dim, int ntau, double beta, int nu, const int *uidx, const double *ut,
+                       const double *gt, double *st_out, int flags) {
+    if (!ctx || dim < 1 || ntau < 1 || nu < 0 || !gt || !st_out || (nu > 0 && (!uidx || !ut))) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    DgUList U;
+    DG_TRY(dg_ulist(ctx, dim, nu, uidx, ut, U));
+    const double2 *dG = (const double2 *)dg_in(ctx, gt, (ntau + 1) * dd * sizeof(double2), flags, "io.s2_gt", &st);
+    if (st) return st;
+    double2 *dS = (double2 *)dg_out(ctx, st_out, (ntau + 1) * dd * sizeof(double2), flags, "io.s2_st", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_sigma2_dev(ctx, dim, ntau, beta, U, dG, dS));
+    DG_TRY(dg_out_done(ctx, st_out, dS, (ntau + 1) * dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_fock(dmftgpu_ctx *ctx, int dim, int nu, const int *uidx, const double *ut, const double *occ, double *fock,
+                 int flags) {
+    if (!ctx || dim < 1 || nu < 0 || !occ || !fock) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    DgUList U;
+    DG_TRY(dg_ulist(ctx, dim, nu, uidx, ut, U));
+    const double2 *dO = (const double2 *)dg_in(ctx, occ, dd * sizeof(double2), flags, "io.fk_occ", &st);
+    if (st) return st;
+    double2 *dF = (double2 *)dg_out(ctx, fock, dd * sizeof(double2), flags, "io.fk_out", &st);
+    if (st) return st;
+    DG_TRY(dg_fock_dev(ctx, dim, U, dO, dF));
+    DG_TRY(dg_out_done(ctx, fock, dF, dd * sizeof(double2), flags));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return DMFTGPU_OK;
+}
+
+int dmftgpu_dyson(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, double mu, const double *himp, const double *delta,
+                  const double *fock, const double *sigma2, double *gw, int flags) {
+    if (!ctx || dim < 1 || nfreq < 1 || !himp || !delta || !fock || !sigma2 || !gw) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, himp, dd * sizeof(double2), flags, "io.dy_h", &st);
+    if (st) return st;
+    const double2 *dD = (const double2 *)dg_in(ctx, delta, nfreq * dd * sizeof(double2), flags, "io.dy_d", &st);
+    if (st) return st;
+    const double2 *dF = (const double2 *)dg_in(ctx, fock, dd * sizeof(double2), flags, "io.dy_f", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma2, nfreq * dd * sizeof(double2), flags, "io.dy_s", &st);
+    if (st) return st;
+    double2 *dG = (double2 *)dg_out(ctx, gw, nfreq * dd * sizeof(double2), flags, "io.dy_g", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_dyson_dev(ctx, dim, nfreq, beta, mu, dH, dD, dF, dS, dG, true));
+    DG_TRY(dg_out_done(ctx, gw, dG, nfreq * dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_occupation(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double *gw, double *occ, int flags) {
+    if (!ctx || dim < 1 || nfreq < 1 || !gw || !occ) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    const double2 *dG = (const double2 *)dg_in(ctx, gw, nfreq * dd * sizeof(double2), flags, "io.oc_g", &st);
+    if (st) return st;
+    double2 *dO = (double2 *)dg_out(ctx, occ, dd * sizeof(double2), flags, "io.oc_o", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_occ_dev(ctx, dim, nfreq, beta, dG, dO));
+    DG_TRY(dg_out_done(ctx, occ, dO, dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+int dmftgpu_estimate_asymto(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, double *f, int order, int flags) {
+    if (!ctx || dim < 1 || nfreq < 3 || !f || order < 1 || order > 3) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim, bytes = (nfreq + 3) * dd * sizeof(double2);
+    int st;
+    double2 *dF = (double2 *)dg_in(ctx, f, bytes, flags, "io.ea_f", &st);
+    if (st) return st;
+    DG_TRY(dg_estimate_asymto_dev(ctx, dim, nfreq, beta, dF, order));
+    DG_TRY(dg_out_done(ctx, f, dF, bytes, flags));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return DMFTGPU_OK;
+}
+
+}  // extern "C"

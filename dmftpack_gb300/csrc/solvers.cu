@@ -1,0 +1,128 @@
+// solvers.cu -- weak-coupling impurity solvers driven from the host, every step on the device:
+//   IPT (src/SCGF2_fullLoop.cpp:873-1065): Kajueter-Kotliar interpolated second-order self-energy on two
+//   spin-orbitals.  The host only sequences kernels and reads back the two 2x2 occupation matrices the
+//   interpolation coefficients need.
+#include <cstring>
+#include <vector>
+
+#include "impurity.h"
+
+namespace {
+
+__global__ void k_set_identity(int d, double2 *m) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < d * d) m[q] = cmk((q % d) == (q / d) ? 1.0 : 0.0, 0.0);
+}
+
+// writeResults (src/SCGF2_fullLoop.cpp:696-720): SE_out and Gwimp_out in ImgFreqFtn slot order
+__global__ void k_write_results(int d, int nfreq, const double2 *s2, const double2 *fock, const double2 *gimp,
+                                double2 *se_out, double2 *gimp_out) {
+    const size_t dd = (size_t)d * d;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)(nfreq + 5) * dd) return;
+    const int slot = (int)(t / dd), e = (int)(t % dd);
+    double2 se = cmk(0, 0), g = cmk(0, 0);
+    if (slot < nfreq) {
+        se = cadd(s2[t], fock[e]);
+        g = gimp[t];
+    } else if (slot == nfreq) {
+        se = fock[e];
+    } else {
+        const int k = slot - nfreq;  // 1..4
+        if (k == 1) se = s2[(size_t)nfreq * dd + e];
+        if (k == 2) se = s2[(size_t)(nfreq + 1) * dd + e];
+        g = gimp[(size_t)(nfreq + k - 1) * dd + e];
+    }
+    se_out[t] = se;
+    if (gimp_out) gimp_out[t] = g;
+}
+
+}  // namespace
+
+// IPT on device pointers.  delta: nfreq slots; se_out, gimp_out: nfreq+5 slots; occ_in/occ_out: d x d.
+int dg_ipt_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double U, double mu, const double2 *himp,
+               const double2 *delta, const double2 *occ_in, const DgUList &Ul, double2 *se_out, double2 *gimp_out,
+               double2 *occ_out) {
+    if (d != 2) return dg_fail(ctx, DMFTGPU_BADARG, "IPT is defined for two spin-orbitals");
+    const size_t dd = (size_t)d * d;
+    cudaStream_t s = ctx->stream;
+    double2 *fock = (double2 *)dg_buf(ctx, "ipt.fock", dd * sizeof(double2));
+    double2 *s2 = (double2 *)dg_buf(ctx, "ipt.s2", (size_t)(nfreq + 3) * dd * sizeof(double2));
+    double2 *gw0 = (double2 *)dg_buf(ctx, "ipt.gw0", (size_t)(nfreq + 4) * dd * sizeof(double2));
+    double2 *gimp = (double2 *)dg_buf(ctx, "ipt.gimp", (size_t)(nfreq + 4) * dd * sizeof(double2));
+    double2 *gt = (double2 *)dg_buf(ctx, "ipt.gt", (size_t)(ntau + 1) * dd * sizeof(double2));
+    double2 *st = (double2 *)dg_buf(ctx, "ipt.st", (size_t)(ntau + 1) * dd * sizeof(double2));
+    if (!fock || !s2 || !gw0 || !gimp || !gt || !st) return DMFTGPU_NOMEM;
+    DG_CUDA(cudaMemsetAsync(s2, 0, (size_t)(nfreq + 3) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemsetAsync(gw0, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemsetAsync(gimp, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
+    // the interpolation coefficients use the input occupation (src/SCGF2_fullLoop.cpp:932-945, 1036-1041)
+    double2 occ_h[4];
+    DG_CUDA(cudaMemcpyAsync(occ_h, occ_in, dd * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    // HF: Fock from the input occupation, Dyson with S2 = 0 at muHF = mu
+    DG_TRY(dg_fock_dev(ctx, d, Ul, occ_in, fock));
+    DG_TRY(dg_dyson_dev(ctx, d, nfreq, beta, mu, himp, delta, fock, s2, gw0, true));
+    k_set_identity<<<1, 32, 0, s>>>(d, gw0 + (size_t)nfreq * dd);
+    DG_LAUNCH(ctx, "k_set_identity");
+    // FourierTransform(Gw0, Gt0, Gw0[N_freq]): non-Green fit, then m0 = 0, m1 = Gw0[N_freq] = I
+    DG_TRY(dg_fourier_dev(ctx, d, nfreq, ntau, beta, gw0, 0, gw0 + (size_t)nfreq * dd, gt));
+    DG_TRY(dg_sigma2_dev(ctx, d, ntau, beta, Ul, gt, st));
+    DG_TRY(dg_tau2w_dev(ctx, d, nfreq, ntau, beta, st, s2, true));
+    DG_CUDA(cudaStreamSynchronize(s));
+    const double n11 = occ_h[3].x, n00 = occ_h[0].x;  // occMat(1,1), occMat(0,0) (real parts)
+    const double muHF = mu;
+    double a[2], b[2], c[2];
+    a[0] = U * U * n11 * (1.0 - n11);
+    a[1] = U * U * n00 * (1.0 - n00);
+    b[0] = (muHF - mu + U * (1.0 - 2.0 * n11));
+    b[1] = (muHF - mu + U * (1.0 - 2.0 * n00));
+    c[0] = U * U * n11 * (1.0 - n11);  // occMatHF == occMat on entry
+    c[1] = U * U * n00 * (1.0 - n00);
+    DG_TRY(dg_ipt_kk_dev(ctx, nfreq, a, b, c, s2));
+    DG_TRY(dg_dyson_dev(ctx, d, nfreq, beta, mu, himp, delta, fock, s2, gimp, true));
+    k_set_identity<<<1, 32, 0, s>>>(d, gimp + (size_t)nfreq * dd);
+    DG_LAUNCH(ctx, "k_set_identity");
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, gimp, 2));
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, gimp, 3));
+    DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, gimp, occ_out));
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 1));
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 2));
+    k_write_results<<<dg_ceil_div((long long)(nfreq + 5) * dd, 128), 128, 0, s>>>(d, nfreq, s2, fock, gimp, se_out,
+                                                                                  gimp_out);
+    DG_LAUNCH(ctx, "k_write_results");
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double U, double mu,
+                           const double *himp, const double *delta, const double *nummat_in, int nu, const int *uidx,
+                           const double *ut, double *se_out, double *gimp_out, double *nummat_out, int flags) {
+    if (!ctx || dim != 2 || nfreq < 8 || ntau < 2 || !himp || !delta || !nummat_in || !se_out || !nummat_out ||
+        nu < 0 || !(beta > 0))
+        return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    DgUList Ul;
+    DG_TRY(dg_ulist(ctx, dim, nu, uidx, ut, Ul));
+    const double2 *dH = (const double2 *)dg_in(ctx, himp, dd * sizeof(double2), flags, "io.ipt_h", &st);
+    if (st) return st;
+    const double2 *dD = (const double2 *)dg_in(ctx, delta, nfreq * dd * sizeof(double2), flags, "io.ipt_d", &st);
+    if (st) return st;
+    const double2 *dN = (const double2 *)dg_in(ctx, nummat_in, dd * sizeof(double2), flags, "io.ipt_n", &st);
+    if (st) return st;
+    double2 *dSE = (double2 *)dg_out(ctx, se_out, (nfreq + 5) * dd * sizeof(double2), flags, "io.ipt_se", &st);
+    if (st) return st;
+    double2 *dGI = gimp_out ? (double2 *)dg_out(ctx, gimp_out, (nfreq + 5) * dd * sizeof(double2), flags, "io.ipt_gi", &st)
+                            : nullptr;
+    if (st) return st;
+    double2 *dNO = (double2 *)dg_out(ctx, nummat_out, dd * sizeof(double2), flags, "io.ipt_no", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_ipt_dev(ctx, dim, nfreq, ntau, beta, U, mu, dH, dD, dN, Ul, dSE, dGI, dNO));
+    DG_TRY(dg_out_done(ctx, se_out, dSE, (nfreq + 5) * dd * sizeof(double2), flags));
+    if (gimp_out) DG_TRY(dg_out_done(ctx, gimp_out, dGI, (nfreq + 5) * dd * sizeof(double2), flags));
+    DG_TRY(dg_out_done(ctx, nummat_out, dNO, dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}

@@ -32,7 +32,8 @@ EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
            "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
-           "dmftgpu_hyb_delta_noalloc"]
+           "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
+           "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_hyb_delta_noalloc"]
 
 
 class DmftGpuError(RuntimeError):
@@ -85,6 +86,16 @@ def load(require_built=True):
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
                                       _vp, C.c_int]
+    lib.dmftgpu_fourier_w2tau.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, C.c_int, _vp, _vp,
+                                          C.c_int]
+    lib.dmftgpu_fourier_tau2w.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, C.c_int]
+    lib.dmftgpu_sigma2_tau.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _ip, _dp, _vp, _vp, C.c_int]
+    lib.dmftgpu_fock.argtypes = [_vp, C.c_int, C.c_int, _ip, _dp, _vp, _vp, C.c_int]
+    lib.dmftgpu_dyson.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_occupation.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, _vp, C.c_int]
+    lib.dmftgpu_estimate_asymto.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, C.c_int, C.c_int]
+    lib.dmftgpu_ipt.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp,
+                                C.c_int, _ip, _dp, _vp, _vp, _vp, C.c_int]
     lib.dmftgpu_hyb_delta_noalloc.argtypes = [C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
                                               C.c_double, _vp, _vp]
     _lib = lib
@@ -290,6 +301,105 @@ class Context:
                                         _vp(g.ptr), _vp(hi.ptr), float(mu), _vp(out.ptr), self._flags(dev))
         self._check("dmftgpu_hyb_delta", st)
         return out.result()
+
+    # ------------------------------------------------------------------ impurity stage
+    @staticmethod
+    def _ulist(uidx, ut):
+        uidx = np.ascontiguousarray(uidx, np.int32).reshape(-1, 4)
+        ut = np.ascontiguousarray(ut, np.complex128).reshape(-1)
+        return uidx, ut, uidx.shape[0]
+
+    def FourierTransform(self, delta_w, beta, ntau, greenFtnAsym=False, moments1=None, moments=None):
+        """FourierTransform (iw -> tau grid, with tail and positivity fix-up): returns (ntau+1, d, d)."""
+        dev = _is_torch(delta_w)
+        a = _Arr(delta_w, dev)
+        nf, d = a.obj.shape[0], a.obj.shape[1]
+        m1 = _Arr(moments1[None] if not dev else moments1.unsqueeze(0), dev) if moments1 is not None else None
+        mo = _Arr(moments, dev) if moments is not None else None
+        out = _Arr.empty((ntau + 1, d, d), dev, like=a.obj)
+        st = self.lib.dmftgpu_fourier_w2tau(self.h, d, nf, ntau, float(beta), _vp(a.ptr), _vp(mo.ptr) if mo else None,
+                                            int(bool(greenFtnAsym)), _vp(m1.ptr) if m1 else None, _vp(out.ptr),
+                                            self._flags(dev))
+        self._check("dmftgpu_fourier_w2tau", st)
+        return out.result()
+
+    def FT_t_to_w(self, delta_t, beta, nfreq, allow_causality=False):
+        dev = _is_torch(delta_t)
+        a = _Arr(delta_t, dev)
+        ntau, d = a.obj.shape[0] - 1, a.obj.shape[1]
+        out = _Arr.empty((nfreq, d, d), dev, like=a.obj)
+        st = self.lib.dmftgpu_fourier_tau2w(self.h, d, nfreq, ntau, float(beta), _vp(a.ptr), _vp(out.ptr),
+                                            self._flags(dev))
+        self._check("dmftgpu_fourier_tau2w", st, (OK, CAUSALITY) if allow_causality else (OK,))
+        return out.result()
+
+    def getStimp(self, Gt, uidx, ut, beta, allow_hermiticity=False):
+        dev = _is_torch(Gt)
+        a = _Arr(Gt, dev)
+        ntau, d = a.obj.shape[0] - 1, a.obj.shape[1]
+        uidx, ut, nu = self._ulist(uidx, ut)
+        out = _Arr.empty((ntau + 1, d, d), dev, like=a.obj)
+        st = self.lib.dmftgpu_sigma2_tau(self.h, d, ntau, float(beta), nu, uidx.ctypes.data_as(_ip),
+                                         ut.view(np.float64).ctypes.data_as(_dp), _vp(a.ptr), _vp(out.ptr),
+                                         self._flags(dev))
+        self._check("dmftgpu_sigma2_tau", st, (OK, HERMITICITY) if allow_hermiticity else (OK,))
+        return out.result()
+
+    def getFockOperator(self, occMat, uidx, ut):
+        dev = _is_torch(occMat)
+        a = _Arr(occMat[None] if not dev else occMat.unsqueeze(0), dev)
+        d = a.obj.shape[1]
+        uidx, ut, nu = self._ulist(uidx, ut)
+        out = _Arr.empty((1, d, d), dev, like=a.obj)
+        st = self.lib.dmftgpu_fock(self.h, d, nu, uidx.ctypes.data_as(_ip), ut.view(np.float64).ctypes.data_as(_dp),
+                                   _vp(a.ptr), _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_fock", st)
+        return out.result()[0]
+
+    def getGwimp(self, himp, delta_w, fock, sigma2, mu, beta, allow_causality=False):
+        dev = _is_torch(delta_w)
+        one = (lambda x: x[None]) if not dev else (lambda x: x.unsqueeze(0))
+        h, dl, fk, s2 = _Arr(one(himp), dev), _Arr(delta_w, dev), _Arr(one(fock), dev), _Arr(sigma2, dev)
+        nf, d = dl.obj.shape[0], dl.obj.shape[1]
+        out = _Arr.empty((nf, d, d), dev, like=dl.obj)
+        st = self.lib.dmftgpu_dyson(self.h, d, nf, float(beta), float(mu), _vp(h.ptr), _vp(dl.ptr), _vp(fk.ptr),
+                                    _vp(s2.ptr), _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_dyson", st, (OK, CAUSALITY) if allow_causality else (OK,))
+        return out.result()
+
+    def getoccMat(self, Gwimp, beta):
+        dev = _is_torch(Gwimp)
+        a = _Arr(Gwimp, dev)
+        nf, d = a.obj.shape[0], a.obj.shape[1]
+        out = _Arr.empty((1, d, d), dev, like=a.obj)
+        st = self.lib.dmftgpu_occupation(self.h, d, nf, float(beta), _vp(a.ptr), _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_occupation", st)
+        return out.result()[0]
+
+    def estimate_asymto(self, F, nfreq, beta, order):
+        """F: (nfreq+3, d, d); returns a copy with slot nfreq+order-1 written."""
+        dev = _is_torch(F)
+        a = _Arr(F, dev)
+        d = a.obj.shape[1]
+        st = self.lib.dmftgpu_estimate_asymto(self.h, d, nfreq, float(beta), _vp(a.ptr), int(order), self._flags(dev))
+        self._check("dmftgpu_estimate_asymto", st)
+        return a.result()
+
+    def IPT(self, himp, weiss_field, projNumMatrix, uidx, ut, U, mu, beta, ntau):
+        """IPT solver: returns (SE_out[nfreq+5], Gwimp_out[nfreq+5], projNumMatrix)."""
+        dev = _is_torch(weiss_field)
+        one = (lambda x: x[None]) if not dev else (lambda x: x.unsqueeze(0))
+        h, dl, nm = _Arr(one(himp), dev), _Arr(weiss_field, dev), _Arr(one(projNumMatrix), dev)
+        nf, d = dl.obj.shape[0], dl.obj.shape[1]
+        uidx, ut, nu = self._ulist(uidx, ut)
+        se = _Arr.empty((nf + 5, d, d), dev, like=dl.obj)
+        gi = _Arr.empty((nf + 5, d, d), dev, like=dl.obj)
+        no = _Arr.empty((1, d, d), dev, like=dl.obj)
+        st = self.lib.dmftgpu_ipt(self.h, d, nf, ntau, float(beta), float(U), float(mu), _vp(h.ptr), _vp(dl.ptr),
+                                  _vp(nm.ptr), nu, uidx.ctypes.data_as(_ip), ut.view(np.float64).ctypes.data_as(_dp),
+                                  _vp(se.ptr), _vp(gi.ptr), _vp(no.ptr), self._flags(dev))
+        self._check("dmftgpu_ipt", st)
+        return se.result(), gi.result(), no.result()[0]
 
 
 def kmesh(kx, ky, kz):

@@ -108,6 +108,43 @@ int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, doub
                       const double *sigma, const double *gw, const double *himp, double mu, double *delta,
                       int flags);
 
+/* ---------------------------------------------------------------------------------------------
+ * Impurity stage.  Matrices are dim x dim; U lists are gen_Uijkl's (src/gen_Uijkl.cpp:9-87):
+ * uidx[nu][4] = (i, j, k, l), ut[nu] complex; both always host pointers.
+ * --------------------------------------------------------------------------------------------- */
+
+/* FourierTransform (src/FourierTransform.cpp:470-488 -> FourierTransform_, :126-178): fw[nfreq] -> ft[ntau+1],
+ * tau_j = j beta / ntau, including the positivity fix-up.  If mom[4] is given it is used as is; else the moments
+ * are fitted (green_asym selects the m0=0, m1=I fit) and, if m1 is given, m0 = 0 and m1 = *m1 (the overload with
+ * the AsymtoV argument). */
+int dmftgpu_fourier_w2tau(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, const double *fw,
+                          const double *mom, int green_asym, const double *m1, double *ft, int flags);
+/* FT_t_to_w (src/FourierTransform.cpp:521-561): ft[ntau+1] -> fw[nfreq]; DMFTGPU_CAUSALITY where the
+ * reference asserts. */
+int dmftgpu_fourier_tau2w(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, const double *ft, double *fw,
+                          int flags);
+/* getStimp (src/SCGF2_fullLoop.cpp:603-690): gt[ntau+1] -> st[ntau+1] (non-skeleton form), with the
+ * Hermiticity checks (DMFTGPU_HERMITICITY) and the positivity fix-up. */
+int dmftgpu_sigma2_tau(dmftgpu_ctx *ctx, int dim, int ntau, double beta, int nu, const int *uidx, const double *ut,
+                       const double *gt, double *st, int flags);
+/* getFockOperator (src/SCGF2_fullLoop.cpp:583-597). */
+int dmftgpu_fock(dmftgpu_ctx *ctx, int dim, int nu, const int *uidx, const double *ut, const double *occ, double *fock,
+                 int flags);
+/* getGwimp (src/SCGF2_fullLoop.cpp:551-578): gw[nfreq] = [(iw+mu) - himp - delta - fock - sigma2]^-1. */
+int dmftgpu_dyson(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, double mu, const double *himp, const double *delta,
+                  const double *fock, const double *sigma2, double *gw, int flags);
+/* getoccMat (src/SCGF2_fullLoop.cpp:539-549): occ = -G(tau = beta^-). */
+int dmftgpu_occupation(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double *gw, double *occ, int flags);
+/* estimate_asymto (src/SCGF2_fullLoop.cpp:736-787): f holds nfreq+3 matrices; writes slot nfreq+order-1. */
+int dmftgpu_estimate_asymto(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, double *f, int order, int flags);
+/* IPT (src/SCGF2_fullLoop.cpp:873-1065, dispatched by SOLVER at src/SOLVER.cpp:411-414): dim = 2.
+ * himp = projimpurity_site_Hamiltonian, delta[nfreq] = projweiss_field, nummat_in = projNumMatrix;
+ * outputs in ImgFreqFtn slot order (src/ImgTimeFtn.cpp:177): se_out[nfreq+5] (SE_out), gimp_out[nfreq+5]
+ * (Gwimp_out, may be NULL) and nummat_out (the updated projNumMatrix). */
+int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double U, double mu, const double *himp,
+                const double *delta, const double *nummat_in, int nu, const int *uidx, const double *ut,
+                double *se_out, double *gimp_out, double *nummat_out, int flags);
+
 /* No counterpart in the reference.  Construct_hyb_delta for callers that cannot allocate device memory
  * (a driver whose HBM belongs to a pool allocator, or one that must not stall the device with a
  * non-stream-ordered cudaMalloc): no context, no allocation, every array argument a DEVICE pointer except

@@ -1,0 +1,117 @@
+"""GPU parity of the impurity stage (FourierTransform, FT_t_to_w, getStimp, getFockOperator, getGwimp,
+getoccMat, estimate_asymto, IPT) against the FP64 oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from dmftpack_gb300 import models
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _two_pole(nf, beta, d=2, seed=0):
+    rng = np.random.default_rng(seed)
+    iw = 1j * np.pi * (2 * np.arange(nf) + 1) / beta
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    H = (A + A.conj().T) / 2
+    B = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    Hb = (B + B.conj().T) / 2
+    G = np.linalg.inv(iw[:, None, None] * np.eye(d) - H - 0.3 * np.linalg.inv(iw[:, None, None] * np.eye(d) - Hb))
+    return G
+
+
+@pytest.mark.parametrize("d,green,m1", [(2, True, False), (2, False, True), (3, False, False), (4, True, False)])
+def test_fourier_w2tau(ctx, orc, d, green, m1):
+    beta, nf, ntau = 10.0, 160, 640
+    G = _two_pole(nf, beta, d, seed=d)
+    M1 = np.eye(d) if m1 else None
+    ref, _ = orc.fourier(G, beta, ntau, green_asym=green, m1=M1)
+    got = ctx.FourierTransform(G, beta, ntau, greenFtnAsym=green, moments1=M1)
+    assert rel_err(got, ref) < TOL
+
+
+def test_fourier_positivity_fixup(ctx, orc):
+    beta, nf, ntau = 8.0, 96, 256
+    G = -_two_pole(nf, beta, 2, seed=5)          # wrong sign: G(tau) positive, every point gets fixed
+    ref, fix = orc.fourier(G, beta, ntau, green_asym=True)
+    assert fix > 0
+    got = ctx.FourierTransform(G, beta, ntau, greenFtnAsym=True)
+    assert rel_err(got, ref) < TOL
+
+
+def test_fourier_with_given_moments(ctx, orc):
+    beta, nf, ntau = 12.0, 128, 512
+    G = _two_pole(nf, beta, 3, seed=9)
+    mom = orc.moments(G, beta, green_asym=True)
+    ref, _ = orc.w2tau(G, mom, beta, ntau)
+    got = ctx.FourierTransform(G, beta, ntau, moments=mom)
+    assert rel_err(got, ref) < TOL
+
+
+def test_ft_t_to_w(ctx, orc):
+    beta, nf, ntau = 10.0, 128, 1024
+    G = _two_pole(nf, beta, 3, seed=2)
+    gt, _ = orc.fourier(G, beta, ntau, green_asym=True)
+    ref, st = orc.tau2w(gt, beta, nf)
+    got = ctx.FT_t_to_w(gt, beta, nf)
+    assert st == 0 and rel_err(got, ref) < TOL
+
+
+@pytest.mark.parametrize("kanamori", [False, True])
+def test_getstimp(ctx, orc, kanamori):
+    beta, nf, ntau = 10.0, 96, 128
+    d = 6 if kanamori else 2
+    G = _two_pole(nf, beta, d, seed=3)
+    gt, _ = orc.fourier(G, beta, ntau, green_asym=True)
+    gt = (gt + np.conj(np.swapaxes(gt, 1, 2))) / 2      # exactly Hermitian, as the reference asserts
+    uidx, ut = orc.gen_uijkl(d, 4.0, 2.6, 0.7, density_density=not kanamori)
+    ref, _, st = orc.sigma2_tau(gt, uidx, ut, beta)
+    got = ctx.getStimp(gt, uidx, ut, beta, allow_hermiticity=(st != 0))
+    assert rel_err(got, ref) < TOL
+
+
+def test_fock_dyson_occ_asymto(ctx, orc):
+    beta, nf, d = 10.0, 200, 3
+    rng = np.random.default_rng(4)
+    occ = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    occ = (occ + occ.conj().T) / 4 + 0.5 * np.eye(d)
+    uidx, ut = orc.gen_uijkl(d, 3.0, 2.0, 0.5)
+    assert rel_err(ctx.getFockOperator(occ, uidx, ut), orc.fock(occ, uidx, ut)) < TOL
+    G = _two_pole(nf, beta, d, seed=6)
+    delta = 0.2 * G
+    himp = np.diag([0.1, -0.2, 0.3]).astype(complex)
+    fk = orc.fock(occ, uidx, ut)
+    s2 = 0.05 * G
+    ref, st = orc.dyson(himp, delta, fk, s2, 0.4, beta)
+    got = ctx.getGwimp(himp, delta, fk, s2, 0.4, beta, allow_causality=(st != 0))
+    assert rel_err(got, ref) < TOL
+    assert rel_err(ctx.getoccMat(ref, beta), orc.occ(ref, beta)) < TOL
+    F = np.zeros((nf + 3, d, d), complex)
+    F[:nf] = ref
+    F[nf] = np.eye(d)
+    for order in (1, 2, 3):
+        r = orc.estimate_asymto(F, nf, beta, order)
+        g = ctx.estimate_asymto(F, nf, beta, order)
+        assert rel_err(g[nf + order - 1], r[nf + order - 1]) < TOL
+
+
+def test_ipt_matches_oracle(ctx, orc):
+    wl = models.hubbard_2d(kx=8, ky=8, nfreq=128, beta=10.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    mu, U = 0.0, wl.extra["U"]
+    gw, _, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, 1, 2)
+    himp = H.mean(0)
+    delta = orc.hyb_delta([0, 1], wl.sigma, gw, himp, mu, wl.beta)
+    uidx, ut = orc.gen_uijkl(2, U, U, 0.0, density_density=True)
+    himp_dc = himp - 0.5 * U * np.eye(2)            # nominal double counting of the example input
+    ntau = 4 * wl.nfreq
+    se, gi, nm, st = orc.ipt(himp_dc, delta, num, uidx, ut, U, mu, wl.beta, ntau)
+    assert st == 0
+    g_se, g_gi, g_nm = ctx.IPT(himp_dc, delta, num, uidx, ut, U, mu, wl.beta, ntau)
+    nf = wl.nfreq
+    assert rel_err(g_se[:nf + 3], se[:nf + 3]) < TOL
+    assert rel_err(g_gi[:nf], gi[:nf]) < TOL
+    assert rel_err(g_gi[nf + 1:nf + 4], gi[nf + 1:nf + 4]) < 1e-9
+    assert rel_err(g_nm, nm) < TOL
