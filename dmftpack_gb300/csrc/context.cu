@@ -32,6 +32,7 @@ void *dg_buf(dmftgpu_ctx *ctx, const char *name, size_t bytes) {
     if (b.bytes < bytes) {
         if (b.p) {
             cudaStreamSynchronize(ctx->stream);
+            if (ctx->side) cudaStreamSynchronize(ctx->side);
             cudaFree(b.p);
             b.p = nullptr;
             b.bytes = 0;
@@ -112,6 +113,9 @@ int dmftgpu_create(dmftgpu_ctx **out, int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         int code = dg_set_cuda_error(ctx, e, "dmftgpu_create");
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -132,6 +136,12 @@ int dmftgpu_destroy(dmftgpu_ctx *ctx) {
     for (auto &kv : ctx->bufs)
         if (kv.second.p) cudaFree(kv.second.p);
     if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return DMFTGPU_OK;

@@ -1,0 +1,193 @@
+// df.cuh -- double-float ("split precision") complex arithmetic on the FP32 pipe.
+//
+// A real number is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving a 48-bit mantissa;
+// products use the FMA error-free transformation (p = a*b, e = fma(a, b, -p)), sums the two-sum
+// transformation (Knuth), so every operation is accurate to ~2^-47 relative.  On GB300 the FP32 pipe issues
+// ~70x the FP64 rate, so a double-float multiply-add (~18 FP32 instructions) is still several times cheaper
+// than an FP64 one.  Values enter from FP64 memory exactly (hi = rn(x), lo = rn(x - hi)) and leave as
+// hi + lo in FP64.
+//
+// Ops policies used by the templated lattice kernels:
+//   OpsD: complex FP64 (double2)       OpsF: complex double-float (cdf)
+#pragma once
+#include "common.cuh"
+
+struct dfl {
+    float h, l;
+};
+struct cdf {
+    dfl re, im;
+};
+
+__device__ __forceinline__ dfl df_make(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(dfl a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    dfl s = two_sum(a.h, b.h);
+    const float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+    return fast_two_sum(s.h, e);
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+// c + a*b with one rounding of the product's error term
+__device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    dfl s = two_sum(c.h, p);
+    const float t = __fadd_rn(s.l, __fadd_rn(c.l, e));
+    return fast_two_sum(s.h, t);
+}
+// 1/a: FP32 reciprocal refined by one Newton step in double-float (24 -> ~48 bits)
+__device__ __forceinline__ dfl df_rcp(dfl a) {
+    const float r = __frcp_rn(a.h);
+    // e = 1 - a*r in double-float
+    dfl ar = df_mul(a, {r, 0.0f});
+    dfl e = df_sub({1.0f, 0.0f}, ar);
+    // r + r*e
+    return df_fma({r, 0.0f}, e, {r, 0.0f});
+}
+
+__device__ __forceinline__ cdf cdf_make(double2 z) { return {df_make(z.x), df_make(z.y)}; }
+__device__ __forceinline__ double2 cdf_val(cdf z) { return make_double2(df_val(z.re), df_val(z.im)); }
+
+struct OpsD {
+    typedef double2 C;
+    typedef double M;  // pivot magnitude type
+    static __device__ __forceinline__ C zero() { return cmk(0, 0); }
+    static __device__ __forceinline__ C one() { return cmk(1, 0); }
+    static __device__ __forceinline__ C from(double2 z) { return z; }
+    static __device__ __forceinline__ double2 to(C z) { return z; }
+    static __device__ __forceinline__ C add(C a, C b) { return cadd(a, b); }
+    static __device__ __forceinline__ C sub(C a, C b) { return csub(a, b); }
+    static __device__ __forceinline__ C neg(C a) { return cneg(a); }
+    static __device__ __forceinline__ C mul(C a, C b) { return cmul(a, b); }
+    static __device__ __forceinline__ C mulc(C a, C b) { return cmulc(a, b); }  // a conj(b)
+    static __device__ __forceinline__ C fma(C a, C b, C acc) { return cfma(a, b, acc); }
+    static __device__ __forceinline__ C fms(C a, C b, C acc) { return cfms(a, b, acc); }
+    static __device__ __forceinline__ C rcp(C a) { return crcp(a); }
+    static __device__ __forceinline__ double re(C a) { return a.x; }
+    static __device__ __forceinline__ double mag2(C a) { return cabs2(a); }
+    static __device__ __forceinline__ C shfl(C v, int src, int w) { return shfl2(v, src, w); }
+};
+
+struct OpsF {
+    typedef cdf C;
+    typedef float M;
+    static __device__ __forceinline__ C zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+    static __device__ __forceinline__ C one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
+    static __device__ __forceinline__ C from(double2 z) { return cdf_make(z); }
+    static __device__ __forceinline__ double2 to(C z) { return cdf_val(z); }
+    static __device__ __forceinline__ C add(C a, C b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+    static __device__ __forceinline__ C sub(C a, C b) { return {df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+    static __device__ __forceinline__ C neg(C a) { return {df_neg(a.re), df_neg(a.im)}; }
+    static __device__ __forceinline__ C mul(C a, C b) {
+        return {df_fma(df_neg(a.im), b.im, df_mul(a.re, b.re)), df_fma(a.im, b.re, df_mul(a.re, b.im))};
+    }
+    static __device__ __forceinline__ C mulc(C a, C b) {  // a conj(b)
+        return {df_fma(a.im, b.im, df_mul(a.re, b.re)), df_fma(df_neg(a.re), b.im, df_mul(a.im, b.re))};
+    }
+    static __device__ __forceinline__ C fma(C a, C b, C acc) {
+        dfl r = df_fma(a.re, b.re, acc.re);
+        r = df_fma(df_neg(a.im), b.im, r);
+        dfl i = df_fma(a.re, b.im, acc.im);
+        i = df_fma(a.im, b.re, i);
+        return {r, i};
+    }
+    static __device__ __forceinline__ C fms(C a, C b, C acc) {
+        dfl r = df_fma(df_neg(a.re), b.re, acc.re);
+        r = df_fma(a.im, b.im, r);
+        dfl i = df_fma(df_neg(a.re), b.im, acc.im);
+        i = df_fma(df_neg(a.im), b.re, i);
+        return {r, i};
+    }
+    static __device__ __forceinline__ C rcp(C a) {  // conj(a)/|a|^2
+        const dfl n = df_fma(a.im, a.im, df_mul(a.re, a.re));
+        const dfl r = df_rcp(n);
+        return {df_mul(a.re, r), df_neg(df_mul(a.im, r))};
+    }
+    static __device__ __forceinline__ double re(C a) { return df_val(a.re); }
+    static __device__ __forceinline__ float mag2(C a) {  // pivot choice only: FP32 magnitude suffices
+        return __fmaf_rn(a.re.h, a.re.h, __fmul_rn(a.im.h, a.im.h));
+    }
+    static __device__ __forceinline__ C shfl(C v, int src, int w) {
+        C o;
+        o.re.h = __shfl_sync(0xffffffffu, v.re.h, src, w);
+        o.re.l = __shfl_sync(0xffffffffu, v.re.l, src, w);
+        o.im.h = __shfl_sync(0xffffffffu, v.im.h, src, w);
+        o.im.l = __shfl_sync(0xffffffffu, v.im.l, src, w);
+        return o;
+    }
+};
+
+// warp_gj_inverse (linalg.cuh) for any Ops policy
+template <class Ops, int N, int W>
+__device__ __forceinline__ bool warp_gj_inverse_t(typename Ops::C (&a)[N], const int c) {
+    typedef typename Ops::C C;
+    typedef typename Ops::M M;
+    static_assert(N <= W && W <= 32 && (W & (W - 1)) == 0, "bad lane group");
+    bool singular = false;
+    int perm[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        M best = M(-1);
+        int p = j;
+#pragma unroll
+        for (int i = j; i < N; i++) {
+            const M v = Ops::mag2(a[i]);
+            if (v > best) {
+                best = v;
+                p = i;
+            }
+        }
+        p = __shfl_sync(0xffffffffu, p, j, W);
+        best = __shfl_sync(0xffffffffu, best, j, W);
+        singular |= !(best > M(0));
+        perm[j] = p;
+#pragma unroll
+        for (int i = j + 1; i < N; i++)
+            if (i == p) {
+                const C t = a[j];
+                a[j] = a[i];
+                a[i] = t;
+            }
+        const C piv = Ops::shfl(a[j], j, W);
+        const C ipiv = Ops::rcp(piv);
+        const C t = Ops::mul(a[j], ipiv);
+        const bool is_piv_col = (c == j);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            if (i == j) continue;
+            const C f = Ops::shfl(a[i], j, W);
+            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+        }
+        a[j] = is_piv_col ? ipiv : t;
+    }
+#pragma unroll
+    for (int j = N - 1; j >= 0; j--) {
+        const int p = perm[j];
+        const int src = (c == j) ? p : ((c == p) ? j : c);
+#pragma unroll
+        for (int i = 0; i < N; i++) a[i] = Ops::shfl(a[i], src, W);
+    }
+    return singular;
+}

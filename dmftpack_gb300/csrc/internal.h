@@ -21,6 +21,8 @@ struct dmftgpu_ctx {
     };
     std::map<std::string, Buf> bufs;  // grow-only named device workspaces
     int *d_status = nullptr;          // device status word (max of kernel-reported codes)
+    cudaStream_t side = nullptr;      // side stream for work that overlaps the main stream's kernels
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool timing = false;              // record CUDA events around the named hot kernels
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };

@@ -295,7 +295,7 @@ using dg::SchurKernel;
 
 struct SInst {
     int DP, W;
-    SchurKernel (*get)(int);
+    SchurKernel (*get)(int, bool);
 };
 const SInst kSInst[] = {
     {1, 1, dg::schur_kernel_1},    {2, 2, dg::schur_kernel_2},    {3, 4, dg::schur_kernel_3},
@@ -317,6 +317,7 @@ struct Prepared {
     const double2 *H;  // permuted
     double2 *sig, *mom, *UP, *m0, *B;
     double *eps, *epsQ;
+    cudaEvent_t static_ready = nullptr;  // recorded on the side stream after the static eigen-decomposition
 };
 
 int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P) {
@@ -366,23 +367,30 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     const int m = n - D;
     P.epsQ = (double *)dg_buf(ctx, "lat.epsQ", (size_t)nk * (m + 1) * sizeof(double));
     P.B = (double2 *)dg_buf(ctx, "lat.B", (size_t)nk * (m + 1) * D * sizeof(double2));
-    double2 *qwork = (double2 *)dg_buf(ctx, "lat.qwork", (size_t)nk * 3 * (m * m + 1) * sizeof(double2));
+    double2 *qwork = (double2 *)dg_buf(ctx, "lat.qwork", (size_t)nk * 3 * ((size_t)m * m + 1) * sizeof(double2));
     int *qiwork = (int *)dg_buf(ctx, "lat.qiwork", (size_t)nk * (m + 1) * sizeof(int));
-    if (!P.m0 || !P.epsQ || !P.B || !qwork || !qiwork) return DMFTGPU_NOMEM;
     double2 *work = (double2 *)dg_buf(ctx, "lat.eigwork", (size_t)nk * 3 * n * n * sizeof(double2));
     int *iwork = (int *)dg_buf(ctx, "lat.eigiwork", (size_t)nk * n * sizeof(int));
-    if (!P.mom || !P.sig || !P.eps || !P.UP || !work || !iwork) return DMFTGPU_NOMEM;
+    if (!P.m0 || !P.epsQ || !P.B || !qwork || !qiwork || !work || !iwork) return DMFTGPU_NOMEM;
+    if (!P.mom || !P.sig || !P.eps || !P.UP) return DMFTGPU_NOMEM;
     DG_TRY(dg_moments_dev(ctx, D, Nf, P.beta, dS, 0, P.mom));
     long long tot = 2LL * Nf * D * D;
     k_sigall<<<dg_ceil_div(tot, 256), 256, 0, s>>>(Nf, D, P.nh, mask, P.beta, dS, P.mom, P.sig, P.m0);
     DG_LAUNCH(ctx, "k_sigall");
-    k_static_eig<<<dg_ceil_div(nk, 64), 64, 0, s>>>(nk, n, D, P.nh, mask, P.H, P.mom, work, iwork, P.eps, P.UP,
-                                                    ctx->d_status);
-    DG_LAUNCH(ctx, "k_static_eig");
+    // the Schur data (eigen-decomposition of H_QQ) is needed first, by k_schur, on the main stream; the
+    // static eigen-decomposition of H + m0 feeds only the Fermi terms, so it runs on the side stream
+    // (FP64-pipe work) while the lattice kernel (FP32 pipe in the mixed form) proceeds
     if (m > 0) {
-        k_schur_prep<<<dg_ceil_div(nk, 64), 64, 0, s>>>(nk, n, D, P.H, qwork, qiwork, P.epsQ, P.B, ctx->d_status);
+        k_schur_prep<<<dg_ceil_div(nk, 32), 32, 0, s>>>(nk, n, D, P.H, qwork, qiwork, P.epsQ, P.B, ctx->d_status);
         DG_LAUNCH(ctx, "k_schur_prep");
     }
+    DG_CUDA(cudaEventRecord(ctx->ev_fork, s));
+    DG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    k_static_eig<<<dg_ceil_div(nk, 32), 32, 0, ctx->side>>>(nk, n, D, P.nh, mask, P.H, P.m0, work, iwork, P.eps, P.UP,
+                                                            ctx->d_status);
+    DG_LAUNCH(ctx, "k_static_eig");
+    DG_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+    P.static_ready = ctx->ev_join;
     return DMFTGPU_OK;
 }
 
@@ -429,18 +437,57 @@ int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid
 }
 
 
+// fixed-order sum of the per-chunk partial sums
+__global__ void k_schur_reduce(int nchunk, int nf2, int DD, int mode, const double2 *pblk, const double2 *pblk0,
+                               const double2 *ptr, double2 *blk, double2 *blk0, double *tr, double *dtr) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (mode & dg::S_BLOCK) {
+        if (t >= (long long)nf2 * DD) return;
+        double2 s = cmk(0, 0), s0 = cmk(0, 0);
+        for (int q = 0; q < nchunk; q++) {
+            s = cadd(s, pblk[(size_t)q * nf2 * DD + t]);
+            s0 = cadd(s0, pblk0[(size_t)q * nf2 * DD + t]);
+        }
+        blk[t] = s;
+        blk0[t] = s0;
+    } else {
+        if (t >= nf2) return;
+        double a = 0, b = 0;
+        for (int q = 0; q < nchunk; q++) {
+            a += ptr[(size_t)q * nf2 + t].x;
+            b += ptr[(size_t)q * nf2 + t].y;
+        }
+        tr[t] = a;
+        if (dtr) dtr[t] = b;
+    }
+}
+
 // the Schur-form pass (default); mode: dg::S_BLOCK (GreenFtn_w) or S_TRACE[|S_DERIV] (N(mu))
 int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
-              double *tr, double *dtr) {
+              double *tr, double *dtr, bool mixed) {
     const SInst *in = pick_schur(P.D);
-    SchurKernel kern = in->get(mode);
-    const int m = P.n - P.D;
-    int fpb = 8;
-    while (fpb > 1 && dg::schur_smem(in->DP, in->W, mode, fpb, P.D, m) > 160 * 1024) fpb--;
-    size_t smem = dg::schur_smem(in->DP, in->W, mode, fpb, P.D, m);
-    if (smem > 220 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
+    SchurKernel kern = in->get(mode, mixed);
+    const int m = P.n - P.D, NG = 128 / in->W, nf2 = 2 * P.Nf, DD = P.D * P.D;
+    int kc = 16;
+    while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m) > 48 * 1024) kc /= 2;
+    const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m);
+    if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
     DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    SchurArgs g;
+    // k chunks: enough CTAs for ~8 per SM, at least 64 k points per chunk
+    const int fblocks = dg_ceil_div(nf2, NG);
+    int nchunk = std::max(1, std::min(dg_ceil_div(P.nk, 64), dg_ceil_div(8 * 152, fblocks)));
+    const int kchunk = dg_ceil_div(P.nk, nchunk);
+    nchunk = dg_ceil_div(P.nk, kchunk);
+    double2 *pblk = nullptr, *pblk0 = nullptr, *ptr = nullptr;
+    if (mode & dg::S_BLOCK) {
+        pblk = (double2 *)dg_buf(ctx, "schur.pblk", (size_t)nchunk * nf2 * DD * sizeof(double2));
+        pblk0 = (double2 *)dg_buf(ctx, "schur.pblk0", (size_t)nchunk * nf2 * DD * sizeof(double2));
+        if (!pblk || !pblk0) return DMFTGPU_NOMEM;
+    } else {
+        ptr = (double2 *)dg_buf(ctx, "schur.ptr", (size_t)nchunk * nf2 * sizeof(double2));
+        if (!ptr) return DMFTGPU_NOMEM;
+    }
+    dg::SchurArgs g;
     g.H = P.H;
     g.B = P.B;
     g.epsQ = P.epsQ;
@@ -449,34 +496,42 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.n = P.n;
     g.m = m;
     g.nk = P.nk;
-    g.nf2 = 2 * P.Nf;
+    g.nf2 = nf2;
     g.D = P.D;
-    g.fpb = fpb;
     g.wgrid = wgrid;
+    g.kc = kc;
+    g.kchunk = kchunk;
     g.beta = P.beta;
     g.mu = mu;
-    g.blk = blk;
-    g.blk0 = blk0;
-    g.tr = tr;
-    g.dtr = dtr;
+    g.pblk = pblk;
+    g.pblk0 = pblk0;
+    g.ptr = ptr;
     g.status = ctx->d_status;
     {
         DgTimer tm(ctx, "k_schur");
-        kern<<<dg_ceil_div(g.nf2, fpb), 128, smem, ctx->stream>>>(g);
+        kern<<<dim3(fblocks, nchunk), 128, smem, ctx->stream>>>(g);
     }
     DG_LAUNCH(ctx, "k_schur");
+    const long long nred = (mode & dg::S_BLOCK) ? (long long)nf2 * DD : nf2;
+    k_schur_reduce<<<dg_ceil_div(nred, 256), 256, 0, ctx->stream>>>(nchunk, nf2, DD, mode, pblk, pblk0, ptr, blk, blk0,
+                                                                     tr, dtr);
+    DG_LAUNCH(ctx, "k_schur_reduce");
     return DMFTGPU_OK;
 }
 
 // one N(mu) evaluation on a prepared lattice; result (N, dN/dmu) in device out[2]
-int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *dout, bool explicit_inv) {
+int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *dout, bool explicit_inv,
+              bool mixed) {
     const int nf2 = 2 * P.Nf;
     double *tr = (double *)dg_buf(ctx, "nele.tr", nf2 * sizeof(double));
     double *dtr = (double *)dg_buf(ctx, "nele.dtr", nf2 * sizeof(double));
     double *fs = (double *)dg_buf(ctx, "nele.fs", 2 * (size_t)P.nk * sizeof(double));
     if (!tr || !dtr || !fs) return DMFTGPU_NOMEM;
+    if (explicit_inv && mixed) return dg_fail(ctx, DMFTGPU_BADARG, "nele: the explicit form is FP64 only");
     if (explicit_inv) DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
-    else DG_TRY(run_schur(ctx, P, deriv ? (dg::S_TRACE | dg::S_DERIV) : dg::S_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+    else DG_TRY(run_schur(ctx, P, deriv ? (dg::S_TRACE | dg::S_DERIV) : dg::S_TRACE, mu, 1, nullptr, nullptr, tr, dtr,
+                          mixed));
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     k_fermi<<<dg_ceil_div(P.nk, 128), 128, 0, ctx->stream>>>(P.nk, P.n, P.D, P.beta, mu, P.eps, P.UP, nullptr, fs);
     DG_LAUNCH(ctx, "k_fermi");
     k_nele_finalize<<<1, 256, 0, ctx->stream>>>(nf2, P.nk, P.beta, tr, dtr, fs, deriv ? 1 : 0, dout);
@@ -484,10 +539,11 @@ int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double
     return DMFTGPU_OK;
 }
 
-int nele_host(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *N, double *dN, bool explicit_inv) {
+int nele_host(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double *N, double *dN, bool explicit_inv,
+              bool mixed) {
     double *dout = (double *)dg_buf(ctx, "nele.out", 2 * sizeof(double));
     if (!dout) return DMFTGPU_NOMEM;
-    DG_TRY(nele_pass(ctx, P, mu, deriv, dout, explicit_inv));
+    DG_TRY(nele_pass(ctx, P, mu, deriv, dout, explicit_inv, mixed));
     double h[2];
     DG_CUDA(cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     DG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -554,7 +610,8 @@ int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double
 int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
                        double *gw, double *gwhf, double *nummat, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !gw || !nummat) return DMFTGPU_BADARG;
-    if (flags & DMFTGPU_MIXED) return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w: mixed precision not built yet");
+    if ((flags & DMFTGPU_MIXED) && (flags & DMFTGPU_EXPLICIT))
+        return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w: the explicit form is FP64 only");
     cudaSetDevice(ctx->device);
     const int D = L->ncl * L->nh, Nf = L->nfreq;
     const size_t DD = (size_t)D * D;
@@ -578,7 +635,8 @@ int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double 
     double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
     if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
     if (flags & DMFTGPU_EXPLICIT) DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
-    else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr, (flags & DMFTGPU_MIXED) != 0));
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
     DG_LAUNCH(ctx, "k_fermi");
     k_gloc_scale<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, ctx->stream>>>(Nf, L->nk, D, L->nh, blk, blk0, dG, dG0);
@@ -606,7 +664,8 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, c
     DG_TRY(dg_status_reset(ctx));
     Prepared P;
     DG_TRY(prepare(ctx, L, dH, dS, 1, P));
-    DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele, (flags & DMFTGPU_EXPLICIT) != 0));
+    DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele, (flags & DMFTGPU_EXPLICIT) != 0,
+                     (flags & DMFTGPU_MIXED) != 0));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     if (!std::isfinite(*nele)) return DMFTGPU_NAN;
@@ -629,7 +688,8 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
     int evals = 0;
     auto N = [&](double m, double *out, double *dout) {
         evals++;
-        return nele_host(ctx, P, m, dout != nullptr, out, dout, (flags & DMFTGPU_EXPLICIT) != 0);
+        return nele_host(ctx, P, m, dout != nullptr, out, dout, (flags & DMFTGPU_EXPLICIT) != 0,
+                         (flags & DMFTGPU_MIXED) != 0);
     };
     const double goal = n_target;
     if (flags & DMFTGPU_NEWTON) {

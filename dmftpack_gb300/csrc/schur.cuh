@@ -13,10 +13,14 @@
 // inversion to O(D^2 m + D^3).  d/dmu of the trace (Newton's dN/dmu, = -Tr G^2 + Tr G0^2) follows by
 // differentiating the same expression: dG_PP/dz = -G S' G with S' = I + sum_l w_l^2 b_l b_l^H.
 //
-// Mapping: a lane group of W lanes handles one (k, iw) item at a time, lane c holding column c of S (and
-// of S0), both inverted with warp_gj_inverse<DP,W> (DP >= D padded with identity).  A CTA owns fpb
-// frequencies and sweeps all k; per-group shared-memory accumulators are reduced in a fixed order.
+// Mapping: a lane group of W lanes owns one Matsubara frequency and sweeps a chunk of k points; lane c holds
+// column c of S (and S0), inverted with warp_gj_inverse_t<Ops,DP,W> (DP >= D padded with identity), and
+// accumulates column c of the k sum in registers.  A CTA = 128/W frequencies x one k chunk; the per-k data
+// (b_l, mu - e_l, -H_PP) of kc k points at a time is staged once in shared memory in the kernel's
+// arithmetic type.  Per-chunk sums are reduced over chunks in a fixed order by a second kernel.
+// Ops = OpsD (FP64) or OpsF (double-float on the FP32 pipe; FP64 appears only when staging and storing).
 #pragma once
+#include "df.cuh"
 #include "linalg.cuh"
 
 namespace dg {
@@ -29,10 +33,10 @@ struct SchurArgs {
     const double *epsQ;   // [nk][m]
     const double2 *sig;   // [2 Nf][D][D]
     const double2 *m0;    // [D][D]
-    int n, m, nk, nf2, D, fpb, wgrid;
+    int n, m, nk, nf2, D, wgrid, kc, kchunk;  // kc: k points staged per round; kchunk: k points per CTA
     double beta, mu;
-    double2 *blk, *blk0;  // [nf2][D][D]
-    double *tr, *dtr;     // [nf2]
+    double2 *pblk, *pblk0;  // [nchunk][nf2][D][D]  per-chunk k sums (BLOCK)
+    double2 *ptr;           // [nchunk][nf2]         per-chunk trace sums (x = tr, y = dtr)
     int *status;
 };
 
@@ -43,113 +47,118 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
-template <int DP, int W, int MODE>
+// staged per-k data in shared memory (arithmetic type C): B[kc][m][D], e[kc][m] (mu - e_l, real),
+// hpp[kc][D][D] (-H_PP), then once m0[D][D]
+template <class Ops>
+__device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc, typename Ops::C *st) {
+    typedef typename Ops::C C;
+    const int m = g.m, D = g.D, DD = D * D;
+    C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
+    for (int t = threadIdx.x; t < nkc * m * D; t += blockDim.x) sB[t] = Ops::from(g.B[(size_t)k0 * m * D + t]);
+    for (int t = threadIdx.x; t < nkc * m; t += blockDim.x)
+        sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k0 * m + t], 0.0));
+    for (int t = threadIdx.x; t < nkc * DD; t += blockDim.x) {
+        const int kk = t / DD, e = t % DD, a = e % D, b = e / D;
+        sH[t] = Ops::from(cneg(g.H[(size_t)(k0 + kk) * g.n * g.n + a + (size_t)b * g.n]));
+    }
+}
+
+// Lane group = one Matsubara frequency; CTA = NG frequencies x one chunk of k points.
+template <class Ops, int DP, int W, int MODE>
 __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
+    typedef typename Ops::C C;
     constexpr int NG = 128 / W;
     extern __shared__ double2 sm[];
-    const int D = g.D, DD = D * D, fpb = g.fpb, m = g.m, n = g.n;
-    // shared: acc[NG][fpb][DD], acc0[NG][fpb][DD], acct[NG][fpb], bs[NG][m][D], wls[NG][m], es[NG][m] (double),
-    //         tiles[NG][3][DP][DP] (DERIV)
-    double2 *acc = sm;
-    double2 *acc0 = acc + (size_t)NG * fpb * DD;
-    double2 *acct = acc0 + (size_t)NG * fpb * DD;
-    double2 *bsa = acct + (size_t)NG * fpb;
-    double2 *wla = bsa + (size_t)NG * m * D;
-    double2 *tla = wla + (size_t)NG * m;
-    double *esa = (double *)(tla + ((MODE & S_DERIV) ? (size_t)NG * 3 * DP * DP : 0));
-    for (int t = threadIdx.x; t < NG * fpb * DD; t += blockDim.x) acc[t] = acc0[t] = cmk(0, 0);
-    for (int t = threadIdx.x; t < NG * fpb; t += blockDim.x) acct[t] = cmk(0, 0);
-    __syncthreads();
-
+    const int D = g.D, DD = D * D, m = g.m;
+    C *st = reinterpret_cast<C *>(sm);
+    C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
+    C *sM0 = sH + (size_t)g.kc * DD;
+    C *wla = sM0 + DD;                                                   // reciprocals [NG][m]
+    C *tla = wla + (size_t)NG * m;                                        // DERIV tiles [NG][3][DP][DP]
     const int c = threadIdx.x & (W - 1);
     const int grp = threadIdx.x / W;
-    const int f0 = blockIdx.x * fpb;
-    const int nfl = min(fpb, g.nf2 - f0);
-    double2 *myacc = acc + (size_t)grp * fpb * DD, *myacc0 = acc0 + (size_t)grp * fpb * DD;
-    double2 *myacct = acct + (size_t)grp * fpb;
-    double2 *bs = bsa + (size_t)grp * m * D, *wl = wla + (size_t)grp * m;
-    double *es = esa + (size_t)grp * m;
-    double2 *tS = tla + (size_t)grp * 3 * DP * DP, *tG = tS + DP * DP, *tG0 = tG + DP * DP;
+    const int f_raw = blockIdx.x * NG + grp;
+    const bool fvalid = f_raw < g.nf2;
+    const int f = fvalid ? f_raw : g.nf2 - 1;
+    const int chunk = blockIdx.y;
+    const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
+    C *tS = tla + (size_t)grp * 3 * DP * DP, *tG = tS + DP * DP, *tG0 = tG + DP * DP;
+    C *wl = wla + (size_t)grp * m;
     const bool col = c < D;
+    for (int t = threadIdx.x; t < DD; t += blockDim.x) sM0[t] = Ops::from(g.m0[t]);
+    // per-group frequency constants: iw (as a complex with zero real part), z = mu + iw, Sigma(:, c)
+    const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
+    const C zc = Ops::from(cmk(g.mu, w));
+    const C iwc = Ops::from(cmk(0.0, w));
+    C sgc[DP];
+#pragma unroll
+    for (int a = 0; a < DP; a++) sgc[a] = (col && a < D) ? Ops::from(g.sig[(size_t)f * DD + a + (size_t)c * D]) : Ops::zero();
+    C accG[DP], accG0[DP];
+#pragma unroll
+    for (int a = 0; a < DP; a++) accG[a] = accG0[a] = Ops::zero();
+    double acct1 = 0.0, acct2 = 0.0;
     bool sing = false;
 
-    for (int base = 0; base < g.nk; base += NG) {
-        const int k = base + grp;
-        const bool valid = k < g.nk;
-        const int kk = valid ? k : 0;
-        __syncwarp();
-        for (int t = c; t < m * D; t += W) bs[t] = g.B[(size_t)kk * m * D + t];
-        for (int t = c; t < m; t += W) es[t] = g.epsQ[(size_t)kk * m + t];
-        __syncwarp();
-        // -H_PP(:, c) and the static moment column
-        double2 hc[DP], mc[DP];
-#pragma unroll
-        for (int a = 0; a < DP; a++) {
-            hc[a] = (col && a < D) ? cneg(g.H[(size_t)kk * n * n + a + (size_t)c * n]) : cmk(0, 0);
-            mc[a] = (col && a < D) ? g.m0[a + c * D] : cmk(0, 0);
-        }
-        for (int fl = 0; fl < nfl; fl++) {
-            const int f = f0 + fl;
-            const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
-            const double2 z = cmk(g.mu, w);
+    for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
+        const int nkc = min(g.kc, kend - k0);
+        __syncthreads();
+        schur_stage<Ops>(g, k0, nkc, st);
+        __syncthreads();
+        for (int kk = 0; kk < nkc; kk++) {
+            const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
+            // w_l = 1/(z - e_l), shared by the group's lanes
             __syncwarp();
-            for (int l = c; l < m; l += W) wl[l] = crcp(cmk(g.mu - es[l], w));
+            for (int l = c; l < m; l += W) wl[l] = Ops::rcp(Ops::add(es[l], iwc));
             __syncwarp();
-            const double2 *sg = g.sig + (size_t)f * DD + (size_t)c * D;
-            double2 s[DP], s0[DP];
+            C s[DP], s0[DP];
 #pragma unroll
             for (int a = 0; a < DP; a++) {
-                if (col && a < D) s[a] = csub(hc[a], sg[a]);
-                else s[a] = cmk(a == c ? 1.0 : 0.0, 0.0);
-                if (a == c && col) s[a] = cadd(s[a], z);
+                if (col && a < D) s[a] = Ops::sub(hp[a + c * D], sgc[a]);
+                else s[a] = (a == c) ? Ops::one() : Ops::zero();
+                if (a == c && col) s[a] = Ops::add(s[a], zc);
             }
             if (col) {
                 for (int l = 0; l < m; l++) {
-                    const double2 q = cmulc(wl[l], bs[l * D + c]);  // w_l conj(b_l(c))
+                    const C q = Ops::mulc(wl[l], bs[l * D + c]);     // w_l conj(b_l(c))
 #pragma unroll
                     for (int a = 0; a < DP; a++)
-                        if (a < D) s[a] = cfms(bs[l * D + a], q, s[a]);
+                        if (a < D) s[a] = Ops::fms(bs[l * D + a], q, s[a]);
                 }
             }
 #pragma unroll
-            for (int a = 0; a < DP; a++) s0[a] = (col && a < D) ? csub(cadd(s[a], sg[a]), mc[a]) : s[a];
-            double2 sp[DP];  // S' = I + sum_l w_l^2 b_l b_l^H (DERIV only)
+            for (int a = 0; a < DP; a++)
+                s0[a] = (col && a < D) ? Ops::sub(Ops::add(s[a], sgc[a]), sM0[a + c * D]) : s[a];
+            C sp[DP];  // S' = I + sum_l w_l^2 b_l b_l^H (DERIV only)
             if (MODE & S_DERIV) {
 #pragma unroll
-                for (int a = 0; a < DP; a++) sp[a] = cmk((a == c && col) ? 1.0 : 0.0, 0.0);
+                for (int a = 0; a < DP; a++) sp[a] = (a == c && col) ? Ops::one() : Ops::zero();
                 if (col)
                     for (int l = 0; l < m; l++) {
-                        const double2 q = cmulc(cmul(wl[l], wl[l]), bs[l * D + c]);
+                        const C q = Ops::mulc(Ops::mul(wl[l], wl[l]), bs[l * D + c]);
 #pragma unroll
                         for (int a = 0; a < DP; a++)
-                            if (a < D) sp[a] = cfma(bs[l * D + a], q, sp[a]);
+                            if (a < D) sp[a] = Ops::fma(bs[l * D + a], q, sp[a]);
                     }
             }
-            sing |= warp_gj_inverse<DP, W>(s, c) && valid;
-            sing |= warp_gj_inverse<DP, W>(s0, c) && valid;
+            sing |= warp_gj_inverse_t<Ops, DP, W>(s, c);
+            sing |= warp_gj_inverse_t<Ops, DP, W>(s0, c);
             if (MODE & S_BLOCK) {
-                if (valid && col) {
 #pragma unroll
-                    for (int a = 0; a < DP; a++)
-                        if (a < D) {
-                            const size_t o = (size_t)fl * DD + a + c * D;
-                            myacc[o] = cadd(myacc[o], s[a]);
-                            myacc0[o] = cadd(myacc0[o], s0[a]);
-                        }
+                for (int a = 0; a < DP; a++) {
+                    accG[a] = Ops::add(accG[a], s[a]);
+                    accG0[a] = Ops::add(accG0[a], s0[a]);
                 }
             }
             if (MODE & S_TRACE) {
-                // X = G - G0 (column c); t1 = Re[X(c,c) + sum_l w_l^2 b_l^H X b_l]
-                double2 x[DP];
+                C x[DP];
 #pragma unroll
-                for (int a = 0; a < DP; a++) x[a] = csub(s[a], s0[a]);
-                double2 acc1 = cmk(0, 0), acc2 = cmk(0, 0);
+                for (int a = 0; a < DP; a++) x[a] = Ops::sub(s[a], s0[a]);
+                C acc1 = Ops::zero(), acc2 = Ops::zero();
 #pragma unroll
                 for (int a = 0; a < DP; a++)
                     if (a == c && col) acc1 = x[a];
-                double2 y[DP];
+                C y[DP];
                 if (MODE & S_DERIV) {
-                    // Y = G S' G - G0 S' G0 through the group's shared tiles
                     __syncwarp();
                     if (c < DP) {
 #pragma unroll
@@ -160,110 +169,100 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         }
                     }
                     __syncwarp();
-                    double2 u[DP], u0[DP];
+                    C u[DP], u0[DP];
 #pragma unroll
                     for (int a = 0; a < DP; a++) {
-                        u[a] = cmk(0, 0);
-                        u0[a] = cmk(0, 0);
+                        u[a] = Ops::zero();
+                        u0[a] = Ops::zero();
 #pragma unroll
                         for (int b = 0; b < DP; b++) {
-                            u[a] = cfma(tS[a + b * DP], s[b], u[a]);
-                            u0[a] = cfma(tS[a + b * DP], s0[b], u0[a]);
+                            u[a] = Ops::fma(tS[a + b * DP], s[b], u[a]);
+                            u0[a] = Ops::fma(tS[a + b * DP], s0[b], u0[a]);
                         }
                     }
 #pragma unroll
                     for (int a = 0; a < DP; a++) {
-                        double2 v = cmk(0, 0);
+                        C v = Ops::zero();
 #pragma unroll
                         for (int b = 0; b < DP; b++) {
-                            v = cfma(tG[a + b * DP], u[b], v);
-                            v = cfms(tG0[a + b * DP], u0[b], v);
+                            v = Ops::fma(tG[a + b * DP], u[b], v);
+                            v = Ops::fms(tG0[a + b * DP], u0[b], v);
                         }
                         y[a] = v;
                     }
                     __syncwarp();
 #pragma unroll
                     for (int a = 0; a < DP; a++)
-                        if (a == c && col) acc2 = cneg(y[a]);  // -Tr Y
+                        if (a == c && col) acc2 = Ops::neg(y[a]);
                 }
                 if (col) {
                     for (int l = 0; l < m; l++) {
-                        const double2 bc = bs[l * D + c];
-                        double2 px = cmk(0, 0), py = cmk(0, 0);
+                        const C bc = bs[l * D + c];
+                        C px = Ops::zero(), py = Ops::zero();
 #pragma unroll
                         for (int a = 0; a < DP; a++)
                             if (a < D) {
-                                const double2 ba = cconj(bs[l * D + a]);
-                                px = cfma(ba, x[a], px);
-                                if (MODE & S_DERIV) py = cfma(ba, y[a], py);
+                                px = Ops::add(px, Ops::mulc(x[a], bs[l * D + a]));
+                                if (MODE & S_DERIV) py = Ops::add(py, Ops::mulc(y[a], bs[l * D + a]));
                             }
-                        const double2 w2 = cmul(wl[l], wl[l]);
-                        acc1 = cfma(w2, cmul(px, bc), acc1);
+                        const C w2 = Ops::mul(wl[l], wl[l]);
+                        acc1 = Ops::fma(w2, Ops::mul(px, bc), acc1);
                         if (MODE & S_DERIV) {
-                            const double2 w3 = cmul(w2, wl[l]);
-                            acc2 = cfms(cscale(w3, 2.0), cmul(px, bc), acc2);
-                            acc2 = cfms(w2, cmul(py, bc), acc2);
+                            const C w3 = Ops::mul(w2, wl[l]);
+                            acc2 = Ops::fms(Ops::add(w3, w3), Ops::mul(px, bc), acc2);
+                            acc2 = Ops::fms(w2, Ops::mul(py, bc), acc2);
                         }
                     }
                 }
-                const double t1 = group_sum<DP, W>(col ? acc1.x : 0.0);
-                const double t2 = (MODE & S_DERIV) ? group_sum<DP, W>(col ? acc2.x : 0.0) : 0.0;
-                if (valid && c == 0) {
-                    myacct[fl].x += t1;
-                    myacct[fl].y += t2;
+                acct1 += group_sum<DP, W>(col ? Ops::re(acc1) : 0.0);
+                if (MODE & S_DERIV) acct2 += group_sum<DP, W>(col ? Ops::re(acc2) : 0.0);
+            }
+        }
+    }
+    if (sing && fvalid) dg_flag(g.status, DG_SINGULAR);
+    if (!fvalid) return;
+    if (MODE & S_BLOCK) {
+        if (col) {
+            const size_t o = ((size_t)chunk * g.nf2 + f) * DD + (size_t)c * D;
+#pragma unroll
+            for (int a = 0; a < DP; a++)
+                if (a < D) {
+                    g.pblk[o + a] = Ops::to(accG[a]);
+                    g.pblk0[o + a] = Ops::to(accG0[a]);
                 }
-            }
         }
     }
-    if (sing) dg_flag(g.status, DG_SINGULAR);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nfl * DD; t += blockDim.x) {
-        const int fl = t / DD, e = t % DD;
-        if (MODE & S_BLOCK) {
-            double2 s = cmk(0, 0), s0 = cmk(0, 0);
-            for (int q = 0; q < NG; q++) {
-                s = cadd(s, acc[((size_t)q * fpb + fl) * DD + e]);
-                s0 = cadd(s0, acc0[((size_t)q * fpb + fl) * DD + e]);
-            }
-            g.blk[(size_t)(f0 + fl) * DD + e] = s;
-            g.blk0[(size_t)(f0 + fl) * DD + e] = s0;
-        }
-    }
-    if (MODE & S_TRACE)
-        for (int fl = threadIdx.x; fl < nfl; fl += blockDim.x) {
-            double s = 0, s2 = 0;
-            for (int q = 0; q < NG; q++) {
-                s += acct[(size_t)q * fpb + fl].x;
-                s2 += acct[(size_t)q * fpb + fl].y;
-            }
-            g.tr[f0 + fl] = s;
-            if (MODE & S_DERIV) g.dtr[f0 + fl] = s2;
-        }
+    if ((MODE & S_TRACE) && c == 0) g.ptr[(size_t)chunk * g.nf2 + f] = cmk(acct1, acct2);
 }
 
 // shared-memory bytes of one k_schur launch
-inline size_t schur_smem(int DP, int W, int mode, int fpb, int D, int m) {
+inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m) {
     const int NG = 128 / W;
-    size_t s = (size_t)NG * fpb * D * D * 2 + (size_t)NG * fpb + (size_t)NG * m * D + (size_t)NG * m;
+    size_t s = (size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D + (size_t)NG * m;
     if (mode & S_DERIV) s += (size_t)NG * 3 * DP * DP;
-    return s * sizeof(double2) + (size_t)NG * m * sizeof(double);
+    return s * 16;
 }
 
 typedef void (*SchurKernel)(SchurArgs);
 
-template <int DP, int W>
-SchurKernel schur_pick(int mode) {
+template <class Ops, int DP, int W>
+SchurKernel schur_pick_ops(int mode) {
     switch (mode) {
-        case S_BLOCK: return k_schur<DP, W, S_BLOCK>;
-        case S_TRACE: return k_schur<DP, W, S_TRACE>;
-        case S_TRACE | S_DERIV: return k_schur<DP, W, S_TRACE | S_DERIV>;
+        case S_BLOCK: return k_schur<Ops, DP, W, S_BLOCK>;
+        case S_TRACE: return k_schur<Ops, DP, W, S_TRACE>;
+        case S_TRACE | S_DERIV: return k_schur<Ops, DP, W, S_TRACE | S_DERIV>;
         default: return nullptr;
     }
 }
+// mixed = true selects the double-float arithmetic
+template <int DP, int W>
+SchurKernel schur_pick(int mode, bool mixed) {
+    return mixed ? schur_pick_ops<OpsF, DP, W>(mode) : schur_pick_ops<OpsD, DP, W>(mode);
+}
 
 #define DG_SCHUR_INST(DP, W) \
-    SchurKernel schur_kernel_##DP(int mode) { return schur_pick<DP, W>(mode); }
-#define DG_SCHUR_DECL(DP) SchurKernel schur_kernel_##DP(int mode);
+    SchurKernel schur_kernel_##DP(int mode, bool mixed) { return schur_pick<DP, W>(mode, mixed); }
+#define DG_SCHUR_DECL(DP) SchurKernel schur_kernel_##DP(int mode, bool mixed);
 DG_SCHUR_DECL(1)
 DG_SCHUR_DECL(2)
 DG_SCHUR_DECL(3)

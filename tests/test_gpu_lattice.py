@@ -153,6 +153,29 @@ def test_adjust_mu_bisection_matches_oracle_and_newton_converges(ctx, orc):
     assert ne_n < ne_o
 
 
+TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_mixed_precision_lattice_sum(ctx, orc, case):
+    wl = CASES[case]()
+    H, lat = _setup(orc, wl)
+    gw, gwhf, num = orc.greenftn_w(H, wl.sigma, 0.25, wl.beta, wl.ncl, wl.nh)
+    m_gw, m_gwhf, m_num = ctx.GreenFtn_w(lat, H, wl.sigma, 0.25, mixed=True)
+    assert rel_err(m_gw, gw) < TOL_MIXED and rel_err(m_gwhf, gwhf) < TOL_MIXED and rel_err(m_num, num) < TOL_MIXED
+    N, dN = orc.nele(H, wl.sigma, 0.25, wl.beta, wl.ncl, wl.nh, deriv=True)
+    gN, gdN = ctx.GiwToNele(lat, H, wl.sigma, 0.25, deriv=True, mixed=True)
+    assert abs(gN - N) < TOL_MIXED * abs(N) and abs(gdN - dN) < 1e-7 * abs(dN)
+
+
+def test_mixed_precision_newton_mu(ctx, orc):
+    wl = CASES["t2g_p"]()
+    H, lat = _setup(orc, wl)
+    mu_n, ne = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, 7.3, newton=True, mixed=True)
+    assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, wl.ncl, wl.nh) - 7.3) < 1e-9
+    assert ne <= 8
+
+
 def test_hyb_delta_matches_oracle(ctx, orc):
     wl = CASES["t2g_p"]()
     H, lat = _setup(orc, wl)
