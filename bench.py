@@ -191,6 +191,51 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
+    """s/DMFT-iter on the single-band square-lattice Hubbard model (k grid 64x64, beta=50, N_freq=2048,
+    N_tau=8192, U=2, IPT, bisection mu to n=1): the full dmft_main loop body on the device, FP64 and mixed.
+    Returns {precision: {"s_per_iter", "residuals"}} plus the mixed-vs-FP64 G_loc difference after the same
+    iterations."""
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.hubbard_2d(kx=64, ky=64, beta=50.0, nfreq=2048, ntau=8192)
+    U = wl.extra["U"]
+    uidx, ut = models.gen_Uijkl(2, U, U, 0.0, density_density=True)
+    p = dict(ntau=wl.ntau, n_electrons=1.0, U=U, Uprime=U, J=0.0, mixing=0.5, magnetism=0, dctype=1,
+             nominal_charge=1.0, uidx=uidx, ut=ut)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    Hcm = Hd.transpose(-1, -2).contiguous()
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
+    out, glocs = {}, {}
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    himp = Hd[:, :2, :2].mean(0)
+    tcm = lambda t: t.transpose(-1, -2).contiguous()
+    for prec in ("fp64", "mixed"):
+        mixed = prec == "mixed"
+        # first TightBinding call (mu search, G_loc, Delta) before the loop, as in dmft_main
+        mu, _ = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, 1.0, mixed=mixed)
+        gl, _, nm = ctx.GreenFtn_w(lat, Hd, sig, mu, mixed=mixed, with_gwhf=False)
+        we = ctx.Construct_hyb_delta([0, 1], sig, gl, mu, wl.beta, himp)
+        se, we, nm = tcm(sig), tcm(we), tcm(nm)
+        times, res = [], None
+        for it in range(1, n_iter + 1):
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            mu, gl, gi, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, mu, mixed=mixed)
+            e.record(stream)
+            e.synchronize()
+            times.append(s.elapsed_time(e) / 1e3)
+        glocs[prec] = gl
+        out[prec] = {"s_per_iter": statistics.median(times[1:]) if len(times) > 1 else times[0],
+                     "iterations": n_iter, "mu": mu, "residuals": {"GwRD": res[0], "GwRD_low": res[1],
+                                                                  "GwRD_max": res[2], "NumMatRD": res[3]}}
+    out["G_loc_mixed_vs_fp64"] = float((glocs["mixed"] - glocs["fp64"]).abs().max() / glocs["fp64"].abs().max())
+    out["workload"] = ("single-band Hubbard, 2D square lattice, k grid 64x64, beta=50, N_freq=2048, N_tau=8192, "
+                       "U=2, t=1, t'=-0.25, IPT, Sigma seeded U^2/(4 iw), half filling")
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from dmftpack_gb300 import lib
@@ -304,6 +349,7 @@ def run_ours(args, rank, world, local_rank):
         t_o = s.elapsed_time(e) / 1e3
         variants["explicit" if not explicit else "schur"] = {"value": inv_per_step / t_o, "unit": UNIT,
                                                               "ms_per_step": t_o * 1e3}
+    dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     if rank != 0:
         return
     # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
@@ -323,7 +369,7 @@ def run_ours(args, rank, world, local_rank):
            "data": "synthetic (seeded t(R), Sigma = -0.5i/(w_n+1) on the 3 d orbitals)",
            "config": dict(describe(wl), precision=args.precision, algorithm=args.algo,
                           l2="1 GiB buffer written between timed steps", replicas=world),
-           "variants": variants, "error_vs_fp64": err,
+           "variants": variants, "error_vs_fp64": err, "dmft_iteration": dmft_iter,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "fp64" if not mixed else "fp32", "achieved": achieved,

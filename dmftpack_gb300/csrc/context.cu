@@ -133,6 +133,7 @@ int dmftgpu_destroy(dmftgpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     dg_clear_events(ctx);
+    delete ctx->pulay;
     for (auto &kv : ctx->bufs)
         if (kv.second.p) cudaFree(kv.second.p);
     if (ctx->d_status) cudaFree(ctx->d_status);

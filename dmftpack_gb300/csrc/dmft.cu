@@ -1,0 +1,320 @@
+// dmft.cu -- one DMFT self-consistency iteration (the body of the loop in src/dmft_main.cpp:343-570) for a
+// single correlated cluster/atom with the IPT impurity solver, every array on the device:
+//   SOLVER (src/SOLVER.cpp:105-502): proj_to_site (H_imp - DC), IPT, the magnetism == 0 spin average,
+//     NumMatrix update; SE_out = Sigma_imp - DC (src/dmft_main.cpp:489-525)
+//   Pulay mixing of SelfEnergy_w (pulayMixing(2, 5, N_freq, D, D), src/pulay.cpp:48-167, used at
+//     src/dmft_main.cpp:529-533): residual Gram matrix and combinations on the device, the (h+1)^2 DIIS
+//     solve on the host
+//   TightBinding (src/TB.cpp:97-369): mu search, GreenFtn_w, Construct_hyb_delta, impurity_site_Hamiltonian
+//     (k average of the correlated block, src/downfolding.cpp:86-121)
+//   dmft_scf_check residuals (src/dmft_main.cpp:902-1014) on the in-memory G_imp and G_loc
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "impurity.h"
+
+int dg_ipt_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double U, double mu, const double2 *himp,
+               const double2 *delta, const double2 *occ_in, const DgUList &Ul, double2 *se_out, double2 *gimp_out,
+               double2 *occ_out);
+
+namespace {
+
+// k average of the correlated block of H(k)
+__global__ void k_himp(int nk, int n, int D, const double2 *H, double2 *himp) {
+    __shared__ double2 red[256];
+    const int e = blockIdx.x, a = e % D, b = e / D;
+    double2 s = cmk(0, 0);
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) s = cadd(s, H[(size_t)k * n * n + a + (size_t)b * n]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + h]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) himp[e] = cmk(red[0].x / nk, red[0].y / nk);
+}
+
+// proj_to_site: H_imp - DC (src/SOLVER.cpp:514-521)
+__global__ void k_sub(int n, const double2 *a, const double2 *b, double2 *out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = csub(a[t], b[t]);
+}
+
+// magnetism == 0 spin average of SE_out (all nfreq+5 slots) and projNumMatrix (src/SOLVER.cpp:440-456)
+__global__ void k_spin_average(int d, int nslots, double2 *se, double2 *occ) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int npair = d / 2;
+    if (t >= (long long)(nslots + 1) * npair) return;
+    const int slot = (int)(t / npair), n = 2 * (int)(t % npair);
+    double2 *M = (slot < nslots) ? se + (size_t)slot * d * d : occ;
+    const double2 avg = cscale(cadd(DG_AT(M, d, n, n), DG_AT(M, d, n + 1, n + 1)), 0.5);
+    DG_AT(M, d, n, n) = avg;
+    DG_AT(M, d, n + 1, n + 1) = avg;
+    DG_AT(M, d, n, n + 1) = cmk(0, 0);
+    DG_AT(M, d, n + 1, n) = cmk(0, 0);
+}
+
+// SelfEnergy_w_out = SE_out - DC for w < N_freq (only these slots reach SelfEnergy_w, src/ImgTimeFtn.cpp:575-606)
+__global__ void k_se_combine(int nfreq, int d, const double2 *se, const double2 *dc, double2 *out) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int dd = d * d;
+    if (t >= (long long)nfreq * dd) return;
+    out[t] = csub(se[t], dc[t % dd]);
+}
+
+// Pulay: Gram entry g = sum_w Re Tr(r0^H rk) = sum over all elements of Re(conj(r0) rk)
+__global__ void k_dot_re(long long n, const double2 *a, const double2 *b, double *out) {
+    __shared__ double red[256];
+    double s = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        s += a[t].x * b[t].x + a[t].y * b[t].y;
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+__global__ void k_axpby(long long n, double a, const double2 *x, double b, const double2 *y, double2 *out) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = cadd(cscale(x[t], a), cscale(y[t], b));
+}
+
+// scf residual sums over n < N_freq (src/dmft_main.cpp:971-997): per frequency |Gimp - Gloc|^2, |Gloc|^2
+__global__ void k_scf_terms(int nfreq, int d, const double2 *gimp, const double2 *gloc, double *rd, double *nrm) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nfreq) return;
+    const int dd = d * d;
+    double a = 0, b = 0;
+    for (int e = 0; e < dd; e++) {
+        double2 x = csub(gimp[(size_t)n * dd + e], gloc[(size_t)n * dd + e]);
+        a += cabs2(x);
+        b += cabs2(gloc[(size_t)n * dd + e]);
+    }
+    rd[n] = a;
+    nrm[n] = b;
+}
+
+double2 *buf2(dmftgpu_ctx *ctx, const char *name, size_t count) {
+    return (double2 *)dg_buf(ctx, name, count * sizeof(double2));
+}
+
+// Eigen::FullPivLU(A).isInvertible() and A x = b for the small real DIIS matrix (complete pivoting)
+bool solve_full_pivot(int n, std::vector<double> A, std::vector<double> b, std::vector<double> &x) {
+    std::vector<int> cperm(n);
+    for (int i = 0; i < n; i++) cperm[i] = i;
+    double maxpiv = 0;
+    std::vector<double> piv(n);
+    for (int k = 0; k < n; k++) {
+        int pr = k, pc = k;
+        double best = -1;
+        for (int j = k; j < n; j++)
+            for (int i = k; i < n; i++)
+                if (std::fabs(A[i + j * n]) > best) {
+                    best = std::fabs(A[i + j * n]);
+                    pr = i;
+                    pc = j;
+                }
+        piv[k] = best;
+        maxpiv = std::max(maxpiv, best);
+        for (int j = 0; j < n; j++) std::swap(A[k + j * n], A[pr + j * n]);
+        std::swap(b[k], b[pr]);
+        for (int i = 0; i < n; i++) std::swap(A[i + k * n], A[i + pc * n]);
+        std::swap(cperm[k], cperm[pc]);
+        if (best == 0) continue;
+        for (int i = k + 1; i < n; i++) {
+            const double f = A[i + k * n] / A[k + k * n];
+            for (int j = k; j < n; j++) A[i + j * n] -= f * A[k + j * n];
+            b[i] -= f * b[k];
+        }
+    }
+    const double thr = 2.220446049250313e-16 * n * maxpiv;  // Eigen's default rank threshold
+    for (int k = 0; k < n; k++)
+        if (!(piv[k] > thr)) return false;
+    std::vector<double> y(n);
+    for (int i = n - 1; i >= 0; i--) {
+        double s = b[i];
+        for (int j = i + 1; j < n; j++) s -= A[i + j * n] * y[j];
+        y[i] = s / A[i + i * n];
+    }
+    x.assign(n, 0.0);
+    for (int k = 0; k < n; k++) x[cperm[k]] = y[k];
+    return true;
+}
+
+}  // namespace
+
+static int pulay_mixing(dmftgpu_ctx *ctx, DgPulay &P, long long len, double2 *in, double2 *out, double mixing, int it) {
+    const int h = P.hist, H1 = h + 1;
+    double2 *inh = buf2(ctx, "pulay.in", (size_t)h * len), *resh = buf2(ctx, "pulay.res", (size_t)h * len);
+    double *part = (double *)dg_buf(ctx, "pulay.part", 256 * sizeof(double));
+    if (!inh || !resh || !part) return DMFTGPU_NOMEM;
+    cudaStream_t s = ctx->stream;
+    if (P.len != len) {
+        P.len = len;
+        P.om.assign(H1 * H1, 0.0);
+        for (int k = 0; k < h; k++) {
+            P.om[h + k * H1] = -1;
+            P.om[k + h * H1] = -1;
+        }
+        P.om[(h - 1) + (h - 1) * H1] = -100.;
+        P.om[h + h * H1] = 0.;
+        DG_CUDA(cudaMemsetAsync(inh, 0, (size_t)h * len * sizeof(double2), s));
+        DG_CUDA(cudaMemsetAsync(resh, 0, (size_t)h * len * sizeof(double2), s));
+    }
+    const int removeComp = h - 1;
+    for (int k = removeComp; k > 0; k--) {
+        DG_CUDA(cudaMemcpyAsync(inh + (size_t)k * len, inh + (size_t)(k - 1) * len, len * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(resh + (size_t)k * len, resh + (size_t)(k - 1) * len, len * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, s));
+    }
+    DG_CUDA(cudaMemcpyAsync(inh, in, len * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    k_axpby<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, 1.0, out, -1.0, in, resh);  // res = out - in
+    DG_LAUNCH(ctx, "k_axpby");
+    if (it > P.start) {
+        std::vector<double> tmp((h - 1) * (h - 1));
+        for (int k = 0; k < h - 1; k++)
+            for (int l = 0; l < h - 1; l++) {
+                int ik = k >= removeComp ? k + 1 : k, il = l >= removeComp ? l + 1 : l;
+                tmp[k + l * (h - 1)] = P.om[ik + il * H1];
+            }
+        for (int k = 1; k < h; k++)
+            for (int l = 1; l < h; l++) P.om[k + l * H1] = tmp[(k - 1) + (l - 1) * (h - 1)];
+        for (int k = 0; k < h; k++) {
+            k_dot_re<<<256, 256, 0, s>>>(len, resh, resh + (size_t)k * len, part);
+            DG_LAUNCH(ctx, "k_dot_re");
+            double hp[256];
+            DG_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, s));
+            DG_CUDA(cudaStreamSynchronize(s));
+            double g = 0;
+            for (int q = 0; q < 256; q++) g += hp[q];
+            P.om[0 + k * H1] = g;
+            P.om[k + 0 * H1] = g;
+        }
+    }
+    std::vector<double> beta;
+    std::vector<double> rhs(H1, 0.0);
+    rhs[h] = -1;
+    const bool use = it > h + P.start && solve_full_pivot(H1, P.om, rhs, beta);
+    double2 *opt = buf2(ctx, "pulay.opt", len), *optr = buf2(ctx, "pulay.optr", len);
+    if (!opt || !optr) return DMFTGPU_NOMEM;
+    if (use) {
+        DG_CUDA(cudaMemsetAsync(opt, 0, len * sizeof(double2), s));
+        DG_CUDA(cudaMemsetAsync(optr, 0, len * sizeof(double2), s));
+        for (int k = 0; k < h; k++) {
+            k_axpby<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, 1.0, opt, beta[k], inh + (size_t)k * len, opt);
+            DG_LAUNCH(ctx, "k_axpby");
+            k_axpby<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, 1.0, optr, beta[k], resh + (size_t)k * len, optr);
+            DG_LAUNCH(ctx, "k_axpby");
+        }
+        k_axpby<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, 1.0, opt, mixing, optr, out);
+    } else {
+        k_axpby<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, 1.0, in, mixing, resh, out);
+    }
+    DG_LAUNCH(ctx, "k_axpby");
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk,
+                                      const dmftgpu_dmft_params *p, int iteration, double *selfe, double *weiss,
+                                      double *nummat, double *mu, double *gloc, double *gimp, double *resid,
+                                      int flags) {
+    if (!ctx || !L || !hk || !p || !selfe || !weiss || !nummat || !mu || !gloc || !gimp || !resid)
+        return DMFTGPU_BADARG;
+    if (!(flags & DMFTGPU_DEVICE_PTRS)) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: device pointers only");
+    if (p->solver != DMFTGPU_SOLVER_IPT) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: solver");
+    const int D = L->ncl * L->nh, Nf = L->nfreq, DD = D * D;
+    if (L->ncl != 1 || D != 2) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: one cluster of 2 spin-orbitals");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const int dflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NEWTON));
+    double2 *dSE = (double2 *)selfe, *dW = (double2 *)weiss, *dN = (double2 *)nummat, *dG = (double2 *)gloc,
+            *dGI = (double2 *)gimp;
+    DgUList Ul;
+    DG_TRY(dg_ulist(ctx, D, p->nu, p->uidx, p->ut, Ul));
+    double2 *himp = buf2(ctx, "dmft.himp", DD), *hdc = buf2(ctx, "dmft.hdc", DD), *dc = buf2(ctx, "dmft.dc", DD);
+    double2 *seimp = buf2(ctx, "dmft.seimp", (size_t)(Nf + 5) * DD), *seout = buf2(ctx, "dmft.seout", (size_t)Nf * DD);
+    double2 *occ = buf2(ctx, "dmft.occ", DD), *nm_imp = buf2(ctx, "dmft.nmimp", DD);
+    double *rd = (double *)dg_buf(ctx, "dmft.rd", 2 * (size_t)Nf * sizeof(double));
+    if (!himp || !hdc || !dc || !seimp || !seout || !occ || !nm_imp || !rd) return DMFTGPU_NOMEM;
+    // impurity_site_Hamiltonian (k average of H_PP) and the double counting (dc_for_dmft, nominal)
+    k_himp<<<DD, 256, 0, s>>>(L->nk, L->n, D, (const double2 *)hk, himp);
+    DG_LAUNCH(ctx, "k_himp");
+    {
+        const int Nh = D;  // N_peratom_HartrOrbit
+        const double averU = (Nh * p->U + Nh * (Nh - 1) * p->Uprime) / (double)(Nh * Nh);
+        const double v = averU * (p->nominal_charge - 0.5) - p->J * (p->nominal_charge / 2.0 - 0.5);
+        std::vector<double2> h(DD, make_double2(0, 0));
+        for (int i = 0; i < D; i++) h[i + i * D] = make_double2(p->dctype == DMFTGPU_DC_NOMINAL ? v : 0.0, 0.0);
+        DG_CUDA(cudaMemcpyAsync(dc, h.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+    }
+    // ---- SOLVER: proj_to_site, IPT, spin average, NumMatrix
+    k_sub<<<1, 64, 0, s>>>(DD, himp, dc, hdc);
+    DG_LAUNCH(ctx, "k_sub");
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, hdc, dW, dN, Ul, seimp, dGI, occ));
+    if (p->magnetism == 0) {
+        k_spin_average<<<dg_ceil_div((long long)(Nf + 6) * (D / 2), 128), 128, 0, s>>>(D, Nf + 5, seimp, occ);
+        DG_LAUNCH(ctx, "k_spin_average");
+    }
+    DG_CUDA(cudaMemcpyAsync(dN, occ, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    DG_CUDA(cudaMemcpyAsync(nm_imp, occ, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    k_se_combine<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, s>>>(Nf, D, seimp, dc, seout);
+    DG_LAUNCH(ctx, "k_se_combine");
+    // ---- Pulay mixing of SelfEnergy_w (w < N_freq)
+    if (!ctx->pulay) ctx->pulay = new DgPulay();
+    if (iteration <= 1) *ctx->pulay = DgPulay();
+    DG_TRY(pulay_mixing(ctx, *ctx->pulay, (long long)Nf * DD, dSE, seout, p->mixing, iteration));
+    DG_CUDA(cudaMemcpyAsync(dSE, seout, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    if (code) return code;
+    // ---- TightBinding: mu search, GreenFtn_w, Construct_hyb_delta
+    double mu_new = *mu;
+    int nev = 0;
+    DG_TRY(dmftgpu_adjust_mu(ctx, L, hk, selfe, *mu, 1.0, p->n_electrons, &mu_new, &nev, dflags));
+    *mu = mu_new;
+    DG_TRY(dmftgpu_greenftn_w(ctx, L, hk, selfe, *mu, gloc, nullptr, nummat, dflags & ~DMFTGPU_NEWTON));
+    std::vector<int> orb(D);
+    for (int i = 0; i < D; i++) orb[i] = i;
+    DG_TRY(dmftgpu_hyb_delta(ctx, D, orb.data(), Nf, L->beta, D, selfe, gloc, (const double *)himp, *mu, weiss,
+                             DMFTGPU_DEVICE_PTRS));
+    // ---- dmft_scf_check residuals
+    k_scf_terms<<<dg_ceil_div(Nf, 128), 128, 0, s>>>(Nf, D, dGI, dG, rd, rd + Nf);
+    DG_LAUNCH(ctx, "k_scf_terms");
+    std::vector<double> h(2 * (size_t)Nf);
+    std::vector<double2> nl(DD), ni(DD);
+    DG_CUDA(cudaMemcpyAsync(h.data(), rd, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(cudaMemcpyAsync(nl.data(), dN, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(cudaMemcpyAsync(ni.data(), nm_imp, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    double GwNorm = 1e-10, GwlowNorm = 1e-10, GwRD = 0, GwRD_low = 0, GwRD_max = 0;
+    const double wcut = std::min(p->U, 3.0);
+    for (int n = 0; n < Nf; n++) {
+        const double wn = DG_PI * (2. * n + 1) / L->beta;
+        if (wn < wcut) {
+            GwRD_low += h[n];
+            GwlowNorm += h[Nf + n];
+        }
+        GwRD += h[n];
+        GwNorm += h[Nf + n];
+        const double r = h[n] / (h[Nf + n] + 1e-10);
+        if (r > GwRD_max) GwRD_max = r;
+    }
+    double dn = 0, nn = 0;
+    for (int e = 0; e < DD; e++) {
+        dn += (nl[e].x - ni[e].x) * (nl[e].x - ni[e].x) + (nl[e].y - ni[e].y) * (nl[e].y - ni[e].y);
+        nn += nl[e].x * nl[e].x + nl[e].y * nl[e].y;
+    }
+    resid[0] = std::sqrt(GwRD / GwNorm);
+    resid[1] = std::sqrt(GwRD_low / GwlowNorm);
+    resid[2] = std::sqrt(GwRD_max);
+    resid[3] = std::sqrt(dn) / std::sqrt(nn);
+    return DMFTGPU_OK;
+}

@@ -9,6 +9,14 @@
 
 #include "dmftgpu.h"
 
+// DMFT-level Pulay mixer state (pulayMixing(2, 5, ...), src/pulay.cpp:11-46): history on the device, the
+// (hist+1) x (hist+1) DIIS matrix on the host
+struct DgPulay {
+    int hist = 2, start = 5;
+    long long len = 0;
+    std::vector<double> om;
+};
+
 struct dmftgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -23,6 +31,7 @@ struct dmftgpu_ctx {
     int *d_status = nullptr;          // device status word (max of kernel-reported codes)
     cudaStream_t side = nullptr;      // side stream for work that overlaps the main stream's kernels
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    DgPulay *pulay = nullptr;         // mixer state of dmftgpu_dmft_iteration
     bool timing = false;              // record CUDA events around the named hot kernels
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };

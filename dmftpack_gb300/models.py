@@ -125,3 +125,26 @@ def dp28(k=32, beta=40.0, nfreq=4096, ntau=8192, seed=20250105, rmax=4, U=4.0, J
         sigma[:, d, d] = -0.5j / (wn + 1.0)
     return Workload("dp28", n, rows, vals, (k, k, k), beta, nfreq, ntau, 1, 10, sigma, 20.0,
                     {"U": U, "J": J, "Up": U - 2 * J})
+
+
+def gen_Uijkl(n_spinorb, U, Uprime, JH, density_density=False):
+    """Interaction list (U_index (nu, 4) int32, U_tensor (nu,) complex) for H_int = 1/2 sum U_ijkl c+_i c+_j c_l c_k
+    on spin-orbitals ordered (orbital, spin) = (i // 2, i % 2): gen_Uijkl (Slater-Kanamori: density-density,
+    spin-flip and pair-hopping terms, src/gen_Uijkl.cpp:9-58) or gen_Uijkl_density_density (all (n, m, n, m),
+    src/gen_Uijkl.cpp:60-87).  Entries come in the reference's (i, j, k, l) loop order."""
+    n = int(n_spinorb)
+    if density_density:
+        a, b = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        a, b = a.ravel(), b.ravel()
+        v = np.where(a // 2 == b // 2, U, Uprime) - np.where(a % 2 == b % 2, JH, 0.0)
+        return np.stack([a, b, a, b], 1).astype(np.int32), v.astype(np.complex128)
+    i, j, k, l = (x.ravel() for x in np.meshgrid(*(np.arange(n),) * 4, indexing="ij"))
+    io, jo, ko, lo = i // 2, j // 2, k // 2, l // 2
+    is_, js, ks, ls = i % 2, j % 2, k % 2, l % 2
+    dd = (i == k) & (j == l)
+    flip = (ko == io) & (lo == jo) & (ko != lo) & (ks != is_) & (ls != js) & (ks != ls)
+    pair = (ko == lo) & (ko != io) & (io == jo) & (ks != ls) & (ks == is_) & (ls == js)
+    c = np.where(dd, np.where(io == jo, U, Uprime) - np.where(is_ == js, JH, 0.0),
+                 np.where(flip | pair, JH, 0.0))
+    keep = c != 0
+    return np.stack([i, j, k, l], 1)[keep].astype(np.int32), c[keep].astype(np.complex128)

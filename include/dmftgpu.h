@@ -145,6 +145,39 @@ int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, dou
                 const double *delta, const double *nummat_in, int nu, const int *uidx, const double *ut,
                 double *se_out, double *gimp_out, double *nummat_out, int flags);
 
+/* ---------------------------------------------------------------------------------------------
+ * One DMFT self-consistency iteration: the body of the loop of src/dmft_main.cpp:343-570 for one correlated
+ * cluster of two spin-orbitals solved by IPT (the example model of the reference).
+ * --------------------------------------------------------------------------------------------- */
+#define DMFTGPU_SOLVER_IPT 0
+#define DMFTGPU_DC_NONE 0
+#define DMFTGPU_DC_NOMINAL 1 /* dc_for_dmft "nominal" (src/dmft_main.cpp:665-677) */
+typedef struct {
+    int solver;            /* DMFTGPU_SOLVER_IPT */
+    int ntau;              /* N_TAU */
+    double n_electrons;    /* N_ELECTRONS: target of the mu search */
+    double U, Uprime, J;   /* U, U', J */
+    double mixing;         /* MIXING (Pulay, history 2, start 5) */
+    int magnetism;         /* MAGNETISM (0: spin-averaged self-energy and occupation) */
+    int dctype;            /* DMFTGPU_DC_* */
+    double nominal_charge; /* N_d */
+    int nu;                /* U_{ijkl} list of the correlated space (gen_Uijkl), host pointers */
+    const int *uidx;
+    const double *ut;
+} dmftgpu_dmft_params;
+
+/* SOLVER (IPT) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing
+ * of SelfEnergy_w (src/dmft_main.cpp:529-533), TightBinding's mu search, GreenFtn_w and Construct_hyb_delta
+ * (src/TB.cpp:297-331) and the dmft_scf_check residuals (src/dmft_main.cpp:902-1014), all on the device.
+ * Device pointers only (flags must contain DMFTGPU_DEVICE_PTRS; DMFTGPU_MIXED / DMFTGPU_NEWTON select the
+ * lattice-sum precision and the mu search).  State, updated in place: selfe[nfreq][D][D] (SelfEnergy_w),
+ * weiss[nfreq][D][D] (weiss_fieldTB), nummat[D][D] (NumMatrix), *mu (host).  Outputs: gloc[nfreq][D][D],
+ * gimp[nfreq+5][D][D] and resid[4] (host) = GwRD, GwRD_low, GwRD_max, NumMatRD.  `iteration` is the
+ * reference's currentIt (1 on the first call restarts the mixer history). */
+int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk,
+                           const dmftgpu_dmft_params *params, int iteration, double *selfe, double *weiss,
+                           double *nummat, double *mu, double *gloc, double *gimp, double *resid, int flags);
+
 /* No counterpart in the reference.  Construct_hyb_delta for callers that cannot allocate device memory
  * (a driver whose HBM belongs to a pool allocator, or one that must not stall the device with a
  * non-stream-ordered cudaMalloc): no context, no allocation, every array argument a DEVICE pointer except

@@ -303,3 +303,89 @@ def ipt(himp, delta, nummat, uidx, ut, U, mu, beta, ntau):
                        _i(uidx), _d(ut.view(np.float64)), _d(se.view(np.float64)), _d(gi.view(np.float64)),
                        _d(nm.view(np.float64)))
     return from_cm(se), from_cm(gi), from_cm(nm[None])[0], st
+
+
+# ---------------------------------------------------------------------------------------------------------
+# Pulay mixer and one DMFT iteration, composed from the functions above (numpy restatement of the glue)
+# ---------------------------------------------------------------------------------------------------------
+class Pulay:
+    """pulayMixing(mixing_history, start_mixing, ...) with parallel_pulay (src/pulay.cpp:11-167)."""
+
+    def __init__(self, hist=2, start=5):
+        self.h, self.start = hist, start
+        self.inp = None
+        self.om = np.zeros((hist + 1, hist + 1))
+        for k in range(hist):
+            self.om[hist, k] = -1
+            self.om[k, hist] = -1
+            self.om[hist - 1, hist - 1] = -100.0
+        self.om[hist, hist] = 0.0
+
+    def mixing(self, inp, out, mix, it, step=1):
+        h = self.h
+        if self.inp is None:
+            self.inp = [np.zeros_like(inp) for _ in range(h)]
+            self.res = [np.zeros_like(inp) for _ in range(h)]
+        rc = h - 1
+        for k in range(rc, 0, -1):
+            self.inp[k] = self.inp[k - 1].copy()
+            self.res[k] = self.res[k - 1].copy()
+        self.inp[0] = inp.copy()
+        self.res[0] = out - inp
+        if it > self.start:
+            idx = [k if k < rc else k + 1 for k in range(h - 1)]
+            tmp = self.om[np.ix_(idx, idx)].copy()
+            self.om[1:h, 1:h] = tmp
+            for k in range(h):
+                g = float(np.sum(np.real(np.conj(self.res[0]) * self.res[k])))
+                self.om[0, k] = g
+                self.om[k, 0] = g
+        use = False
+        if it > h + self.start and it % step == 0:
+            use = np.linalg.matrix_rank(self.om) == h + 1
+        if use:
+            rhs = np.zeros(h + 1)
+            rhs[h] = -1
+            beta = np.linalg.solve(self.om, rhs)
+            opt = sum(beta[k] * self.inp[k] for k in range(h))
+            optr = sum(beta[k] * self.res[k] for k in range(h))
+        else:
+            opt, optr = inp, self.res[0]
+        return opt + mix * optr
+
+
+def dmft_iteration(H, state, p, it, pulay):
+    """The dmft_main loop body for one cluster of 2 spin-orbitals with IPT (src/dmft_main.cpp:343-570):
+    state = dict(selfe, weiss, nummat, mu, beta); p = dict(ntau, n_electrons, U, Uprime, J, mixing, uidx, ut,
+    nominal_charge).  Returns (new state, gloc, gimp, residuals)."""
+    beta, D = state["beta"], 2
+    nf = state["selfe"].shape[0]
+    himp = H[:, :D, :D].mean(0)
+    averU = (D * p["U"] + D * (D - 1) * p["Uprime"]) / (D * D)
+    dc = (averU * (p["nominal_charge"] - 0.5) - p["J"] * (p["nominal_charge"] / 2 - 0.5)) * np.eye(D)
+    se, gi, nm, st = ipt(himp - dc, state["weiss"], state["nummat"], p["uidx"], p["ut"], p["U"], state["mu"], beta,
+                         p["ntau"])
+    if st != 0:
+        raise RuntimeError("oracle IPT status %d" % st)
+    for M in list(se) + [nm]:
+        for n in range(0, D, 2):
+            avg = (M[n, n] + M[n + 1, n + 1]) / 2
+            M[n, n] = M[n + 1, n + 1] = avg
+            M[n, n + 1] = M[n + 1, n] = 0
+    nm_imp = nm.copy()
+    seout = se[:nf] - dc[None]
+    selfe = pulay.mixing(state["selfe"], seout, p["mixing"], it)
+    mu, nev = adjust_mu(H, selfe, state["mu"], beta, 1, D, p["n_electrons"])
+    gloc, _, nummat = greenftn_w(H, selfe, mu, beta, 1, D)
+    weiss = hyb_delta(list(range(D)), selfe, gloc, himp, mu, beta)
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    d2 = np.abs(gi[:nf] - gloc) ** 2
+    n2 = np.abs(gloc) ** 2
+    low = wn < min(p["U"], 3.0)
+    rd_n = d2.sum((1, 2))
+    nr_n = n2.sum((1, 2))
+    res = [np.sqrt(rd_n.sum() / (1e-10 + nr_n.sum())), np.sqrt(rd_n[low].sum() / (1e-10 + nr_n[low].sum())),
+           np.sqrt(np.max(np.concatenate([[0.0], rd_n / (1e-10 + nr_n)]))),
+           np.linalg.norm(nummat - nm_imp) / np.linalg.norm(nummat)]
+    new = dict(state, selfe=selfe, weiss=weiss, nummat=nummat, mu=mu)
+    return new, gloc, gi, np.array(res)

@@ -45,3 +45,11 @@ def test_hwr_round_trip_and_reference_example():
     if os.path.exists(ex):  # only in the build container
         norb, r, h = hwr.read_hr(ex, num_atoms=1)
         assert norb == [2] and r.shape == (8, 5) and np.allclose(h, -0.25)
+
+
+@pytest.mark.parametrize("nso,dd", [(2, True), (2, False), (6, False), (10, True), (10, False)])
+def test_gen_uijkl_matches_oracle(orc, nso, dd):
+    from dmftpack_gb300 import models
+    ui, ut = models.gen_Uijkl(nso, 4.0, 2.6, 0.7, density_density=dd)
+    oi, ot = orc.gen_uijkl(nso, 4.0, 2.6, 0.7, density_density=dd)
+    assert np.array_equal(ui, oi) and np.array_equal(ut, ot)

@@ -115,3 +115,42 @@ def test_ipt_matches_oracle(ctx, orc):
     assert rel_err(g_gi[:nf], gi[:nf]) < TOL
     assert rel_err(g_gi[nf + 1:nf + 4], gi[nf + 1:nf + 4]) < 1e-9
     assert rel_err(g_nm, nm) < TOL
+
+
+def _dmft_setup(orc, nfreq=64, kx=8, beta=10.0):
+    wl = models.hubbard_2d(kx=kx, ky=kx, nfreq=nfreq, beta=beta)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    U = wl.extra["U"]
+    uidx, ut = orc.gen_uijkl(2, U, U, 0.0, density_density=True)
+    p = dict(ntau=4 * nfreq, n_electrons=1.0, U=U, Uprime=U, J=0.0, mixing=0.5, magnetism=0, dctype=1,
+             nominal_charge=1.0, uidx=uidx, ut=ut)
+    # the first TightBinding call of dmft_main (src/dmft_main.cpp:300)
+    mu, _ = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, 1, 2, 1.0)
+    gloc, _, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, 1, 2)
+    weiss = orc.hyb_delta([0, 1], wl.sigma, gloc, H[:, :2, :2].mean(0), mu, wl.beta)
+    state = dict(selfe=wl.sigma.copy(), weiss=weiss, nummat=num, mu=mu, beta=wl.beta)
+    return wl, H, p, state
+
+
+def test_dmft_iterations_match_oracle(ctx, orc):
+    """Nine dmft_main iterations (IPT, Pulay with the DIIS step from iteration 8, bisection mu) on the device
+    against the oracle composition."""
+    import torch
+    from dmftpack_gb300 import lib
+    wl, H, p, state = _dmft_setup(orc)
+    dev = torch.device("cuda:0")
+    cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
+    Hd, se, we, nm = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["nummat"][None])[0].contiguous()
+    mu_g = state["mu"]
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
+    pulay = orc.Pulay()
+    for it in range(1, 10):
+        state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
+        mu_g, gloc_g, gimp_g, res_g = ctx.DMFT_iteration(lat, Hd, p, it, se, we, nm, mu_g)
+        torch.cuda.synchronize()
+        back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
+        assert abs(mu_g - state["mu"]) < 1e-12, it
+        assert rel_err(back(se), state["selfe"]) < 1e-9, it
+        assert rel_err(back(gloc_g), gloc) < 1e-9, it
+        assert rel_err(back(we), state["weiss"]) < 1e-9, it
+        assert np.allclose(res_g, res, rtol=1e-6, atol=1e-12), (it, res_g, res)
