@@ -7,6 +7,7 @@ import concurrent.futures as cf
 import glob
 import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -43,6 +44,18 @@ def _stamp():
     return h.hexdigest()
 
 
+def _headers_hash():
+    h = hashlib.sha256()
+    h.update(" ".join(NVCC_FLAGS).encode())
+    h.update(platform.machine().encode())
+    for p in sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+                    + glob.glob(os.path.join(INCLUDE, "*.h"))):
+        h.update(os.path.basename(p).encode())
+        with open(p, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
 def build(verbose=False, force=False):
     """Compile every CUDA translation unit for sm_103a and link libdmftgpu.so; returns its path."""
     os.makedirs(os.path.join(BUILD, "obj"), exist_ok=True)
@@ -56,12 +69,23 @@ def build(verbose=False, force=False):
     srcs = _sources()
     objs = [os.path.join(BUILD, "obj", os.path.basename(s)[:-3] + ".o") for s in srcs]
 
+    hh = _headers_hash()
+
     def compile_one(pair):
         src, obj = pair
+        with open(src, "rb") as f:
+            key = hashlib.sha256(hh.encode() + f.read()).hexdigest()
+        key_path = obj + ".key"
+        if not force and os.path.exists(obj) and os.path.exists(key_path):
+            with open(key_path) as f:
+                if f.read().strip() == key:
+                    return obj  # this object is up to date for this machine, flags and headers
         cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+        with open(key_path, "w") as f:
+            f.write(key)
         if verbose:
             print("compiled", os.path.basename(src), flush=True)
         return obj

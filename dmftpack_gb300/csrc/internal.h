@@ -32,6 +32,8 @@ struct dmftgpu_ctx {
     cudaStream_t side = nullptr;      // side stream for work that overlaps the main stream's kernels
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     DgPulay *pulay = nullptr;         // mixer state of dmftgpu_dmft_iteration
+    double scgf_prev_norm = 0.0;      // mixing_check_outer's previous residual (a function static in the
+                                      // reference, src/SCGF2_fullLoop.cpp:722-727): kept across SCGF2 calls
     bool timing = false;              // record CUDA events around the named hot kernels
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
@@ -76,6 +78,10 @@ int dg_out_done(dmftgpu_ctx *ctx, void *host, const void *dev, size_t bytes, int
 // internal device-to-device entry points (all pointers device, enqueue only)
 int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const double2 *fw, int green,
                    double2 *mom);
+// Pulay mixing (mixing.cu): on return `out` holds the mixed input for the next iteration; `tag` names the
+// history workspaces of this mixer instance
+int dg_pulay_mixing(dmftgpu_ctx *ctx, DgPulay &P, const char *tag, long long len, double2 *in, double2 *out,
+                    double mixing, int it);
 
 #define DG_LAUNCH(ctx, what)                     \
     do {                                         \
