@@ -216,13 +216,13 @@ def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
         mu, _ = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, 1.0, mixed=mixed)
         gl, _, nm = ctx.GreenFtn_w(lat, Hd, sig, mu, mixed=mixed, with_gwhf=False)
         we = ctx.Construct_hyb_delta([0, 1], sig, gl, mu, wl.beta, himp)
-        se, we, nm = tcm(sig), tcm(we), tcm(nm)
+        se, we, nm, gl = tcm(sig), tcm(we), tcm(nm), tcm(gl)
         times, res = [], None
         for it in range(1, n_iter + 1):
             torch.cuda.synchronize()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            mu, gl, gi, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, mu, mixed=mixed)
+            mu, gi, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, gl, mu, mixed=mixed)
             e.record(stream)
             e.synchronize()
             times.append(s.elapsed_time(e) / 1e3)

@@ -1,7 +1,9 @@
 // dmft.cu -- one DMFT self-consistency iteration (the body of the loop in src/dmft_main.cpp:343-570) for a
-// single correlated cluster/atom with the IPT impurity solver, every array on the device:
-//   SOLVER (src/SOLVER.cpp:105-502): proj_to_site (H_imp - DC), IPT, the magnetism == 0 spin average,
-//     NumMatrix update; SE_out = Sigma_imp - DC (src/dmft_main.cpp:489-525)
+// single correlated cluster/atom with the IPT or the SC2PT (SCGF2) impurity solver, every array on the device:
+//   SOLVER (src/SOLVER.cpp:105-502): proj_to_site (H_imp - DC), IPT or SCGF2 (the latter started from the
+//     lattice G_loc block, src/dmft_main.cpp:389-405), the magnetism == 0 spin average, NumMatrix update
+//     (IPT's occupation; SCGF2 leaves projNumMatrix as proj_to_site copied it); SE_out = Sigma_imp - DC
+//     (src/dmft_main.cpp:489-525)
 //   Pulay mixing of SelfEnergy_w (pulayMixing(2, 5, N_freq, D, D), used at src/dmft_main.cpp:529-533;
 //     mixing.cu)
 //   TightBinding (src/TB.cpp:97-369): mu search, GreenFtn_w, Construct_hyb_delta, impurity_site_Hamiltonian
@@ -17,13 +19,16 @@
 int dg_ipt_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double U, double mu, const double2 *himp,
                const double2 *delta, const double2 *occ_in, const DgUList &Ul, double2 *se_out, double2 *gimp_out,
                double2 *occ_out);
+int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double mu, double mixing,
+                 const double2 *himp, const double2 *weiss, double2 *gimp, const DgUList &Ul, int max_iter,
+                 double2 *se_out, int *loops);
 
 namespace {
 
-// k average of the correlated block of H(k)
-__global__ void k_himp(int nk, int n, int D, const double2 *H, double2 *himp) {
+// k average of the correlated block of H(k): rows/columns hartr[a], hartr[b]
+__global__ void k_himp(int nk, int n, int D, const int *hartr, const double2 *H, double2 *himp) {
     __shared__ double2 red[256];
-    const int e = blockIdx.x, a = e % D, b = e / D;
+    const int e = blockIdx.x, a = hartr[e % D], b = hartr[e / D];
     double2 s = cmk(0, 0);
     for (int k = threadIdx.x; k < nk; k += blockDim.x) s = cadd(s, H[(size_t)k * n * n + a + (size_t)b * n]);
     red[threadIdx.x] = s;
@@ -91,9 +96,14 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     if (!ctx || !L || !hk || !p || !selfe || !weiss || !nummat || !mu || !gloc || !gimp || !resid)
         return DMFTGPU_BADARG;
     if (!(flags & DMFTGPU_DEVICE_PTRS)) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: device pointers only");
-    if (p->solver != DMFTGPU_SOLVER_IPT) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: solver");
+    if (p->solver != DMFTGPU_SOLVER_IPT && p->solver != DMFTGPU_SOLVER_SC2PT)
+        return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: solver");
     const int D = L->ncl * L->nh, Nf = L->nfreq, DD = D * D;
-    if (L->ncl != 1 || D != 2) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: one cluster of 2 spin-orbitals");
+    if (L->ncl != 1) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: one correlated cluster");
+    if (p->solver == DMFTGPU_SOLVER_IPT && D != 2)
+        return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: IPT needs 2 spin-orbitals");
+    if (D > 32 || (p->magnetism == 0 && D % 2))
+        return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: correlated block must be <= 32 spin-orbital pairs");
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     const int dflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NEWTON));
@@ -105,9 +115,18 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     double2 *seimp = buf2(ctx, "dmft.seimp", (size_t)(Nf + 5) * DD), *seout = buf2(ctx, "dmft.seout", (size_t)Nf * DD);
     double2 *occ = buf2(ctx, "dmft.occ", DD), *nm_imp = buf2(ctx, "dmft.nmimp", DD);
     double *rd = (double *)dg_buf(ctx, "dmft.rd", 2 * (size_t)Nf * sizeof(double));
-    if (!himp || !hdc || !dc || !seimp || !seout || !occ || !nm_imp || !rd) return DMFTGPU_NOMEM;
+    int *dhartr = (int *)dg_buf(ctx, "dmft.hartr", D * sizeof(int));
+    if (!himp || !hdc || !dc || !seimp || !seout || !occ || !nm_imp || !rd || !dhartr) return DMFTGPU_NOMEM;
+    {
+        std::vector<int> h(D);
+        for (int i = 0; i < D; i++) h[i] = L->hartr ? L->hartr[i] : i;
+        for (int i = 0; i < D; i++)
+            if (h[i] < 0 || h[i] >= L->n) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: bad HartrIndex");
+        DG_CUDA(cudaMemcpyAsync(dhartr, h.data(), D * sizeof(int), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+    }
     // impurity_site_Hamiltonian (k average of H_PP) and the double counting (dc_for_dmft, nominal)
-    k_himp<<<DD, 256, 0, s>>>(L->nk, L->n, D, (const double2 *)hk, himp);
+    k_himp<<<DD, 256, 0, s>>>(L->nk, L->n, D, dhartr, (const double2 *)hk, himp);
     DG_LAUNCH(ctx, "k_himp");
     {
         const int Nh = D;  // N_peratom_HartrOrbit
@@ -118,11 +137,20 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
         DG_CUDA(cudaMemcpyAsync(dc, h.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
         DG_CUDA(cudaStreamSynchronize(s));
     }
-    // ---- SOLVER: proj_to_site, IPT, spin average, NumMatrix
-    k_sub<<<1, 64, 0, s>>>(DD, himp, dc, hdc);
+    // ---- SOLVER: proj_to_site, IPT or SCGF2, spin average, NumMatrix
+    k_sub<<<dg_ceil_div(DD, 64), 64, 0, s>>>(DD, himp, dc, hdc);
     DG_LAUNCH(ctx, "k_sub");
     DG_TRY(dg_status_reset(ctx));
-    DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, hdc, dW, dN, Ul, seimp, dGI, occ));
+    int loops = 0;
+    if (p->solver == DMFTGPU_SOLVER_IPT) {
+        DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, hdc, dW, dN, Ul, seimp, dGI, occ));
+    } else {
+        // Gw_strong: the lattice G_loc of the last TightBinding call starts the SCGF2 loop
+        DG_CUDA(cudaMemcpyAsync(dGI, dG, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_scgf2_dev(ctx, D, Nf, p->ntau, L->beta, *mu, p->mixing, hdc, dW, dGI, Ul,
+                            p->scgf_max_iter > 0 ? p->scgf_max_iter : 2000, seimp, &loops));
+        DG_CUDA(cudaMemcpyAsync(occ, dN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    }
     if (p->magnetism == 0) {
         k_spin_average<<<dg_ceil_div((long long)(Nf + 6) * (D / 2), 128), 128, 0, s>>>(D, Nf + 5, seimp, occ);
         DG_LAUNCH(ctx, "k_spin_average");
@@ -180,5 +208,6 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     resid[1] = std::sqrt(GwRD_low / GwlowNorm);
     resid[2] = std::sqrt(GwRD_max);
     resid[3] = std::sqrt(dn) / std::sqrt(nn);
+    resid[4] = loops;
     return DMFTGPU_OK;
 }

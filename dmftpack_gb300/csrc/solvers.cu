@@ -2,6 +2,11 @@
 //   IPT (src/SCGF2_fullLoop.cpp:873-1065): Kajueter-Kotliar interpolated second-order self-energy on two
 //   spin-orbitals.  The host only sequences kernels and reads back the two 2x2 occupation matrices the
 //   interpolation coefficients need.
+//   SCGF2 (src/SCGF2_fullLoop.cpp:392-533): the self-consistent second-order (SC2PT) loop on G_imp with Pulay
+//   mixing.  The host reads back two residual norms and the status word per loop iteration (the loop's
+//   stopping test).
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -35,6 +40,43 @@ __global__ void k_write_results(int d, int nfreq, const double2 *s2, const doubl
     }
     se_out[t] = se;
     if (gimp_out) gimp_out[t] = g;
+}
+
+// MatsubaraFtnnorm (src/SCGF2_fullLoop.cpp:791-805) of g - gin (gin == nullptr: of g) squared, and
+// ||occ - occ_in||_F^2; one block, fixed-order reduction
+__global__ void k_scgf_norms(int d, int nfreq, double beta, const double2 *gin, const double2 *g,
+                             const double2 *occ_in, const double2 *occ, double *out) {
+    __shared__ double red[256];
+    const size_t dd = (size_t)d * d;
+    double s = 0;
+    for (int n = threadIdx.x; n < nfreq; n += blockDim.x) {
+        const double wn = (2 * n + 1) * DG_PI / beta;
+        double a = 0;
+        for (size_t e = 0; e < dd; e++) {
+            const double2 x = gin ? csub(gin[(size_t)n * dd + e], g[(size_t)n * dd + e]) : g[(size_t)n * dd + e];
+            a += cabs2(x);
+        }
+        s += a / wn;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double o = 0;
+        if (occ_in)
+            for (size_t e = 0; e < dd; e++) o += cabs2(csub(occ[e], occ_in[e]));
+        out[0] = red[0];
+        out[1] = o;
+    }
+}
+
+// (1 - a) x + a y over n elements (the linear mixing branch of SCGF2, :481-485)
+__global__ void k_lin_mix(long long n, double a, const double2 *x, double2 *y) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) y[t] = cadd(cscale(x[t], 1.0 - a), cscale(y[t], a));
 }
 
 }  // namespace
@@ -91,6 +133,120 @@ int dg_ipt_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double
                                                                                   gimp_out);
     DG_LAUNCH(ctx, "k_write_results");
     return DMFTGPU_OK;
+}
+
+// SCGF2 on device pointers.  weiss: nfreq slots; gimp: in, nfreq slots (the initial G_imp); out, nfreq+5
+// slots; se_out: nfreq+5 slots.  *loops receives the number of loop iterations run.
+int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, double mu, double mixing,
+                 const double2 *himp, const double2 *weiss, double2 *gimp, const DgUList &Ul, int max_iter,
+                 double2 *se_out, int *loops) {
+    const size_t dd = (size_t)d * d;
+    const long long len = (long long)nfreq * dd;
+    cudaStream_t s = ctx->stream;
+    double2 *G = (double2 *)dg_buf(ctx, "scgf.g", (size_t)(nfreq + 4) * dd * sizeof(double2));
+    double2 *Gin = (double2 *)dg_buf(ctx, "scgf.gin", (size_t)nfreq * dd * sizeof(double2));
+    double2 *s2 = (double2 *)dg_buf(ctx, "scgf.s2", (size_t)(nfreq + 3) * dd * sizeof(double2));
+    double2 *gt = (double2 *)dg_buf(ctx, "scgf.gt", (size_t)(ntau + 1) * dd * sizeof(double2));
+    double2 *st = (double2 *)dg_buf(ctx, "scgf.st", (size_t)(ntau + 1) * dd * sizeof(double2));
+    double2 *occ = (double2 *)dg_buf(ctx, "scgf.occ", 2 * dd * sizeof(double2));
+    double2 *fock = (double2 *)dg_buf(ctx, "scgf.fock", dd * sizeof(double2));
+    double *nrm = (double *)dg_buf(ctx, "scgf.norms", 2 * sizeof(double));
+    if (!G || !Gin || !s2 || !gt || !st || !occ || !fock || !nrm) return DMFTGPU_NOMEM;
+    double2 *occ_in = occ + dd;
+    DG_CUDA(cudaMemsetAsync(G, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemsetAsync(s2, 0, (size_t)(nfreq + 3) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemsetAsync(fock, 0, dd * sizeof(double2), s));
+    DG_CUDA(cudaMemcpyAsync(G, gimp, len * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    double2 *Gtail = G + (size_t)nfreq * dd;  // Gwimp[N_freq] = I (the m1 tail of every transform of G)
+    k_set_identity<<<1, 32 * (int)((dd + 31) / 32), 0, s>>>(d, Gtail);
+    DG_LAUNCH(ctx, "k_set_identity");
+    DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
+    k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, beta, nullptr, G, nullptr, occ, nrm);
+    DG_LAUNCH(ctx, "k_scgf_norms");
+    double hn[2];
+    DG_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    const double normUnit = std::sqrt(hn[0]);
+    int loop = 0;
+    double normOuter = 0, normOcc = 0, mix = mixing / 10.;
+    DgPulay P;
+    P.hist = 2;
+    P.start = 100;
+    while ((loop < 10 || normOuter > 1e-6 || normOcc > 1e-6) && loop < max_iter) {
+        DG_CUDA(cudaMemcpyAsync(Gin, G, len * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(occ_in, occ, dd * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        // HF
+        DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
+        DG_TRY(dg_fock_dev(ctx, d, Ul, occ, fock));
+        // Sigma^(2): G(iw) -> G(tau) (green tail, m1 = I) -> Sigma(tau) -> Sigma(iw)
+        DG_TRY(dg_fourier_dev(ctx, d, nfreq, ntau, beta, G, 1, Gtail, gt));
+        DG_TRY(dg_sigma2_dev(ctx, d, ntau, beta, Ul, gt, st));
+        DG_TRY(dg_tau2w_dev(ctx, d, nfreq, ntau, beta, st, s2, true));
+        // G = [(iw + mu) - H_imp - Delta - F - Sigma^(2)]^-1
+        DG_TRY(dg_dyson_dev(ctx, d, nfreq, beta, mu, himp, weiss, fock, s2, G, true));
+        DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
+        k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, beta, Gin, G, occ_in, occ, nrm);
+        DG_LAUNCH(ctx, "k_scgf_norms");
+        DG_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s));
+        int code = 0;
+        DG_TRY(dg_status_read(ctx, &code));  // synchronises the stream
+        if (code) return code;
+        normOcc = std::sqrt(hn[1]);
+        normOuter = std::sqrt(hn[0]) / normUnit;
+        if (loop % 500 == 0) mix /= 1.5;
+        if (loop < 1500) {
+            DG_TRY(dg_pulay_mixing(ctx, P, "scgf.pulay", len, Gin, G, mix, loop));
+        } else {
+            k_lin_mix<<<dg_ceil_div(len, 256), 256, 0, s>>>(len, mix, Gin, G);
+            DG_LAUNCH(ctx, "k_lin_mix");
+        }
+        // mixing_check_outer (:722-727)
+        if (loop % 10 == 0) {
+            double &prev = ctx->scgf_prev_norm;
+            if (prev > normOuter) mix = std::min(1.07 * mix, 0.5);
+            else if (prev < normOuter) mix = std::max(1. / 1.09 * mix, 1e-3);
+            prev = normOuter;
+        }
+        loop++;
+    }
+    *loops = loop;
+    // writeResults (:696-720)
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 1));
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 2));
+    k_write_results<<<dg_ceil_div((long long)(nfreq + 5) * dd, 128), 128, 0, s>>>(d, nfreq, s2, fock, G, se_out,
+                                                                                  gimp);
+    DG_LAUNCH(ctx, "k_write_results");
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_scgf2(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double mu, double mixing,
+                             const double *himp, const double *weiss, double *gimp, int nu, const int *uidx,
+                             const double *ut, int max_iter, double *se_out, int *loops, int flags) {
+    if (!ctx || dim < 1 || dim > 32 || nfreq < 8 || ntau < 2 || !himp || !weiss || !gimp || !se_out || !loops ||
+        nu < 0 || !(beta > 0) || max_iter < 1)
+        return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    DgUList Ul;
+    DG_TRY(dg_ulist(ctx, dim, nu, uidx, ut, Ul));
+    const double2 *dH = (const double2 *)dg_in(ctx, himp, dd * sizeof(double2), flags, "io.scgf_h", &st);
+    if (st) return st;
+    const double2 *dW = (const double2 *)dg_in(ctx, weiss, nfreq * dd * sizeof(double2), flags, "io.scgf_w", &st);
+    if (st) return st;
+    double2 *dG = (double2 *)dg_out(ctx, gimp, (nfreq + 5) * dd * sizeof(double2), flags, "io.scgf_g", &st);
+    if (st) return st;
+    if (!(flags & DMFTGPU_DEVICE_PTRS))
+        DG_CUDA(cudaMemcpyAsync(dG, gimp, nfreq * dd * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    double2 *dSE = (double2 *)dg_out(ctx, se_out, (nfreq + 5) * dd * sizeof(double2), flags, "io.scgf_se", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_scgf2_dev(ctx, dim, nfreq, ntau, beta, mu, mixing, dH, dW, dG, Ul, max_iter, dSE, loops));
+    DG_TRY(dg_out_done(ctx, gimp, dG, (nfreq + 5) * dd * sizeof(double2), flags));
+    DG_TRY(dg_out_done(ctx, se_out, dSE, (nfreq + 5) * dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
 }
 
 extern "C" int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double U, double mu,

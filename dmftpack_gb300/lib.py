@@ -33,7 +33,7 @@ EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
            "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
-           "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_dmft_iteration",
+           "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
 
 
@@ -47,7 +47,8 @@ class DmftParams(C.Structure):
     """dmftgpu_dmft_params (include/dmftgpu.h)."""
     _fields_ = [("solver", C.c_int), ("ntau", C.c_int), ("n_electrons", C.c_double), ("U", C.c_double),
                 ("Uprime", C.c_double), ("J", C.c_double), ("mixing", C.c_double), ("magnetism", C.c_int),
-                ("dctype", C.c_int), ("nominal_charge", C.c_double), ("nu", C.c_int), ("uidx", _ip), ("ut", _dp)]
+                ("dctype", C.c_int), ("nominal_charge", C.c_double), ("nu", C.c_int), ("uidx", _ip), ("ut", _dp),
+                ("scgf_max_iter", C.c_int)]
 
 
 class _Lat(C.Structure):
@@ -104,6 +105,8 @@ def load(require_built=True):
     lib.dmftgpu_estimate_asymto.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, C.c_int, C.c_int]
     lib.dmftgpu_ipt.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp,
                                 C.c_int, _ip, _dp, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_scgf2.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp,
+                                  C.c_int, _ip, _dp, C.c_int, _vp, P(C.c_int), C.c_int]
     lib.dmftgpu_dmft_iteration.argtypes = [_vp, P(_Lat), _vp, P(DmftParams), C.c_int, _vp, _vp, _vp, _dp, _vp, _vp,
                                            _dp, C.c_int]
     lib.dmftgpu_hyb_delta_noalloc.argtypes = [C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
@@ -411,32 +414,53 @@ class Context:
         self._check("dmftgpu_ipt", st)
         return se.result(), gi.result(), no.result()[0]
 
+    def SCGF2(self, himp, weiss_field, Gwimp, uidx, ut, mu, beta, ntau, mixing, max_iter=2000):
+        """SC2PT solver (SCGF2): Gwimp (nfreq slots) is the initial G_imp.  Returns (SE_out[nfreq+5],
+        Gwimp_out[nfreq+5], loops)."""
+        dev = _is_torch(weiss_field)
+        one = (lambda x: x[None]) if not dev else (lambda x: x.unsqueeze(0))
+        h, dl = _Arr(one(himp), dev), _Arr(weiss_field, dev)
+        nf, d = dl.obj.shape[0], dl.obj.shape[1]
+        g = _Arr.empty((nf + 5, d, d), dev, like=dl.obj)
+        g.obj[:nf] = _Arr(Gwimp[:nf], dev).obj
+        uidx, ut, nu = self._ulist(uidx, ut)
+        se = _Arr.empty((nf + 5, d, d), dev, like=dl.obj)
+        loops = C.c_int()
+        st = self.lib.dmftgpu_scgf2(self.h, d, nf, ntau, float(beta), float(mu), float(mixing), _vp(h.ptr),
+                                    _vp(dl.ptr), _vp(g.ptr), nu, uidx.ctypes.data_as(_ip),
+                                    ut.view(np.float64).ctypes.data_as(_dp), int(max_iter), _vp(se.ptr),
+                                    C.byref(loops), self._flags(dev))
+        self._check("dmftgpu_scgf2", st)
+        return se.result(), g.result(), loops.value
+
     # ------------------------------------------------------------------ DMFT iteration
-    def DMFT_iteration(self, lat, Hk_cm, params, iteration, selfe_cm, weiss_cm, nummat_cm, mu, mixed=False,
-                       newton=False):
+    def DMFT_iteration(self, lat, Hk_cm, params, iteration, selfe_cm, weiss_cm, nummat_cm, gloc_cm, mu,
+                       mixed=False, newton=False):
         """One dmft_main loop iteration on device state kept in the library's column-major layout (CUDA
-        tensors, updated in place).  params: dict(ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype,
-        nominal_charge, uidx, ut).  Returns (mu, gloc_cm, gimp_cm, residuals[4])."""
+        tensors, updated in place: SelfEnergy_w, weiss_fieldTB, NumMatrix, G_loc).  params: dict(solver ("IPT" or
+        "SC2PT"), ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype, nominal_charge, uidx, ut,
+        scgf_max_iter).  Returns (mu, gimp_cm[nfreq+5], residuals[5] = GwRD, GwRD_low, GwRD_max, NumMatRD,
+        SCGF2 loops)."""
         import torch
         nf, D = lat.nfreq, lat.D
         uidx = np.ascontiguousarray(params["uidx"], np.int32).reshape(-1, 4)
         ut = np.ascontiguousarray(params["ut"], np.complex128).reshape(-1)
-        P = DmftParams(0, params["ntau"], params["n_electrons"], params["U"], params["Uprime"], params["J"],
+        solver = {"IPT": 0, "SC2PT": 1}[params.get("solver", "IPT")]
+        P = DmftParams(solver, params["ntau"], params["n_electrons"], params["U"], params["Uprime"], params["J"],
                        params["mixing"], params.get("magnetism", 0), params.get("dctype", 1),
                        params.get("nominal_charge", 1.0), uidx.shape[0], uidx.ctypes.data_as(_ip),
-                       ut.view(np.float64).ctypes.data_as(_dp))
-        gloc = torch.empty((nf, D, D), dtype=torch.complex128, device=selfe_cm.device)
+                       ut.view(np.float64).ctypes.data_as(_dp), params.get("scgf_max_iter", 0))
         gimp = torch.empty((nf + 5, D, D), dtype=torch.complex128, device=selfe_cm.device)
         m = C.c_double(mu)
-        res = np.zeros(4)
+        res = np.zeros(5)
         L = lat._c()
         fl = self._flags(True, (MIXED if mixed else 0) | (NEWTON if newton else 0))
         st = self.lib.dmftgpu_dmft_iteration(self.h, C.byref(L), _vp(Hk_cm.data_ptr()), C.byref(P), int(iteration),
                                              _vp(selfe_cm.data_ptr()), _vp(weiss_cm.data_ptr()),
-                                             _vp(nummat_cm.data_ptr()), C.byref(m), _vp(gloc.data_ptr()),
+                                             _vp(nummat_cm.data_ptr()), C.byref(m), _vp(gloc_cm.data_ptr()),
                                              _vp(gimp.data_ptr()), res.ctypes.data_as(_dp), fl)
         self._check("dmftgpu_dmft_iteration", st)
-        return m.value, gloc, gimp, res
+        return m.value, gimp, res
 
 
 def kmesh(kx, ky, kz):

@@ -144,16 +144,29 @@ int dmftgpu_estimate_asymto(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, d
 int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double U, double mu, const double *himp,
                 const double *delta, const double *nummat_in, int nu, const int *uidx, const double *ut,
                 double *se_out, double *gimp_out, double *nummat_out, int flags);
+/* SCGF2 (src/SCGF2_fullLoop.cpp:392-533, dispatched by SOLVER for SOLVER_TYPE = SC2PT at
+ * src/SOLVER.cpp:393-399): the self-consistent second-order loop on G_imp with Pulay mixing (history 2, DIIS
+ * from loop 101), run until the reference's stopping test (at least 10 loops, then until both the G_imp and
+ * the occupation residual are <= 1e-6) or max_iter loops (the reference's 2000).  himp =
+ * projimpurity_site_Hamiltonian, weiss[nfreq] = projweiss_field, mu = muTB, mixing = MIXING; gimp[nfreq+5] is
+ * Gwimp_in_out: its first nfreq slots are read as the initial G_imp and all nfreq+5 are written;
+ * se_out[nfreq+5] = SE_out; *loops = loop iterations run.  mixing_check_outer's residual memory (a function
+ * static of the reference) lives in the context. */
+int dmftgpu_scgf2(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, double mu, double mixing,
+                  const double *himp, const double *weiss, double *gimp, int nu, const int *uidx, const double *ut,
+                  int max_iter, double *se_out, int *loops, int flags);
 
 /* ---------------------------------------------------------------------------------------------
  * One DMFT self-consistency iteration: the body of the loop of src/dmft_main.cpp:343-570 for one correlated
- * cluster of two spin-orbitals solved by IPT (the example model of the reference).
+ * cluster solved by IPT (two spin-orbitals, the example model of the reference) or by SC2PT (SCGF2, up to 32
+ * spin-orbitals).
  * --------------------------------------------------------------------------------------------- */
 #define DMFTGPU_SOLVER_IPT 0
+#define DMFTGPU_SOLVER_SC2PT 1 /* SCGF2 */
 #define DMFTGPU_DC_NONE 0
 #define DMFTGPU_DC_NOMINAL 1 /* dc_for_dmft "nominal" (src/dmft_main.cpp:665-677) */
 typedef struct {
-    int solver;            /* DMFTGPU_SOLVER_IPT */
+    int solver;            /* DMFTGPU_SOLVER_IPT or DMFTGPU_SOLVER_SC2PT */
     int ntau;              /* N_TAU */
     double n_electrons;    /* N_ELECTRONS: target of the mu search */
     double U, Uprime, J;   /* U, U', J */
@@ -164,15 +177,17 @@ typedef struct {
     int nu;                /* U_{ijkl} list of the correlated space (gen_Uijkl), host pointers */
     const int *uidx;
     const double *ut;
+    int scgf_max_iter;     /* SCGF2 loop limit (0: the reference's 2000) */
 } dmftgpu_dmft_params;
 
-/* SOLVER (IPT) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing
+/* SOLVER (IPT or SCGF2) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing
  * of SelfEnergy_w (src/dmft_main.cpp:529-533), TightBinding's mu search, GreenFtn_w and Construct_hyb_delta
  * (src/TB.cpp:297-331) and the dmft_scf_check residuals (src/dmft_main.cpp:902-1014), all on the device.
  * Device pointers only (flags must contain DMFTGPU_DEVICE_PTRS; DMFTGPU_MIXED / DMFTGPU_NEWTON select the
  * lattice-sum precision and the mu search).  State, updated in place: selfe[nfreq][D][D] (SelfEnergy_w),
- * weiss[nfreq][D][D] (weiss_fieldTB), nummat[D][D] (NumMatrix), *mu (host).  Outputs: gloc[nfreq][D][D],
- * gimp[nfreq+5][D][D] and resid[4] (host) = GwRD, GwRD_low, GwRD_max, NumMatRD.  `iteration` is the
+ * weiss[nfreq][D][D] (weiss_fieldTB), nummat[D][D] (NumMatrix), *mu (host), gloc[nfreq][D][D] (G_loc of
+ * the last TightBinding call: read as SCGF2's initial G_imp, then overwritten).  Outputs: gimp[nfreq+5][D][D]
+ * and resid[5] (host) = GwRD, GwRD_low, GwRD_max, NumMatRD, SCGF2 loop count (0 for IPT).  `iteration` is the
  * reference's currentIt (1 on the first call restarts the mixer history). */
 int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk,
                            const dmftgpu_dmft_params *params, int iteration, double *selfe, double *weiss,

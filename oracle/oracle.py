@@ -354,19 +354,89 @@ class Pulay:
         return opt + mix * optr
 
 
+def matsubara_norm2(f, beta):
+    """MatsubaraFtnnorm squared (src/SCGF2_fullLoop.cpp:791-805): sum_n ||f_n||_F^2 / w_n."""
+    wn = np.pi * (2 * np.arange(f.shape[0]) + 1) / beta
+    return float(np.sum(np.sum(np.abs(f) ** 2, axis=(1, 2)) / wn))
+
+
+def scgf2(himp, weiss, gimp_init, uidx, ut, mu, beta, ntau, mixing, max_iter=2000, static=None):
+    """SCGF2 (src/SCGF2_fullLoop.cpp:392-533) composed from the functions above.  weiss, gimp_init: nfreq
+    slots.  static: dict carrying mixing_check_outer's function-static previous residual across calls
+    (:722-727).  Returns (SE_out[nfreq+5], Gwimp_out[nfreq+5], loops)."""
+    if static is None:
+        static = {"prev": 0.0}
+    nf, d = weiss.shape[0], weiss.shape[1]
+    eye = np.eye(d, dtype=np.complex128)
+    G = np.array(gimp_init[:nf], np.complex128)
+    occ_m = occ(G, beta)
+    unit = np.sqrt(matsubara_norm2(G, beta))
+    loop, n_out, n_occ, mix = 0, 0.0, 0.0, mixing / 10.0
+    pul = Pulay(2, 100)
+    s2 = np.zeros((nf + 3, d, d), np.complex128)
+    F = np.zeros((d, d), np.complex128)
+    while (loop < 10 or n_out > 1e-6 or n_occ > 1e-6) and loop < max_iter:
+        Gin, occ_in = G.copy(), occ_m.copy()
+        occ_m = occ(G, beta)
+        F = fock(occ_m, uidx, ut)
+        gt, _ = fourier(G, beta, ntau, True, eye)
+        st, _, stat = sigma2_tau(gt, uidx, ut, beta)
+        _check(stat, "sigma2_tau")
+        s2w, stat = tau2w(st, beta, nf)
+        _check(stat, "tau2w")
+        s2[:nf] = s2w
+        G, stat = dyson(himp, weiss, F, s2[:nf], mu, beta)
+        _check(stat, "dyson")
+        occ_m = occ(G, beta)
+        n_occ = float(np.linalg.norm(occ_m - occ_in))
+        n_out = np.sqrt(matsubara_norm2(Gin - G, beta)) / unit
+        if loop % 500 == 0:
+            mix /= 1.5
+        if loop < 1500:
+            G = pul.mixing(Gin, G, mix, loop)
+        else:
+            G = (1 - mix) * Gin + mix * G
+        if loop % 10 == 0:
+            if static["prev"] > n_out:
+                mix = min(1.07 * mix, 0.5)
+            elif static["prev"] < n_out:
+                mix = max(mix / 1.09, 1e-3)
+            static["prev"] = n_out
+        loop += 1
+    s2 = estimate_asymto(s2, nf, beta, 1)
+    s2 = estimate_asymto(s2, nf, beta, 2)
+    se = np.zeros((nf + 5, d, d), np.complex128)
+    se[:nf] = s2[:nf] + F
+    se[nf] = F
+    se[nf + 1] = s2[nf]
+    se[nf + 2] = s2[nf + 1]
+    go = np.zeros((nf + 5, d, d), np.complex128)
+    go[:nf] = G
+    go[nf + 1] = eye
+    return se, go, loop
+
+
 def dmft_iteration(H, state, p, it, pulay):
-    """The dmft_main loop body for one cluster of 2 spin-orbitals with IPT (src/dmft_main.cpp:343-570):
-    state = dict(selfe, weiss, nummat, mu, beta); p = dict(ntau, n_electrons, U, Uprime, J, mixing, uidx, ut,
-    nominal_charge).  Returns (new state, gloc, gimp, residuals)."""
-    beta, D = state["beta"], 2
-    nf = state["selfe"].shape[0]
+    """The dmft_main loop body for one correlated cluster (the first D orbitals) with IPT (D = 2) or SC2PT
+    (SCGF2) (src/dmft_main.cpp:343-570): state = dict(selfe, weiss, nummat, mu, beta, gloc, scgf_static);
+    p = dict(solver, ntau, n_electrons, U, Uprime, J, mixing, uidx, ut, nominal_charge, scgf_max_iter).
+    Returns (new state, gloc, gimp, residuals[5])."""
+    beta = state["beta"]
+    nf, D = state["selfe"].shape[0], state["selfe"].shape[1]
     himp = H[:, :D, :D].mean(0)
     averU = (D * p["U"] + D * (D - 1) * p["Uprime"]) / (D * D)
     dc = (averU * (p["nominal_charge"] - 0.5) - p["J"] * (p["nominal_charge"] / 2 - 0.5)) * np.eye(D)
-    se, gi, nm, st = ipt(himp - dc, state["weiss"], state["nummat"], p["uidx"], p["ut"], p["U"], state["mu"], beta,
-                         p["ntau"])
-    if st != 0:
-        raise RuntimeError("oracle IPT status %d" % st)
+    loops = 0
+    if p.get("solver", "IPT") == "SC2PT":
+        se, gi, loops = scgf2(himp - dc, state["weiss"], state["gloc"], p["uidx"], p["ut"], state["mu"], beta,
+                              p["ntau"], p["mixing"], max_iter=p.get("scgf_max_iter", 0) or 2000,
+                              static=state.setdefault("scgf_static", {"prev": 0.0}))
+        nm = state["nummat"].copy()
+    else:
+        se, gi, nm, st = ipt(himp - dc, state["weiss"], state["nummat"], p["uidx"], p["ut"], p["U"], state["mu"],
+                             beta, p["ntau"])
+        if st != 0:
+            raise RuntimeError("oracle IPT status %d" % st)
     for M in list(se) + [nm]:
         for n in range(0, D, 2):
             avg = (M[n, n] + M[n + 1, n + 1]) / 2
@@ -386,6 +456,6 @@ def dmft_iteration(H, state, p, it, pulay):
     nr_n = n2.sum((1, 2))
     res = [np.sqrt(rd_n.sum() / (1e-10 + nr_n.sum())), np.sqrt(rd_n[low].sum() / (1e-10 + nr_n[low].sum())),
            np.sqrt(np.max(np.concatenate([[0.0], rd_n / (1e-10 + nr_n)]))),
-           np.linalg.norm(nummat - nm_imp) / np.linalg.norm(nummat)]
-    new = dict(state, selfe=selfe, weiss=weiss, nummat=nummat, mu=mu)
+           np.linalg.norm(nummat - nm_imp) / np.linalg.norm(nummat), loops]
+    new = dict(state, selfe=selfe, weiss=weiss, nummat=nummat, mu=mu, gloc=gloc)
     return new, gloc, gi, np.array(res)

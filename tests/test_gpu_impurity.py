@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_err
-from dmftpack_gb300 import models
+from dmftpack_gb300 import lib, models
 
 pytestmark = pytest.mark.gpu
 
@@ -128,7 +128,7 @@ def _dmft_setup(orc, nfreq=64, kx=8, beta=10.0):
     mu, _ = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, 1, 2, 1.0)
     gloc, _, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, 1, 2)
     weiss = orc.hyb_delta([0, 1], wl.sigma, gloc, H[:, :2, :2].mean(0), mu, wl.beta)
-    state = dict(selfe=wl.sigma.copy(), weiss=weiss, nummat=num, mu=mu, beta=wl.beta)
+    state = dict(selfe=wl.sigma.copy(), weiss=weiss, nummat=num, mu=mu, beta=wl.beta, gloc=gloc)
     return wl, H, p, state
 
 
@@ -141,12 +141,13 @@ def test_dmft_iterations_match_oracle(ctx, orc):
     dev = torch.device("cuda:0")
     cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
     Hd, se, we, nm = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["nummat"][None])[0].contiguous()
+    gloc_g = cm(state["gloc"])
     mu_g = state["mu"]
     lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
     pulay = orc.Pulay()
     for it in range(1, 10):
         state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
-        mu_g, gloc_g, gimp_g, res_g = ctx.DMFT_iteration(lat, Hd, p, it, se, we, nm, mu_g)
+        mu_g, gimp_g, res_g = ctx.DMFT_iteration(lat, Hd, p, it, se, we, nm, gloc_g, mu_g)
         torch.cuda.synchronize()
         back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
         assert abs(mu_g - state["mu"]) < 1e-12, it
@@ -154,3 +155,79 @@ def test_dmft_iterations_match_oracle(ctx, orc):
         assert rel_err(back(gloc_g), gloc) < 1e-9, it
         assert rel_err(back(we), state["weiss"]) < 1e-9, it
         assert np.allclose(res_g, res, rtol=1e-6, atol=1e-12), (it, res_g, res)
+
+
+def _scgf_case(orc, d=4, nfreq=64, ntau=256, beta=10.0, seed=7):
+    """A small d-spin-orbital impurity: random Hermitian H_imp, a causal hybridisation Delta(iw) =
+    sum_l V_l V_l^H / (iw - e_l), G_imp initialised to the non-interacting G, Kanamori U."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    himp = 0.3 * (A + A.conj().T) / 2
+    wn = np.pi * (2 * np.arange(nfreq) + 1) / beta
+    poles = rng.uniform(-2, 2, size=6)
+    weiss = np.zeros((nfreq, d, d), np.complex128)
+    for e in poles:
+        v = 0.4 * (rng.normal(size=d) + 1j * rng.normal(size=d))
+        weiss += np.einsum("i,j->ij", v, v.conj())[None] / (1j * wn[:, None, None] - e)
+    mu = 0.2
+    g0 = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - himp[None] - weiss)
+    uidx, ut = orc.gen_uijkl(d, 2.0, 1.4, 0.3)
+    return himp, weiss, g0, uidx, ut, mu, beta, ntau
+
+
+@pytest.mark.parametrize("max_iter", [12, 2000])
+def test_scgf2_matches_oracle(orc, max_iter):
+    """SCGF2 loop (SC2PT solver) against the oracle composition: 12 loops, and the full run to the reference's
+    stopping test (135 loops here, including the Pulay DIIS steps from loop 102).  Both sides start
+    mixing_check_outer's memory from zero."""
+    himp, weiss, g0, uidx, ut, mu, beta, ntau = _scgf_case(orc)
+    se_o, g_o, loops_o = orc.scgf2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=max_iter,
+                                   static={"prev": 0.0})
+    c2 = lib.Context(0)
+    try:
+        se, g, loops = c2.SCGF2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=max_iter)
+    finally:
+        c2.close()
+    assert loops == loops_o
+    assert rel_err(se, se_o) < 1e-9
+    assert rel_err(g, g_o) < 1e-9
+
+
+def test_dmft_iterations_sc2pt_match_oracle(orc):
+    """Three dmft_main iterations with the SC2PT solver (SCGF2 from the lattice G_loc, Kanamori U on 10
+    spin-orbitals of a seeded 28-orbital d+p model) against the oracle composition."""
+    import torch
+    wl = models.dp28(k=3, nfreq=48, ntau=192, beta=10.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    D = wl.D
+    uidx, ut = orc.gen_uijkl(D, 4.0, 2.6, 0.7)
+    ne = wl.n_electrons
+    p = dict(solver="SC2PT", ntau=wl.ntau, n_electrons=ne, U=4.0, Uprime=2.6, J=0.7, mixing=0.5, magnetism=0,
+             dctype=1, nominal_charge=2.0, uidx=uidx, ut=ut, scgf_max_iter=40)
+    mu, _ = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, 1, D, ne)
+    gloc, _, num = orc.greenftn_w(H, wl.sigma, mu, wl.beta, 1, D)
+    weiss = orc.hyb_delta(list(range(D)), wl.sigma, gloc, H[:, :D, :D].mean(0), mu, wl.beta)
+    state = dict(selfe=wl.sigma.copy(), weiss=weiss, nummat=num, mu=mu, beta=wl.beta, gloc=gloc)
+    dev = torch.device("cuda:0")
+    cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
+    back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
+    Hd, se, we, gl = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["gloc"])
+    nm = cm(state["nummat"][None])[0].contiguous()
+    mu_g = mu
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, D)
+    pulay = orc.Pulay()
+    c2 = lib.Context(0)
+    try:
+        for it in range(1, 4):
+            state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
+            mu_g, gimp_g, res_g = c2.DMFT_iteration(lat, Hd, p, it, se, we, nm, gl, mu_g)
+            torch.cuda.synchronize()
+            assert res_g[4] == res[4], it
+            assert abs(mu_g - state["mu"]) < 1e-12, it
+            assert rel_err(back(gimp_g)[:wl.nfreq], gimp[:wl.nfreq]) < 1e-9, it
+            assert rel_err(back(se), state["selfe"]) < 1e-9, it
+            assert rel_err(back(gl), gloc) < 1e-9, it
+            assert rel_err(back(we), state["weiss"]) < 1e-9, it
+            assert np.allclose(res_g, res, rtol=1e-6, atol=1e-12), (it, res_g, res)
+    finally:
+        c2.close()
