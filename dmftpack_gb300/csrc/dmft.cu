@@ -105,6 +105,7 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     if (D > 32 || (p->magnetism == 0 && D % 2))
         return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: correlated block must be <= 32 spin-orbital pairs");
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     cudaStream_t s = ctx->stream;
     const int dflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NEWTON));
     double2 *dSE = (double2 *)selfe, *dW = (double2 *)weiss, *dN = (double2 *)nummat, *dG = (double2 *)gloc,

@@ -6,6 +6,16 @@
 //   getFockOperator, getGwimp, getoccMat, estimate_asymto  (src/SCGF2_fullLoop.cpp:539-597, 736-787)
 // Matsubara phases are taken from an exact table of exp(-i pi q / N_tau), q = (2n+1) j mod 2 N_tau, instead
 // of exp(-i w tau) of a rounded product (the reference's phase error grows to ~1e-12 at w tau ~ 1e4).
+// Both transforms are discrete Fourier sums over the grids w_n = pi (2n+1)/beta, tau_j = j beta / N_tau:
+//   iw -> tau:  S_j = sum_n D_n e^{-i w_n tau_j} = e^{-i pi j/N} X_{j mod N},  X = DFT_N of D (zero padded)
+//   tau -> iw:  the exact integral of the piecewise-linear F(tau) against e^{i w tau} (FT_t_to_w) is, summed
+//     over hat functions, W_n = dt K(t_n) (Y_n - F_0) + dt (F_0 E(t_n) - F_N conj E(t_n)), t_n = w_n dt,
+//     Y_n = sum_{s<N} F_s e^{i w_n tau_s} (an inverse DFT_N of F_s e^{i pi s/N}), K(t) = (sin(t/2)/(t/2))^2,
+//     E(t) = (e^{it} - 1 - it)/(it)^2
+// so for N_tau a power of two <= 8192 both run as shared-memory radix-2 FFTs (O(N log N) per element instead of
+// O(N_w N_tau)).  The FFT form is also free of the cancellation in the reference's per-segment formula, which
+// loses ~1e-10 relative at the lowest frequencies; DMFTGPU_DIRECT_DFT selects the direct per-point sums that
+// follow the reference's arithmetic.
 #include <vector>
 
 #include "impurity.h"
@@ -189,6 +199,94 @@ __global__ void __launch_bounds__(FT_TJ) k_ft_sum(int dd, int nfreq, int ntau, c
     }
     if (j <= ntau)
         for (int e = 0; e < ne; e++) S[(size_t)j * dd + e0 + e] = acc[e];
+}
+
+// ---------------------------------------------------------------------------------------------------
+// FFT path (N = 2^logn <= 8192): one CTA per matrix element, the whole sequence in shared memory
+// ---------------------------------------------------------------------------------------------------
+constexpr int FFT_MAX_LOG = 13;
+constexpr int FFT_THREADS = 1024;
+
+// in-place radix-2 decimation-in-time FFT (forward, omega = e^{-2 pi i / N}) of x, loaded in bit-reversed
+// order; twiddles e^{-2 pi i k / len} = ph[2 k N / len] from the exact table ph[q] = e^{-i pi q / N}
+__device__ void smem_fft(double2 *x, int logn, const double2 *__restrict__ ph) {
+    const int N = 1 << logn;
+    for (int ls = 1; ls <= logn; ls++) {
+        const int half = 1 << (ls - 1), tstep = 2 * (N >> ls);
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int k = b & (half - 1), i0 = ((b >> (ls - 1)) << ls) + k, i1 = i0 + half;
+            const double2 t = cmul(ph[k * tstep], x[i1]);
+            const double2 u = x[i0];
+            x[i0] = cadd(u, t);
+            x[i1] = csub(u, t);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int bitrev(int i, int logn) { return (int)(__brev((unsigned)i) >> (32 - logn)); }
+
+// S_j = e^{-i pi j/N} X_{j mod N}, X = DFT_N of the Dw column folded modulo N; j = 0..N
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_w2tau(int dd, int nfreq, int logn, const double2 *__restrict__ Dw,
+                                                           const double2 *__restrict__ ph, double2 *__restrict__ S) {
+    extern __shared__ double2 x[];
+    const int e = blockIdx.x, N = 1 << logn;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double2 v = cmk(0, 0);
+        for (int i2 = i; i2 < nfreq; i2 += N) v = cadd(v, Dw[(size_t)i2 * dd + e]);
+        x[bitrev(i, logn)] = v;
+    }
+    __syncthreads();
+    smem_fft(x, logn, ph);
+    for (int j = threadIdx.x; j <= N; j += blockDim.x) S[(size_t)j * dd + e] = cmul(ph[j], x[j & (N - 1)]);
+}
+
+// FT_t_to_w by hat functions: W_n = dt K (Y_n - F_0) + dt (F_0 E - F_N conj E)
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_tau2w(int dd, int nfreq, int logn, double beta,
+                                                           const double2 *__restrict__ Ft,
+                                                           const double2 *__restrict__ ph, double2 *__restrict__ W) {
+    extern __shared__ double2 x[];
+    const int e = blockIdx.x, N = 1 << logn;
+    // conj(F_s e^{i pi s/N}) = conj(F_s) ph[s]: a forward FFT of it, conjugated, gives Y
+    for (int s = threadIdx.x; s < N; s += blockDim.x) x[bitrev(s, logn)] = cmul(cconj(Ft[(size_t)s * dd + e]), ph[s]);
+    __syncthreads();
+    smem_fft(x, logn, ph);
+    const double dt = beta / N;
+    const double2 f0 = Ft[e], fN = Ft[(size_t)N * dd + e];
+    for (int n = threadIdx.x; n < nfreq; n += blockDim.x) {
+        const double2 Y = cconj(x[n & (N - 1)]);
+        const double q = (2.0 * n + 1.0) / N;  // t_n / pi
+        const double t = DG_PI * q;
+        const double sh = sinpi(0.5 * q);
+        const double K = (sh / (0.5 * t)) * (sh / (0.5 * t));
+        double eim;  // (t - sin t) / t^2
+        if (t < 1.0) {
+            // sum_{k>=1} (-1)^{k+1} t^{2k-1} / (2k+1)!, nine terms (truncation < 1e-17 relative for t < 1)
+            const double t2 = t * t;
+            double term = t / 6.0, acc = 0.0;
+            for (int k = 1; k <= 9; k++) {
+                acc += term;
+                term *= -t2 / ((2.0 * k + 2.0) * (2.0 * k + 3.0));
+            }
+            eim = acc;
+        } else {
+            eim = (t - sinpi(q)) / (t * t);
+        }
+        const double2 E = cmk(0.5 * K, eim);
+        double2 w = cscale(csub(Y, f0), dt * K);
+        w = cadd(w, cscale(csub(cmul(f0, E), cmul(fN, cconj(E))), dt));
+        W[(size_t)n * dd + e] = w;
+    }
+}
+
+__host__ bool fft_ok(dmftgpu_ctx *ctx, int ntau) {
+    if (ctx->ft_direct || ntau < 2 || (ntau & (ntau - 1))) return false;
+    return ntau <= (1 << FFT_MAX_LOG);
+}
+__host__ int ilog2(int n) {
+    int l = 0;
+    while ((1 << l) < n) l++;
+    return l;
 }
 
 // one thread per tau: (S + S^H)/beta + V^H G0_H V/2 + V^H G0_H2 V/2, symmetrised (:62-90); minimum eigenvalue
@@ -513,12 +611,22 @@ int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
     DG_LAUNCH(ctx, "k_tail_setup");
     k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, fw, T, Dw, sw);
     DG_LAUNCH(ctx, "k_ft_subtract");
-    dim3 grid(dg_ceil_div(ntau + 1, FT_TJ), dg_ceil_div((int)dd, 16));
-    {
-        DgTimer tm(ctx, "k_ft_sum");
-        k_ft_sum<<<grid, FT_TJ, FT_IB * 16 * sizeof(double2), s>>>((int)dd, nfreq, ntau, Dw, ph, S);
+    if (fft_ok(ctx, ntau)) {
+        const size_t sm = (size_t)ntau * sizeof(double2);
+        DG_CUDA(cudaFuncSetAttribute(k_fft_w2tau, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        {
+            DgTimer tm(ctx, "k_fft_w2tau");
+            k_fft_w2tau<<<(int)dd, FFT_THREADS, sm, s>>>((int)dd, nfreq, ilog2(ntau), Dw, ph, S);
+        }
+        DG_LAUNCH(ctx, "k_fft_w2tau");
+    } else {
+        dim3 grid(dg_ceil_div(ntau + 1, FT_TJ), dg_ceil_div((int)dd, 16));
+        {
+            DgTimer tm(ctx, "k_ft_sum");
+            k_ft_sum<<<grid, FT_TJ, FT_IB * 16 * sizeof(double2), s>>>((int)dd, nfreq, ntau, Dw, ph, S);
+        }
+        DG_LAUNCH(ctx, "k_ft_sum");
     }
-    DG_LAUNCH(ctx, "k_ft_sum");
     k_ft_finish<<<dg_ceil_div(ntau + 1, 64), 64, 0, s>>>(d, ntau, beta, T, S, ft, mineig, fw2, fiw);
     DG_LAUNCH(ctx, "k_ft_finish");
     return dg_fixup_dev(ctx, d, ntau, beta, ft, mineig);
@@ -542,11 +650,22 @@ int dg_tau2w_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
     const size_t dd = (size_t)d * d;
     double2 *ph;
     DG_TRY(dg_phase_table(ctx, ntau, &ph));
-    {
-        DgTimer tm(ctx, "k_tau2w");
-        k_tau2w<<<dg_ceil_div((long long)nfreq * dd, 128), 128, 0, ctx->stream>>>((int)dd, nfreq, ntau, beta, ft, ph, fw);
+    if (fft_ok(ctx, ntau)) {
+        const size_t sm = (size_t)ntau * sizeof(double2);
+        DG_CUDA(cudaFuncSetAttribute(k_fft_tau2w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        {
+            DgTimer tm(ctx, "k_fft_tau2w");
+            k_fft_tau2w<<<(int)dd, FFT_THREADS, sm, ctx->stream>>>((int)dd, nfreq, ilog2(ntau), beta, ft, ph, fw);
+        }
+        DG_LAUNCH(ctx, "k_fft_tau2w");
+    } else {
+        {
+            DgTimer tm(ctx, "k_tau2w");
+            k_tau2w<<<dg_ceil_div((long long)nfreq * dd, 128), 128, 0, ctx->stream>>>((int)dd, nfreq, ntau, beta, ft,
+                                                                                      ph, fw);
+        }
+        DG_LAUNCH(ctx, "k_tau2w");
     }
-    DG_LAUNCH(ctx, "k_tau2w");
     if (check) {
         double2 *w = (double2 *)dg_buf(ctx, "imp.causwork", (size_t)nfreq * 3 * dd * sizeof(double2));
         int *iw = (int *)dg_buf(ctx, "imp.causiwork", (size_t)nfreq * d * sizeof(int));
@@ -770,6 +889,7 @@ int dmftgpu_fourier_w2tau(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double
                           const double *mom, int green_asym, const double *m1, double *ft, int flags) {
     if (!ctx || dim < 1 || nfreq < 1 || ntau < 1 || !fw || !ft || !(beta > 0)) return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     const size_t dd = (size_t)dim * dim;
     int st;
     const double2 *dF = (const double2 *)dg_in(ctx, fw, nfreq * dd * sizeof(double2), flags, "io.ft_fw", &st);
@@ -793,6 +913,7 @@ int dmftgpu_fourier_tau2w(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double
                           int flags) {
     if (!ctx || dim < 1 || nfreq < 1 || ntau < 1 || !fw || !ft || !(beta > 0)) return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     const size_t dd = (size_t)dim * dim;
     int st;
     const double2 *dT = (const double2 *)dg_in(ctx, ft, (ntau + 1) * dd * sizeof(double2), flags, "io.t2w_ft", &st);

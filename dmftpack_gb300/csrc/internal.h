@@ -34,8 +34,17 @@ struct dmftgpu_ctx {
     DgPulay *pulay = nullptr;         // mixer state of dmftgpu_dmft_iteration
     double scgf_prev_norm = 0.0;      // mixing_check_outer's previous residual (a function static in the
                                       // reference, src/SCGF2_fullLoop.cpp:722-727): kept across SCGF2 calls
+    bool ft_direct = false;           // DMFTGPU_DIRECT_DFT of the current call
     bool timing = false;              // record CUDA events around the named hot kernels
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
+};
+
+// sets ctx->ft_direct from a call's flags for the call's duration
+struct DgFtMode {
+    dmftgpu_ctx *ctx;
+    bool saved;
+    DgFtMode(dmftgpu_ctx *c, int flags) : ctx(c), saved(c->ft_direct) { ctx->ft_direct = (flags & DMFTGPU_DIRECT_DFT) != 0; }
+    ~DgFtMode() { ctx->ft_direct = saved; }
 };
 
 // event pair around one launch of `name` when ctx->timing is on (no-op otherwise)

@@ -226,6 +226,7 @@ extern "C" int dmftgpu_scgf2(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, dou
         nu < 0 || !(beta > 0) || max_iter < 1)
         return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     const size_t dd = (size_t)dim * dim;
     int st;
     DgUList Ul;
@@ -256,6 +257,7 @@ extern "C" int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, doubl
         nu < 0 || !(beta > 0))
         return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     const size_t dd = (size_t)dim * dim;
     int st;
     DgUList Ul;

@@ -25,7 +25,7 @@ _vp = C.c_void_p
 OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
 STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
                 6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
-DEVICE_PTRS, MIXED, NEWTON, EXPLICIT = 0x1, 0x2, 0x4, 0x8
+DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT = 0x1, 0x2, 0x4, 0x8, 0x10
 
 # every symbol include/dmftgpu.h declares
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
@@ -322,7 +322,7 @@ class Context:
         ut = np.ascontiguousarray(ut, np.complex128).reshape(-1)
         return uidx, ut, uidx.shape[0]
 
-    def FourierTransform(self, delta_w, beta, ntau, greenFtnAsym=False, moments1=None, moments=None):
+    def FourierTransform(self, delta_w, beta, ntau, greenFtnAsym=False, moments1=None, moments=None, direct=False):
         """FourierTransform (iw -> tau grid, with tail and positivity fix-up): returns (ntau+1, d, d)."""
         dev = _is_torch(delta_w)
         a = _Arr(delta_w, dev)
@@ -332,17 +332,17 @@ class Context:
         out = _Arr.empty((ntau + 1, d, d), dev, like=a.obj)
         st = self.lib.dmftgpu_fourier_w2tau(self.h, d, nf, ntau, float(beta), _vp(a.ptr), _vp(mo.ptr) if mo else None,
                                             int(bool(greenFtnAsym)), _vp(m1.ptr) if m1 else None, _vp(out.ptr),
-                                            self._flags(dev))
+                                            self._flags(dev, DIRECT_DFT if direct else 0))
         self._check("dmftgpu_fourier_w2tau", st)
         return out.result()
 
-    def FT_t_to_w(self, delta_t, beta, nfreq, allow_causality=False):
+    def FT_t_to_w(self, delta_t, beta, nfreq, allow_causality=False, direct=False):
         dev = _is_torch(delta_t)
         a = _Arr(delta_t, dev)
         ntau, d = a.obj.shape[0] - 1, a.obj.shape[1]
         out = _Arr.empty((nfreq, d, d), dev, like=a.obj)
         st = self.lib.dmftgpu_fourier_tau2w(self.h, d, nfreq, ntau, float(beta), _vp(a.ptr), _vp(out.ptr),
-                                            self._flags(dev))
+                                            self._flags(dev, DIRECT_DFT if direct else 0))
         self._check("dmftgpu_fourier_tau2w", st, (OK, CAUSALITY) if allow_causality else (OK,))
         return out.result()
 
@@ -398,7 +398,7 @@ class Context:
         self._check("dmftgpu_estimate_asymto", st)
         return a.result()
 
-    def IPT(self, himp, weiss_field, projNumMatrix, uidx, ut, U, mu, beta, ntau):
+    def IPT(self, himp, weiss_field, projNumMatrix, uidx, ut, U, mu, beta, ntau, direct=False):
         """IPT solver: returns (SE_out[nfreq+5], Gwimp_out[nfreq+5], projNumMatrix)."""
         dev = _is_torch(weiss_field)
         one = (lambda x: x[None]) if not dev else (lambda x: x.unsqueeze(0))
@@ -410,11 +410,11 @@ class Context:
         no = _Arr.empty((1, d, d), dev, like=dl.obj)
         st = self.lib.dmftgpu_ipt(self.h, d, nf, ntau, float(beta), float(U), float(mu), _vp(h.ptr), _vp(dl.ptr),
                                   _vp(nm.ptr), nu, uidx.ctypes.data_as(_ip), ut.view(np.float64).ctypes.data_as(_dp),
-                                  _vp(se.ptr), _vp(gi.ptr), _vp(no.ptr), self._flags(dev))
+                                  _vp(se.ptr), _vp(gi.ptr), _vp(no.ptr), self._flags(dev, DIRECT_DFT if direct else 0))
         self._check("dmftgpu_ipt", st)
         return se.result(), gi.result(), no.result()[0]
 
-    def SCGF2(self, himp, weiss_field, Gwimp, uidx, ut, mu, beta, ntau, mixing, max_iter=2000):
+    def SCGF2(self, himp, weiss_field, Gwimp, uidx, ut, mu, beta, ntau, mixing, max_iter=2000, direct=False):
         """SC2PT solver (SCGF2): Gwimp (nfreq slots) is the initial G_imp.  Returns (SE_out[nfreq+5],
         Gwimp_out[nfreq+5], loops)."""
         dev = _is_torch(weiss_field)
@@ -429,13 +429,13 @@ class Context:
         st = self.lib.dmftgpu_scgf2(self.h, d, nf, ntau, float(beta), float(mu), float(mixing), _vp(h.ptr),
                                     _vp(dl.ptr), _vp(g.ptr), nu, uidx.ctypes.data_as(_ip),
                                     ut.view(np.float64).ctypes.data_as(_dp), int(max_iter), _vp(se.ptr),
-                                    C.byref(loops), self._flags(dev))
+                                    C.byref(loops), self._flags(dev, DIRECT_DFT if direct else 0))
         self._check("dmftgpu_scgf2", st)
         return se.result(), g.result(), loops.value
 
     # ------------------------------------------------------------------ DMFT iteration
     def DMFT_iteration(self, lat, Hk_cm, params, iteration, selfe_cm, weiss_cm, nummat_cm, gloc_cm, mu,
-                       mixed=False, newton=False):
+                       mixed=False, newton=False, direct=False):
         """One dmft_main loop iteration on device state kept in the library's column-major layout (CUDA
         tensors, updated in place: SelfEnergy_w, weiss_fieldTB, NumMatrix, G_loc).  params: dict(solver ("IPT" or
         "SC2PT"), ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype, nominal_charge, uidx, ut,
@@ -454,7 +454,7 @@ class Context:
         m = C.c_double(mu)
         res = np.zeros(5)
         L = lat._c()
-        fl = self._flags(True, (MIXED if mixed else 0) | (NEWTON if newton else 0))
+        fl = self._flags(True, (MIXED if mixed else 0) | (NEWTON if newton else 0) | (DIRECT_DFT if direct else 0))
         st = self.lib.dmftgpu_dmft_iteration(self.h, C.byref(L), _vp(Hk_cm.data_ptr()), C.byref(P), int(iteration),
                                              _vp(selfe_cm.data_ptr()), _vp(weiss_cm.data_ptr()),
                                              _vp(nummat_cm.data_ptr()), C.byref(m), _vp(gloc_cm.data_ptr()),

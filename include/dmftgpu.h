@@ -39,6 +39,8 @@ enum {
 #define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
 #define DMFTGPU_EXPLICIT 0x8    /* lattice sums by explicit n x n inversion of every (k, iw) matrix, as the
                                    reference does (default: the exact correlated-block Schur form) */
+#define DMFTGPU_DIRECT_DFT 0x10 /* iw <-> tau transforms by the reference's direct per-point sums (default: the
+                                   same sums by FFT when N_tau is a power of two <= 8192) */
 
 typedef struct dmftgpu_ctx dmftgpu_ctx;
 

@@ -22,13 +22,16 @@ def _two_pole(nf, beta, d=2, seed=0):
     return G
 
 
-@pytest.mark.parametrize("d,green,m1", [(2, True, False), (2, False, True), (3, False, False), (4, True, False)])
-def test_fourier_w2tau(ctx, orc, d, green, m1):
-    beta, nf, ntau = 10.0, 160, 640
+@pytest.mark.parametrize("direct", [False, True])
+@pytest.mark.parametrize("d,green,m1,ntau", [(2, True, False, 640), (2, False, True, 512), (3, False, False, 640),
+                                             (4, True, False, 512)])
+def test_fourier_w2tau(ctx, orc, d, green, m1, ntau, direct):
+    """ntau = 512 runs the FFT path unless direct; 640 (not a power of two) always the direct sums."""
+    beta, nf = 10.0, 160
     G = _two_pole(nf, beta, d, seed=d)
     M1 = np.eye(d) if m1 else None
     ref, _ = orc.fourier(G, beta, ntau, green_asym=green, m1=M1)
-    got = ctx.FourierTransform(G, beta, ntau, greenFtnAsym=green, moments1=M1)
+    got = ctx.FourierTransform(G, beta, ntau, greenFtnAsym=green, moments1=M1, direct=direct)
     assert rel_err(got, ref) < TOL
 
 
@@ -50,13 +53,28 @@ def test_fourier_with_given_moments(ctx, orc):
     assert rel_err(got, ref) < TOL
 
 
-def test_ft_t_to_w(ctx, orc):
+@pytest.mark.parametrize("direct", [False, True])
+def test_ft_t_to_w(ctx, orc, direct):
     beta, nf, ntau = 10.0, 128, 1024
     G = _two_pole(nf, beta, 3, seed=2)
     gt, _ = orc.fourier(G, beta, ntau, green_asym=True)
     ref, st = orc.tau2w(gt, beta, nf)
-    got = ctx.FT_t_to_w(gt, beta, nf)
+    got = ctx.FT_t_to_w(gt, beta, nf, direct=direct)
     assert st == 0 and rel_err(got, ref) < TOL
+
+
+def test_ft_t_to_w_fft_against_exact_integral(ctx):
+    """The FFT form of FT_t_to_w against the 40-digit evaluation in tests/golden/tau2w_exact.npz (white noise
+    on 256 tau points): it reaches FP64 rounding (1e-14), while the per-segment form of the reference, run by
+    the direct path, carries the cancellation error of its a/w^2 and tau/w terms."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "tau2w_exact.npz"))
+    ft, beta, nf, exact = z["ft"], float(z["beta"]), int(z["nfreq"]), z["w"]
+    fft = ctx.FT_t_to_w(ft, beta, nf, allow_causality=True)
+    direct = ctx.FT_t_to_w(ft, beta, nf, allow_causality=True, direct=True)
+    e_fft, e_dir = rel_err(fft, exact), rel_err(direct, exact)
+    assert e_fft < 1e-14, e_fft
+    assert e_dir < 1e-10, e_dir
 
 
 @pytest.mark.parametrize("kanamori", [False, True])

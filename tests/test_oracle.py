@@ -156,3 +156,12 @@ def test_gen_uijkl_counts(orc):
     assert len(ut) == 180
     uidx, ut = orc.gen_uijkl(2, 2.0, 2.0, 0.0, density_density=True)
     assert len(ut) == 4
+
+
+def test_oracle_tau2w_against_exact_integral(orc):
+    """The oracle's FT_t_to_w (the reference's per-segment formula) against the 40-digit evaluation of the same
+    integral in tests/golden/tau2w_exact.npz."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "tau2w_exact.npz"))
+    got, _ = orc.tau2w(z["ft"], float(z["beta"]), int(z["nfreq"]))
+    assert np.abs(got - z["w"]).max() / np.abs(z["w"]).max() < 1e-10
