@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "impurity.h"
+#include "smallmat.cuh"
 
 namespace {
 
@@ -53,9 +54,11 @@ __global__ void k_hyb_delta(int dim, int nfreq, int D, double beta, double mu, c
 // ---------------------------------------------------------------------------------------------------
 // FourierTransform_tau: the tau-independent tail data (src/FourierTransform.cpp:22-44, 66-83)
 // ---------------------------------------------------------------------------------------------------
-// T layout (complex slots, d x d each): V, H, H2, UH, UH2, then eH, eH2 (d doubles each, in a slot)
+// T layout (complex slots, d x d each): V, H, H2, UH, UH2, then eH, eH2 (d doubles each, in a slot), then
+// W1 = UH^H V, W2 = UH2^H V (the tail term V^H G0_H(tau) V = W1^H diag(g(tau)) W1)
+constexpr int TAIL_SLOTS = 9;
 struct TailPtrs {
-    double2 *V, *H, *H2, *UH, *UH2;
+    double2 *V, *H, *H2, *UH, *UH2, *W1, *W2;
     double *eH, *eH2;
 };
 __device__ TailPtrs tail_ptrs(double2 *T, int d) {
@@ -68,60 +71,163 @@ __device__ TailPtrs tail_ptrs(double2 *T, int d) {
     p.UH2 = T + 4 * dd;
     p.eH = (double *)(T + 5 * dd);
     p.eH2 = (double *)(T + 6 * dd);
+    p.W1 = T + 7 * dd;
+    p.W2 = T + 8 * dd;
     return p;
 }
 
-// single thread: V = sqrt(m1); M2' = V^-H (2 m2) V^-1, M3' likewise; H = M2'/2 + sqrt(M3'/2 - M2'^2/4)
-// (or M2'/2 if that is not positive), H2 = M2' - H; eigen-decompositions of H and H2
-__global__ void k_tail_setup(int d, const double2 *mom, double2 *T, double2 *w, int *iw, int *status) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const size_t dd = (size_t)d * d;
+// FourierTransform_tau's tail data (src/FourierTransform.cpp:22-44, 66-83) by one block, the smallmat.cuh
+// routines in shared memory: V = sqrt(m1); M2' = V^-H (2 m2) V^-1, M3' likewise; H = M2'/2 + sqrt(M3'/2 -
+// M2'^2/4) (or M2'/2 if that is not positive), H2 = M2' - H; eigen-decompositions of H and H2.  V^-1 =
+// U diag(ev^-1/2) U^H comes from the same eigen-decomposition as V = U diag(ev^1/2) U^H.
+constexpr int TAIL_THREADS = 128;
+__host__ __device__ inline size_t tail_smem_bytes(int d) {
+    return (size_t)8 * d * d * sizeof(double2) + 32 * sizeof(double) + 32 * sizeof(int) + 17 * sizeof(DgRot) +
+           TAIL_THREADS * sizeof(double);
+}
+__global__ void __launch_bounds__(TAIL_THREADS) k_tail_setup_blk(int d, const double2 *mom, double2 *T, int *status) {
+    extern __shared__ double2 sm[];
+    const int dd = d * d, tid = threadIdx.x, nt = blockDim.x;
+    double2 *A = sm, *U = A + dd, *X = U + dd, *M2 = X + dd, *M3 = M2 + dd, *t1 = M3 + dd, *V = t1 + dd, *Vi = V + dd;
+    double *ev = (double *)(Vi + dd);
+    int *ord = (int *)(ev + 32);
+    DgRot *rot = (DgRot *)(ord + 32);
+    double *red = (double *)(rot + 17);
     TailPtrs p = tail_ptrs(T, d);
     const double2 *m1 = mom + dd, *m2 = mom + 2 * dd, *m3 = mom + 3 * dd;
-    double2 *A = w, *U = w + dd, *X = w + 2 * dd, *Vi = w + 3 * dd, *Vai = w + 4 * dd, *M2 = w + 5 * dd,
-            *M3 = w + 6 * dd, *t1 = w + 7 * dd;
-    double *ev = (double *)(w + 8 * dd);
-    int *ord = iw, *perm = iw + d;
-    if (thread_heig(d, m1, A, U, ev, ord)) dg_flag(status, DG_NONCONV);
-    if (ev[0] > 0) {
-        // V = U sqrt(ev) U^H
-        for (int j = 0; j < d; j++)
-            for (int i = 0; i < d; i++) {
-                double2 s = cmk(0, 0);
-                for (int l = 0; l < d; l++) s = cfma(cscale(DG_AT(U, d, i, l), sqrt(ev[l])), cconj(DG_AT(U, d, j, l)), s);
-                DG_AT(p.V, d, i, j) = s;
+    int st = block_heig(d, m1, A, U, ev, ord, rot, red);
+    const bool pos = ev[0] > 0;
+    if (pos) {
+        for (int e = tid; e < dd; e += nt) {
+            const int i = e % d, j = e / d;
+            double2 sv = cmk(0, 0), si = cmk(0, 0);
+            for (int l = 0; l < d; l++) {
+                const double2 uu = cmul(DG_AT(U, d, i, l), cconj(DG_AT(U, d, j, l)));
+                const double r = sqrt(ev[l]);
+                sv = cadd(sv, cscale(uu, r));
+                si = cadd(si, cscale(uu, 1.0 / r));
             }
-        for (size_t q = 0; q < dd; q++) Vi[q] = p.V[q];
-        thread_gj_inverse(d, Vi, perm);
-        for (int j = 0; j < d; j++)
-            for (int i = 0; i < d; i++) DG_AT(Vai, d, i, j) = cconj(DG_AT(p.V, d, j, i));
-        thread_gj_inverse(d, Vai, perm);
-        for (size_t q = 0; q < dd; q++) X[q] = cscale(m2[q], 2.0);
-        thread_matmul(d, Vai, X, t1);
-        thread_matmul(d, t1, Vi, M2);
-        for (size_t q = 0; q < dd; q++) X[q] = cscale(m3[q], 2.0);
-        thread_matmul(d, Vai, X, t1);
-        thread_matmul(d, t1, Vi, M3);
-        thread_matmul(d, M2, M2, t1);
-        for (size_t q = 0; q < dd; q++) X[q] = csub(cscale(M3[q], 0.5), cscale(t1[q], 0.25));
-        thread_heig(d, X, A, U, ev, ord);
-        if (ev[0] > 0) {
-            for (int j = 0; j < d; j++)
-                for (int i = 0; i < d; i++) {
-                    double2 s = cmk(0, 0);
-                    for (int l = 0; l < d; l++) s = cfma(cscale(DG_AT(U, d, i, l), sqrt(ev[l])), cconj(DG_AT(U, d, j, l)), s);
-                    DG_AT(p.H, d, i, j) = cadd(cscale(DG_AT(M2, d, i, j), 0.5), s);
-                }
-        } else {
-            for (size_t q = 0; q < dd; q++) p.H[q] = cscale(M2[q], 0.5);
+            V[e] = sv;
+            Vi[e] = si;
+            X[e] = cscale(m2[e], 2.0);
         }
-        for (size_t q = 0; q < dd; q++) p.H2[q] = csub(M2[q], p.H[q]);
+        __syncthreads();
+        block_matmul(d, Vi, X, t1);
+        block_matmul(d, t1, Vi, M2);                      // M2' = V^-H (2 m2) V^-1
+        for (int e = tid; e < dd; e += nt) X[e] = cscale(m3[e], 2.0);
+        __syncthreads();
+        block_matmul(d, Vi, X, t1);
+        block_matmul(d, t1, Vi, M3);                      // M3'
+        block_matmul(d, M2, M2, t1);
+        for (int e = tid; e < dd; e += nt) X[e] = csub(cscale(M3[e], 0.5), cscale(t1[e], 0.25));
+        __syncthreads();
+        st |= block_heig(d, X, A, U, ev, ord, rot, red);
+        const bool pos2 = ev[0] > 0;
+        for (int e = tid; e < dd; e += nt) {
+            const int i = e % d, j = e / d;
+            double2 h = cscale(M2[e], 0.5);
+            if (pos2)
+                for (int l = 0; l < d; l++)
+                    h = cadd(h, cscale(cmul(DG_AT(U, d, i, l), cconj(DG_AT(U, d, j, l))), sqrt(ev[l])));
+            p.H[e] = h;
+            p.H2[e] = csub(M2[e], h);
+            p.V[e] = V[e];
+        }
     } else {
-        for (size_t q = 0; q < dd; q++) p.V[q] = p.H[q] = p.H2[q] = cmk(0, 0);
+        for (int e = tid; e < dd; e += nt) {
+            V[e] = cmk(0, 0);
+            p.V[e] = p.H[e] = p.H2[e] = cmk(0, 0);
+        }
     }
-    thread_heig(d, p.H, A, p.UH, p.eH, ord);
-    thread_heig(d, p.H2, A, p.UH2, p.eH2, ord);
+    __syncthreads();
+    st |= block_heig(d, p.H, A, U, ev, ord, rot, red);
+    for (int e = tid; e < dd; e += nt) {
+        p.UH[e] = U[e];
+        M3[e] = U[e];
+    }
+    for (int l = tid; l < d; l += nt) p.eH[l] = ev[l];
+    __syncthreads();
+    st |= block_heig(d, p.H2, A, U, ev, ord, rot, red);
+    for (int e = tid; e < dd; e += nt) {
+        p.UH2[e] = U[e];
+        const int i = e % d, j = e / d;
+        double2 w1 = cmk(0, 0), w2 = cmk(0, 0);
+        for (int l = 0; l < d; l++) {
+            w1 = cfma(cconj(DG_AT(M3, d, l, i)), DG_AT(V, d, l, j), w1);
+            w2 = cfma(cconj(DG_AT(U, d, l, i)), DG_AT(V, d, l, j), w2);
+        }
+        p.W1[e] = w1;
+        p.W2[e] = w2;
+    }
+    for (int l = tid; l < d; l += nt) p.eH2[l] = ev[l];
+    if (st && tid == 0) dg_flag(status, DG_NONCONV);
 }
+
+// g(tau) of the two tail poles: G[t * 2d + l] = -1/(exp(e_l tau) + exp(e_l (tau - beta))), e = (eH, eH2)
+__global__ void k_tail_g(int d, int ntau, double beta, const double2 *T, double *G) {
+    long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)(ntau + 1) * 2 * d) return;
+    const int t = (int)(x / (2 * d)), l = (int)(x % (2 * d));
+    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
+    const double e = l < d ? p.eH[l] : p.eH2[l - d];
+    const double tau = t * beta / ntau;
+    G[x] = -1.0 / (exp(e * tau) + exp(e * (tau - beta)));
+}
+
+// one thread per (tau, element): (S + S^H)/beta + V^H G0_H V/2 + V^H G0_H2 V/2, symmetrised
+__global__ void k_ft_finish_el(int d, int ntau, double beta, const double2 *T, const double *G, const double2 *S,
+                               double2 *out) {
+    const int dd = d * d;
+    long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)(ntau + 1) * dd) return;
+    const int t = (int)(x / dd), e = (int)(x % dd), a = e % d, b = e / d;
+    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
+    const double2 *Sj = S + (size_t)t * dd;
+    const double *g = G + (size_t)t * 2 * d;
+    double2 tab = cmk(0, 0), tba = cmk(0, 0);
+    for (int l = 0; l < d; l++) {
+        const double2 w1a = DG_AT(p.W1, d, l, a), w1b = DG_AT(p.W1, d, l, b);
+        const double2 w2a = DG_AT(p.W2, d, l, a), w2b = DG_AT(p.W2, d, l, b);
+        tab = cadd(tab, cadd(cscale(cmul(cconj(w1a), w1b), g[l]), cscale(cmul(cconj(w2a), w2b), g[d + l])));
+        tba = cadd(tba, cadd(cscale(cmul(cconj(w1b), w1a), g[l]), cscale(cmul(cconj(w2b), w2a), g[d + l])));
+    }
+    const double2 sab = cadd(DG_AT(Sj, d, a, b), cconj(DG_AT(Sj, d, b, a)));
+    const double2 sba = cadd(DG_AT(Sj, d, b, a), cconj(DG_AT(Sj, d, a, b)));
+    const double2 Aab = cadd(cscale(sab, 1.0 / beta), cscale(tab, 0.5));
+    const double2 Aba = cadd(cscale(sba, 1.0 / beta), cscale(tba, 0.5));
+    out[x] = cscale(cadd(Aab, cconj(Aba)), 0.5);
+}
+
+// Definiteness of nmat Hermitian d x d matrices, one thread each, lower triangles interleaved in shared memory.
+// mode 0: sign * lower(M_t) - shift I; mode 1: sign * (W_t - W_t^H)/(2i).  flag[t] = +1 if positive definite
+// (strict) or semidefinite (!strict), else -1; if status != nullptr, `code` is flagged when the answer is
+// `when` (0: not definite, 1: definite).
+__global__ void k_posdef(int d, int nmat, const double2 *M, int mode, double sign, double shift, int strict,
+                         double *flag, int *status, int code, int when) {
+    extern __shared__ double2 tri[];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmat) return;
+    const int stride = blockDim.x;
+    double2 *my = tri + threadIdx.x;
+    const double2 *Mt = M + (size_t)t * d * d;
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j <= i; j++) {
+            double2 v;
+            if (mode == 0) {
+                v = DG_AT(Mt, d, i, j);
+            } else {
+                const double2 x = csub(DG_AT(Mt, d, i, j), cconj(DG_AT(Mt, d, j, i)));
+                v = cmk(x.y / 2, -x.x / 2);
+            }
+            v = cscale(v, sign);
+            if (i == j) v = cmk(v.x - shift, 0.0);
+            my[(size_t)((i * (i + 1)) / 2 + j) * stride] = v;
+        }
+    const bool ok = posdef_tri(d, my, stride, strict != 0);
+    if (flag) flag[t] = ok ? 1.0 : -1.0;
+    if (status && (int)ok == when) dg_flag(status, code);
+}
+
 
 // one thread per frequency: Dw_i = F_i - V^H [(iw - H)^-1 + (iw - H2)^-1] V / 2  (:55-60; the inverses
 // through the eigen-decompositions of H and H2)
@@ -289,58 +395,6 @@ __host__ int ilog2(int n) {
     return l;
 }
 
-// one thread per tau: (S + S^H)/beta + V^H G0_H V/2 + V^H G0_H2 V/2, symmetrised (:62-90); minimum eigenvalue
-__global__ void k_ft_finish(int d, int ntau, double beta, const double2 *T, const double2 *S, double2 *out,
-                            double *mineig, double2 *work, int *iwork) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j > ntau) return;
-    const size_t dd = (size_t)d * d;
-    TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
-    const double tau = j * beta / ntau;
-    double2 *A = work + (size_t)j * 4 * dd, *B = A + dd, *C = B + dd, *E = C + dd;
-    const double2 *Sj = S + (size_t)j * dd;
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 v = cadd(DG_AT(Sj, d, a, b), cconj(DG_AT(Sj, d, b, a)));
-            DG_AT(A, d, a, b) = cscale(v, 1.0 / beta);
-        }
-    // G0 tail terms: M = UH diag(g) UH^H + UH2 diag(g2) UH2^H, g = -1/(exp(e tau) + exp(e (tau - beta)))
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) {
-                double g1 = -1.0 / (exp(p.eH[l] * tau) + exp(p.eH[l] * (tau - beta)));
-                double g2 = -1.0 / (exp(p.eH2[l] * tau) + exp(p.eH2[l] * (tau - beta)));
-                s = cfma(cscale(DG_AT(p.UH, d, a, l), g1), cconj(DG_AT(p.UH, d, b, l)), s);
-                s = cfma(cscale(DG_AT(p.UH2, d, a, l), g2), cconj(DG_AT(p.UH2, d, b, l)), s);
-            }
-            DG_AT(B, d, a, b) = s;
-        }
-    thread_matmul(d, B, p.V, C);  // C = M V
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(C, d, l, b), s);
-            DG_AT(A, d, a, b) = cadd(DG_AT(A, d, a, b), cscale(s, 0.5));
-        }
-    double2 *O = out + (size_t)j * dd;
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++)
-            DG_AT(O, d, a, b) = cscale(cadd(DG_AT(A, d, a, b), cconj(DG_AT(A, d, b, a))), 0.5);
-    thread_heig(d, O, B, nullptr, (double *)E, iwork + (size_t)j * d);
-    mineig[j] = ((double *)E)[0];
-}
-
-// one thread per tau: minimum eigenvalue of M[t] (lower triangle), used by the fix-up scan
-__global__ void k_mineig(int d, int nt1, const double2 *M, double *mineig, double2 *work, int *iwork) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt1) return;
-    const size_t dd = (size_t)d * d;
-    double2 *A = work + (size_t)t * 2 * dd;
-    thread_heig(d, M + (size_t)t * dd, A, nullptr, (double *)(A + dd), iwork + (size_t)t * d);
-    mineig[t] = ((double *)(A + dd))[0];
-}
-
 // single thread: the sequential positivity fix-up (src/FourierTransform.cpp:145-175,
 // src/SCGF2_fullLoop.cpp:657-688); eigenvalues of untouched points come precomputed in mineig
 __global__ void k_fixup_scan(int d, int ntau, double beta, double2 *M, const double *mineig, double2 *work,
@@ -416,24 +470,6 @@ __global__ void k_tau2w(int dd, int nfreq, int ntau, double beta, const double2 
         e0 = e1;
     }
     W[t] = acc;
-}
-
-// causality check of FT_t_to_w (:551-558) and getGwimp (:564-568): max eig of (W - W^H)/(2i)
-__global__ void k_causal(int d, int nfreq, const double2 *W, double2 *work, int *iwork, int strict, int *status) {
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nfreq) return;
-    const size_t dd = (size_t)d * d;
-    double2 *A = work + (size_t)n * 3 * dd, *B = A + dd;
-    const double2 *Wn = W + (size_t)n * dd;
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 v = csub(DG_AT(Wn, d, a, b), cconj(DG_AT(Wn, d, b, a)));  // (W - W^H)
-            DG_AT(A, d, a, b) = cmk(v.y / 2, -v.x / 2);                        // / (2i)
-        }
-    double *ev = (double *)(B + dd);
-    thread_heig(d, A, B, nullptr, ev, iwork + (size_t)n * d);
-    const double mx = ev[d - 1];
-    if (strict ? !(mx < 0) : (mx > 0)) dg_flag(status, DG_CAUSAL);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -581,6 +617,27 @@ int dg_phase_table(dmftgpu_ctx *ctx, int ntau, double2 **ph) {
     return DMFTGPU_OK;
 }
 
+int dg_tail_setup_dev(dmftgpu_ctx *ctx, int d, const double2 *mom, double2 *T) {
+    const size_t sm = tail_smem_bytes(d);
+    DG_CUDA(cudaFuncSetAttribute(k_tail_setup_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_tail_setup_blk<<<1, TAIL_THREADS, sm, ctx->stream>>>(d, mom, T, ctx->d_status);
+    DG_LAUNCH(ctx, "k_tail_setup_blk");
+    return DMFTGPU_OK;
+}
+
+// flags (and/or status) from the definiteness of nmat d x d matrices; the fix-up reads flag >= 0 as
+// "minimum eigenvalue >= 0"
+int dg_posdef_dev(dmftgpu_ctx *ctx, int d, int nmat, const double2 *M, int mode, double sign, double shift,
+                  bool strict, double *flag, int code, int when) {
+    const int nt = posdef_threads(d);
+    const size_t sm = (size_t)nt * d * (d + 1) / 2 * sizeof(double2);
+    DG_CUDA(cudaFuncSetAttribute(k_posdef, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_posdef<<<dg_ceil_div(nmat, nt), nt, sm, ctx->stream>>>(d, nmat, M, mode, sign, shift, strict ? 1 : 0, flag,
+                                                             code ? ctx->d_status : nullptr, code, when);
+    DG_LAUNCH(ctx, "k_posdef");
+    return DMFTGPU_OK;
+}
+
 int dg_fixup_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, double2 *M, const double *mineig) {
     double2 *w = (double2 *)dg_buf(ctx, "imp.fixwork", 4 * (size_t)d * d * sizeof(double2) + 64);
     int *iw = (int *)dg_buf(ctx, "imp.fixiwork", (size_t)(d + 1) * sizeof(int));
@@ -595,20 +652,16 @@ int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
                  double2 *ft) {
     const size_t dd = (size_t)d * d;
     cudaStream_t s = ctx->stream;
-    double2 *T = (double2 *)dg_buf(ctx, "imp.tail", 8 * dd * sizeof(double2));
-    double2 *tw = (double2 *)dg_buf(ctx, "imp.tailwork", 10 * dd * sizeof(double2));
-    int *tiw = (int *)dg_buf(ctx, "imp.tailiwork", 2 * (size_t)d * sizeof(int));
+    double2 *T = (double2 *)dg_buf(ctx, "imp.tail", TAIL_SLOTS * dd * sizeof(double2));
+    double *gtail = (double *)dg_buf(ctx, "imp.gtail", (size_t)(ntau + 1) * 2 * d * sizeof(double));
     double2 *Dw = (double2 *)dg_buf(ctx, "imp.Dw", (size_t)nfreq * dd * sizeof(double2));
     double2 *sw = (double2 *)dg_buf(ctx, "imp.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
     double2 *S = (double2 *)dg_buf(ctx, "imp.Ssum", (size_t)(ntau + 1) * dd * sizeof(double2));
-    double2 *fw2 = (double2 *)dg_buf(ctx, "imp.finwork", (size_t)(ntau + 1) * 4 * dd * sizeof(double2));
-    int *fiw = (int *)dg_buf(ctx, "imp.finiwork", (size_t)(ntau + 1) * d * sizeof(int));
     double *mineig = (double *)dg_buf(ctx, "imp.mineig", (size_t)(ntau + 1) * sizeof(double));
-    if (!T || !tw || !tiw || !Dw || !sw || !S || !fw2 || !fiw || !mineig) return DMFTGPU_NOMEM;
+    if (!T || !gtail || !Dw || !sw || !S || !mineig) return DMFTGPU_NOMEM;
     double2 *ph;
     DG_TRY(dg_phase_table(ctx, ntau, &ph));
-    k_tail_setup<<<1, 1, 0, s>>>(d, mom, T, tw, tiw, ctx->d_status);
-    DG_LAUNCH(ctx, "k_tail_setup");
+    DG_TRY(dg_tail_setup_dev(ctx, d, mom, T));
     k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, fw, T, Dw, sw);
     DG_LAUNCH(ctx, "k_ft_subtract");
     if (fft_ok(ctx, ntau)) {
@@ -627,8 +680,11 @@ int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
         }
         DG_LAUNCH(ctx, "k_ft_sum");
     }
-    k_ft_finish<<<dg_ceil_div(ntau + 1, 64), 64, 0, s>>>(d, ntau, beta, T, S, ft, mineig, fw2, fiw);
-    DG_LAUNCH(ctx, "k_ft_finish");
+    k_tail_g<<<dg_ceil_div((long long)(ntau + 1) * 2 * d, 256), 256, 0, s>>>(d, ntau, beta, T, gtail);
+    DG_LAUNCH(ctx, "k_tail_g");
+    k_ft_finish_el<<<dg_ceil_div((long long)(ntau + 1) * dd, 256), 256, 0, s>>>(d, ntau, beta, T, gtail, S, ft);
+    DG_LAUNCH(ctx, "k_ft_finish_el");
+    DG_TRY(dg_posdef_dev(ctx, d, ntau + 1, ft, 0, 1.0, 0.0, false, mineig, 0, 0));
     return dg_fixup_dev(ctx, d, ntau, beta, ft, mineig);
 }
 
@@ -667,11 +723,8 @@ int dg_tau2w_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
         DG_LAUNCH(ctx, "k_tau2w");
     }
     if (check) {
-        double2 *w = (double2 *)dg_buf(ctx, "imp.causwork", (size_t)nfreq * 3 * dd * sizeof(double2));
-        int *iw = (int *)dg_buf(ctx, "imp.causiwork", (size_t)nfreq * d * sizeof(int));
-        if (!w || !iw) return DMFTGPU_NOMEM;
-        k_causal<<<dg_ceil_div(nfreq, 64), 64, 0, ctx->stream>>>(d, nfreq, fw, w, iw, 0, ctx->d_status);
-        DG_LAUNCH(ctx, "k_causal");
+        // FT_t_to_w asserts max eig of (W - W^H)/2i <= 0: -(W - W^H)/2i positive semidefinite
+        DG_TRY(dg_posdef_dev(ctx, d, nfreq, fw, 1, -1.0, 0.0, false, nullptr, DG_CAUSAL, 0));
     }
     return DMFTGPU_OK;
 }
@@ -684,12 +737,9 @@ int dg_sigma2_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, const DgUList 
                                                                            U.uidx, U.ut, gt, st, ctx->d_status);
     }
     DG_LAUNCH(ctx, "k_sigma2");
-    double2 *w = (double2 *)dg_buf(ctx, "imp.s2work", (size_t)(ntau + 1) * 2 * dd * sizeof(double2) + 64);
-    int *iw = (int *)dg_buf(ctx, "imp.s2iwork", (size_t)(ntau + 1) * d * sizeof(int));
     double *mineig = (double *)dg_buf(ctx, "imp.s2mineig", (size_t)(ntau + 1) * sizeof(double));
-    if (!w || !iw || !mineig) return DMFTGPU_NOMEM;
-    k_mineig<<<dg_ceil_div(ntau + 1, 64), 64, 0, ctx->stream>>>(d, ntau + 1, st, mineig, w, iw);
-    DG_LAUNCH(ctx, "k_mineig");
+    if (!mineig) return DMFTGPU_NOMEM;
+    DG_TRY(dg_posdef_dev(ctx, d, ntau + 1, st, 0, 1.0, 0.0, false, mineig, 0, 0));
     return dg_fixup_dev(ctx, d, ntau, beta, st, mineig);
 }
 
@@ -708,11 +758,8 @@ int dg_dyson_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, double mu, con
                                                             ctx->d_status);
     DG_LAUNCH(ctx, "k_dyson");
     if (check) {
-        double2 *w = (double2 *)dg_buf(ctx, "imp.causwork", (size_t)nfreq * 3 * dd * sizeof(double2));
-        int *iw2 = (int *)dg_buf(ctx, "imp.causiwork", (size_t)nfreq * d * sizeof(int));
-        if (!w || !iw2) return DMFTGPU_NOMEM;
-        k_causal<<<dg_ceil_div(nfreq, 64), 64, 0, ctx->stream>>>(d, nfreq, gw, w, iw2, 1, ctx->d_status);
-        DG_LAUNCH(ctx, "k_causal");
+        // getGwimp asserts max eig of (G - G^H)/2i < 0: -(G - G^H)/2i positive definite
+        DG_TRY(dg_posdef_dev(ctx, d, nfreq, gw, 1, -1.0, 0.0, true, nullptr, DG_CAUSAL, 0));
     }
     return DMFTGPU_OK;
 }
@@ -723,51 +770,35 @@ int dg_estimate_asymto_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, doub
     return DMFTGPU_OK;
 }
 
-// getoccMat: n = -G(tau = beta) with the m0 = 0, m1 = I green tail (src/SCGF2_fullLoop.cpp:539-549)
-__global__ void k_occ_finish(int d, int nfreq, double beta, const double2 *T, const double2 *Dw, double2 *occ,
-                             double2 *work) {
-    // single block: S(beta) = sum_i Dw_i exp(-i w_i beta) = -sum_i Dw_i (exp(-i pi (2i+1)) = -1)
-    __shared__ double2 red[256];
-    const size_t dd = (size_t)d * d;
-    for (size_t e = 0; e < dd; e++) {
+// getoccMat: n = -G(tau = beta) with the m0 = 0, m1 = I green tail (src/SCGF2_fullLoop.cpp:539-549).
+// S(beta) = sum_i Dw_i exp(-i w_i beta) = -sum_i Dw_i (exp(-i pi (2i+1)) = -1); one block, a thread per element
+// (sequential sum over frequencies), then the tail term per element
+__global__ void k_occ_finish_blk(int d, int nfreq, double beta, const double2 *T, const double2 *Dw, double2 *occ) {
+    extern __shared__ double2 sw[];  // dd
+    const int dd = d * d;
+    for (int e = threadIdx.x; e < dd; e += blockDim.x) {
         double2 s = cmk(0, 0);
-        for (int i = threadIdx.x; i < nfreq; i += blockDim.x) s = csub(s, Dw[(size_t)i * dd + e]);
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-            if (threadIdx.x < h) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + h]);
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) work[e] = red[0];
-        __syncthreads();
+        for (int i = 0; i < nfreq; i++) s = csub(s, Dw[(size_t)i * dd + e]);
+        sw[e] = s;
     }
-    if (threadIdx.x != 0) return;
+    __syncthreads();
     TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
-    const double tau = beta;
-    double2 *A = work + dd, *B = A + dd, *C = B + dd;
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++)
-            DG_AT(A, d, a, b) = cscale(cadd(work[a + b * d], cconj(work[b + a * d])), 1.0 / beta);
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) {
-                double g1 = -1.0 / (exp(p.eH[l] * tau) + exp(p.eH[l] * (tau - beta)));
-                double g2 = -1.0 / (exp(p.eH2[l] * tau) + exp(p.eH2[l] * (tau - beta)));
-                s = cfma(cscale(DG_AT(p.UH, d, a, l), g1), cconj(DG_AT(p.UH, d, b, l)), s);
-                s = cfma(cscale(DG_AT(p.UH2, d, a, l), g2), cconj(DG_AT(p.UH2, d, b, l)), s);
-            }
-            DG_AT(B, d, a, b) = s;
+    for (int e = threadIdx.x; e < dd; e += blockDim.x) {
+        const int a = e % d, b = e / d;
+        double2 tab = cmk(0, 0), tba = cmk(0, 0);
+        for (int l = 0; l < d; l++) {
+            const double e1 = p.eH[l], e2 = p.eH2[l];
+            const double g1 = -1.0 / (exp(e1 * beta) + exp(e1 * (beta - beta)));
+            const double g2 = -1.0 / (exp(e2 * beta) + exp(e2 * (beta - beta)));
+            const double2 w1a = DG_AT(p.W1, d, l, a), w1b = DG_AT(p.W1, d, l, b);
+            const double2 w2a = DG_AT(p.W2, d, l, a), w2b = DG_AT(p.W2, d, l, b);
+            tab = cadd(tab, cadd(cscale(cmul(cconj(w1a), w1b), g1), cscale(cmul(cconj(w2a), w2b), g2)));
+            tba = cadd(tba, cadd(cscale(cmul(cconj(w1b), w1a), g1), cscale(cmul(cconj(w2b), w2a), g2)));
         }
-    thread_matmul(d, B, p.V, C);
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(C, d, l, b), s);
-            DG_AT(A, d, a, b) = cadd(DG_AT(A, d, a, b), cscale(s, 0.5));
-        }
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) DG_AT(occ, d, a, b) = cscale(cadd(DG_AT(A, d, a, b), cconj(DG_AT(A, d, b, a))), -0.5);
+        const double2 Aab = cadd(cscale(cadd(sw[a + b * d], cconj(sw[b + a * d])), 1.0 / beta), cscale(tab, 0.5));
+        const double2 Aba = cadd(cscale(cadd(sw[b + a * d], cconj(sw[a + b * d])), 1.0 / beta), cscale(tba, 0.5));
+        occ[e] = cscale(cadd(Aab, cconj(Aba)), -0.5);
+    }
 }
 
 __global__ void k_set_identity_slot(int d, double2 *m1) {
@@ -779,22 +810,18 @@ int dg_occ_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *g
     const size_t dd = (size_t)d * d;
     cudaStream_t s = ctx->stream;
     double2 *mom = (double2 *)dg_buf(ctx, "occ.mom", 4 * dd * sizeof(double2));
-    double2 *T = (double2 *)dg_buf(ctx, "occ.tail", 8 * dd * sizeof(double2));
-    double2 *tw = (double2 *)dg_buf(ctx, "occ.tailwork", 10 * dd * sizeof(double2));
-    int *tiw = (int *)dg_buf(ctx, "occ.tailiwork", 2 * (size_t)d * sizeof(int));
+    double2 *T = (double2 *)dg_buf(ctx, "occ.tail", TAIL_SLOTS * dd * sizeof(double2));
     double2 *Dw = (double2 *)dg_buf(ctx, "occ.Dw", (size_t)nfreq * dd * sizeof(double2));
     double2 *sw = (double2 *)dg_buf(ctx, "occ.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
-    double2 *fw = (double2 *)dg_buf(ctx, "occ.finwork", 4 * dd * sizeof(double2));
-    if (!mom || !T || !tw || !tiw || !Dw || !sw || !fw) return DMFTGPU_NOMEM;
+    if (!mom || !T || !Dw || !sw) return DMFTGPU_NOMEM;
     DG_TRY(dg_moments_dev(ctx, d, nfreq, beta, gw, 1, mom));
     k_set_identity_slot<<<dg_ceil_div((int)dd, 64), 64, 0, s>>>(d, mom + dd);  // m1 = I (m0 = 0 already)
     DG_LAUNCH(ctx, "k_set_identity_slot");
-    k_tail_setup<<<1, 1, 0, s>>>(d, mom, T, tw, tiw, ctx->d_status);
-    DG_LAUNCH(ctx, "k_tail_setup");
+    DG_TRY(dg_tail_setup_dev(ctx, d, mom, T));
     k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, gw, T, Dw, sw);
     DG_LAUNCH(ctx, "k_ft_subtract");
-    k_occ_finish<<<1, 256, 0, s>>>(d, nfreq, beta, T, Dw, occ, fw);
-    DG_LAUNCH(ctx, "k_occ_finish");
+    k_occ_finish_blk<<<1, 128, dd * sizeof(double2), s>>>(d, nfreq, beta, T, Dw, occ);
+    DG_LAUNCH(ctx, "k_occ_finish_blk");
     return DMFTGPU_OK;
 }
 

@@ -7,7 +7,7 @@
 // partial pivoting, and then reproduces the reference's window averaging (2Nv+1 windows, Nv = N_freq/20),
 // the variance of the trace of each moment, the positivity gates on the averaged moments, the first-minimum
 // window choice (sequential argmin started at the last window) and the final Hermitisation.
-#include "linalg.cuh"
+#include "smallmat.cuh"
 
 namespace {
 
@@ -217,6 +217,26 @@ __global__ void k_mom_gate(MomArgs g) {
     g.ok[ci] = okv;
 }
 
+// the green-tail gate (m0 = 0, m1 = I fixed): min eig of (avg1 - avg0^2) > 1, i.e. (avg1 - avg0^2) - I positive
+// definite, by a Cholesky factorisation of the lower triangle (the triangle the eigensolver would read)
+__global__ void k_mom_gate_green(MomArgs g) {
+    extern __shared__ double2 tri[];
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= g.C) return;
+    const int D = g.D, DD = D * D, stride = blockDim.x;
+    double2 *my = tri + threadIdx.x;
+    const double2 *m0 = g.avg + ((size_t)0 * g.C + ci) * DD;
+    const double2 *m1 = g.avg + ((size_t)1 * g.C + ci) * DD;
+    for (int i = 0; i < D; i++)
+        for (int j = 0; j <= i; j++) {
+            double2 x = DG_AT(m1, D, i, j);
+            for (int k = 0; k < D; k++) x = csub(x, cmul(DG_AT(m0, D, i, k), DG_AT(m0, D, k, j)));
+            if (i == j) x = cmk(x.x - 1.0, 0.0);
+            my[(size_t)((i * (i + 1)) / 2 + j) * stride] = x;
+        }
+    g.ok[ci] = posdef_tri(D, my, stride, true) ? 1 : 0;
+}
+
 // single block: window choice per moment and the final averaged, Hermitised moments
 __global__ void k_mom_final(MomArgs g) {
     __shared__ int win[4];
@@ -317,8 +337,16 @@ int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const doub
     long long navg = (long long)g.C * DD * g.ncol + (long long)g.C * g.ncol;
     k_mom_avg<<<dg_ceil_div(navg, 256), 256, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_avg");
-    k_mom_gate<<<dg_ceil_div(g.C, 64), 64, 0, s>>>(g);
-    DG_LAUNCH(ctx, "k_mom_gate");
+    if (g.green) {
+        const int nt = posdef_threads(dim);
+        const size_t sm = (size_t)nt * dim * (dim + 1) / 2 * sizeof(double2);
+        DG_CUDA(cudaFuncSetAttribute(k_mom_gate_green, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_mom_gate_green<<<dg_ceil_div(g.C, nt), nt, sm, s>>>(g);
+        DG_LAUNCH(ctx, "k_mom_gate_green");
+    } else {
+        k_mom_gate<<<dg_ceil_div(g.C, 64), 64, 0, s>>>(g);
+        DG_LAUNCH(ctx, "k_mom_gate");
+    }
     k_mom_final<<<1, 256, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_final");
     return DMFTGPU_OK;

@@ -1,0 +1,81 @@
+"""Run one named hot-path case on cuda:0 and print its device time; the command the ncu summaries under
+profiles/ are taken with.
+
+    python -m dmftpack_gb300.profile_case gloc  [--k 16 --nfreq 2048 --precision mixed|fp64 --algo schur|explicit]
+    python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct]
+
+gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
+scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
+       U' = 2.6 (the SC2PT workload's impurity sizes by default: d = 10, N_w = 4096, N_tau = 8192, beta = 40).
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def _impurity(d, nfreq, beta, seed=11):
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    himp = 0.3 * (A + A.conj().T) / 2
+    wn = np.pi * (2 * np.arange(nfreq) + 1) / beta
+    weiss = np.zeros((nfreq, d, d), np.complex128)
+    for e in rng.uniform(-3, 3, size=8):
+        v = 0.4 * (rng.normal(size=d) + 1j * rng.normal(size=d))
+        weiss += np.einsum("i,j->ij", v, v.conj())[None] / (1j * wn[:, None, None] - e)
+    mu = 0.5
+    g0 = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - himp[None] - weiss)
+    return himp, weiss, g0, mu
+
+
+def main():
+    import torch
+    from dmftpack_gb300 import lib, models
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["gloc", "scgf2"])
+    ap.add_argument("--k", type=int, default=16)
+    ap.add_argument("--nfreq", type=int, default=None)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--algo", default="schur", choices=["schur", "explicit"])
+    ap.add_argument("--d", type=int, default=10)
+    ap.add_argument("--ntau", type=int, default=8192)
+    ap.add_argument("--loops", type=int, default=2)
+    ap.add_argument("--direct", action="store_true")
+    ap.add_argument("--repeat", type=int, default=2)
+    a = ap.parse_args()
+    dev = torch.device("cuda:0")
+    ctx = lib.Context(0)
+    out = {"case": a.case}
+    if a.case == "gloc":
+        wl = models.t2g_p(k=a.k, nfreq=a.nfreq or 2048, beta=40.0)
+        Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+        S = torch.from_numpy(wl.sigma).to(dev)
+        lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, wl.ncl, wl.nh)
+
+        def run():
+            return ctx.GreenFtn_w(lat, Hd, S, 0.0, mixed=a.precision == "mixed", explicit=a.algo == "explicit")
+        out.update(nk=wl.nk, nfreq=wl.nfreq, n=wl.n, D=wl.D, precision=a.precision, algo=a.algo)
+    else:
+        nfreq = a.nfreq or 4096
+        himp, weiss, g0, mu = _impurity(a.d, nfreq, 40.0)
+        uidx, ut = models.gen_Uijkl(a.d, 4.0, 2.6, 0.7)
+        W, G0, Hi = (torch.from_numpy(x).to(dev) for x in (weiss, g0, himp))
+
+        def run():
+            return ctx.SCGF2(Hi, W, G0, uidx, ut, mu, 40.0, a.ntau, 0.5, max_iter=a.loops, direct=a.direct)
+        out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct)
+    times = []
+    for _ in range(a.repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    out["seconds"] = times
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
