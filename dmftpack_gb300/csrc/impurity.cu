@@ -16,6 +16,7 @@
 // O(N_w N_tau)).  The FFT form is also free of the cancellation in the reference's per-segment formula, which
 // loses ~1e-10 relative at the lowest frequencies; DMFTGPU_DIRECT_DFT selects the direct per-point sums that
 // follow the reference's arithmetic.
+#include <algorithm>
 #include <vector>
 
 #include "impurity.h"
@@ -229,36 +230,21 @@ __global__ void k_posdef(int d, int nmat, const double2 *M, int mode, double sig
 }
 
 
-// one thread per frequency: Dw_i = F_i - V^H [(iw - H)^-1 + (iw - H2)^-1] V / 2  (:55-60; the inverses
-// through the eigen-decompositions of H and H2)
-__global__ void k_ft_subtract(int d, int nfreq, double beta, const double2 *F, const double2 *T, double2 *Dw,
-                              double2 *work) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nfreq) return;
-    const size_t dd = (size_t)d * d;
+// one thread per (frequency, element): Dw_i = F_i - V^H [(iw - H)^-1 + (iw - H2)^-1] V / 2 (:55-60), the
+// inverses through the eigen-decompositions of H and H2: V^H (iw - H)^-1 V = W1^H diag(1/(iw - eH)) W1
+__global__ void k_ft_subtract_el(int d, int nfreq, double beta, const double2 *F, const double2 *T, double2 *Dw) {
+    const int dd = d * d;
+    long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)nfreq * dd) return;
+    const int i = (int)(x / dd), e = (int)(x % dd), a = e % d, b = e / d;
     TailPtrs p = tail_ptrs(const_cast<double2 *>(T), d);
     const double w = (DG_PI / beta) + i * ((2 * DG_PI) / beta);
-    double2 *R = work + (size_t)i * 2 * dd, *Q = R + dd;
-    // R = UH diag(1/(iw - eH)) UH^H + UH2 diag(1/(iw - eH2)) UH2^H
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) {
-                s = cfma(cmul(DG_AT(p.UH, d, a, l), crcp(cmk(-p.eH[l], w))), cconj(DG_AT(p.UH, d, b, l)), s);
-                s = cfma(cmul(DG_AT(p.UH2, d, a, l), crcp(cmk(-p.eH2[l], w))), cconj(DG_AT(p.UH2, d, b, l)), s);
-            }
-            DG_AT(R, d, a, b) = s;
-        }
-    // Q = R V ; tail = V^H Q / 2
-    thread_matmul(d, R, p.V, Q);
-    const double2 *Fi = F + (size_t)i * dd;
-    double2 *Di = Dw + (size_t)i * dd;
-    for (int b = 0; b < d; b++)
-        for (int a = 0; a < d; a++) {
-            double2 s = cmk(0, 0);
-            for (int l = 0; l < d; l++) s = cfma(cconj(DG_AT(p.V, d, l, a)), DG_AT(Q, d, l, b), s);
-            DG_AT(Di, d, a, b) = csub(DG_AT(Fi, d, a, b), cscale(s, 0.5));
-        }
+    double2 tl = cmk(0, 0);
+    for (int l = 0; l < d; l++) {
+        tl = cadd(tl, cmul(cmul(cconj(DG_AT(p.W1, d, l, a)), DG_AT(p.W1, d, l, b)), crcp(cmk(-p.eH[l], w))));
+        tl = cadd(tl, cmul(cmul(cconj(DG_AT(p.W2, d, l, a)), DG_AT(p.W2, d, l, b)), crcp(cmk(-p.eH2[l], w))));
+    }
+    Dw[x] = csub(F[x], cscale(tl, 0.5));
 }
 
 // exact phase table: ph[q] = exp(-i pi q / ntau), q in [0, 2 ntau)
@@ -397,21 +383,45 @@ __host__ int ilog2(int n) {
 
 // single thread: the sequential positivity fix-up (src/FourierTransform.cpp:145-175,
 // src/SCGF2_fullLoop.cpp:657-688); eigenvalues of untouched points come precomputed in mineig
-__global__ void k_fixup_scan(int d, int ntau, double beta, double2 *M, const double *mineig, double2 *work,
-                             int *iwork, int *nfix) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One block.  Only points whose minimum eigenvalue is >= 0 are ever touched, and handling point t reads only
+// M[t-1] (already final) and the untouched M[t1 > t], so the block first lists those points in order (a
+// parallel compaction) and one thread then runs the reference's sequential scan over the list alone.
+constexpr int FIX_THREADS = 1024;
+__global__ void __launch_bounds__(FIX_THREADS) k_fixup_scan(int d, int ntau, double beta, double2 *M,
+                                                            const double *mineig, double2 *work, int *iwork,
+                                                            int *list, int *nfix) {
+    __shared__ int cnt[FIX_THREADS];
+    const int n1 = ntau + 1, per = (n1 + FIX_THREADS - 1) / FIX_THREADS;
+    const int t0 = threadIdx.x * per, t1e = min(n1, t0 + per);
+    int c = 0;
+    for (int t = t0; t < t1e; t++) c += (mineig[t] >= 0);
+    cnt[threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int i = 0; i < FIX_THREADS; i++) {
+            const int v = cnt[i];
+            cnt[i] = acc;
+            acc += v;
+        }
+        *nfix = acc;
+    }
+    __syncthreads();
+    int o = cnt[threadIdx.x];
+    for (int t = t0; t < t1e; t++)
+        if (mineig[t] >= 0) list[o++] = t;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     const size_t dd = (size_t)d * d;
-    double2 *A = work, *X = work + dd;
+    double2 *A = work;
     double *ev = (double *)(work + 2 * dd);
-    int fixed = 0;
-    for (int t = 0; t < ntau + 1; t++) {
+    const int nl = *nfix;
+    for (int li = 0; li < nl; li++) {
+        const int t = list[li];
         const double tau = t * beta / ntau;
-        const double mineigval = mineig[t];
-        double m11 = mineigval;
-        bool touched = false;
+        double m11 = mineig[t];
         double2 *Mt = M + (size_t)t * dd;
-        if (mineigval >= 0 && (t != 0 && t != ntau)) {
-            touched = true;
+        if (t != 0 && t != ntau) {
             for (int t1 = t + 1; t1 < ntau + 1; t1++) {
                 const double tau1 = t1 * beta / ntau, tprev = (t - 1) * beta / ntau;
                 const double2 *M1 = M + (size_t)t1 * dd, *M0 = M + (size_t)(t - 1) * dd;
@@ -425,15 +435,10 @@ __global__ void k_fixup_scan(int d, int ntau, double beta, double2 *M, const dou
                 if (m11 < 0) break;
             }
         }
-        if (m11 >= 0) {
-            touched = true;
+        if (m11 >= 0)
             for (int b = 0; b < d; b++)
                 for (int a = 0; a < d; a++) DG_AT(Mt, d, a, b) = cmk(a == b ? -1e-10 : 0.0, 0.0);
-        }
-        if (touched) fixed++;
     }
-    (void)X;
-    *nfix = fixed;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -473,50 +478,72 @@ __global__ void k_tau2w(int dd, int nfreq, int ntau, double beta, const double2 
 }
 
 // ---------------------------------------------------------------------------------------------------
-// getStimp (src/SCGF2_fullLoop.cpp:603-653): one block per tau point, one thread per output (i, j);
-// the U list is pre-sorted on the host by its first index (idx1 role) and by its last index (idx2 role)
+// getStimp (src/SCGF2_fullLoop.cpp:603-653): Sigma_ij(tau) = sum over U entries x1 = (i,q,m,k), x2 = (l,n,p,j)
+// of U1 U2 (-G_pq(beta - tau)) (G_kn G_ml - G_kl G_mn).  One block per S2_TB tau points, one thread per output
+// (i, j) for all of them; the U list is pre-sorted on the host by its first index (x1 role) and by its last
+// index (x2 role).  Per (x1, x2) pair the thread forms the 2x2 minor G_kn G_ml - G_kl G_mn once per tau and
+// accumulates U2 G'_pq times it; U1 multiplies the inner sum.
 // ---------------------------------------------------------------------------------------------------
+constexpr int S2_TB = 4;
 __global__ void k_sigma2(int d, int ntau, const int *__restrict__ byI, const int *__restrict__ byIoff,
                          const int *__restrict__ byJ, const int *__restrict__ byJoff, const int *__restrict__ uidx,
                          const double2 *__restrict__ ut, const double2 *__restrict__ G, double2 *__restrict__ S,
                          int *status) {
-    extern __shared__ double2 sg[];  // G(tau) [dd], G(beta - tau) [dd]
-    const int t = blockIdx.x;
-    const size_t dd = (size_t)d * d;
-    for (int q = threadIdx.x; q < (int)dd; q += blockDim.x) {
-        sg[q] = G[(size_t)t * dd + q];
-        sg[dd + q] = G[(size_t)(ntau - t) * dd + q];
+    extern __shared__ double2 sg[];  // per tau point b: G(tau) [dd], G(beta - tau) [dd]
+    const int t0 = blockIdx.x * S2_TB;
+    const int dd = d * d;
+    const int nb = min(S2_TB, ntau + 1 - t0);
+    for (int x = threadIdx.x; x < nb * dd; x += blockDim.x) {
+        const int b = x / dd, q = x % dd;
+        sg[(size_t)b * 2 * dd + q] = G[(size_t)(t0 + b) * dd + q];
+        sg[(size_t)b * 2 * dd + dd + q] = G[(size_t)(ntau - t0 - b) * dd + q];
     }
     __syncthreads();
-    const double2 *Gt = sg, *Gm = sg + dd;
-    for (int o = threadIdx.x; o < (int)dd; o += blockDim.x) {
+    for (int o = threadIdx.x; o < dd; o += blockDim.x) {
         const int i = o % d, j = o / d;
-        double2 acc = cmk(0, 0);
+        double2 acc[S2_TB];
+#pragma unroll
+        for (int b = 0; b < S2_TB; b++) acc[b] = cmk(0, 0);
         for (int a1 = byIoff[i]; a1 < byIoff[i + 1]; a1++) {
             const int x1 = byI[a1];
             const int qq = uidx[4 * x1 + 1], m = uidx[4 * x1 + 2], k = uidx[4 * x1 + 3];
-            const double2 u1 = ut[x1];
+            double2 in[S2_TB];
+#pragma unroll
+            for (int b = 0; b < S2_TB; b++) in[b] = cmk(0, 0);
             for (int a2 = byJoff[j]; a2 < byJoff[j + 1]; a2++) {
                 const int x2 = byJ[a2];
                 const int l = uidx[4 * x2], n = uidx[4 * x2 + 1], p = uidx[4 * x2 + 2];
-                const double2 u12 = cmul(u1, ut[x2]);
-                const double2 mg = cneg(DG_AT(Gm, d, p, qq));
-                // (-1) G_kl G_mn (-G'_pq) U1 U2 + G_kn G_ml (-G'_pq) U1 U2
-                const double2 bub = cmul(cmul(DG_AT(Gt, d, k, l), DG_AT(Gt, d, m, n)), mg);
-                const double2 exc = cmul(cmul(DG_AT(Gt, d, k, n), DG_AT(Gt, d, m, l)), mg);
-                acc = cadd(acc, cmul(csub(exc, bub), u12));
+                const double2 u2 = ut[x2];
+                const int ikn = k + n * d, iml = m + l * d, ikl = k + l * d, imn = m + n * d, ipq = p + qq * d;
+#pragma unroll
+                for (int b = 0; b < S2_TB; b++) {
+                    const double2 *Gt = sg + (size_t)b * 2 * dd, *Gm = Gt + dd;
+                    // minor = G_kn G_ml - G_kl G_mn
+                    double2 mn = cmul(Gt[ikn], Gt[iml]);
+                    const double2 g1 = Gt[ikl], g2 = Gt[imn];
+                    mn.x = fma(-g1.x, g2.x, fma(g1.y, g2.y, mn.x));
+                    mn.y = fma(-g1.x, g2.y, fma(-g1.y, g2.x, mn.y));
+                    // in -= U2 G'_pq minor
+                    in[b] = cfms(u2, cmul(Gm[ipq], mn), in[b]);
+                }
             }
+            const double2 u1 = ut[x1];
+#pragma unroll
+            for (int b = 0; b < S2_TB; b++) acc[b] = cfma(u1, in[b], acc[b]);
         }
-        S[(size_t)t * dd + o] = acc;
+        for (int b = 0; b < nb; b++) S[(size_t)(t0 + b) * dd + o] = acc[b];
     }
     __syncthreads();
     // Hermiticity asserts of the reference (:641-651): ||(G - G^H)/2i|| > 1e-10, ||(S - S^H)/2i|| > 1e-5
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < nb) {
+        const int b = threadIdx.x;
+        const double2 *Gt = sg + (size_t)b * 2 * dd;
+        const double2 *St = S + (size_t)(t0 + b) * dd;
         double ng = 0, ns = 0;
-        for (int b = 0; b < d; b++)
+        for (int c = 0; c < d; c++)
             for (int a = 0; a < d; a++) {
-                double2 vg = csub(DG_AT(Gt, d, a, b), cconj(DG_AT(Gt, d, b, a)));
-                double2 vs = csub(S[(size_t)t * dd + a + b * d], cconj(S[(size_t)t * dd + b + a * d]));
+                double2 vg = csub(DG_AT(Gt, d, a, c), cconj(DG_AT(Gt, d, c, a)));
+                double2 vs = csub(DG_AT(St, d, a, c), cconj(DG_AT(St, d, c, a)));
                 ng += cabs2(vg) / 4;
                 ns += cabs2(vs) / 4;
             }
@@ -642,28 +669,34 @@ int dg_fixup_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, double2 *M, con
     double2 *w = (double2 *)dg_buf(ctx, "imp.fixwork", 4 * (size_t)d * d * sizeof(double2) + 64);
     int *iw = (int *)dg_buf(ctx, "imp.fixiwork", (size_t)(d + 1) * sizeof(int));
     int *nfix = (int *)dg_buf(ctx, "imp.nfix", sizeof(int));
-    if (!w || !iw || !nfix) return DMFTGPU_NOMEM;
-    k_fixup_scan<<<1, 1, 0, ctx->stream>>>(d, ntau, beta, M, mineig, w, iw, nfix);
+    int *list = (int *)dg_buf(ctx, "imp.fixlist", (size_t)(ntau + 1) * sizeof(int));
+    if (!w || !iw || !nfix || !list) return DMFTGPU_NOMEM;
+    k_fixup_scan<<<1, FIX_THREADS, 0, ctx->stream>>>(d, ntau, beta, M, mineig, w, iw, list, nfix);
     DG_LAUNCH(ctx, "k_fixup_scan");
     return DMFTGPU_OK;
 }
 
-int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *fw, const double2 *mom,
-                 double2 *ft) {
+// tail data and Dw = F - tail for moments `mom`: the part of FourierTransform shared by every tau
+int dg_tail_prepare_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *fw, const double2 *mom,
+                        double2 *T, double2 *Dw) {
+    const size_t dd = (size_t)d * d;
+    DG_TRY(dg_tail_setup_dev(ctx, d, mom, T));
+    k_ft_subtract_el<<<dg_ceil_div((long long)nfreq * dd, 256), 256, 0, ctx->stream>>>(d, nfreq, beta, fw, T, Dw);
+    DG_LAUNCH(ctx, "k_ft_subtract_el");
+    return DMFTGPU_OK;
+}
+
+// the tau grid from prepared tail data: Fourier sums, tail terms, symmetrisation, positivity fix-up
+int dg_w2tau_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *T, const double2 *Dw,
+                      double2 *ft) {
     const size_t dd = (size_t)d * d;
     cudaStream_t s = ctx->stream;
-    double2 *T = (double2 *)dg_buf(ctx, "imp.tail", TAIL_SLOTS * dd * sizeof(double2));
     double *gtail = (double *)dg_buf(ctx, "imp.gtail", (size_t)(ntau + 1) * 2 * d * sizeof(double));
-    double2 *Dw = (double2 *)dg_buf(ctx, "imp.Dw", (size_t)nfreq * dd * sizeof(double2));
-    double2 *sw = (double2 *)dg_buf(ctx, "imp.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
     double2 *S = (double2 *)dg_buf(ctx, "imp.Ssum", (size_t)(ntau + 1) * dd * sizeof(double2));
     double *mineig = (double *)dg_buf(ctx, "imp.mineig", (size_t)(ntau + 1) * sizeof(double));
-    if (!T || !gtail || !Dw || !sw || !S || !mineig) return DMFTGPU_NOMEM;
+    if (!gtail || !S || !mineig) return DMFTGPU_NOMEM;
     double2 *ph;
     DG_TRY(dg_phase_table(ctx, ntau, &ph));
-    DG_TRY(dg_tail_setup_dev(ctx, d, mom, T));
-    k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, fw, T, Dw, sw);
-    DG_LAUNCH(ctx, "k_ft_subtract");
     if (fft_ok(ctx, ntau)) {
         const size_t sm = (size_t)ntau * sizeof(double2);
         DG_CUDA(cudaFuncSetAttribute(k_fft_w2tau, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -686,6 +719,16 @@ int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, cons
     DG_LAUNCH(ctx, "k_ft_finish_el");
     DG_TRY(dg_posdef_dev(ctx, d, ntau + 1, ft, 0, 1.0, 0.0, false, mineig, 0, 0));
     return dg_fixup_dev(ctx, d, ntau, beta, ft, mineig);
+}
+
+int dg_w2tau_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *fw, const double2 *mom,
+                 double2 *ft) {
+    const size_t dd = (size_t)d * d;
+    double2 *T = (double2 *)dg_buf(ctx, "imp.tail", TAIL_SLOTS * dd * sizeof(double2));
+    double2 *Dw = (double2 *)dg_buf(ctx, "imp.Dw", (size_t)nfreq * dd * sizeof(double2));
+    if (!T || !Dw) return DMFTGPU_NOMEM;
+    DG_TRY(dg_tail_prepare_dev(ctx, d, nfreq, beta, fw, mom, T, Dw));
+    return dg_w2tau_tail_dev(ctx, d, nfreq, ntau, beta, T, Dw, ft);
 }
 
 int dg_fourier_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *fw, int green,
@@ -733,8 +776,11 @@ int dg_sigma2_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, const DgUList 
     const size_t dd = (size_t)d * d;
     {
         DgTimer tm(ctx, "k_sigma2");
-        k_sigma2<<<ntau + 1, 128, 2 * dd * sizeof(double2), ctx->stream>>>(d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff,
-                                                                           U.uidx, U.ut, gt, st, ctx->d_status);
+        const int nt = std::min(1024, (int)((dd + 31) / 32 * 32));
+        DG_CUDA(cudaFuncSetAttribute(k_sigma2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(S2_TB * 2 * dd * sizeof(double2))));
+        k_sigma2<<<dg_ceil_div(ntau + 1, S2_TB), nt, S2_TB * 2 * dd * sizeof(double2), ctx->stream>>>(
+            d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff, U.uidx, U.ut, gt, st, ctx->d_status);
     }
     DG_LAUNCH(ctx, "k_sigma2");
     double *mineig = (double *)dg_buf(ctx, "imp.s2mineig", (size_t)(ntau + 1) * sizeof(double));
@@ -771,14 +817,25 @@ int dg_estimate_asymto_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, doub
 }
 
 // getoccMat: n = -G(tau = beta) with the m0 = 0, m1 = I green tail (src/SCGF2_fullLoop.cpp:539-549).
-// S(beta) = sum_i Dw_i exp(-i w_i beta) = -sum_i Dw_i (exp(-i pi (2i+1)) = -1); one block, a thread per element
-// (sequential sum over frequencies), then the tail term per element
-__global__ void k_occ_finish_blk(int d, int nfreq, double beta, const double2 *T, const double2 *Dw, double2 *occ) {
-    extern __shared__ double2 sw[];  // dd
-    const int dd = d * d;
+// S(beta) = sum_i Dw_i exp(-i w_i beta) = -sum_i Dw_i (exp(-i pi (2i+1)) = -1); one block: per element, P
+// threads sum fixed frequency ranges and the ranges are combined in order; then the tail term per element
+constexpr int OCC_THREADS = 1024;
+__global__ void __launch_bounds__(OCC_THREADS) k_occ_finish_blk(int d, int nfreq, double beta, const double2 *T,
+                                                                const double2 *Dw, double2 *occ) {
+    extern __shared__ double2 sw[];  // dd sums, then dd * P partials
+    const int dd = d * d, P = max(1, OCC_THREADS / dd), chunk = (nfreq + P - 1) / P;
+    double2 *part = sw + dd;
+    for (int x = threadIdx.x; x < dd * P; x += blockDim.x) {
+        const int e = x % dd, pp = x / dd;
+        double2 s = cmk(0, 0);
+        const int i1 = min(nfreq, (pp + 1) * chunk);
+        for (int i = pp * chunk; i < i1; i++) s = csub(s, Dw[(size_t)i * dd + e]);
+        part[x] = s;
+    }
+    __syncthreads();
     for (int e = threadIdx.x; e < dd; e += blockDim.x) {
         double2 s = cmk(0, 0);
-        for (int i = 0; i < nfreq; i++) s = csub(s, Dw[(size_t)i * dd + e]);
+        for (int pp = 0; pp < P; pp++) s = cadd(s, part[pp * dd + e]);
         sw[e] = s;
     }
     __syncthreads();
@@ -806,23 +863,35 @@ __global__ void k_set_identity_slot(int d, double2 *m1) {
     if (q < d * d) m1[q] = cmk((q % d) == (q / d) ? 1.0 : 0.0, 0.0);
 }
 
-int dg_occ_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *occ) {
+// occupation from prepared green-tail data (T, Dw of G)
+int dg_occ_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *T, const double2 *Dw,
+                    double2 *occ) {
     const size_t dd = (size_t)d * d;
-    cudaStream_t s = ctx->stream;
-    double2 *mom = (double2 *)dg_buf(ctx, "occ.mom", 4 * dd * sizeof(double2));
-    double2 *T = (double2 *)dg_buf(ctx, "occ.tail", TAIL_SLOTS * dd * sizeof(double2));
-    double2 *Dw = (double2 *)dg_buf(ctx, "occ.Dw", (size_t)nfreq * dd * sizeof(double2));
-    double2 *sw = (double2 *)dg_buf(ctx, "occ.subwork", (size_t)nfreq * 2 * dd * sizeof(double2));
-    if (!mom || !T || !Dw || !sw) return DMFTGPU_NOMEM;
-    DG_TRY(dg_moments_dev(ctx, d, nfreq, beta, gw, 1, mom));
-    k_set_identity_slot<<<dg_ceil_div((int)dd, 64), 64, 0, s>>>(d, mom + dd);  // m1 = I (m0 = 0 already)
-    DG_LAUNCH(ctx, "k_set_identity_slot");
-    DG_TRY(dg_tail_setup_dev(ctx, d, mom, T));
-    k_ft_subtract<<<dg_ceil_div(nfreq, 64), 64, 0, s>>>(d, nfreq, beta, gw, T, Dw, sw);
-    DG_LAUNCH(ctx, "k_ft_subtract");
-    k_occ_finish_blk<<<1, 128, dd * sizeof(double2), s>>>(d, nfreq, beta, T, Dw, occ);
+    const int P = std::max(1, OCC_THREADS / (int)dd);
+    k_occ_finish_blk<<<1, OCC_THREADS, dd * (1 + P) * sizeof(double2), ctx->stream>>>(d, nfreq, beta, T, Dw, occ);
     DG_LAUNCH(ctx, "k_occ_finish_blk");
     return DMFTGPU_OK;
+}
+
+// green-tail moments of G (m0 = 0, m1 = I), tail data and Dw: what getoccMat and FourierTransform(G, ., I,
+// true) share
+int dg_green_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *T, double2 *Dw) {
+    const size_t dd = (size_t)d * d;
+    double2 *mom = (double2 *)dg_buf(ctx, "occ.mom", 4 * dd * sizeof(double2));
+    if (!mom) return DMFTGPU_NOMEM;
+    DG_TRY(dg_moments_dev(ctx, d, nfreq, beta, gw, 1, mom));
+    k_set_identity_slot<<<dg_ceil_div((int)dd, 64), 64, 0, ctx->stream>>>(d, mom + dd);  // m1 = I (m0 = 0 already)
+    DG_LAUNCH(ctx, "k_set_identity_slot");
+    return dg_tail_prepare_dev(ctx, d, nfreq, beta, gw, mom, T, Dw);
+}
+
+int dg_occ_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *occ) {
+    const size_t dd = (size_t)d * d;
+    double2 *T = (double2 *)dg_buf(ctx, "occ.tail", TAIL_SLOTS * dd * sizeof(double2));
+    double2 *Dw = (double2 *)dg_buf(ctx, "occ.Dw", (size_t)nfreq * dd * sizeof(double2));
+    if (!T || !Dw) return DMFTGPU_NOMEM;
+    DG_TRY(dg_green_tail_dev(ctx, d, nfreq, beta, gw, T, Dw));
+    return dg_occ_tail_dev(ctx, d, nfreq, beta, T, Dw, occ);
 }
 
 int dg_ipt_kk_dev(dmftgpu_ctx *ctx, int nfreq, const double *a, const double *b, const double *c, double2 *s2) {

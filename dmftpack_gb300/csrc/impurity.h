@@ -24,4 +24,10 @@ int dg_dyson_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, double mu, con
                  const double2 *delta, const double2 *fock, const double2 *s2, double2 *gw, bool check);
 int dg_estimate_asymto_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, double2 *f, int order);
 int dg_occ_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *occ);
+// the shared parts of getoccMat and FourierTransform: T = tail data (9 d x d slots), Dw = F - tail
+int dg_green_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *gw, double2 *T, double2 *Dw);
+int dg_occ_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, double beta, const double2 *T, const double2 *Dw,
+                    double2 *occ);
+int dg_w2tau_tail_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, const double2 *T, const double2 *Dw,
+                      double2 *ft);
 int dg_ipt_kk_dev(dmftgpu_ctx *ctx, int nfreq, const double *a, const double *b, const double *c, double2 *s2);

@@ -145,21 +145,22 @@ __global__ void k_mom_trace(MomArgs g) {
 
 // one thread per (centre, element, moment): window averages; one per (centre, moment): variance
 __global__ void k_mom_avg(MomArgs g) {
+    // thread order: window centre fastest, so neighbouring threads read overlapping windows of one series
     const int DD = g.D * g.D;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long navg = (long long)g.C * DD * g.ncol;
     if (t < navg) {
-        int i = (int)(t % g.ncol);
-        long long r = t / g.ncol;
-        int ab = (int)(r % DD), ci = (int)(r / DD);
-        int a = ab / g.D, b = ab % g.D;
+        const int ci = (int)(t % g.C);
+        const long long r = t / g.C;
+        const int i = (int)(r % g.ncol), ab = (int)(r / g.ncol);
+        const int a = ab / g.D, b = ab % g.D;
         double2 s = cmk(0, 0);
         for (int iw = ci; iw <= ci + 2 * g.Nv; iw++) s = cadd(s, g.mt[((size_t)ab * g.R + iw) * g.ncol + i]);
         // Eigen MatrixXcd(a,b) with ab = a*Dim + b; stored column-major
         g.avg[((size_t)i * g.C + ci) * DD + a + b * g.D] = cmk(s.x / (2 * g.Nv + 1), s.y / (2 * g.Nv + 1));
     } else if (t < navg + (long long)g.C * g.ncol) {
-        long long u = t - navg;
-        int i = (int)(u % g.ncol), ci = (int)(u / g.ncol);
+        const long long u = t - navg;
+        const int ci = (int)(u % g.C), i = (int)(u / g.C);
         const double *tr = g.tr + (size_t)i * g.R + ci;
         int L = 2 * g.Nv + 1;
         double mean = 0;
@@ -240,16 +241,40 @@ __global__ void k_mom_gate_green(MomArgs g) {
 // single block: window choice per moment and the final averaged, Hermitised moments
 __global__ void k_mom_final(MomArgs g) {
     __shared__ int win[4];
+    __shared__ double rv[256];
+    __shared__ int ri[256];
     const int D = g.D, DD = D * D;
-    if (threadIdx.x < g.ncol) {
-        int m = threadIdx.x;
+    // sequential argmin of the reference (minPos = C-1; minPos = i when ok[i] and var[i] < var[minPos]) as a
+    // block reduction: the first index of the smallest var[i] among ok candidates with var[i] < var[C-1],
+    // else C-1
+    for (int m = 0; m < g.ncol; m++) {
         const double *var = g.var + (size_t)m * g.C;
-        int minPos = g.C - 1;
-        for (int i = 0; i < g.C; i++)
-            if (g.ok[i] && var[i] < var[minPos]) minPos = i;
-        win[m] = minPos;  // centre = minPos + Nv, window iw in [minPos, minPos + 2 Nv]
+        const double vlast = var[g.C - 1];
+        double bv = 0;
+        int bi = -1;
+        for (int i = threadIdx.x; i < g.C; i += blockDim.x)
+            if (g.ok[i] && var[i] < vlast && (bi < 0 || var[i] < bv)) {
+                bv = var[i];
+                bi = i;
+            }
+        rv[threadIdx.x] = bv;
+        ri[threadIdx.x] = bi;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if (threadIdx.x < h) {
+                const int oi = ri[threadIdx.x + h];
+                const double ov = rv[threadIdx.x + h];
+                const int mi = ri[threadIdx.x];
+                if (oi >= 0 && (mi < 0 || ov < rv[threadIdx.x] || (ov == rv[threadIdx.x] && oi < mi))) {
+                    rv[threadIdx.x] = ov;
+                    ri[threadIdx.x] = oi;
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) win[m] = ri[0] >= 0 ? ri[0] : g.C - 1;  // window iw in [win, win + 2 Nv]
+        __syncthreads();
     }
-    __syncthreads();
     for (int t = threadIdx.x; t < 4 * DD; t += blockDim.x) {
         int mom = t / DD, e = t % DD;
         int a = e % D, b = e / D;  // column-major element (a, b)

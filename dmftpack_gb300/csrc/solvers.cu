@@ -151,13 +151,15 @@ int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, doub
     double2 *occ = (double2 *)dg_buf(ctx, "scgf.occ", 2 * dd * sizeof(double2));
     double2 *fock = (double2 *)dg_buf(ctx, "scgf.fock", dd * sizeof(double2));
     double *nrm = (double *)dg_buf(ctx, "scgf.norms", 2 * sizeof(double));
-    if (!G || !Gin || !s2 || !gt || !st || !occ || !fock || !nrm) return DMFTGPU_NOMEM;
+    double2 *gT = (double2 *)dg_buf(ctx, "scgf.tail", 9 * dd * sizeof(double2));
+    double2 *gDw = (double2 *)dg_buf(ctx, "scgf.Dw", (size_t)nfreq * dd * sizeof(double2));
+    if (!G || !Gin || !s2 || !gt || !st || !occ || !fock || !nrm || !gT || !gDw) return DMFTGPU_NOMEM;
     double2 *occ_in = occ + dd;
     DG_CUDA(cudaMemsetAsync(G, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
     DG_CUDA(cudaMemsetAsync(s2, 0, (size_t)(nfreq + 3) * dd * sizeof(double2), s));
     DG_CUDA(cudaMemsetAsync(fock, 0, dd * sizeof(double2), s));
     DG_CUDA(cudaMemcpyAsync(G, gimp, len * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-    double2 *Gtail = G + (size_t)nfreq * dd;  // Gwimp[N_freq] = I (the m1 tail of every transform of G)
+    double2 *Gtail = G + (size_t)nfreq * dd;  // Gwimp[N_freq] = I
     k_set_identity<<<1, 32 * (int)((dd + 31) / 32), 0, s>>>(d, Gtail);
     DG_LAUNCH(ctx, "k_set_identity");
     DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
@@ -175,11 +177,13 @@ int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, doub
     while ((loop < 10 || normOuter > 1e-6 || normOcc > 1e-6) && loop < max_iter) {
         DG_CUDA(cudaMemcpyAsync(Gin, G, len * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         DG_CUDA(cudaMemcpyAsync(occ_in, occ, dd * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        // HF
-        DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
+        // HF, then Sigma^(2): G(iw) -> G(tau) -> Sigma(tau) -> Sigma(iw).  getoccMat(G) and
+        // FourierTransform(G, ., Gwimp[N_freq] = I, true) fit the same green-tail moments of the same G, so
+        // the moments, tail data and F - tail are formed once for both.
+        DG_TRY(dg_green_tail_dev(ctx, d, nfreq, beta, G, gT, gDw));
+        DG_TRY(dg_occ_tail_dev(ctx, d, nfreq, beta, gT, gDw, occ));
         DG_TRY(dg_fock_dev(ctx, d, Ul, occ, fock));
-        // Sigma^(2): G(iw) -> G(tau) (green tail, m1 = I) -> Sigma(tau) -> Sigma(iw)
-        DG_TRY(dg_fourier_dev(ctx, d, nfreq, ntau, beta, G, 1, Gtail, gt));
+        DG_TRY(dg_w2tau_tail_dev(ctx, d, nfreq, ntau, beta, gT, gDw, gt));
         DG_TRY(dg_sigma2_dev(ctx, d, ntau, beta, Ul, gt, st));
         DG_TRY(dg_tau2w_dev(ctx, d, nfreq, ntau, beta, st, s2, true));
         // G = [(iw + mu) - H_imp - Delta - F - Sigma^(2)]^-1
