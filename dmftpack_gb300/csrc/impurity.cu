@@ -21,6 +21,7 @@
 
 #include "impurity.h"
 #include "smallmat.cuh"
+#include "df.cuh"
 
 namespace {
 
@@ -81,7 +82,7 @@ __device__ TailPtrs tail_ptrs(double2 *T, int d) {
 // routines in shared memory: V = sqrt(m1); M2' = V^-H (2 m2) V^-1, M3' likewise; H = M2'/2 + sqrt(M3'/2 -
 // M2'^2/4) (or M2'/2 if that is not positive), H2 = M2' - H; eigen-decompositions of H and H2.  V^-1 =
 // U diag(ev^-1/2) U^H comes from the same eigen-decomposition as V = U diag(ev^1/2) U^H.
-constexpr int TAIL_THREADS = 128;
+constexpr int TAIL_THREADS = 32;  // one warp: the Jacobi steps are short and barrier-bound
 __host__ __device__ inline size_t tail_smem_bytes(int d) {
     return (size_t)8 * d * d * sizeof(double2) + 32 * sizeof(double) + 32 * sizeof(int) + 17 * sizeof(DgRot) +
            TAIL_THREADS * sizeof(double);
@@ -551,6 +552,76 @@ __global__ void k_sigma2(int d, int ntau, const int *__restrict__ byI, const int
     }
 }
 
+// getStimp in double-float (df.cuh) on the FP32 pipe: the same sums as k_sigma2 with every complex product
+// and sum formed as an unevaluated pair of floats (~2^-47 relative per operation); selected by
+// DMFTGPU_MIXED.  G enters from FP64 exactly split into hi + lo, S leaves as hi + lo in FP64.
+__global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, const int *__restrict__ byI,
+                                                   const int *__restrict__ byIoff, const int *__restrict__ byJ,
+                                                   const int *__restrict__ byJoff, const int *__restrict__ uidx,
+                                                   const double2 *__restrict__ ut, const double2 *__restrict__ G,
+                                                   double2 *__restrict__ S, int *status) {
+    extern __shared__ cdf sgf[];  // per tau point b: G(tau) [dd], G(beta - tau) [dd]
+    typedef OpsF O;
+    const int t0 = blockIdx.x * S2_TB;
+    const int dd = d * d;
+    const int nb = min(S2_TB, ntau + 1 - t0);
+    for (int x = threadIdx.x; x < nb * dd; x += blockDim.x) {
+        const int b = x / dd, q = x % dd;
+        sgf[(size_t)b * 2 * dd + q] = O::from(G[(size_t)(t0 + b) * dd + q]);
+        sgf[(size_t)b * 2 * dd + dd + q] = O::from(G[(size_t)(ntau - t0 - b) * dd + q]);
+    }
+    for (int x = nb * dd + threadIdx.x; x < S2_TB * dd; x += blockDim.x) {  // unused tau slots of the last block
+        const int b = x / dd, q = x % dd;
+        sgf[(size_t)b * 2 * dd + q] = O::zero();
+        sgf[(size_t)b * 2 * dd + dd + q] = O::zero();
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < dd; o += blockDim.x) {
+        const int i = o % d, j = o / d;
+        cdf acc[S2_TB];
+#pragma unroll
+        for (int b = 0; b < S2_TB; b++) acc[b] = O::zero();
+        for (int a1 = byIoff[i]; a1 < byIoff[i + 1]; a1++) {
+            const int x1 = byI[a1];
+            const int qq = uidx[4 * x1 + 1], m = uidx[4 * x1 + 2], k = uidx[4 * x1 + 3];
+            cdf in[S2_TB];
+#pragma unroll
+            for (int b = 0; b < S2_TB; b++) in[b] = O::zero();
+            for (int a2 = byJoff[j]; a2 < byJoff[j + 1]; a2++) {
+                const int x2 = byJ[a2];
+                const int l = uidx[4 * x2], n = uidx[4 * x2 + 1], p = uidx[4 * x2 + 2];
+                const cdf u2 = O::from(ut[x2]);
+                const int ikn = k + n * d, iml = m + l * d, ikl = k + l * d, imn = m + n * d, ipq = p + qq * d;
+#pragma unroll
+                for (int b = 0; b < S2_TB; b++) {
+                    const cdf *Gt = sgf + (size_t)b * 2 * dd, *Gm = Gt + dd;
+                    const cdf mn = O::fms(Gt[ikl], Gt[imn], O::mul(Gt[ikn], Gt[iml]));  // G_kn G_ml - G_kl G_mn
+                    in[b] = O::fms(u2, O::mul(Gm[ipq], mn), in[b]);
+                }
+            }
+            const cdf u1 = O::from(ut[x1]);
+#pragma unroll
+            for (int b = 0; b < S2_TB; b++) acc[b] = O::fma(u1, in[b], acc[b]);
+        }
+        for (int b = 0; b < nb; b++) S[(size_t)(t0 + b) * dd + o] = O::to(acc[b]);
+    }
+    __syncthreads();
+    if (threadIdx.x < nb) {
+        const int b = threadIdx.x;
+        const double2 *Gt = G + (size_t)(t0 + b) * dd;
+        const double2 *St = S + (size_t)(t0 + b) * dd;
+        double ng = 0, ns = 0;
+        for (int c = 0; c < d; c++)
+            for (int a = 0; a < d; a++) {
+                double2 vg = csub(DG_AT(Gt, d, a, c), cconj(DG_AT(Gt, d, c, a)));
+                double2 vs = csub(DG_AT(St, d, a, c), cconj(DG_AT(St, d, c, a)));
+                ng += cabs2(vg) / 4;
+                ns += cabs2(vs) / 4;
+            }
+        if (sqrt(ng) > 1e-10 || sqrt(ns) > 1e-5) dg_flag(status, DG_HERMIT);
+    }
+}
+
 // getFockOperator (:583-597), single thread
 __global__ void k_fock(int d, int nu, const int *uidx, const double2 *ut, const double2 *occ, double2 *fock) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -776,11 +847,18 @@ int dg_sigma2_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, const DgUList 
     const size_t dd = (size_t)d * d;
     {
         DgTimer tm(ctx, "k_sigma2");
-        const int nt = std::min(1024, (int)((dd + 31) / 32 * 32));
-        DG_CUDA(cudaFuncSetAttribute(k_sigma2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(S2_TB * 2 * dd * sizeof(double2))));
-        k_sigma2<<<dg_ceil_div(ntau + 1, S2_TB), nt, S2_TB * 2 * dd * sizeof(double2), ctx->stream>>>(
-            d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff, U.uidx, U.ut, gt, st, ctx->d_status);
+        const size_t sm = S2_TB * 2 * dd * sizeof(double2);
+        if (ctx->imp_mixed) {
+            DG_CUDA(cudaFuncSetAttribute(k_sigma2_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_sigma2_df<<<dg_ceil_div(ntau + 1, S2_TB), 128, sm, ctx->stream>>>(
+                d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff, U.uidx, U.ut, gt, st, ctx->d_status);
+        } else {
+            const int nt = std::min(1024, (int)((dd + 31) / 32 * 32));
+            DG_CUDA(cudaFuncSetAttribute(k_sigma2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_sigma2<<<dg_ceil_div(ntau + 1, S2_TB), nt, sm, ctx->stream>>>(d, ntau, U.byI, U.byIoff, U.byJ,
+                                                                               U.byJoff, U.uidx, U.ut, gt, st,
+                                                                               ctx->d_status);
+        }
     }
     DG_LAUNCH(ctx, "k_sigma2");
     double *mineig = (double *)dg_buf(ctx, "imp.s2mineig", (size_t)(ntau + 1) * sizeof(double));
@@ -1028,6 +1106,7 @@ int dmftgpu_sigma2_tau(dmftgpu_ctx *ctx, int dim, int ntau, double beta, int nu,
                        const double *gt, double *st_out, int flags) {
     if (!ctx || dim < 1 || ntau < 1 || nu < 0 || !gt || !st_out || (nu > 0 && (!uidx || !ut))) return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
     const size_t dd = (size_t)dim * dim;
     int st;
     DgUList U;

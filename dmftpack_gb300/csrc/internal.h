@@ -35,16 +35,23 @@ struct dmftgpu_ctx {
     double scgf_prev_norm = 0.0;      // mixing_check_outer's previous residual (a function static in the
                                       // reference, src/SCGF2_fullLoop.cpp:722-727): kept across SCGF2 calls
     bool ft_direct = false;           // DMFTGPU_DIRECT_DFT of the current call
+    bool imp_mixed = false;           // DMFTGPU_MIXED of the current call, for the impurity kernels
     bool timing = false;              // record CUDA events around the named hot kernels
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
 
-// sets ctx->ft_direct from a call's flags for the call's duration
+// sets ctx->ft_direct and ctx->imp_mixed from a call's flags for the call's duration
 struct DgFtMode {
     dmftgpu_ctx *ctx;
-    bool saved;
-    DgFtMode(dmftgpu_ctx *c, int flags) : ctx(c), saved(c->ft_direct) { ctx->ft_direct = (flags & DMFTGPU_DIRECT_DFT) != 0; }
-    ~DgFtMode() { ctx->ft_direct = saved; }
+    bool saved, saved_mixed;
+    DgFtMode(dmftgpu_ctx *c, int flags) : ctx(c), saved(c->ft_direct), saved_mixed(c->imp_mixed) {
+        ctx->ft_direct = (flags & DMFTGPU_DIRECT_DFT) != 0;
+        ctx->imp_mixed = (flags & DMFTGPU_MIXED) != 0;
+    }
+    ~DgFtMode() {
+        ctx->ft_direct = saved;
+        ctx->imp_mixed = saved_mixed;
+    }
 };
 
 // event pair around one launch of `name` when ctx->timing is on (no-op otherwise)

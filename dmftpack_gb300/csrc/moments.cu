@@ -144,25 +144,33 @@ __global__ void k_mom_trace(MomArgs g) {
 }
 
 // one thread per (centre, element, moment): window averages; one per (centre, moment): variance
+// window averages of the fitted moments and variances of their traces over 2 Nv + 1 consecutive windows.
+// One thread per run of AVG_RUN consecutive centres of one series: the first window is summed directly and
+// the next ones by sliding (add the entering, drop the leaving term), restarting every AVG_RUN centres
+constexpr int AVG_RUN = 32;
 __global__ void k_mom_avg(MomArgs g) {
-    // thread order: window centre fastest, so neighbouring threads read overlapping windows of one series
-    const int DD = g.D * g.D;
+    const int DD = g.D * g.D, L = 2 * g.Nv + 1;
+    const int nrun = (g.C + AVG_RUN - 1) / AVG_RUN;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long navg = (long long)g.C * DD * g.ncol;
+    long long navg = (long long)nrun * DD * g.ncol;
     if (t < navg) {
-        const int ci = (int)(t % g.C);
-        const long long r = t / g.C;
+        const int run = (int)(t % nrun);
+        const long long r = t / nrun;
         const int i = (int)(r % g.ncol), ab = (int)(r / g.ncol);
         const int a = ab / g.D, b = ab % g.D;
+        const double2 *x = g.mt + (size_t)ab * g.R * g.ncol + i;  // x[iw * ncol]
+        const int c0 = run * AVG_RUN, c1 = min(g.C, c0 + AVG_RUN);
         double2 s = cmk(0, 0);
-        for (int iw = ci; iw <= ci + 2 * g.Nv; iw++) s = cadd(s, g.mt[((size_t)ab * g.R + iw) * g.ncol + i]);
-        // Eigen MatrixXcd(a,b) with ab = a*Dim + b; stored column-major
-        g.avg[((size_t)i * g.C + ci) * DD + a + b * g.D] = cmk(s.x / (2 * g.Nv + 1), s.y / (2 * g.Nv + 1));
+        for (int iw = c0; iw < c0 + L; iw++) s = cadd(s, x[(size_t)iw * g.ncol]);
+        for (int ci = c0; ci < c1; ci++) {
+            if (ci > c0) s = csub(cadd(s, x[(size_t)(ci + L - 1) * g.ncol]), x[(size_t)(ci - 1) * g.ncol]);
+            // Eigen MatrixXcd(a,b) with ab = a*Dim + b; stored column-major
+            g.avg[((size_t)i * g.C + ci) * DD + a + b * g.D] = cmk(s.x / L, s.y / L);
+        }
     } else if (t < navg + (long long)g.C * g.ncol) {
         const long long u = t - navg;
         const int ci = (int)(u % g.C), i = (int)(u / g.C);
         const double *tr = g.tr + (size_t)i * g.R + ci;
-        int L = 2 * g.Nv + 1;
         double mean = 0;
         for (int j = 0; j < L; j++) mean += tr[j];
         mean /= L;
@@ -359,7 +367,7 @@ int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const doub
     DG_LAUNCH(ctx, "k_mom_solve");
     k_mom_trace<<<dg_ceil_div(g.R * g.ncol, 256), 256, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_trace");
-    long long navg = (long long)g.C * DD * g.ncol + (long long)g.C * g.ncol;
+    long long navg = (long long)((g.C + AVG_RUN - 1) / AVG_RUN) * DD * g.ncol + (long long)g.C * g.ncol;
     k_mom_avg<<<dg_ceil_div(navg, 256), 256, 0, s>>>(g);
     DG_LAUNCH(ctx, "k_mom_avg");
     if (g.green) {

@@ -42,22 +42,26 @@ __global__ void k_write_results(int d, int nfreq, const double2 *s2, const doubl
     if (gimp_out) gimp_out[t] = g;
 }
 
-// MatsubaraFtnnorm (src/SCGF2_fullLoop.cpp:791-805) of g - gin (gin == nullptr: of g) squared, and
-// ||occ - occ_in||_F^2; one block, fixed-order reduction
-__global__ void k_scgf_norms(int d, int nfreq, double beta, const double2 *gin, const double2 *g,
-                             const double2 *occ_in, const double2 *occ, double *out) {
-    __shared__ double red[256];
+// MatsubaraFtnnorm (src/SCGF2_fullLoop.cpp:791-805) of g - gin (gin == nullptr: of g) squared, per frequency
+__global__ void k_scgf_norm_terms(int d, int nfreq, double beta, const double2 *gin, const double2 *g, double *terms) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nfreq) return;
     const size_t dd = (size_t)d * d;
-    double s = 0;
-    for (int n = threadIdx.x; n < nfreq; n += blockDim.x) {
-        const double wn = (2 * n + 1) * DG_PI / beta;
-        double a = 0;
-        for (size_t e = 0; e < dd; e++) {
-            const double2 x = gin ? csub(gin[(size_t)n * dd + e], g[(size_t)n * dd + e]) : g[(size_t)n * dd + e];
-            a += cabs2(x);
-        }
-        s += a / wn;
+    const double wn = (2 * n + 1) * DG_PI / beta;
+    double a = 0;
+    for (size_t e = 0; e < dd; e++) {
+        const double2 x = gin ? csub(gin[(size_t)n * dd + e], g[(size_t)n * dd + e]) : g[(size_t)n * dd + e];
+        a += cabs2(x);
     }
+    terms[n] = a / wn;
+}
+
+// fixed-order sum of the per-frequency terms, and ||occ - occ_in||_F^2; one block
+__global__ void k_scgf_norms(int d, int nfreq, const double *terms, const double2 *occ_in, const double2 *occ,
+                             double *out) {
+    __shared__ double red[256];
+    double s = 0;
+    for (int n = threadIdx.x; n < nfreq; n += blockDim.x) s += terms[n];
     red[threadIdx.x] = s;
     __syncthreads();
     for (int h = blockDim.x / 2; h > 0; h >>= 1) {
@@ -67,7 +71,7 @@ __global__ void k_scgf_norms(int d, int nfreq, double beta, const double2 *gin, 
     if (threadIdx.x == 0) {
         double o = 0;
         if (occ_in)
-            for (size_t e = 0; e < dd; e++) o += cabs2(csub(occ[e], occ_in[e]));
+            for (int e = 0; e < d * d; e++) o += cabs2(csub(occ[e], occ_in[e]));
         out[0] = red[0];
         out[1] = o;
     }
@@ -151,9 +155,10 @@ int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, doub
     double2 *occ = (double2 *)dg_buf(ctx, "scgf.occ", 2 * dd * sizeof(double2));
     double2 *fock = (double2 *)dg_buf(ctx, "scgf.fock", dd * sizeof(double2));
     double *nrm = (double *)dg_buf(ctx, "scgf.norms", 2 * sizeof(double));
+    double *nterm = (double *)dg_buf(ctx, "scgf.nterms", (size_t)nfreq * sizeof(double));
     double2 *gT = (double2 *)dg_buf(ctx, "scgf.tail", 9 * dd * sizeof(double2));
     double2 *gDw = (double2 *)dg_buf(ctx, "scgf.Dw", (size_t)nfreq * dd * sizeof(double2));
-    if (!G || !Gin || !s2 || !gt || !st || !occ || !fock || !nrm || !gT || !gDw) return DMFTGPU_NOMEM;
+    if (!G || !Gin || !s2 || !gt || !st || !occ || !fock || !nrm || !nterm || !gT || !gDw) return DMFTGPU_NOMEM;
     double2 *occ_in = occ + dd;
     DG_CUDA(cudaMemsetAsync(G, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
     DG_CUDA(cudaMemsetAsync(s2, 0, (size_t)(nfreq + 3) * dd * sizeof(double2), s));
@@ -163,7 +168,9 @@ int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, doub
     k_set_identity<<<1, 32 * (int)((dd + 31) / 32), 0, s>>>(d, Gtail);
     DG_LAUNCH(ctx, "k_set_identity");
     DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
-    k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, beta, nullptr, G, nullptr, occ, nrm);
+    k_scgf_norm_terms<<<dg_ceil_div(nfreq, 128), 128, 0, s>>>(d, nfreq, beta, nullptr, G, nterm);
+    DG_LAUNCH(ctx, "k_scgf_norm_terms");
+    k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, nterm, nullptr, occ, nrm);
     DG_LAUNCH(ctx, "k_scgf_norms");
     double hn[2];
     DG_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s));
@@ -189,7 +196,9 @@ int dg_scgf2_dev(dmftgpu_ctx *ctx, int d, int nfreq, int ntau, double beta, doub
         // G = [(iw + mu) - H_imp - Delta - F - Sigma^(2)]^-1
         DG_TRY(dg_dyson_dev(ctx, d, nfreq, beta, mu, himp, weiss, fock, s2, G, true));
         DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
-        k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, beta, Gin, G, occ_in, occ, nrm);
+        k_scgf_norm_terms<<<dg_ceil_div(nfreq, 128), 128, 0, s>>>(d, nfreq, beta, Gin, G, nterm);
+        DG_LAUNCH(ctx, "k_scgf_norm_terms");
+        k_scgf_norms<<<1, 256, 0, s>>>(d, nfreq, nterm, occ_in, occ, nrm);
         DG_LAUNCH(ctx, "k_scgf_norms");
         DG_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s));
         int code = 0;

@@ -346,7 +346,7 @@ class Context:
         self._check("dmftgpu_fourier_tau2w", st, (OK, CAUSALITY) if allow_causality else (OK,))
         return out.result()
 
-    def getStimp(self, Gt, uidx, ut, beta, allow_hermiticity=False):
+    def getStimp(self, Gt, uidx, ut, beta, allow_hermiticity=False, mixed=False):
         dev = _is_torch(Gt)
         a = _Arr(Gt, dev)
         ntau, d = a.obj.shape[0] - 1, a.obj.shape[1]
@@ -354,7 +354,7 @@ class Context:
         out = _Arr.empty((ntau + 1, d, d), dev, like=a.obj)
         st = self.lib.dmftgpu_sigma2_tau(self.h, d, ntau, float(beta), nu, uidx.ctypes.data_as(_ip),
                                          ut.view(np.float64).ctypes.data_as(_dp), _vp(a.ptr), _vp(out.ptr),
-                                         self._flags(dev))
+                                         self._flags(dev, MIXED if mixed else 0))
         self._check("dmftgpu_sigma2_tau", st, (OK, HERMITICITY) if allow_hermiticity else (OK,))
         return out.result()
 
@@ -414,7 +414,8 @@ class Context:
         self._check("dmftgpu_ipt", st)
         return se.result(), gi.result(), no.result()[0]
 
-    def SCGF2(self, himp, weiss_field, Gwimp, uidx, ut, mu, beta, ntau, mixing, max_iter=2000, direct=False):
+    def SCGF2(self, himp, weiss_field, Gwimp, uidx, ut, mu, beta, ntau, mixing, max_iter=2000, direct=False,
+              mixed=False):
         """SC2PT solver (SCGF2): Gwimp (nfreq slots) is the initial G_imp.  Returns (SE_out[nfreq+5],
         Gwimp_out[nfreq+5], loops)."""
         dev = _is_torch(weiss_field)
@@ -429,7 +430,8 @@ class Context:
         st = self.lib.dmftgpu_scgf2(self.h, d, nf, ntau, float(beta), float(mu), float(mixing), _vp(h.ptr),
                                     _vp(dl.ptr), _vp(g.ptr), nu, uidx.ctypes.data_as(_ip),
                                     ut.view(np.float64).ctypes.data_as(_dp), int(max_iter), _vp(se.ptr),
-                                    C.byref(loops), self._flags(dev, DIRECT_DFT if direct else 0))
+                                    C.byref(loops),
+                                    self._flags(dev, (DIRECT_DFT if direct else 0) | (MIXED if mixed else 0)))
         self._check("dmftgpu_scgf2", st)
         return se.result(), g.result(), loops.value
 

@@ -2,7 +2,7 @@
 profiles/ are taken with.
 
     python -m dmftpack_gb300.profile_case gloc  [--k 16 --nfreq 2048 --precision mixed|fp64 --algo schur|explicit]
-    python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct]
+    python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct --mixed]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
@@ -42,6 +42,7 @@ def main():
     ap.add_argument("--ntau", type=int, default=8192)
     ap.add_argument("--loops", type=int, default=2)
     ap.add_argument("--direct", action="store_true")
+    ap.add_argument("--mixed", action="store_true", help="scgf2: double-float getStimp")
     ap.add_argument("--repeat", type=int, default=2)
     a = ap.parse_args()
     dev = torch.device("cuda:0")
@@ -63,8 +64,10 @@ def main():
         W, G0, Hi = (torch.from_numpy(x).to(dev) for x in (weiss, g0, himp))
 
         def run():
-            return ctx.SCGF2(Hi, W, G0, uidx, ut, mu, 40.0, a.ntau, 0.5, max_iter=a.loops, direct=a.direct)
-        out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct)
+            return ctx.SCGF2(Hi, W, G0, uidx, ut, mu, 40.0, a.ntau, 0.5, max_iter=a.loops, direct=a.direct,
+                             mixed=a.mixed)
+        out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
+                   mixed=a.mixed)
     times = []
     for _ in range(a.repeat):
         torch.cuda.synchronize()

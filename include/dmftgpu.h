@@ -35,7 +35,7 @@ enum {
 };
 
 #define DMFTGPU_DEVICE_PTRS 0x1 /* array arguments live in device memory */
-#define DMFTGPU_MIXED 0x2       /* FP32 factorisation + double-float (FP32-pair) refinement */
+#define DMFTGPU_MIXED 0x2       /* double-float (FP32-pair) arithmetic on the FP32 pipe: lattice sums and getStimp */
 #define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
 #define DMFTGPU_EXPLICIT 0x8    /* lattice sums by explicit n x n inversion of every (k, iw) matrix, as the
                                    reference does (default: the exact correlated-block Schur form) */

@@ -77,8 +77,11 @@ def test_ft_t_to_w_fft_against_exact_integral(ctx):
     assert e_dir < 1e-10, e_dir
 
 
+@pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("kanamori", [False, True])
-def test_getstimp(ctx, orc, kanamori):
+def test_getstimp(ctx, orc, kanamori, mixed):
+    """FP64 and double-float (mixed) getStimp against the oracle; the double-float sums carry ~1e-14 relative
+    rounding per term."""
     beta, nf, ntau = 10.0, 96, 128
     d = 6 if kanamori else 2
     G = _two_pole(nf, beta, d, seed=3)
@@ -86,7 +89,7 @@ def test_getstimp(ctx, orc, kanamori):
     gt = (gt + np.conj(np.swapaxes(gt, 1, 2))) / 2      # exactly Hermitian, as the reference asserts
     uidx, ut = orc.gen_uijkl(d, 4.0, 2.6, 0.7, density_density=not kanamori)
     ref, _, st = orc.sigma2_tau(gt, uidx, ut, beta)
-    got = ctx.getStimp(gt, uidx, ut, beta, allow_hermiticity=(st != 0))
+    got = ctx.getStimp(gt, uidx, ut, beta, allow_hermiticity=(st != 0), mixed=mixed)
     assert rel_err(got, ref) < TOL
 
 
@@ -193,8 +196,8 @@ def _scgf_case(orc, d=4, nfreq=64, ntau=256, beta=10.0, seed=7):
     return himp, weiss, g0, uidx, ut, mu, beta, ntau
 
 
-@pytest.mark.parametrize("max_iter", [12, 2000])
-def test_scgf2_matches_oracle(orc, max_iter):
+@pytest.mark.parametrize("max_iter,mixed", [(12, False), (2000, False), (12, True), (130, True)])
+def test_scgf2_matches_oracle(orc, max_iter, mixed):
     """SCGF2 loop (SC2PT solver) against the oracle composition: 12 loops, and the full run to the reference's
     stopping test (135 loops here, including the Pulay DIIS steps from loop 102).  Both sides start
     mixing_check_outer's memory from zero."""
@@ -203,7 +206,7 @@ def test_scgf2_matches_oracle(orc, max_iter):
                                    static={"prev": 0.0})
     c2 = lib.Context(0)
     try:
-        se, g, loops = c2.SCGF2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=max_iter)
+        se, g, loops = c2.SCGF2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=max_iter, mixed=mixed)
     finally:
         c2.close()
     assert loops == loops_o
