@@ -82,7 +82,7 @@ __device__ TailPtrs tail_ptrs(double2 *T, int d) {
 // routines in shared memory: V = sqrt(m1); M2' = V^-H (2 m2) V^-1, M3' likewise; H = M2'/2 + sqrt(M3'/2 -
 // M2'^2/4) (or M2'/2 if that is not positive), H2 = M2' - H; eigen-decompositions of H and H2.  V^-1 =
 // U diag(ev^-1/2) U^H comes from the same eigen-decomposition as V = U diag(ev^1/2) U^H.
-constexpr int TAIL_THREADS = 32;  // one warp: the Jacobi steps are short and barrier-bound
+constexpr int TAIL_THREADS = 128;
 __host__ __device__ inline size_t tail_smem_bytes(int d) {
     return (size_t)8 * d * d * sizeof(double2) + 32 * sizeof(double) + 32 * sizeof(int) + 17 * sizeof(DgRot) +
            TAIL_THREADS * sizeof(double);

@@ -3,10 +3,13 @@ profiles/ are taken with.
 
     python -m dmftpack_gb300.profile_case gloc  [--k 16 --nfreq 2048 --precision mixed|fp64 --algo schur|explicit]
     python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct --mixed]
+    python -m dmftpack_gb300.profile_case dmft  [--k 32 --nfreq 4096 --ntau 8192 --iters 2 --mixed --newton]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
        U' = 2.6 (the SC2PT workload's impurity sizes by default: d = 10, N_w = 4096, N_tau = 8192, beta = 40).
+dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
+       spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
 """
 import argparse
 import json
@@ -29,11 +32,51 @@ def _impurity(d, nfreq, beta, seed=11):
     return himp, weiss, g0, mu
 
 
+def run_dmft(ctx, dev, a):
+    """DMFT iterations (SC2PT) on the d+p model: returns per-iteration seconds, SCGF2 loops and residuals."""
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.dp28(k=a.k, nfreq=a.nfreq or 4096, ntau=a.ntau, beta=40.0)
+    D = wl.D
+    uidx, ut = models.gen_Uijkl(D, 4.0, 2.6, 0.7)
+    p = dict(solver="SC2PT", ntau=wl.ntau, n_electrons=wl.n_electrons, U=4.0, Uprime=2.6, J=0.7, mixing=0.5,
+             magnetism=0, dctype=1, nominal_charge=2.0, uidx=uidx, ut=ut, scgf_max_iter=a.scgf_max)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, D)
+    mixed = a.mixed
+    tcm = lambda t: t.transpose(-1, -2).contiguous()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    torch.cuda.synchronize()
+    t_hk = time.perf_counter() - t0
+    Hcm = tcm(Hd)
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    mu, _ = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, wl.n_electrons, mixed=mixed, newton=a.newton)
+    gl, _, nm = ctx.GreenFtn_w(lat, Hd, sig, mu, mixed=mixed, with_gwhf=False)
+    we = ctx.Construct_hyb_delta(list(range(D)), sig, gl, mu, wl.beta, Hd[:, :D, :D].mean(0))
+    se, we, nm, gl = tcm(sig), tcm(we), tcm(nm), tcm(gl)
+    iters = []
+    for it in range(1, a.iters + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)  # TightBinding rebuilds H(k)
+        Hcm = tcm(Hd)
+        mu, gi, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, gl, mu, mixed=mixed, newton=a.newton)
+        torch.cuda.synchronize()
+        iters.append({"seconds": time.perf_counter() - t0, "scgf_loops": int(res[4]), "mu": mu,
+                      "GwRD": float(res[0]), "NumMatRD": float(res[3])})
+    return {"nk": wl.nk, "n": wl.n, "D": D, "nfreq": wl.nfreq, "ntau": wl.ntau, "hk_seconds": t_hk,
+            "mixed": mixed, "newton": a.newton, "iterations": iters}
+
+
 def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft"])
+    ap.add_argument("--iters", type=int, default=2)
+    ap.add_argument("--newton", action="store_true")
+    ap.add_argument("--scgf-max", type=int, default=0)
     ap.add_argument("--k", type=int, default=16)
     ap.add_argument("--nfreq", type=int, default=None)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -68,6 +111,11 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
+    if a.case == "dmft":
+        out.update(run_dmft(ctx, dev, a))
+        print(json.dumps(out), flush=True)
+        ctx.close()
+        return
     times = []
     for _ in range(a.repeat):
         torch.cuda.synchronize()
