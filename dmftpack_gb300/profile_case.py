@@ -4,10 +4,12 @@ profiles/ are taken with.
     python -m dmftpack_gb300.profile_case gloc  [--k 16 --nfreq 2048 --precision mixed|fp64 --algo schur|explicit]
     python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct --mixed]
     python -m dmftpack_gb300.profile_case dmft  [--k 32 --nfreq 4096 --ntau 8192 --iters 2 --mixed --newton]
+    python -m dmftpack_gb300.profile_case lattice [--k 16 --nfreq 4096 --mixed --newton]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
        U' = 2.6 (the SC2PT workload's impurity sizes by default: d = 10, N_w = 4096, N_tau = 8192, beta = 40).
+lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
 """
@@ -30,6 +32,25 @@ def _impurity(d, nfreq, beta, seed=11):
     mu = 0.5
     g0 = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - himp[None] - weiss)
     return himp, weiss, g0, mu
+
+
+def run_lattice(ctx, dev, a):
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.dp28(k=a.k, nfreq=a.nfreq or 4096, ntau=a.ntau, beta=40.0)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, wl.D)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mu, npass = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, wl.n_electrons, mixed=a.mixed, newton=a.newton)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ctx.GreenFtn_w(lat, Hd, sig, mu, mixed=a.mixed)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq, "mixed": a.mixed, "newton": a.newton, "mu": mu,
+            "n_passes": npass, "mu_search_seconds": t1 - t0, "greenftn_w_seconds": t2 - t1}
 
 
 def run_dmft(ctx, dev, a):
@@ -73,7 +94,7 @@ def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2", "dmft"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice"])
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--newton", action="store_true")
     ap.add_argument("--scgf-max", type=int, default=0)
@@ -111,8 +132,8 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case == "dmft":
-        out.update(run_dmft(ctx, dev, a))
+    if a.case in ("dmft", "lattice"):
+        out.update(run_dmft(ctx, dev, a) if a.case == "dmft" else run_lattice(ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
         return
