@@ -20,6 +20,7 @@
 
 #include "gloc.cuh"
 #include "schur.cuh"
+#include "smallmat.cuh"
 
 namespace {
 
@@ -113,46 +114,82 @@ __global__ void k_sigall(int Nf, int D, int nh, int mask, double beta, const dou
     sig[t] = v;
 }
 
-// static eigen-decomposition of H(k) + S_inf on the correlated block (src/GreenFtn.cpp:197-215)
-// outputs eps[k][n], UP[k][l][a] = U(a,l) for a < D (correlated rows of the eigenvectors)
-__global__ void k_static_eig(int nk, int n, int D, int nh, int mask, const double2 *__restrict__ H,
-                             const double2 *__restrict__ m0, double2 *work, int *iwork, double *eps,
-                             double2 *UP, int *status) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
-    size_t nn = (size_t)n * n;
-    double2 *A0 = work + (size_t)k * 3 * nn, *A = A0 + nn, *U = A + nn;
-    const double2 *Hk = H + (size_t)k * nn;
-    for (size_t q = 0; q < nn; q++) A0[q] = Hk[q];
-    for (int b = 0; b < D; b++)
-        for (int a = 0; a < D; a++)
-            if (!mask || a / nh == b / nh) DG_AT(A0, n, a, b) = cadd(DG_AT(A0, n, a, b), m0[a + b * D]);
-    int st = thread_heig(n, A0, A, U, eps + (size_t)k * n, iwork + (size_t)k * n);
-    if (st) dg_flag(status, DG_NONCONV);
-    for (int l = 0; l < n; l++)
-        for (int a = 0; a < D; a++) UP[((size_t)k * n + l) * D + a] = DG_AT(U, n, a, l);
+// static eigen-decomposition of H(k) + S_inf on the correlated block (src/GreenFtn.cpp:197-215): outputs
+// eps[k][n], UP[k][l][a] = U(a,l) for a < D (correlated rows of the eigenvectors); and the per-k data of the
+// Schur form: H_QQ = V diag(e) V^H, b_l = H_PQ V(:,l) (Q = orbitals D..n-1).
+// One block per k, in shared memory (smallmat.cuh's block_heig): the static eigen-decomposition of H(k) + m0
+// (same output as k_static_eig) and the Schur data (same output as k_schur_prep).  Shared-memory layout:
+// three n x n complex matrices, then eigenvalues [64], order [64], rotations [33], reduction scratch [128].
+constexpr int EIG_THREADS = 128, EIG_NMAX = 64;
+inline size_t eig_blk_smem(int n) {
+    return (size_t)3 * n * n * sizeof(double2) + EIG_NMAX * sizeof(double) + EIG_NMAX * sizeof(int) +
+           (EIG_NMAX / 2 + 1) * sizeof(DgRot) + EIG_THREADS * sizeof(double);
+}
+struct EigSmem {
+    double2 *A0, *A, *U;
+    double *w;
+    int *ord;
+    DgRot *rot;
+    double *red;
+};
+__device__ inline EigSmem eig_smem(double2 *sm, int n) {
+    EigSmem e;
+    const size_t nn = (size_t)n * n;
+    e.A0 = sm;
+    e.A = sm + nn;
+    e.U = sm + 2 * nn;
+    e.w = (double *)(sm + 3 * nn);
+    e.ord = (int *)(e.w + EIG_NMAX);
+    e.rot = (DgRot *)(e.ord + EIG_NMAX);
+    e.red = (double *)(e.rot + EIG_NMAX / 2 + 1);
+    return e;
 }
 
-// per-k data of the Schur form: H_QQ = V diag(e) V^H, b_l = H_PQ V(:,l)   (Q = orbitals D..n-1)
-__global__ void k_schur_prep(int nk, int n, int D, const double2 *__restrict__ H, double2 *work, int *iwork,
-                             double *epsQ, double2 *B, int *status) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
-    const int m = n - D;
-    if (m == 0) return;
-    const size_t mm = (size_t)m * m;
-    double2 *A0 = work + (size_t)k * 3 * mm, *A = A0 + mm, *V = A + mm;
+__global__ void __launch_bounds__(EIG_THREADS) k_static_eig_blk(int n, int D, int nh, int mask,
+                                                                const double2 *__restrict__ H,
+                                                                const double2 *__restrict__ m0, double *eps,
+                                                                double2 *UP, int *status) {
+    extern __shared__ double2 esm[];
+    const int k = blockIdx.x;
+    const size_t nn = (size_t)n * n;
+    EigSmem e = eig_smem(esm, n);
+    const double2 *Hk = H + (size_t)k * nn;
+    for (int q = threadIdx.x; q < (int)nn; q += blockDim.x) {
+        const int a = q % n, b = q / n;
+        double2 v = Hk[q];
+        if (a < D && b < D && (!mask || a / nh == b / nh)) v = cadd(v, m0[a + b * D]);
+        e.A0[q] = v;
+    }
+    __syncthreads();
+    const int st = block_heig(n, e.A0, e.A, e.U, e.w, e.ord, e.rot, e.red);
+    for (int l = threadIdx.x; l < n; l += blockDim.x) eps[(size_t)k * n + l] = e.w[l];
+    for (int q = threadIdx.x; q < n * D; q += blockDim.x) {
+        const int l = q / D, a = q % D;
+        UP[((size_t)k * n + l) * D + a] = DG_AT(e.U, n, a, l);
+    }
+    if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
+}
+
+__global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, const double2 *__restrict__ H,
+                                                                double *epsQ, double2 *B, int *status) {
+    extern __shared__ double2 esm[];
+    const int k = blockIdx.x, m = n - D;
+    EigSmem e = eig_smem(esm, m);
     const double2 *Hk = H + (size_t)k * n * n;
-    for (int j = 0; j < m; j++)
-        for (int i = 0; i < m; i++) DG_AT(A0, m, i, j) = Hk[(D + i) + (size_t)(D + j) * n];
-    int st = thread_heig(m, A0, A, V, epsQ + (size_t)k * m, iwork + (size_t)k * m);
-    if (st) dg_flag(status, DG_NONCONV);
-    for (int l = 0; l < m; l++)
-        for (int a = 0; a < D; a++) {
-            double2 s = cmk(0, 0);
-            for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(V, m, j, l), s);
-            B[((size_t)k * m + l) * D + a] = s;
-        }
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+        const int i = q % m, j = q / m;
+        e.A0[q] = Hk[(D + i) + (size_t)(D + j) * n];
+    }
+    __syncthreads();
+    const int st = block_heig(m, e.A0, e.A, e.U, e.w, e.ord, e.rot, e.red);
+    for (int l = threadIdx.x; l < m; l += blockDim.x) epsQ[(size_t)k * m + l] = e.w[l];
+    for (int q = threadIdx.x; q < m * D; q += blockDim.x) {
+        const int l = q / D, a = q % D;
+        double2 s = cmk(0, 0);
+        for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(e.U, m, j, l), s);
+        B[((size_t)k * m + l) * D + a] = s;
+    }
+    if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
 }
 
 // Fermi parts: occ_k = P U f U^H P (with the +-100 cut-offs of src/GreenFtn.cpp:314-316) for NumMatrix,
@@ -367,11 +404,8 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     const int m = n - D;
     P.epsQ = (double *)dg_buf(ctx, "lat.epsQ", (size_t)nk * (m + 1) * sizeof(double));
     P.B = (double2 *)dg_buf(ctx, "lat.B", (size_t)nk * (m + 1) * D * sizeof(double2));
-    double2 *qwork = (double2 *)dg_buf(ctx, "lat.qwork", (size_t)nk * 3 * ((size_t)m * m + 1) * sizeof(double2));
-    int *qiwork = (int *)dg_buf(ctx, "lat.qiwork", (size_t)nk * (m + 1) * sizeof(int));
-    double2 *work = (double2 *)dg_buf(ctx, "lat.eigwork", (size_t)nk * 3 * n * n * sizeof(double2));
-    int *iwork = (int *)dg_buf(ctx, "lat.eigiwork", (size_t)nk * n * sizeof(int));
-    if (!P.m0 || !P.epsQ || !P.B || !qwork || !qiwork || !work || !iwork) return DMFTGPU_NOMEM;
+    if (!P.m0 || !P.epsQ || !P.B) return DMFTGPU_NOMEM;
+    if (n > EIG_NMAX) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: n > 64");
     if (!P.mom || !P.sig || !P.eps || !P.UP) return DMFTGPU_NOMEM;
     DG_TRY(dg_moments_dev(ctx, D, Nf, P.beta, dS, 0, P.mom));
     long long tot = 2LL * Nf * D * D;
@@ -381,14 +415,19 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     // static eigen-decomposition of H + m0 feeds only the Fermi terms, so it runs on the side stream
     // (FP64-pipe work) while the lattice kernel (FP32 pipe in the mixed form) proceeds
     if (m > 0) {
-        k_schur_prep<<<dg_ceil_div(nk, 32), 32, 0, s>>>(nk, n, D, P.H, qwork, qiwork, P.epsQ, P.B, ctx->d_status);
-        DG_LAUNCH(ctx, "k_schur_prep");
+        const size_t sm = eig_blk_smem(m);
+        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_schur_prep_blk<<<nk, EIG_THREADS, sm, s>>>(n, D, P.H, P.epsQ, P.B, ctx->d_status);
+        DG_LAUNCH(ctx, "k_schur_prep_blk");
     }
     DG_CUDA(cudaEventRecord(ctx->ev_fork, s));
     DG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-    k_static_eig<<<dg_ceil_div(nk, 32), 32, 0, ctx->side>>>(nk, n, D, P.nh, mask, P.H, P.m0, work, iwork, P.eps, P.UP,
-                                                            ctx->d_status);
-    DG_LAUNCH(ctx, "k_static_eig");
+    {
+        const size_t sm = eig_blk_smem(n);
+        DG_CUDA(cudaFuncSetAttribute(k_static_eig_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_static_eig_blk<<<nk, EIG_THREADS, sm, ctx->side>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, ctx->d_status);
+    }
+    DG_LAUNCH(ctx, "k_static_eig_blk");
     DG_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
     P.static_ready = ctx->ev_join;
     return DMFTGPU_OK;
@@ -469,8 +508,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     SchurKernel kern = in->get(mode, mixed);
     const int m = P.n - P.D, NG = 128 / in->W, nf2 = 2 * P.Nf, DD = P.D * P.D;
     int kc = 16;
-    while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m) > 48 * 1024) kc /= 2;
-    const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m);
+    while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n) > 96 * 1024) kc /= 2;
+    const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n);
     if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
     DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // k chunks: enough CTAs for ~8 per SM, at least 64 k points per chunk
@@ -493,6 +532,7 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.epsQ = P.epsQ;
     g.sig = P.sig;
     g.m0 = P.m0;
+    g.eps0 = P.eps;
     g.n = P.n;
     g.m = m;
     g.nk = P.nk;
@@ -507,6 +547,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.pblk0 = pblk0;
     g.ptr = ptr;
     g.status = ctx->d_status;
+    // the TRACE passes read the static eigenvalues (Tr G0), computed on the side stream
+    if (mode & dg::S_TRACE) DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     {
         DgTimer tm(ctx, "k_schur");
         kern<<<dim3(fblocks, nchunk), 128, smem, ctx->stream>>>(g);

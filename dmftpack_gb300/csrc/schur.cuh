@@ -6,12 +6,14 @@
 //   G_PP(z)  = S(z)^-1,   S(z)  = z - H_PP - Sigma(z) - sum_l w_l b_l b_l^H,   w_l = 1/(z - e_l),
 //   G0_PP(z) = S0(z)^-1,  S0(z) = S(z) + Sigma(z) - m0        (the reference's GwHF: Sigma -> its static
 //                                                              moment m0, src/GreenFtn.cpp:197-262)
-//   Tr G - Tr G0 = Tr (G_PP - G0_PP) + sum_l w_l^2 b_l^H (G_PP - G0_PP) b_l,
+//   Tr G(z) = Tr G_PP + sum_l w_l + sum_l w_l^2 b_l^H G_PP b_l,      Tr G0(z) = sum_j 1/(z - e0_j),
 //
-// with b_l = H_PQ V(:,l).  These are exact identities (block inversion), so G_loc, GwHF, NumMatrix and the
-// occupation sum of GiwToNele are the reference's quantities; the work per (k, iw) drops from an n x n
-// inversion to O(D^2 m + D^3).  d/dmu of the trace (Newton's dN/dmu, = -Tr G^2 + Tr G0^2) follows by
-// differentiating the same expression: dG_PP/dz = -G S' G with S' = I + sum_l w_l^2 b_l b_l^H.
+// with b_l = H_PQ V(:,l) and e0_j the eigenvalues of H + m0 (the reference's static spectrum, whose
+// resolvent U (z - e0)^-1 U^H is its G0, src/GreenFtn.cpp:197-262).  These are exact identities (block
+// inversion), so G_loc, GwHF, NumMatrix and the occupation sum of GiwToNele are the reference's quantities;
+// the work per (k, iw) drops from an n x n inversion to O(D^2 m + D^3).  d/dmu of the trace (Newton's
+// dN/dmu) is d/dz of the same expression: dG_PP/dz = -G S' G with S' = I + sum_l w_l^2 b_l b_l^H, dw_l/dz =
+// -w_l^2.  The BLOCK pass (G_loc, GwHF) inverts S and S0; the TRACE passes of the mu search invert S only.
 //
 // Mapping: a lane group of W lanes owns one Matsubara frequency and sweeps a chunk of k points; lane c holds
 // column c of S (and S0), inverted with warp_gj_inverse_t<Ops,DP,W> (DP >= D padded with identity), and
@@ -33,6 +35,7 @@ struct SchurArgs {
     const double *epsQ;   // [nk][m]
     const double2 *sig;   // [2 Nf][D][D]
     const double2 *m0;    // [D][D]
+    const double *eps0;   // [nk][n] eigenvalues of H + m0 (TRACE modes)
     int n, m, nk, nf2, D, wgrid, kc, kchunk;  // kc: k points staged per round; kchunk: k points per CTA
     double beta, mu;
     double2 *pblk, *pblk0;  // [nchunk][nf2][D][D]  per-chunk k sums (BLOCK)
@@ -48,12 +51,16 @@ __device__ __forceinline__ double group_sum(double v) {
 }
 
 // staged per-k data in shared memory (arithmetic type C): B[kc][m][D], e[kc][m] (mu - e_l, real),
-// hpp[kc][D][D] (-H_PP), then once m0[D][D]
+// hpp[kc][D][D] (-H_PP), e0[kc][n] (mu - e0_j, TRACE modes), then once m0[D][D]
 template <class Ops>
-__device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc, typename Ops::C *st) {
+__device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc, typename Ops::C *st, bool trace) {
     typedef typename Ops::C C;
     const int m = g.m, D = g.D, DD = D * D;
     C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
+    C *sE0 = sH + (size_t)g.kc * DD;
+    if (trace)
+        for (int t = threadIdx.x; t < nkc * g.n; t += blockDim.x)
+            sE0[t] = Ops::from(cmk(g.mu - g.eps0[(size_t)k0 * g.n + t], 0.0));
     for (int t = threadIdx.x; t < nkc * m * D; t += blockDim.x) sB[t] = Ops::from(g.B[(size_t)k0 * m * D + t]);
     for (int t = threadIdx.x; t < nkc * m; t += blockDim.x)
         sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k0 * m + t], 0.0));
@@ -70,11 +77,14 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     constexpr int NG = 128 / W;
     extern __shared__ double2 sm[];
     const int D = g.D, DD = D * D, m = g.m;
+    constexpr bool TR = (MODE & S_TRACE) != 0;
     C *st = reinterpret_cast<C *>(sm);
     C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
-    C *sM0 = sH + (size_t)g.kc * DD;
+    C *sE0 = sH + (size_t)g.kc * DD;                                      // [kc][n], TRACE modes
+    C *sM0 = sE0 + (TR ? (size_t)g.kc * g.n : 0);
     C *wla = sM0 + DD;                                                   // reciprocals [NG][m]
-    C *tla = wla + (size_t)NG * m;                                        // DERIV tiles [NG][3][DP][DP]
+    C *rla = wla + (size_t)NG * m;                                        // static reciprocals [NG][n] (TRACE)
+    C *tla = rla + (TR ? (size_t)NG * g.n : 0);                           // DERIV tiles [NG][2][DP][DP]
     const int c = threadIdx.x & (W - 1);
     const int grp = threadIdx.x / W;
     const int f_raw = blockIdx.x * NG + grp;
@@ -82,8 +92,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     const int f = fvalid ? f_raw : g.nf2 - 1;
     const int chunk = blockIdx.y;
     const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
-    C *tS = tla + (size_t)grp * 3 * DP * DP, *tG = tS + DP * DP, *tG0 = tG + DP * DP;
+    C *tS = tla + (size_t)grp * 2 * DP * DP, *tG = tS + DP * DP;
     C *wl = wla + (size_t)grp * m;
+    C *rl = rla + (size_t)grp * g.n;
     const bool col = c < D;
     for (int t = threadIdx.x; t < DD; t += blockDim.x) sM0[t] = Ops::from(g.m0[t]);
     // per-group frequency constants: iw (as a complex with zero real part), z = mu + iw, Sigma(:, c)
@@ -102,15 +113,19 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
         const int nkc = min(g.kc, kend - k0);
         __syncthreads();
-        schur_stage<Ops>(g, k0, nkc, st);
+        schur_stage<Ops>(g, k0, nkc, st, TR);
         __syncthreads();
         for (int kk = 0; kk < nkc; kk++) {
             const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
-            // w_l = 1/(z - e_l), shared by the group's lanes
+            // w_l = 1/(z - e_l), shared by the group's lanes; TRACE: r_j = 1/(z - e0_j)
             __syncwarp();
             for (int l = c; l < m; l += W) wl[l] = Ops::rcp(Ops::add(es[l], iwc));
+            if (TR) {
+                const C *e0s = sE0 + (size_t)kk * g.n;
+                for (int j = c; j < g.n; j += W) rl[j] = Ops::rcp(Ops::add(e0s[j], iwc));
+            }
             __syncwarp();
-            C s[DP], s0[DP];
+            C s[DP], s0[DP];  // s0: BLOCK mode only
 #pragma unroll
             for (int a = 0; a < DP; a++) {
                 if (col && a < D) s[a] = Ops::sub(hp[a + c * D], sgc[a]);
@@ -125,11 +140,14 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         if (a < D) s[a] = Ops::fms(bs[l * D + a], q, s[a]);
                 }
             }
+            if (MODE & S_BLOCK) {
 #pragma unroll
-            for (int a = 0; a < DP; a++)
-                s0[a] = (col && a < D) ? Ops::sub(Ops::add(s[a], sgc[a]), sM0[a + c * D]) : s[a];
-            C sp[DP];  // S' = I + sum_l w_l^2 b_l b_l^H (DERIV only)
+                for (int a = 0; a < DP; a++)
+                    s0[a] = (col && a < D) ? Ops::sub(Ops::add(s[a], sgc[a]), sM0[a + c * D]) : s[a];
+            }
             if (MODE & S_DERIV) {
+                // S' = I + sum_l w_l^2 b_l b_l^H, column c, straight into the group's tile
+                C sp[DP];
 #pragma unroll
                 for (int a = 0; a < DP; a++) sp[a] = (a == c && col) ? Ops::one() : Ops::zero();
                 if (col)
@@ -139,10 +157,15 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         for (int a = 0; a < DP; a++)
                             if (a < D) sp[a] = Ops::fma(bs[l * D + a], q, sp[a]);
                     }
+                __syncwarp();
+                if (c < DP) {
+#pragma unroll
+                    for (int a = 0; a < DP; a++) tS[a + c * DP] = sp[a];
+                }
             }
             sing |= warp_gj_inverse_t<Ops, DP, W>(s, c);
-            sing |= warp_gj_inverse_t<Ops, DP, W>(s0, c);
             if (MODE & S_BLOCK) {
+                sing |= warp_gj_inverse_t<Ops, DP, W>(s0, c);
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     accG[a] = Ops::add(accG[a], s[a]);
@@ -150,50 +173,46 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                 }
             }
             if (MODE & S_TRACE) {
-                C x[DP];
-#pragma unroll
-                for (int a = 0; a < DP; a++) x[a] = Ops::sub(s[a], s0[a]);
+                // lane c: column c of G_PP in s.  acc1 -> Tr G - Tr G0, acc2 -> d/dz of it (summed over lanes)
                 C acc1 = Ops::zero(), acc2 = Ops::zero();
 #pragma unroll
                 for (int a = 0; a < DP; a++)
-                    if (a == c && col) acc1 = x[a];
+                    if (a == c && col) acc1 = s[a];
+                for (int l = c; l < m; l += W) {
+                    acc1 = Ops::add(acc1, wl[l]);
+                    if (MODE & S_DERIV) acc2 = Ops::sub(acc2, Ops::mul(wl[l], wl[l]));
+                }
+                for (int j = c; j < g.n; j += W) {
+                    acc1 = Ops::sub(acc1, rl[j]);
+                    if (MODE & S_DERIV) acc2 = Ops::add(acc2, Ops::mul(rl[j], rl[j]));
+                }
                 C y[DP];
                 if (MODE & S_DERIV) {
+                    // Y = G S' G, column c: u = S' G(:,c), y = G u
                     __syncwarp();
                     if (c < DP) {
 #pragma unroll
-                        for (int a = 0; a < DP; a++) {
-                            tS[a + c * DP] = sp[a];
-                            tG[a + c * DP] = s[a];
-                            tG0[a + c * DP] = s0[a];
-                        }
+                        for (int a = 0; a < DP; a++) tG[a + c * DP] = s[a];
                     }
                     __syncwarp();
-                    C u[DP], u0[DP];
+                    C u[DP];
 #pragma unroll
                     for (int a = 0; a < DP; a++) {
                         u[a] = Ops::zero();
-                        u0[a] = Ops::zero();
 #pragma unroll
-                        for (int b = 0; b < DP; b++) {
-                            u[a] = Ops::fma(tS[a + b * DP], s[b], u[a]);
-                            u0[a] = Ops::fma(tS[a + b * DP], s0[b], u0[a]);
-                        }
+                        for (int b = 0; b < DP; b++) u[a] = Ops::fma(tS[a + b * DP], s[b], u[a]);
                     }
 #pragma unroll
                     for (int a = 0; a < DP; a++) {
                         C v = Ops::zero();
 #pragma unroll
-                        for (int b = 0; b < DP; b++) {
-                            v = Ops::fma(tG[a + b * DP], u[b], v);
-                            v = Ops::fms(tG0[a + b * DP], u0[b], v);
-                        }
+                        for (int b = 0; b < DP; b++) v = Ops::fma(tG[a + b * DP], u[b], v);
                         y[a] = v;
                     }
                     __syncwarp();
 #pragma unroll
                     for (int a = 0; a < DP; a++)
-                        if (a == c && col) acc2 = Ops::neg(y[a]);
+                        if (a == c && col) acc2 = Ops::sub(acc2, y[a]);
                 }
                 if (col) {
                     for (int l = 0; l < m; l++) {
@@ -202,7 +221,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 #pragma unroll
                         for (int a = 0; a < DP; a++)
                             if (a < D) {
-                                px = Ops::add(px, Ops::mulc(x[a], bs[l * D + a]));
+                                px = Ops::add(px, Ops::mulc(s[a], bs[l * D + a]));
                                 if (MODE & S_DERIV) py = Ops::add(py, Ops::mulc(y[a], bs[l * D + a]));
                             }
                         const C w2 = Ops::mul(wl[l], wl[l]);
@@ -214,8 +233,8 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         }
                     }
                 }
-                acct1 += group_sum<DP, W>(col ? Ops::re(acc1) : 0.0);
-                if (MODE & S_DERIV) acct2 += group_sum<DP, W>(col ? Ops::re(acc2) : 0.0);
+                acct1 += group_sum<DP, W>(Ops::re(acc1));
+                if (MODE & S_DERIV) acct2 += group_sum<DP, W>(Ops::re(acc2));
             }
         }
     }
@@ -236,10 +255,11 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 }
 
 // shared-memory bytes of one k_schur launch
-inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m) {
+inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m, int n) {
     const int NG = 128 / W;
     size_t s = (size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D + (size_t)NG * m;
-    if (mode & S_DERIV) s += (size_t)NG * 3 * DP * DP;
+    if (mode & S_TRACE) s += (size_t)kc * n + (size_t)NG * n;
+    if (mode & S_DERIV) s += (size_t)NG * 2 * DP * DP;
     return s * 16;
 }
 
