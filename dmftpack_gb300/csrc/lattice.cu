@@ -21,6 +21,7 @@
 #include "gloc.cuh"
 #include "schur.cuh"
 #include "smallmat.cuh"
+#include "adjoint.cuh"
 
 namespace {
 
@@ -600,6 +601,96 @@ int check_lat(const dmftgpu_lattice *L) {
     return DMFTGPU_OK;
 }
 
+
+// fixed-order sums over chunks of the derivative kernel's partials, scaled by -1/N_k
+__global__ void k_ad_reduce(int nchunk, long long len, double scale, const double2 *p, double2 *out) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= len) return;
+    double2 s = cmk(0, 0);
+    for (int q = 0; q < nchunk; q++) s = cadd(s, p[(size_t)q * len + t]);
+    out[t] = cscale(s, scale);
+}
+__global__ void k_ad_mu(int n, double scale, const double *p, double *out) {
+    __shared__ double red[256];
+    double s = 0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s += p[t];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0] * scale;
+}
+
+struct AdInst {
+    int DP, W;
+    dg::AdKernel (*get)(int);
+};
+const AdInst kAdInst[] = {
+    {1, 1, dg::ad_kernel_1},    {2, 2, dg::ad_kernel_2},    {3, 4, dg::ad_kernel_3},   {4, 4, dg::ad_kernel_4},
+    {6, 8, dg::ad_kernel_6},    {8, 8, dg::ad_kernel_8},    {10, 16, dg::ad_kernel_10}, {12, 16, dg::ad_kernel_12},
+    {16, 16, dg::ad_kernel_16}, {20, 32, dg::ad_kernel_20},
+};
+
+// one derivative pass: VJP (gin = Gbar; out = Sigma_bar; *dmu_out = mu_bar on the device) or JVP (gin =
+// Sigma_dot, mu_dot; out = G_loc_dot)
+int run_ad(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, const double2 *gin, double mu_dot, double2 *out,
+           double *dmu_out) {
+    const AdInst *in = nullptr;
+    for (const auto &x : kAdInst)
+        if (x.DP >= P.D) {
+            in = &x;
+            break;
+        }
+    if (!in) return dg_fail(ctx, DMFTGPU_BADARG, "derivatives: correlated block larger than 20");
+    dg::AdKernel kern = in->get(mode);
+    const int m = P.n - P.D, NG = 128 / in->W, nf = P.Nf, DD = P.D * P.D;
+    int kc = 16;
+    while (kc > 1 && dg::ad_smem(in->DP, in->W, kc, P.D, m) > 96 * 1024) kc /= 2;
+    const size_t smem = dg::ad_smem(in->DP, in->W, kc, P.D, m);
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int fblocks = dg_ceil_div(nf, NG);
+    int nchunk = std::max(1, std::min(dg_ceil_div(P.nk, 64), dg_ceil_div(8 * 152, fblocks)));
+    const int kchunk = dg_ceil_div(P.nk, nchunk);
+    nchunk = dg_ceil_div(P.nk, kchunk);
+    double2 *pout = (double2 *)dg_buf(ctx, "ad.pout", (size_t)nchunk * nf * DD * sizeof(double2));
+    double *pmu = (double *)dg_buf(ctx, "ad.pmu", (size_t)nchunk * nf * sizeof(double));
+    if (!pout || !pmu) return DMFTGPU_NOMEM;
+    dg::AdArgs g;
+    g.H = P.H;
+    g.B = P.B;
+    g.epsQ = P.epsQ;
+    g.sig = P.sig;  // the first nf slots are the input Sigma(iw_n)
+    g.gin = gin;
+    g.mu_dot = mu_dot;
+    g.n = P.n;
+    g.m = m;
+    g.nk = P.nk;
+    g.nf = nf;
+    g.D = P.D;
+    g.kc = kc;
+    g.kchunk = kchunk;
+    g.beta = P.beta;
+    g.mu = mu;
+    g.pout = pout;
+    g.pmu = pmu;
+    g.status = ctx->d_status;
+    {
+        DgTimer tm(ctx, "k_gloc_ad");
+        kern<<<dim3(fblocks, nchunk), 128, smem, ctx->stream>>>(g);
+    }
+    DG_LAUNCH(ctx, "k_gloc_ad");
+    const long long len = (long long)nf * DD;
+    k_ad_reduce<<<dg_ceil_div(len, 256), 256, 0, ctx->stream>>>(nchunk, len, -1.0 / P.nk, pout, out);
+    DG_LAUNCH(ctx, "k_ad_reduce");
+    if (mode == dg::AD_VJP) {
+        k_ad_mu<<<1, 256, 0, ctx->stream>>>(nchunk * nf, -1.0 / P.nk, pmu, dmu_out);
+        DG_LAUNCH(ctx, "k_ad_mu");
+    }
+    return DMFTGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -688,6 +779,65 @@ int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double 
     DG_TRY(dg_out_done(ctx, gw, dG, Nf * DD * sizeof(double2), flags));
     if (gwhf) DG_TRY(dg_out_done(ctx, gwhf, dG0, Nf * DD * sizeof(double2), flags));
     DG_TRY(dg_out_done(ctx, nummat, dN, DD * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// reverse mode: Sigma_bar = -(1/N_k) sum_k G^H Gbar G^H, mu_bar = -(1/N_k) sum Re Tr[(G S' G)^H Gbar]
+int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                     const double *gbar, double *sigma_bar, double *mu_bar, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !gbar || !sigma_bar || !mu_bar) return DMFTGPU_BADARG;
+    if (L->ncl != 1) return dg_fail(ctx, DMFTGPU_BADARG, "gloc_vjp: one correlated cluster");
+    cudaSetDevice(ctx->device);
+    const int D = L->nh, Nf = L->nfreq;
+    const size_t DD = (size_t)D * D;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, Nf * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    const double2 *dGb = (const double2 *)dg_in(ctx, gbar, Nf * DD * sizeof(double2), flags, "io.gbar", &st);
+    if (st) return st;
+    double2 *dSb = (double2 *)dg_out(ctx, sigma_bar, Nf * DD * sizeof(double2), flags, "io.sigbar", &st);
+    if (st) return st;
+    double *dmu = (double *)dg_buf(ctx, "ad.mubar", sizeof(double));
+    if (!dmu) return DMFTGPU_NOMEM;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
+    DG_TRY(run_ad(ctx, P, dg::AD_VJP, mu, dGb, 0.0, dSb, dmu));
+    DG_TRY(dg_out_done(ctx, sigma_bar, dSb, Nf * DD * sizeof(double2), flags));
+    DG_CUDA(cudaMemcpyAsync(mu_bar, dmu, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// forward mode: G_loc_dot = -(1/N_k) sum_k G (Sigma_dot + mu_dot S') G
+int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                     const double *sigma_dot, double mu_dot, double *gloc_dot, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !sigma_dot || !gloc_dot) return DMFTGPU_BADARG;
+    if (L->ncl != 1) return dg_fail(ctx, DMFTGPU_BADARG, "gloc_jvp: one correlated cluster");
+    cudaSetDevice(ctx->device);
+    const int D = L->nh, Nf = L->nfreq;
+    const size_t DD = (size_t)D * D;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, Nf * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    const double2 *dSd = (const double2 *)dg_in(ctx, sigma_dot, Nf * DD * sizeof(double2), flags, "io.sigdot", &st);
+    if (st) return st;
+    double2 *dGd = (double2 *)dg_out(ctx, gloc_dot, Nf * DD * sizeof(double2), flags, "io.glocdot", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
+    DG_TRY(run_ad(ctx, P, dg::AD_JVP, mu, dSd, mu_dot, dGd, nullptr));
+    DG_TRY(dg_out_done(ctx, gloc_dot, dGd, Nf * DD * sizeof(double2), flags));
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;

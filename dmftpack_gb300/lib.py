@@ -31,7 +31,7 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT = 0x1, 0x2, 0x4, 0x8, 0x10
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -91,6 +91,8 @@ def load(require_built=True):
     lib.dmftgpu_hk.argtypes = [_vp, C.c_int, C.c_int, _ip, _dp, C.c_int, C.c_int, C.c_int, _vp, C.c_int]
     lib.dmftgpu_moments.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, C.c_int, _vp, C.c_int]
     lib.dmftgpu_greenftn_w.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
+    lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
@@ -278,6 +280,32 @@ class Context:
                                          self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)))
         self._check("dmftgpu_greenftn_w", st)
         return gw.result(), (g0.result() if g0 else None), nm.result()
+
+    def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
+        """Reverse mode of G_loc = GreenFtn_w(...)[0]: returns (Sigma_bar[nfreq,D,D], mu_bar) for the cotangent
+        Gbar[nfreq,D,D] (torch's complex-autograd convention: x_bar = J^H y_bar)."""
+        dev = _is_torch(H_k)
+        h, s, gb = _Arr(H_k, dev), _Arr(SelfE_w, dev), _Arr(Gbar, dev)
+        D = lat.D
+        out = _Arr.empty((lat.nfreq, D, D), dev, like=h.obj)
+        mub = C.c_double()
+        L = lat._c()
+        st = self.lib.dmftgpu_gloc_vjp(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(gb.ptr),
+                                       _vp(out.ptr), C.byref(mub), self._flags(dev))
+        self._check("dmftgpu_gloc_vjp", st)
+        return out.result(), mub.value
+
+    def GreenFtn_w_jvp(self, lat, H_k, SelfE_w, mu, Sigma_dot, mu_dot=0.0):
+        """Forward mode of G_loc = GreenFtn_w(...)[0] along (Sigma_dot, mu_dot): returns G_loc_dot."""
+        dev = _is_torch(H_k)
+        h, s, sd = _Arr(H_k, dev), _Arr(SelfE_w, dev), _Arr(Sigma_dot, dev)
+        D = lat.D
+        out = _Arr.empty((lat.nfreq, D, D), dev, like=h.obj)
+        L = lat._c()
+        st = self.lib.dmftgpu_gloc_jvp(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(sd.ptr),
+                                       float(mu_dot), _vp(out.ptr), self._flags(dev))
+        self._check("dmftgpu_gloc_jvp", st)
+        return out.result()
 
     def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False):
         dev = _is_torch(H_k)

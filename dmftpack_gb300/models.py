@@ -127,6 +127,60 @@ def dp28(k=32, beta=40.0, nfreq=4096, ntau=8192, seed=20250105, rmax=4, U=4.0, J
                     {"U": U, "J": J, "Up": U - 2 * J})
 
 
+def _ls_d():
+    """L.S for l = 2 on (m, spin) pairs ordered (m = -2..2) x (up, down), spin-orbital index 2*m_idx + spin."""
+    ms = np.arange(-2, 3)
+    Lz = np.diag(ms).astype(complex)
+    Lp = np.zeros((5, 5), complex)
+    for i, m in enumerate(ms[:-1]):
+        Lp[i + 1, i] = np.sqrt(2 * 3 - m * (m + 1))  # <m+1|L+|m> = sqrt(l(l+1) - m(m+1)), l = 2
+    Lm = Lp.conj().T
+    sz = np.diag([0.5, -0.5]).astype(complex)
+    sp = np.array([[0, 1], [0, 0]], complex)
+    sm = sp.T.copy()
+    return np.kron(Lz, sz) + 0.5 * (np.kron(Lp, sm) + np.kron(Lm, sp))
+
+
+def soc56(k=16, beta=30.0, nfreq=2048, ntau=None, seed=20250103, rmax=3, lam=0.1):
+    """Two correlated sites with spin-orbit coupling: 2 x 5 d + 6 x 3 p = 28 orbitals x 2 spins = 56 x 56
+    complex Hermitian H(k) (spin-orbital index 2*orbital + spin, the d orbitals of both sites first), seeded
+    spin-independent t(R) over |R_i| <= 3 (343 R vectors) with 1/|R|^2 decay, on-site d at 0 and p at -3 eV,
+    SOC lam L.S on each site's d shell; Sigma is a dense 20 x 20 block M0 + M1/(iw) with random Hermitian M0 and
+    positive semidefinite M1 (causal)."""
+    norb = 28
+    n = 2 * norb
+    rng = np.random.default_rng(seed)
+    rvecs = [(a, b, c) for a in range(-rmax, rmax + 1) for b in range(-rmax, rmax + 1) for c in range(-rmax, rmax + 1)]
+
+    def draw(R):
+        r2 = max(1, R[0] ** 2 + R[1] ** 2 + R[2] ** 2)
+        t = (rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb))) / np.sqrt(2) / (2 * r2)
+        return np.kron(t, np.eye(2))
+
+    onsite = np.repeat(np.array([0.0] * 10 + [-3.0] * 18), 2)
+    rows, vals = _hermitian_hoppings(n, rvecs, draw, onsite)
+    soc = lam * _ls_d()
+    extra_r, extra_v = [], []
+    for site in range(2):
+        o = 10 * site
+        for i in range(10):
+            for j in range(10):
+                if soc[i, j] != 0:
+                    extra_r.append((0, 0, 0, o + i, o + j))
+                    extra_v.append(soc[i, j])
+    rows = np.concatenate([rows, np.asarray(extra_r, np.int32)])
+    vals = np.concatenate([vals, np.asarray(extra_v, np.complex128)])
+    D = 20
+    A = rng.normal(size=(D, D)) + 1j * rng.normal(size=(D, D))
+    M0 = 0.2 * (A + A.conj().T) / 2
+    Bm = rng.normal(size=(D, D)) + 1j * rng.normal(size=(D, D))
+    M1 = 0.1 * Bm @ Bm.conj().T / D
+    wn = PI * (2 * np.arange(nfreq) + 1) / beta
+    sigma = M0[None] + M1[None] / (1j * wn[:, None, None])
+    return Workload("soc56", n, rows, vals, (k, k, k), beta, nfreq, ntau if ntau else 2 * nfreq, 1, D, sigma, 40.0,
+                    {"M0": M0, "M1": M1})
+
+
 def gen_Uijkl(n_spinorb, U, Uprime, JH, density_density=False):
     """Interaction list (U_index (nu, 4) int32, U_tensor (nu,) complex) for H_int = 1/2 sum U_ijkl c+_i c+_j c_l c_k
     on spin-orbitals ordered (orbital, spin) = (i // 2, i % 2): gen_Uijkl (Slater-Kanamori: density-density,

@@ -104,6 +104,18 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk,
 int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma,
                       double mu, double dmu, double n_target, double *mu_out, int *n_eval, int flags);
 
+/* Derivatives of GreenFtn_w's G_loc(iw_n) = (1/N_k) sum_k G_PP(k, iw_n), n < nfreq, for one correlated cluster
+ * (no counterpart in the reference, which has no derivatives; they supply dN/dmu-style Newton steps and
+ * Jacobian-vector products of the self-consistency residual).  dG_PP = -G_PP dSigma G_PP - dmu (G^2)_PP, with G
+ * recomputed per (k, iw) from the Schur data (never stored).
+ * dmftgpu_gloc_vjp: gbar[nfreq][D][D] -> sigma_bar[nfreq][D][D] = -(1/N_k) sum_k G^H gbar G^H and *mu_bar (host) =
+ *   -(1/N_k) sum Re Tr[((G^2)_PP)^H gbar] (the adjoint x_bar = J^H y_bar of complex autograd).
+ * dmftgpu_gloc_jvp: (sigma_dot[nfreq][D][D], mu_dot) -> gloc_dot[nfreq][D][D].  FP64. */
+int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
+                     const double *gbar, double *sigma_bar, double *mu_bar, int flags);
+int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
+                     const double *sigma_dot, double mu_dot, double *gloc_dot, int flags);
+
 /* Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119, declared src/TB.h:45-47):
  * delta[nfreq][dim][dim] = (iw+mu) I - himp[orb] - sigma[orb] - (gw[orb])^-1, orb[dim] indexes D. */
 int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, double beta, int D,
