@@ -2,11 +2,11 @@
 // with respect to the self-energy and the chemical potential, k_gloc_ad<DP, W, MODE>.
 //
 // With G = (z - H - Sigma)^-1 on the full orbital space and Sigma acting on the correlated block P:
-//   dG_PP = -G_PP dSigma G_PP                     (dSigma lives on P, so only the P block of G enters)
+//   dG_PP = G_PP dSigma G_PP                      (dSigma lives on P, so only the P block of G enters)
 //   dG_PP = -(G^2)_PP dmu = -G_PP S' G_PP dmu    (S' = I + sum_l w_l^2 b_l b_l^H, the Schur form's dS/dz)
 // so for one frequency
-//   JVP:  dG_loc = -(1/N_k) sum_k G_PP (dSigma + dmu S') G_PP
-//   VJP:  Sigma_bar = -(1/N_k) sum_k G_PP^H Gbar G_PP^H,   mu_bar = -(1/N_k) sum_k Re Tr[(G_PP S' G_PP)^H Gbar]
+//   JVP:  dG_loc = (1/N_k) sum_k G_PP (dSigma - dmu S') G_PP
+//   VJP:  Sigma_bar = (1/N_k) sum_k G_PP^H Gbar G_PP^H,   mu_bar = -(1/N_k) sum_k Re Tr[(G_PP S' G_PP)^H Gbar]
 // (the adjoint of the holomorphic map in the convention of torch's complex autograd: x_bar = J^H y_bar).  G_PP
 // is recomputed for every (k, iw) from the per-k Schur data, as the forward pass does, and never stored: the
 // memory is O(N_freq D^2) whatever N_k, N_freq and n are.
@@ -28,7 +28,7 @@ struct AdArgs {
     double mu_dot;         // JVP
     int n, m, nk, nf, D, kc, kchunk;
     double beta, mu;
-    double2 *pout;         // [nchunk][nf][D][D] per-chunk sums (Sigma_bar or G_loc_dot, before the -1/N_k)
+    double2 *pout;         // [nchunk][nf][D][D] per-chunk sums (Sigma_bar or G_loc_dot, before the 1/N_k)
     double *pmu;           // [nchunk][nf] VJP: per-chunk Re Tr[(G S' G)^H Gbar]
     int *status;
 };
@@ -112,14 +112,14 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
             }
             __syncwarp();
             if (MODE == AD_JVP) {
-                // column c of G (Sigma_dot + mu_dot S') G
+                // column c of G (Sigma_dot - mu_dot S') G
                 C v[DP];
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     C x = cmk(0, 0);
 #pragma unroll
                     for (int b = 0; b < DP; b++)
-                        x = cfma(cadd(tX[a + b * DP], cscale(tS[a + b * DP], g.mu_dot)), s[b], x);
+                        x = cfma(csub(tX[a + b * DP], cscale(tS[a + b * DP], g.mu_dot)), s[b], x);
                     v[a] = x;
                 }
 #pragma unroll

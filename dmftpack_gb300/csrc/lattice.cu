@@ -602,7 +602,7 @@ int check_lat(const dmftgpu_lattice *L) {
 }
 
 
-// fixed-order sums over chunks of the derivative kernel's partials, scaled by -1/N_k
+// fixed-order sums over chunks of the derivative kernel's partials, scaled
 __global__ void k_ad_reduce(int nchunk, long long len, double scale, const double2 *p, double2 *out) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= len) return;
@@ -682,7 +682,7 @@ int run_ad(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, const doubl
     }
     DG_LAUNCH(ctx, "k_gloc_ad");
     const long long len = (long long)nf * DD;
-    k_ad_reduce<<<dg_ceil_div(len, 256), 256, 0, ctx->stream>>>(nchunk, len, -1.0 / P.nk, pout, out);
+    k_ad_reduce<<<dg_ceil_div(len, 256), 256, 0, ctx->stream>>>(nchunk, len, 1.0 / P.nk, pout, out);
     DG_LAUNCH(ctx, "k_ad_reduce");
     if (mode == dg::AD_VJP) {
         k_ad_mu<<<1, 256, 0, ctx->stream>>>(nchunk * nf, -1.0 / P.nk, pmu, dmu_out);
@@ -784,7 +784,7 @@ int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double 
     return code;
 }
 
-// reverse mode: Sigma_bar = -(1/N_k) sum_k G^H Gbar G^H, mu_bar = -(1/N_k) sum Re Tr[(G S' G)^H Gbar]
+// reverse mode: Sigma_bar = (1/N_k) sum_k G^H Gbar G^H, mu_bar = -(1/N_k) sum Re Tr[(G S' G)^H Gbar]
 int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
                      const double *gbar, double *sigma_bar, double *mu_bar, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !gbar || !sigma_bar || !mu_bar) return DMFTGPU_BADARG;
@@ -815,7 +815,7 @@ int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *h
     return code;
 }
 
-// forward mode: G_loc_dot = -(1/N_k) sum_k G (Sigma_dot + mu_dot S') G
+// forward mode: G_loc_dot = (1/N_k) sum_k G (Sigma_dot - mu_dot S') G
 int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
                      const double *sigma_dot, double mu_dot, double *gloc_dot, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !sigma_dot || !gloc_dot) return DMFTGPU_BADARG;

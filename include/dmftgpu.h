@@ -106,9 +106,9 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double
 
 /* Derivatives of GreenFtn_w's G_loc(iw_n) = (1/N_k) sum_k G_PP(k, iw_n), n < nfreq, for one correlated cluster
  * (no counterpart in the reference, which has no derivatives; they supply dN/dmu-style Newton steps and
- * Jacobian-vector products of the self-consistency residual).  dG_PP = -G_PP dSigma G_PP - dmu (G^2)_PP, with G
+ * Jacobian-vector products of the self-consistency residual).  dG_PP = G_PP dSigma G_PP - dmu (G^2)_PP, with G
  * recomputed per (k, iw) from the Schur data (never stored).
- * dmftgpu_gloc_vjp: gbar[nfreq][D][D] -> sigma_bar[nfreq][D][D] = -(1/N_k) sum_k G^H gbar G^H and *mu_bar (host) =
+ * dmftgpu_gloc_vjp: gbar[nfreq][D][D] -> sigma_bar[nfreq][D][D] = (1/N_k) sum_k G^H gbar G^H and *mu_bar (host) =
  *   -(1/N_k) sum Re Tr[((G^2)_PP)^H gbar] (the adjoint x_bar = J^H y_bar of complex autograd).
  * dmftgpu_gloc_jvp: (sigma_dot[nfreq][D][D], mu_dot) -> gloc_dot[nfreq][D][D].  FP64. */
 int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
