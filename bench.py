@@ -338,17 +338,24 @@ def run_ours(args, rank, world, local_rank):
     # side measurement: the other algorithm on the same inputs (one timed step)
     variants = {}
     if not args.no_variants:
-        other = (flags & ~lib.MIXED) ^ lib.EXPLICIT
-        step_dev(other)
-        torch.cuda.synchronize()
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(stream)
-        step_dev(other)
-        e.record(stream)
-        e.synchronize()
-        t_o = s.elapsed_time(e) / 1e3
-        variants["explicit" if not explicit else "schur"] = {"value": inv_per_step / t_o, "unit": UNIT,
-                                                              "ms_per_step": t_o * 1e3}
+        # the other forms on the same inputs, one timed step each: FP64 Schur, FP64 explicit (the reference's
+        # algorithm), and the mixed Schur form when the headline is FP64
+        others = {"schur_fp64": flags & ~(lib.MIXED | lib.EXPLICIT),
+                  "explicit_fp64": (flags & ~lib.MIXED) | lib.EXPLICIT}
+        if not mixed:
+            others["schur_mixed"] = (flags & ~lib.EXPLICIT) | lib.MIXED
+        for name, fl in others.items():
+            if fl == flags:
+                continue
+            step_dev(fl)
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            step_dev(fl)
+            e.record(stream)
+            e.synchronize()
+            t_o = s.elapsed_time(e) / 1e3
+            variants[name] = {"value": inv_per_step / t_o, "unit": UNIT, "ms_per_step": t_o * 1e3}
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     if rank != 0:
         return

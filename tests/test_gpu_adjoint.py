@@ -109,4 +109,4 @@ def test_autograd_gradient_matches_finite_differences(ctx):
             e = torch.zeros(3, dtype=torch.float64, device=dev)
             e[i] = h
             fd[i] = (float(loss(theta + e)) - float(loss(theta - e))) / (2 * h)
-    assert np.allclose(grad, fd, rtol=1e-6, atol=1e-9 * abs(float(L))), (grad, fd)
+    assert np.allclose(grad, fd, rtol=1e-6, atol=1e-9 * abs(L.item())), (grad, fd)
