@@ -555,12 +555,12 @@ __global__ void k_sigma2(int d, int ntau, const int *__restrict__ byI, const int
 // getStimp in double-float (df.cuh) on the FP32 pipe: the same sums as k_sigma2 with every complex product
 // and sum formed as an unevaluated pair of floats (~2^-47 relative per operation); selected by
 // DMFTGPU_MIXED.  G enters from FP64 exactly split into hi + lo, S leaves as hi + lo in FP64.
-__global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, const int *__restrict__ byI,
+__global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, int nu, const int *__restrict__ byI,
                                                    const int *__restrict__ byIoff, const int *__restrict__ byJ,
                                                    const int *__restrict__ byJoff, const int *__restrict__ uidx,
                                                    const double2 *__restrict__ ut, const double2 *__restrict__ G,
                                                    double2 *__restrict__ S, int *status) {
-    extern __shared__ cdf sgf[];  // per tau point b: G(tau) [dd], G(beta - tau) [dd]
+    extern __shared__ cdf sgf[];  // per tau point b: G(tau) [dd], G(beta - tau) [dd]; then the U values [nu]
     typedef OpsF O;
     const int t0 = blockIdx.x * S2_TB;
     const int dd = d * d;
@@ -575,6 +575,8 @@ __global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, const int *_
         sgf[(size_t)b * 2 * dd + q] = O::zero();
         sgf[(size_t)b * 2 * dd + dd + q] = O::zero();
     }
+    cdf *su = sgf + (size_t)S2_TB * 2 * dd;  // U values split once per block, not per (x1, x2) pair
+    for (int x = threadIdx.x; x < nu; x += blockDim.x) su[x] = O::from(ut[x]);
     __syncthreads();
     for (int o = threadIdx.x; o < dd; o += blockDim.x) {
         const int i = o % d, j = o / d;
@@ -590,7 +592,7 @@ __global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, const int *_
             for (int a2 = byJoff[j]; a2 < byJoff[j + 1]; a2++) {
                 const int x2 = byJ[a2];
                 const int l = uidx[4 * x2], n = uidx[4 * x2 + 1], p = uidx[4 * x2 + 2];
-                const cdf u2 = O::from(ut[x2]);
+                const cdf u2 = su[x2];
                 const int ikn = k + n * d, iml = m + l * d, ikl = k + l * d, imn = m + n * d, ipq = p + qq * d;
 #pragma unroll
                 for (int b = 0; b < S2_TB; b++) {
@@ -599,7 +601,7 @@ __global__ void __launch_bounds__(128) k_sigma2_df(int d, int ntau, const int *_
                     in[b] = O::fms(u2, O::mul(Gm[ipq], mn), in[b]);
                 }
             }
-            const cdf u1 = O::from(ut[x1]);
+            const cdf u1 = su[x1];
 #pragma unroll
             for (int b = 0; b < S2_TB; b++) acc[b] = O::fma(u1, in[b], acc[b]);
         }
@@ -849,9 +851,10 @@ int dg_sigma2_dev(dmftgpu_ctx *ctx, int d, int ntau, double beta, const DgUList 
         DgTimer tm(ctx, "k_sigma2");
         const size_t sm = S2_TB * 2 * dd * sizeof(double2);
         if (ctx->imp_mixed) {
-            DG_CUDA(cudaFuncSetAttribute(k_sigma2_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            k_sigma2_df<<<dg_ceil_div(ntau + 1, S2_TB), 128, sm, ctx->stream>>>(
-                d, ntau, U.byI, U.byIoff, U.byJ, U.byJoff, U.uidx, U.ut, gt, st, ctx->d_status);
+            const size_t smf = sm + (size_t)U.nu * sizeof(double2);
+            DG_CUDA(cudaFuncSetAttribute(k_sigma2_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+            k_sigma2_df<<<dg_ceil_div(ntau + 1, S2_TB), 128, smf, ctx->stream>>>(
+                d, ntau, U.nu, U.byI, U.byIoff, U.byJ, U.byJoff, U.uidx, U.ut, gt, st, ctx->d_status);
         } else {
             const int nt = std::min(1024, (int)((dd + 31) / 32 * 32));
             DG_CUDA(cudaFuncSetAttribute(k_sigma2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
