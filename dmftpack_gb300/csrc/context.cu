@@ -28,7 +28,11 @@ int dg_fail(dmftgpu_ctx *ctx, int code, const char *msg) {
 
 void *dg_buf(dmftgpu_ctx *ctx, const char *name, size_t bytes) {
     if (bytes == 0) bytes = 16;
-    auto &b = ctx->bufs[name];
+    auto &b = ctx->bufs[ctx->buf_ns.empty() ? std::string(name) : ctx->buf_ns + name];
+    if (b.bytes < bytes && ctx->capturing) {
+        dg_fail(ctx, DMFTGPU_BADARG, "workspace growth during graph capture");
+        return nullptr;
+    }
     if (b.bytes < bytes) {
         if (b.p) {
             cudaStreamSynchronize(ctx->stream);
@@ -143,6 +147,22 @@ int dmftgpu_destroy(dmftgpu_ctx *ctx) {
     }
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    for (auto &l : ctx->lanes) {
+        if (l.stream) {
+            cudaStreamSynchronize(l.stream);
+            cudaStreamDestroy(l.stream);
+        }
+        if (l.side) {
+            cudaStreamSynchronize(l.side);
+            cudaStreamDestroy(l.side);
+        }
+        if (l.fork) cudaEventDestroy(l.fork);
+        if (l.join) cudaEventDestroy(l.join);
+        if (l.done) cudaEventDestroy(l.done);
+    }
+    if (ctx->ev_batch) cudaEventDestroy(ctx->ev_batch);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return DMFTGPU_OK;

@@ -37,6 +37,19 @@ struct dmftgpu_ctx {
     bool ft_direct = false;           // DMFTGPU_DIRECT_DFT of the current call
     bool imp_mixed = false;           // DMFTGPU_MIXED of the current call, for the impurity kernels
     bool timing = false;              // record CUDA events around the named hot kernels
+    std::string buf_ns;               // workspace namespace (one per problem of a batched call)
+    bool autotune = false;            // time the CTA-per-SM candidates of each Schur kernel on first use
+    bool capturing = false;           // a CUDA graph capture is in progress (no syncs, no tuning)
+    std::map<std::string, int> tuned; // kernel key -> chosen CTAs per SM
+    struct Lane {
+        cudaStream_t stream = nullptr, side = nullptr;
+        cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
+    };
+    std::vector<Lane> lanes;          // stream pairs of batched calls
+    cudaEvent_t ev_batch = nullptr;
+    cudaStream_t cap_stream = nullptr;  // batched graphs are captured here (the caller's stream may be legacy)
+    cudaGraphExec_t graph = nullptr;  // the last captured batched pass
+    std::string graph_key;
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
 

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -513,20 +514,31 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n);
     if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
     DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    // k chunks: enough CTAs for ~8 per SM, at least 64 k points per chunk
+    // k chunks: enough CTAs for `cps` per SM (8 unless tuned), at least 64 k points per chunk
     const int fblocks = dg_ceil_div(nf2, NG);
-    int nchunk = std::max(1, std::min(dg_ceil_div(P.nk, 64), dg_ceil_div(8 * 152, fblocks)));
-    const int kchunk = dg_ceil_div(P.nk, nchunk);
-    nchunk = dg_ceil_div(P.nk, kchunk);
+    int nsm = 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    auto chunks = [&](int cps, int *kchunk_out) {
+        int nc = std::max(1, std::min(dg_ceil_div(P.nk, 64), dg_ceil_div(cps * nsm, fblocks)));
+        const int kch = dg_ceil_div(P.nk, nc);
+        *kchunk_out = kch;
+        return dg_ceil_div(P.nk, kch);
+    };
+    const std::string key = "schur/" + std::to_string(in->DP) + "/" + std::to_string(mode) + "/" +
+                            std::to_string((int)mixed) + "/" + std::to_string(P.nk) + "/" + std::to_string(nf2);
+    int kch_max;
+    const int nchunk_max = chunks(16, &kch_max);
     double2 *pblk = nullptr, *pblk0 = nullptr, *ptr = nullptr;
     if (mode & dg::S_BLOCK) {
-        pblk = (double2 *)dg_buf(ctx, "schur.pblk", (size_t)nchunk * nf2 * DD * sizeof(double2));
-        pblk0 = (double2 *)dg_buf(ctx, "schur.pblk0", (size_t)nchunk * nf2 * DD * sizeof(double2));
+        pblk = (double2 *)dg_buf(ctx, "schur.pblk", (size_t)nchunk_max * nf2 * DD * sizeof(double2));
+        pblk0 = (double2 *)dg_buf(ctx, "schur.pblk0", (size_t)nchunk_max * nf2 * DD * sizeof(double2));
         if (!pblk || !pblk0) return DMFTGPU_NOMEM;
     } else {
-        ptr = (double2 *)dg_buf(ctx, "schur.ptr", (size_t)nchunk * nf2 * sizeof(double2));
+        ptr = (double2 *)dg_buf(ctx, "schur.ptr", (size_t)nchunk_max * nf2 * sizeof(double2));
         if (!ptr) return DMFTGPU_NOMEM;
     }
+    int kchunk;
+    int nchunk = chunks(8, &kchunk);
     dg::SchurArgs g;
     g.H = P.H;
     g.B = P.B;
@@ -550,6 +562,38 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.status = ctx->d_status;
     // the TRACE passes read the static eigenvalues (Tr G0), computed on the side stream
     if (mode & dg::S_TRACE) DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    // autotuning: time 4, 8 and 16 CTAs per SM once per (width, mode, precision, N_k, points) and keep the fastest
+    auto tuned = ctx->tuned.find(key);
+    if (tuned != ctx->tuned.end()) {
+        nchunk = chunks(tuned->second, &kchunk);
+        g.kchunk = kchunk;
+    } else if (ctx->autotune && !ctx->capturing) {
+        cudaEvent_t e0, e1;
+        DG_CUDA(cudaEventCreate(&e0));
+        DG_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int best_cps = 8;
+        for (int cps : {4, 8, 16}) {
+            int kch;
+            const int nc = chunks(cps, &kch);
+            g.kchunk = kch;
+            DG_CUDA(cudaEventRecord(e0, ctx->stream));
+            kern<<<dim3(fblocks, nc), 128, smem, ctx->stream>>>(g);
+            DG_CUDA(cudaEventRecord(e1, ctx->stream));
+            DG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_cps = cps;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->tuned[key] = best_cps;
+        nchunk = chunks(best_cps, &kchunk);
+        g.kchunk = kchunk;
+    }
     {
         DgTimer tm(ctx, "k_schur");
         kern<<<dim3(fblocks, nchunk), 128, smem, ctx->stream>>>(g);
@@ -691,6 +735,31 @@ int run_ad(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, const doubl
     return DMFTGPU_OK;
 }
 
+
+// GreenFtn_w on device arrays, enqueue only (the body of dmftgpu_greenftn_w and of each batched problem)
+int greenftn_w_dev(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, double mu,
+                   double2 *dG, double2 *dG0, double2 *dN, int flags) {
+    const int D = L->ncl * L->nh, Nf = L->nfreq;
+    const size_t DD = (size_t)D * D;
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
+    double2 *blk = (double2 *)dg_buf(ctx, "gloc.blk", 2 * Nf * DD * sizeof(double2));
+    double2 *blk0 = (double2 *)dg_buf(ctx, "gloc.blk0", 2 * Nf * DD * sizeof(double2));
+    double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
+    double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
+    if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
+    if (flags & DMFTGPU_EXPLICIT) DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr, (flags & DMFTGPU_MIXED) != 0));
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
+    DG_LAUNCH(ctx, "k_fermi");
+    k_gloc_scale<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, ctx->stream>>>(Nf, L->nk, D, L->nh, blk, blk0, dG, dG0);
+    DG_LAUNCH(ctx, "k_gloc_scale");
+    k_nummat<<<(int)DD, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->beta, blk, blk0, occ, dN);
+    DG_LAUNCH(ctx, "k_nummat");
+    return DMFTGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -760,25 +829,113 @@ int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double 
     double2 *dN = (double2 *)dg_out(ctx, nummat, DD * sizeof(double2), flags, "io.nummat", &st);
     if (st) return st;
     DG_TRY(dg_status_reset(ctx));
-    Prepared P;
-    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
-    double2 *blk = (double2 *)dg_buf(ctx, "gloc.blk", 2 * Nf * DD * sizeof(double2));
-    double2 *blk0 = (double2 *)dg_buf(ctx, "gloc.blk0", 2 * Nf * DD * sizeof(double2));
-    double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
-    double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
-    if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
-    if (flags & DMFTGPU_EXPLICIT) DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
-    else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr, (flags & DMFTGPU_MIXED) != 0));
-    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
-    k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
-    DG_LAUNCH(ctx, "k_fermi");
-    k_gloc_scale<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, ctx->stream>>>(Nf, L->nk, D, L->nh, blk, blk0, dG, dG0);
-    DG_LAUNCH(ctx, "k_gloc_scale");
-    k_nummat<<<(int)DD, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->beta, blk, blk0, occ, dN);
-    DG_LAUNCH(ctx, "k_nummat");
+    DG_TRY(greenftn_w_dev(ctx, L, dH, dS, mu, dG, dG0, dN, flags));
     DG_TRY(dg_out_done(ctx, gw, dG, Nf * DD * sizeof(double2), flags));
     if (gwhf) DG_TRY(dg_out_done(ctx, gwhf, dG0, Nf * DD * sizeof(double2), flags));
     DG_TRY(dg_out_done(ctx, nummat, dN, DD * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// GreenFtn_w for a batch of independent lattice problems (ragged sizes): each problem has its own workspaces
+// and runs on one of four stream pairs, so small problems overlap; DMFTGPU_GRAPH replays the whole batched pass
+// as one CUDA graph (captured on the first call after a warm-up call with the same problem set);
+// DMFTGPU_AUTOTUNE tunes each Schur kernel's chunking on first use.
+int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattice *lats, const double *const *hk,
+                               const double *const *sigma, const double *mu, double *const *gw, double *const *gwhf,
+                               double *const *nummat, int flags) {
+    if (!ctx || nprob < 1 || !lats || !hk || !sigma || !mu || !gw || !nummat) return DMFTGPU_BADARG;
+    if (!(flags & DMFTGPU_DEVICE_PTRS)) return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w_batched: device pointers only");
+    if (flags & DMFTGPU_EXPLICIT) return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w_batched: Schur form only");
+    for (int i = 0; i < nprob; i++)
+        if (check_lat(&lats[i]) || lats[i].hartr || !hk[i] || !sigma[i] || !gw[i] || !nummat[i])
+            return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w_batched: bad problem (HartrIndex must be the identity)");
+    cudaSetDevice(ctx->device);
+    const int NL = 4;
+    if (ctx->lanes.empty()) {
+        ctx->lanes.resize(NL);
+        for (auto &l : ctx->lanes) {
+            DG_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+            DG_CUDA(cudaStreamCreateWithFlags(&l.side, cudaStreamNonBlocking));
+            DG_CUDA(cudaEventCreateWithFlags(&l.fork, cudaEventDisableTiming));
+            DG_CUDA(cudaEventCreateWithFlags(&l.join, cudaEventDisableTiming));
+            DG_CUDA(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming));
+        }
+        DG_CUDA(cudaEventCreateWithFlags(&ctx->ev_batch, cudaEventDisableTiming));
+        DG_CUDA(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+    }
+    // identity of this batched call: sizes, pointers and flags (a graph replays exactly these)
+    std::string key = std::to_string(flags);
+    for (int i = 0; i < nprob; i++) {
+        const dmftgpu_lattice &L = lats[i];
+        char b[256];
+        snprintf(b, sizeof(b), "|%d,%d,%d,%.17g,%d,%d,%p,%p,%.17g,%p,%p,%p", L.n, L.nk, L.nfreq, L.beta, L.ncl, L.nh,
+                 (const void *)hk[i], (const void *)sigma[i], mu[i], (void *)gw[i], gwhf ? (void *)gwhf[i] : nullptr,
+                 (void *)nummat[i]);
+        key += b;
+    }
+    DG_TRY(dg_status_reset(ctx));
+    if ((flags & DMFTGPU_GRAPH) && ctx->graph && ctx->graph_key == key) {
+        DG_CUDA(cudaGraphLaunch(ctx->graph, ctx->stream));
+    } else {
+        const bool capture = (flags & DMFTGPU_GRAPH) && ctx->graph_key == "warm:" + key;
+        cudaStream_t user = ctx->stream, side0 = ctx->side;
+        cudaStream_t origin = capture ? ctx->cap_stream : user;
+        cudaEvent_t fork0 = ctx->ev_fork, join0 = ctx->ev_join;
+        ctx->autotune = (flags & DMFTGPU_AUTOTUNE) != 0 && !capture;
+        if (capture) {
+            DG_CUDA(cudaEventRecord(ctx->ev_batch, user));
+            DG_CUDA(cudaStreamWaitEvent(origin, ctx->ev_batch, 0));
+            DG_CUDA(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
+            ctx->capturing = true;
+        }
+        int rc = DMFTGPU_OK;
+        if (cudaEventRecord(ctx->ev_batch, origin) != cudaSuccess) rc = DMFTGPU_CUDA_ERROR;
+        for (int l = 0; l < NL && !rc; l++)
+            if (cudaStreamWaitEvent(ctx->lanes[l].stream, ctx->ev_batch, 0) != cudaSuccess) rc = DMFTGPU_CUDA_ERROR;
+        for (int i = 0; i < nprob && !rc; i++) {
+            auto &ln = ctx->lanes[i % NL];
+            ctx->stream = ln.stream;
+            ctx->side = ln.side;
+            ctx->ev_fork = ln.fork;
+            ctx->ev_join = ln.join;
+            ctx->buf_ns = "b" + std::to_string(i) + "/";
+            rc = greenftn_w_dev(ctx, &lats[i], (const double2 *)hk[i], (const double2 *)sigma[i], mu[i],
+                                (double2 *)gw[i], gwhf ? (double2 *)gwhf[i] : nullptr, (double2 *)nummat[i],
+                                flags & ~DMFTGPU_EXPLICIT);
+        }
+        for (int l = 0; l < NL; l++) {
+            cudaEventRecord(ctx->lanes[l].done, ctx->lanes[l].stream);
+            cudaStreamWaitEvent(origin, ctx->lanes[l].done, 0);
+        }
+        ctx->stream = user;
+        ctx->side = side0;
+        ctx->ev_fork = fork0;
+        ctx->ev_join = join0;
+        ctx->buf_ns.clear();
+        ctx->autotune = false;
+        if (capture) {
+            cudaGraph_t graph = nullptr;
+            ctx->capturing = false;
+            cudaError_t e = cudaStreamEndCapture(origin, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return dg_set_cuda_error(ctx, e, "greenftn_w_batched: capture");
+            if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+            e = cudaGraphInstantiate(&ctx->graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return dg_set_cuda_error(ctx, e, "greenftn_w_batched: instantiate");
+            ctx->graph_key = key;
+            DG_CUDA(cudaGraphLaunch(ctx->graph, user));
+        } else {
+            if (rc) return rc;
+            if (flags & DMFTGPU_GRAPH) ctx->graph_key = "warm:" + key;
+        }
+    }
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;

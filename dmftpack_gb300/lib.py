@@ -25,13 +25,13 @@ _vp = C.c_void_p
 OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
 STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
                 6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
-DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT = 0x1, 0x2, 0x4, 0x8, 0x10
+DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40
 
 # every symbol include/dmftgpu.h declares
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -91,6 +91,8 @@ def load(require_built=True):
     lib.dmftgpu_hk.argtypes = [_vp, C.c_int, C.c_int, _ip, _dp, C.c_int, C.c_int, C.c_int, _vp, C.c_int]
     lib.dmftgpu_moments.argtypes = [_vp, C.c_int, C.c_int, C.c_double, _vp, C.c_int, _vp, C.c_int]
     lib.dmftgpu_greenftn_w.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_greenftn_w_batched.argtypes = [_vp, C.c_int, P(_Lat), P(_vp), P(_vp), _dp, P(_vp), P(_vp), P(_vp),
+                                               C.c_int]
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
@@ -280,6 +282,20 @@ class Context:
                                          self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)))
         self._check("dmftgpu_greenftn_w", st)
         return gw.result(), (g0.result() if g0 else None), nm.result()
+
+    def GreenFtn_w_batched(self, lats, Hk_cm, Sig_cm, mus, gw_cm, gwhf_cm, num_cm, mixed=False, graph=False,
+                           autotune=False):
+        """GreenFtn_w over a batch of problems; every array a CUDA tensor in the library's column-major layout,
+        outputs written in place (gwhf_cm may be None)."""
+        import torch  # noqa: F401
+        n = len(lats)
+        Ls = (_Lat * n)(*[lt._c() for lt in lats])
+        ptr = lambda ts: (_vp * n)(*[_vp(t.data_ptr()) for t in ts])
+        st = self.lib.dmftgpu_greenftn_w_batched(
+            self.h, n, Ls, ptr(Hk_cm), ptr(Sig_cm), (C.c_double * n)(*[float(m) for m in mus]), ptr(gw_cm),
+            ptr(gwhf_cm) if gwhf_cm is not None else None, ptr(num_cm),
+            self._flags(True, (MIXED if mixed else 0) | (GRAPH if graph else 0) | (AUTOTUNE if autotune else 0)))
+        self._check("dmftgpu_greenftn_w_batched", st)
 
     def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
         """Reverse mode of G_loc = GreenFtn_w(...)[0]: returns (Sigma_bar[nfreq,D,D], mu_bar) for the cotangent

@@ -181,6 +181,36 @@ def soc56(k=16, beta=30.0, nfreq=2048, ntau=None, seed=20250103, rmax=3, lam=0.1
                     {"M0": M0, "M1": M1})
 
 
+def batched_uneven(nprob=64, seed=20250104, dims=(1, 3, 5, 10, 14, 28), kgrids=(8, 12, 16, 24, 32),
+                   nfreqs=(512, 1024, 2048, 4096), beta_range=(10.0, 100.0), dmax=10):
+    """Independent lattice problems of ragged sizes: orbital dimension from `dims`, k grid k^3 from `kgrids`,
+    beta uniform in `beta_range`, N_freq from `nfreqs`; seeded random Hermitian nearest-cell t(R) scaled to a
+    bandwidth of ~4 eV; Sigma diagonal on the correlated block (the first min(n, dmax) orbitals, a d shell) with
+    Im Sigma = -Gamma/(w_n + Gamma), Gamma ~ U(0.1, 1)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(nprob):
+        n = int(rng.choice(dims))
+        k = int(rng.choice(kgrids))
+        nf = int(rng.choice(nfreqs))
+        beta = float(rng.uniform(*beta_range))
+        rvecs = [(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)]
+        scale = 4.0 / (2 * 27 * np.sqrt(n))
+
+        def draw(R):
+            return scale * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+
+        rows, vals = _hermitian_hoppings(n, rvecs, draw, rng.uniform(-1, 1, size=n))
+        D = min(n, dmax)
+        gam = rng.uniform(0.1, 1.0, size=D)
+        wn = PI * (2 * np.arange(nf) + 1) / beta
+        sigma = np.zeros((nf, D, D), np.complex128)
+        for d in range(D):
+            sigma[:, d, d] = -1j * gam[d] / (wn + gam[d])
+        out.append(Workload("uneven%d" % p, n, rows, vals, (k, k, k), beta, nf, 2 * nf, 1, D, sigma, n / 2.0))
+    return out
+
+
 def gen_Uijkl(n_spinorb, U, Uprime, JH, density_density=False):
     """Interaction list (U_index (nu, 4) int32, U_tensor (nu,) complex) for H_int = 1/2 sum U_ijkl c+_i c+_j c_l c_k
     on spin-orbitals ordered (orbital, spin) = (i // 2, i % 2): gen_Uijkl (Slater-Kanamori: density-density,

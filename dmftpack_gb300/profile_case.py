@@ -5,10 +5,13 @@ profiles/ are taken with.
     python -m dmftpack_gb300.profile_case scgf2 [--d 10 --nfreq 4096 --ntau 8192 --loops 2 --direct --mixed]
     python -m dmftpack_gb300.profile_case dmft  [--k 32 --nfreq 4096 --ntau 8192 --iters 2 --mixed --newton]
     python -m dmftpack_gb300.profile_case lattice [--k 16 --nfreq 4096 --mixed --newton]
+    python -m dmftpack_gb300.profile_case batched [--nprob 64 --mixed --graph --autotune]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
        U' = 2.6 (the SC2PT workload's impurity sizes by default: d = 10, N_w = 4096, N_tau = 8192, beta = 40).
+batched: GreenFtn_w over the ragged batch (64 seeded problems: n in {1,3,5,10,14,28}, k^3 with k in
+       {8,12,16,24,32}, N_freq in {512..4096}, beta in [10, 100]) in one batched call, timed over repeats.
 lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
@@ -32,6 +35,32 @@ def _impurity(d, nfreq, beta, seed=11):
     mu = 0.5
     g0 = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - himp[None] - weiss)
     return himp, weiss, g0, mu
+
+
+def run_batched(ctx, dev, a):
+    import torch
+    from dmftpack_gb300 import lib, models
+    wls = models.batched_uneven(nprob=a.nprob)
+    tcm = lambda t: t.transpose(-1, -2).contiguous()
+    lats, H, S, G, G0, N, mus = [], [], [], [], [], [], []
+    for w in wls:
+        lats.append(lib.Lattice(w.n, w.nk, w.nfreq, w.beta, 1, w.D))
+        H.append(tcm(ctx.Construct_Hk(w.n, w.rindex, w.hr, w.kgrid, device_out=dev)))
+        S.append(tcm(torch.from_numpy(w.sigma).to(dev)))
+        G.append(torch.empty((w.nfreq, w.D, w.D), dtype=torch.complex128, device=dev))
+        G0.append(torch.empty_like(G[-1]))
+        N.append(torch.empty((w.D, w.D), dtype=torch.complex128, device=dev))
+        mus.append(0.0)
+    times = []
+    for _ in range(max(3, a.repeat)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.GreenFtn_w_batched(lats, H, S, mus, G, G0, N, mixed=a.mixed, graph=a.graph, autotune=a.autotune)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    units = sum(w.nk * 2 * w.nfreq for w in wls)
+    return {"nprob": len(wls), "units": units, "mixed": a.mixed, "graph": a.graph, "autotune": a.autotune,
+            "seconds_per_call": times, "units_per_s_last": units / times[-1]}
 
 
 def run_lattice(ctx, dev, a):
@@ -94,7 +123,10 @@ def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched"])
+    ap.add_argument("--nprob", type=int, default=64)
+    ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--newton", action="store_true")
     ap.add_argument("--scgf-max", type=int, default=0)
@@ -132,8 +164,8 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case in ("dmft", "lattice"):
-        out.update(run_dmft(ctx, dev, a) if a.case == "dmft" else run_lattice(ctx, dev, a))
+    if a.case in ("dmft", "lattice", "batched"):
+        out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched}[a.case](ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
         return

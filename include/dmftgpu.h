@@ -39,6 +39,8 @@ enum {
 #define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
 #define DMFTGPU_EXPLICIT 0x8    /* lattice sums by explicit n x n inversion of every (k, iw) matrix, as the
                                    reference does (default: the exact correlated-block Schur form) */
+#define DMFTGPU_GRAPH 0x20     /* dmftgpu_greenftn_w_batched: replay the batched pass as one CUDA graph */
+#define DMFTGPU_AUTOTUNE 0x40  /* dmftgpu_greenftn_w_batched: tune each Schur kernel's k chunking on first use */
 #define DMFTGPU_DIRECT_DFT 0x10 /* iw <-> tau transforms by the reference's direct per-point sums (default: the
                                    same sums by FFT when N_tau is a power of two <= 8192) */
 
@@ -103,6 +105,18 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk,
  * 1e-11 using dN/dmu from the same pass.  *mu_out = mu; *n_eval = number of N(mu) passes. */
 int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma,
                       double mu, double dmu, double n_target, double *mu_out, int *n_eval, int flags);
+
+/* GreenFtn_w over a batch of independent lattice problems of ragged sizes (no counterpart in the reference;
+ * one call per DMFT iteration of many systems).  Device pointers only (flags must contain DMFTGPU_DEVICE_PTRS),
+ * HartrIndex the identity; the Schur form, FP64 or DMFTGPU_MIXED.  Arrays of nprob entries: lats, hk[i], sigma[i],
+ * mu[i], gw[i], gwhf[i] (gwhf may be NULL), nummat[i] (as dmftgpu_greenftn_w).  DMFTGPU_GRAPH: the first call
+ * with a given problem set runs eagerly and sizes the workspaces, the second captures the pass into a CUDA graph
+ * and every later call with the same set (same sizes, pointers, mu and flags) replays it; DMFTGPU_AUTOTUNE
+ * chooses each Schur kernel's CTAs per SM by timing on first use.  Each problem keeps its own workspaces in the
+ * context. */
+int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattice *lats, const double *const *hk,
+                               const double *const *sigma, const double *mu, double *const *gw, double *const *gwhf,
+                               double *const *nummat, int flags);
 
 /* Derivatives of GreenFtn_w's G_loc(iw_n) = (1/N_k) sum_k G_PP(k, iw_n), n < nfreq, for one correlated cluster
  * (no counterpart in the reference, which has no derivatives; they supply dN/dmu-style Newton steps and
