@@ -546,6 +546,7 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.sig = P.sig;
     g.m0 = P.m0;
     g.eps0 = P.eps;
+    g.UP = P.UP;
     g.n = P.n;
     g.m = m;
     g.nk = P.nk;
@@ -561,7 +562,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.ptr = ptr;
     g.status = ctx->d_status;
     // the TRACE passes read the static eigenvalues (Tr G0), computed on the side stream
-    if (mode & dg::S_TRACE) DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    if ((mode & dg::S_TRACE) || ((mode & dg::S_BLOCK) && in->DP >= 8))
+        DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     // autotuning: time 4, 8 and 16 CTAs per SM once per (width, mode, precision, N_k, points) and keep the fastest
     auto tuned = ctx->tuned.find(key);
     if (tuned != ctx->tuned.end()) {

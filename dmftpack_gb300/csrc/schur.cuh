@@ -13,7 +13,9 @@
 // inversion), so G_loc, GwHF, NumMatrix and the occupation sum of GiwToNele are the reference's quantities;
 // the work per (k, iw) drops from an n x n inversion to O(D^2 m + D^3).  d/dmu of the trace (Newton's
 // dN/dmu) is d/dz of the same expression: dG_PP/dz = -G S' G with S' = I + sum_l w_l^2 b_l b_l^H, dw_l/dz =
-// -w_l^2.  The BLOCK pass (G_loc, GwHF) inverts S and S0; the TRACE passes of the mu search invert S only.
+// -w_l^2.  The TRACE passes of the mu search invert S only; the BLOCK pass (G_loc, GwHF) inverts S0 as well for
+// small blocks, and for DP >= 8 forms GwHF as U (z - e0)^-1 U^H from the static eigen-decomposition (the
+// reference's own formula), keeping one unrolled inversion per kernel (instruction-cache bound otherwise).
 //
 // Mapping: a lane group of W lanes owns one Matsubara frequency and sweeps a chunk of k points; lane c holds
 // column c of S (and S0), inverted with warp_gj_inverse_t<Ops,DP,W> (DP >= D padded with identity), and
@@ -35,7 +37,8 @@ struct SchurArgs {
     const double *epsQ;   // [nk][m]
     const double2 *sig;   // [2 Nf][D][D]
     const double2 *m0;    // [D][D]
-    const double *eps0;   // [nk][n] eigenvalues of H + m0 (TRACE modes)
+    const double *eps0;   // [nk][n] eigenvalues of H + m0 (TRACE modes; BLOCK for DP >= 8)
+    const double2 *UP;    // [nk][n][D] correlated rows of their eigenvectors (BLOCK for DP >= 8)
     int n, m, nk, nf2, D, wgrid, kc, kchunk;  // kc: k points staged per round; kchunk: k points per CTA
     double beta, mu;
     double2 *pblk, *pblk0;  // [nchunk][nf2][D][D]  per-chunk k sums (BLOCK)
@@ -53,14 +56,17 @@ __device__ __forceinline__ double group_sum(double v) {
 // staged per-k data in shared memory (arithmetic type C): B[kc][m][D], e[kc][m] (mu - e_l, real),
 // hpp[kc][D][D] (-H_PP), e0[kc][n] (mu - e0_j, TRACE modes), then once m0[D][D]
 template <class Ops>
-__device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc, typename Ops::C *st, bool trace) {
+__device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc, typename Ops::C *st, bool e0,
+                                            bool up) {
     typedef typename Ops::C C;
     const int m = g.m, D = g.D, DD = D * D;
     C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
-    C *sE0 = sH + (size_t)g.kc * DD;
-    if (trace)
+    C *sE0 = sH + (size_t)g.kc * DD, *sU = sE0 + (e0 ? (size_t)g.kc * g.n : 0);
+    if (e0)
         for (int t = threadIdx.x; t < nkc * g.n; t += blockDim.x)
             sE0[t] = Ops::from(cmk(g.mu - g.eps0[(size_t)k0 * g.n + t], 0.0));
+    if (up)
+        for (int t = threadIdx.x; t < nkc * g.n * D; t += blockDim.x) sU[t] = Ops::from(g.UP[(size_t)k0 * g.n * D + t]);
     for (int t = threadIdx.x; t < nkc * m * D; t += blockDim.x) sB[t] = Ops::from(g.B[(size_t)k0 * m * D + t]);
     for (int t = threadIdx.x; t < nkc * m; t += blockDim.x)
         sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k0 * m + t], 0.0));
@@ -78,13 +84,16 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     extern __shared__ double2 sm[];
     const int D = g.D, DD = D * D, m = g.m;
     constexpr bool TR = (MODE & S_TRACE) != 0;
+    constexpr bool G0E = (MODE & S_BLOCK) && DP >= 8;  // GwHF from the static eigen-decomposition
+    constexpr bool E0 = TR || G0E;
     C *st = reinterpret_cast<C *>(sm);
     C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
-    C *sE0 = sH + (size_t)g.kc * DD;                                      // [kc][n], TRACE modes
-    C *sM0 = sE0 + (TR ? (size_t)g.kc * g.n : 0);
+    C *sE0 = sH + (size_t)g.kc * DD;                                      // [kc][n] (E0)
+    C *sU = sE0 + (E0 ? (size_t)g.kc * g.n : 0);                         // [kc][n][D] (G0E)
+    C *sM0 = sU + (G0E ? (size_t)g.kc * g.n * D : 0);
     C *wla = sM0 + DD;                                                   // reciprocals [NG][m]
-    C *rla = wla + (size_t)NG * m;                                        // static reciprocals [NG][n] (TRACE)
-    C *tla = rla + (TR ? (size_t)NG * g.n : 0);                           // DERIV tiles [NG][2][DP][DP]
+    C *rla = wla + (size_t)NG * m;                                        // static reciprocals [NG][n] (E0)
+    C *tla = rla + (E0 ? (size_t)NG * g.n : 0);                           // DERIV tiles [NG][2][DP][DP]
     const int c = threadIdx.x & (W - 1);
     const int grp = threadIdx.x / W;
     const int f_raw = blockIdx.x * NG + grp;
@@ -113,14 +122,14 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
         const int nkc = min(g.kc, kend - k0);
         __syncthreads();
-        schur_stage<Ops>(g, k0, nkc, st, TR);
+        schur_stage<Ops>(g, k0, nkc, st, E0, G0E);
         __syncthreads();
         for (int kk = 0; kk < nkc; kk++) {
             const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
             // w_l = 1/(z - e_l), shared by the group's lanes; TRACE: r_j = 1/(z - e0_j)
             __syncwarp();
             for (int l = c; l < m; l += W) wl[l] = Ops::rcp(Ops::add(es[l], iwc));
-            if (TR) {
+            if (E0) {
                 const C *e0s = sE0 + (size_t)kk * g.n;
                 for (int j = c; j < g.n; j += W) rl[j] = Ops::rcp(Ops::add(e0s[j], iwc));
             }
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         if (a < D) s[a] = Ops::fms(bs[l * D + a], q, s[a]);
                 }
             }
-            if (MODE & S_BLOCK) {
+            if ((MODE & S_BLOCK) && !G0E) {
 #pragma unroll
                 for (int a = 0; a < DP; a++)
                     s0[a] = (col && a < D) ? Ops::sub(Ops::add(s[a], sgc[a]), sM0[a + c * D]) : s[a];
@@ -164,13 +173,26 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                 }
             }
             sing |= warp_gj_inverse_t<Ops, DP, W>(s, c);
-            if (MODE & S_BLOCK) {
+            if ((MODE & S_BLOCK) && !G0E) {
                 sing |= warp_gj_inverse_t<Ops, DP, W>(s0, c);
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     accG[a] = Ops::add(accG[a], s[a]);
                     accG0[a] = Ops::add(accG0[a], s0[a]);
                 }
+            }
+            if (G0E) {
+                // G0(:, c) = sum_j U(:, j) r_j conj(U(c, j))
+                const C *us = sU + (size_t)kk * g.n * D;
+#pragma unroll
+                for (int a = 0; a < DP; a++) accG[a] = Ops::add(accG[a], s[a]);
+                if (col)
+                    for (int j = 0; j < g.n; j++) {
+                        const C q = Ops::mulc(rl[j], us[j * D + c]);
+#pragma unroll
+                        for (int a = 0; a < DP; a++)
+                            if (a < D) accG0[a] = Ops::fma(us[j * D + a], q, accG0[a]);
+                    }
             }
             if (MODE & S_TRACE) {
                 // lane c: column c of G_PP in s.  acc1 -> Tr G - Tr G0, acc2 -> d/dz of it (summed over lanes)
@@ -258,7 +280,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m, int n) {
     const int NG = 128 / W;
     size_t s = (size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D + (size_t)NG * m;
-    if (mode & S_TRACE) s += (size_t)kc * n + (size_t)NG * n;
+    const bool g0e = (mode & S_BLOCK) && DP >= 8;
+    if ((mode & S_TRACE) || g0e) s += (size_t)kc * n + (size_t)NG * n;
+    if (g0e) s += (size_t)kc * n * D;
     if (mode & S_DERIV) s += (size_t)NG * 2 * DP * DP;
     return s * 16;
 }
