@@ -1044,11 +1044,24 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
     };
     const double goal = n_target;
     if (flags & DMFTGPU_NEWTON) {
-        // safeguarded Newton: keep a bracket [lo, hi] with N(lo) < goal < N(hi) once found
+        // safeguarded Newton: keep a bracket [lo, hi] with N(lo) < goal < N(hi) once found.  The first step
+        // uses dN/dmu from the derivative pass; later steps take the secant slope of the last two evaluations
+        // (a plain N(mu) pass costs ~45% of a derivative pass), falling back to a derivative pass whenever
+        // that slope is not positive.
         double lo = -1e300, hi = 1e300, Nv, dN;
+        double pmu = 0, pN = 0;
+        bool need_deriv = true;
         for (int it = 0; it < 100; it++) {
-            DG_TRY(N(mu, &Nv, &dN));
+            if (need_deriv) {
+                DG_TRY(N(mu, &Nv, &dN));
+            } else {
+                DG_TRY(N(mu, &Nv, nullptr));
+                dN = (Nv - pN) / (mu - pmu);
+            }
             if (!std::isfinite(Nv)) return DMFTGPU_NAN;
+            need_deriv = !(dN > 0) || !std::isfinite(dN);
+            pmu = mu;
+            pN = Nv;
             double r = Nv - goal;
             if (r < 0) lo = std::max(lo, mu);
             else hi = std::min(hi, mu);
