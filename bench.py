@@ -236,6 +236,27 @@ def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
     return out
 
 
+def scgf2_timing(ctx, dev, loops=4):
+    """Seconds per SCGF2 loop on a seeded 10 spin-orbital impurity with the SC2PT workload's sizes (N_freq = 4096,
+    N_tau = 8192, beta = 40, Kanamori U = 4, J = 0.7, U' = 2.6), FP64 and mixed (double-float getStimp)."""
+    import torch
+    from dmftpack_gb300 import models
+    from dmftpack_gb300.profile_case import _impurity
+    himp, weiss, g0, mu = _impurity(10, 4096, 40.0)
+    uidx, ut = models.gen_Uijkl(10, 4.0, 2.6, 0.7)
+    W, G0, Hi = (torch.from_numpy(x).to(dev) for x in (weiss, g0, himp))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        ctx.SCGF2(Hi, W, G0, uidx, ut, mu, 40.0, 8192, 0.5, max_iter=1, mixed=prec == "mixed")  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.SCGF2(Hi, W, G0, uidx, ut, mu, 40.0, 8192, 0.5, max_iter=loops, mixed=prec == "mixed")
+        torch.cuda.synchronize()
+        out[prec] = {"s_per_loop": (time.perf_counter() - t0) / loops, "loops": loops}
+    out["workload"] = "10 spin-orbital impurity, N_freq=4096, N_tau=8192, beta=40, Kanamori U=4 J=0.7 U'=2.6 (Nu=180)"
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from dmftpack_gb300 import lib
@@ -357,6 +378,7 @@ def run_ours(args, rank, world, local_rank):
             t_o = s.elapsed_time(e) / 1e3
             variants[name] = {"value": inv_per_step / t_o, "unit": UNIT, "ms_per_step": t_o * 1e3}
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
+    scgf2 = None if args.no_variants else scgf2_timing(ctx, dev)
     if rank != 0:
         return
     # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
@@ -377,6 +399,7 @@ def run_ours(args, rank, world, local_rank):
            "config": dict(describe(wl), precision=args.precision, algorithm=args.algo,
                           l2="1 GiB buffer written between timed steps", replicas=world),
            "variants": variants, "error_vs_fp64": err, "dmft_iteration": dmft_iter,
+           "scgf2_loop": scgf2,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "fp64" if not mixed else "fp32", "achieved": achieved,
