@@ -394,7 +394,7 @@ def run_ours(args, rank, world, local_rank):
     cpu_v, cpu_d = cpu_rate(wl, Hd.cpu().numpy(), seconds=12.0)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64-refine",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32x2 (double-float)",
            "data": "synthetic (seeded t(R), Sigma = -0.5i/(w_n+1) on the 3 d orbitals)",
            "config": dict(describe(wl), precision=args.precision, algorithm=args.algo,
                           l2="1 GiB buffer written between timed steps", replicas=world),
