@@ -509,16 +509,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     const SInst *in = pick_schur(P.D);
     SchurKernel kern = in->get(mode, mixed);
     const int m = P.n - P.D, NG = 128 / in->W, nf2 = 2 * P.Nf, DD = P.D * P.D;
-    // k points staged per round: as many as fit without letting shared memory cut the residency that the
-    // kernel's registers allow (CTAs of 128 threads)
     int kc = 16;
-    {
-        cudaFuncAttributes fa;
-        DG_CUDA(cudaFuncGetAttributes(&fa, kern));
-        const int by_regs = std::max(1, std::min(8, 65536 / std::max(1, fa.numRegs * 128)));
-        const size_t budget = std::min<size_t>(96 * 1024, 226 * 1024 / by_regs - 1024);
-        while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n) > budget) kc /= 2;
-    }
+    while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n) > 96 * 1024) kc /= 2;
     const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n);
     if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
     DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
