@@ -137,6 +137,18 @@ def fp32_peak_tflops(torch, dev):
     return 2 * n ** 3 / best / 1e12
 
 
+def replica_throughput(t_local, units_per_step, steps, world, device):
+    """Replicas-only aggregation: the slowest rank's timed total (max over ranks) and the whole job's throughput,
+    all ranks' units over that time.  Returns (t_max, value)."""
+    t_max = t_local
+    if world > 1:
+        import torch
+        t = torch.tensor([t_local], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    return t_max, world * units_per_step * steps / t_max
+
+
 def cpu_rate(wl, H, seconds=12.0, threads=None):
     """Oracle GreenFtn_w (threads over k) timed on two k subsets; the per-call cost (moment fit of S) and the
     per-k cost are separated and the full pass is extrapolated.  Returns (inversions/s, description)."""
@@ -319,13 +331,8 @@ def run_ours(args, rank, world, local_rank):
     k_ms, k_cnt = ctx.kernel_time(kname)
     ctx.timing(False)
     clk = clocks.stop()
-    t_total = sum(times)
-    if world > 1:
-        t = torch.tensor([t_total], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(t.item())
     inv_per_step = wl.nk * 2 * wl.nfreq
-    value = world * inv_per_step * args.steps / t_total
+    t_total, value = replica_throughput(sum(times), inv_per_step, args.steps, world, dev)
 
     # end-to-end through the C ABI with host buffers (pageable numpy, like the reference's Eigen data)
     Hh = Hcm.cpu().numpy()

@@ -78,3 +78,17 @@ def test_batched_autotune(ctx):
         _check(ctx, probs, res, tol=1e-11)
     finally:
         c2.close()
+
+
+def test_batched_without_gwhf(ctx):
+    import torch
+    probs, dev = _problems(ctx, nprob=3)
+    gw = [torch.zeros((p["w"].nfreq, p["w"].D, p["w"].D), dtype=torch.complex128, device=dev) for p in probs]
+    nm = [torch.zeros((p["w"].D, p["w"].D), dtype=torch.complex128, device=dev) for p in probs]
+    ctx.GreenFtn_w_batched([p["lat"] for p in probs], [p["Hcm"] for p in probs], [p["Scm"] for p in probs],
+                           [p["mu"] for p in probs], gw, None, nm)
+    torch.cuda.synchronize()
+    for i, p in enumerate(probs):
+        g, _, n = ctx.GreenFtn_w(p["lat"], p["H"], p["S"], p["mu"])
+        assert rel_err(gw[i].transpose(-1, -2).cpu().numpy(), g.cpu().numpy()) < 1e-12
+        assert rel_err(nm[i].transpose(-1, -2).cpu().numpy(), n.cpu().numpy()) < 1e-12

@@ -252,3 +252,46 @@ def test_dmft_iterations_sc2pt_match_oracle(orc):
             assert np.allclose(res_g, res, rtol=1e-6, atol=1e-12), (it, res_g, res)
     finally:
         c2.close()
+
+
+@pytest.mark.parametrize("mixed,direct,tol", [(True, False, 1e-9), (False, True, 1e-10)])
+def test_dmft_iterations_variants_match_oracle(orc, mixed, direct, tol):
+    """Three IPT iterations with the double-float lattice sum and getStimp, and with the reference's direct
+    transform sums, against the oracle."""
+    import torch
+    wl, H, p, state = _dmft_setup(orc)
+    dev = torch.device("cuda:0")
+    cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
+    back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
+    Hd, se, we, gl = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["gloc"])
+    nm = cm(state["nummat"][None])[0].contiguous()
+    mu_g = state["mu"]
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
+    pulay = orc.Pulay()
+    c2 = lib.Context(0)
+    try:
+        for it in range(1, 4):
+            state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
+            mu_g, gimp_g, res_g = c2.DMFT_iteration(lat, Hd, p, it, se, we, nm, gl, mu_g, mixed=mixed, direct=direct)
+            torch.cuda.synchronize()
+            assert abs(mu_g - state["mu"]) < 1e-10, it
+            assert rel_err(back(se), state["selfe"]) < tol, it
+            assert rel_err(back(gl), gloc) < tol, it
+            assert rel_err(back(we), state["weiss"]) < tol, it
+    finally:
+        c2.close()
+
+
+def test_scgf2_density_density_two_orbitals(orc):
+    """SCGF2 with the density-density interaction on 2 spin-orbitals (the IPT model's U list)."""
+    himp, weiss, g0, _, _, mu, beta, ntau = _scgf_case(orc, d=2, nfreq=48, ntau=192, seed=3)
+    uidx, ut = orc.gen_uijkl(2, 2.5, 2.5, 0.0, density_density=True)
+    se_o, g_o, loops_o = orc.scgf2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=40,
+                                   static={"prev": 0.0})
+    c2 = lib.Context(0)
+    try:
+        se, g, loops = c2.SCGF2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5, max_iter=40)
+    finally:
+        c2.close()
+    assert loops == loops_o
+    assert rel_err(se, se_o) < 1e-9 and rel_err(g, g_o) < 1e-9

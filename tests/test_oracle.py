@@ -165,3 +165,19 @@ def test_oracle_tau2w_against_exact_integral(orc):
     z = np.load(os.path.join(os.path.dirname(__file__), "golden", "tau2w_exact.npz"))
     got, _ = orc.tau2w(z["ft"], float(z["beta"]), int(z["nfreq"]))
     assert np.abs(got - z["w"]).max() / np.abs(z["w"]).max() < 1e-10
+
+
+def test_oracle_scgf2_without_interaction_keeps_the_bare_green_function(orc):
+    """U = 0: no Fock or second-order term, so SCGF2 stops after the minimum 10 loops with G_imp = the
+    non-interacting G (src/SCGF2_fullLoop.cpp:477-523).  SE_out is not exactly zero: getStimp's positivity fix-up
+    replaces every Sigma(tau) = 0 point (minimum eigenvalue >= 0) by -1e-10 I (src/SCGF2_fullLoop.cpp:657-688)."""
+    d, nf, ntau, beta, mu = 2, 32, 128, 8.0, 0.1
+    himp = np.array([[0.2, 0.05], [0.05, -0.1]], complex)
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    weiss = 0.3 * np.eye(d)[None] / (1j * wn[:, None, None] - 0.4)
+    g0 = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - himp[None] - weiss)
+    uidx, ut = orc.gen_uijkl(d, 0.0, 0.0, 0.0, density_density=True)
+    se, g, loops = orc.scgf2(himp, weiss, g0, uidx, ut, mu, beta, ntau, 0.5)
+    assert loops == 10
+    assert np.abs(se).max() < 1e-9
+    assert np.abs(g[:nf] - g0).max() < 1e-9
