@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
                             sp[a] = cfma(bs[l * D + a], q2, sp[a]);
                         }
                 }
-            sing |= warp_gj_inverse_t<Ops, DP, W>(s, c);  // s = G(:, c)
+            sing |= gj_inverse<Ops, DP, W>(s, c);  // s = G(:, c)
             __syncwarp();
             if (c < DP) {
 #pragma unroll

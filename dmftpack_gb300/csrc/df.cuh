@@ -191,3 +191,65 @@ __device__ __forceinline__ bool warp_gj_inverse_t(typename Ops::C (&a)[N], const
     }
     return singular;
 }
+
+// warp_gj_inverse_t with the elimination steps in a rolled loop: the same arithmetic and pivot choices, but
+// the rows of each lane's column are rotated by one after every step, so the current pivot row is always
+// register a[0] and the loop body is the same for every step (no dynamic register indexing).  The code is N
+// times shorter than the unrolled form, which matters for large N, where the kernels are bound by instruction
+// fetch.  Row r of step j sits in register (r - j) mod N; after N steps every row is back in place.
+template <class Ops, int N, int W>
+__device__ __forceinline__ bool warp_gj_inverse_rolled(typename Ops::C (&a)[N], const int c) {
+    typedef typename Ops::C C;
+    typedef typename Ops::M M;
+    static_assert(N <= W && W <= 32 && (W & (W - 1)) == 0, "bad lane group");
+    bool singular = false;
+    int perm[N];
+#pragma unroll 1
+    for (int j = 0; j < N; j++) {
+        // pivot search over rows j..N-1 (registers 0..N-1-j) of column j (lane j)
+        M best = M(-1);
+        int pp = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const M v = Ops::mag2(a[i]);
+            if (i <= N - 1 - j && v > best) {
+                best = v;
+                pp = i;
+            }
+        }
+        pp = __shfl_sync(0xffffffffu, pp, j, W);
+        best = __shfl_sync(0xffffffffu, best, j, W);
+        singular |= !(best > M(0));
+        perm[j] = pp + j;  // the row index of the pivot
+#pragma unroll
+        for (int i = 1; i < N; i++)
+            if (i == pp) {
+                const C t = a[0];
+                a[0] = a[i];
+                a[i] = t;
+            }
+        const C piv = Ops::shfl(a[0], j, W);
+        const C ipiv = Ops::rcp(piv);
+        const C t = Ops::mul(a[0], ipiv);
+        const bool is_piv_col = (c == j);
+#pragma unroll
+        for (int i = 1; i < N; i++) {
+            const C f = Ops::shfl(a[i], j, W);
+            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+        }
+        a[0] = is_piv_col ? ipiv : t;
+        // rotate: the finished pivot row moves to the end
+        const C r0 = a[0];
+#pragma unroll
+        for (int i = 0; i < N - 1; i++) a[i] = a[i + 1];
+        a[N - 1] = r0;
+    }
+#pragma unroll 1
+    for (int j = N - 1; j >= 0; j--) {
+        const int p = perm[j];
+        const int src = (c == j) ? p : ((c == p) ? j : c);
+#pragma unroll
+        for (int i = 0; i < N; i++) a[i] = Ops::shfl(a[i], src, W);
+    }
+    return singular;
+}

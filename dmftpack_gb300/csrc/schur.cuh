@@ -18,7 +18,7 @@
 // reference's own formula), keeping one unrolled inversion per kernel (instruction-cache bound otherwise).
 //
 // Mapping: a lane group of W lanes owns one Matsubara frequency and sweeps a chunk of k points; lane c holds
-// column c of S (and S0), inverted with warp_gj_inverse_t<Ops,DP,W> (DP >= D padded with identity), and
+// column c of S (and S0), inverted with gj_inverse<Ops,DP,W> (DP >= D padded with identity), and
 // accumulates column c of the k sum in registers.  A CTA = 128/W frequencies x one k chunk; the per-k data
 // (b_l, mu - e_l, -H_PP) of kc k points at a time is staged once in shared memory in the kernel's
 // arithmetic type.  Per-chunk sums are reduced over chunks in a fixed order by a second kernel.
@@ -45,6 +45,13 @@ struct SchurArgs {
     double2 *ptr;           // [nchunk][nf2]         per-chunk trace sums (x = tr, y = dtr)
     int *status;
 };
+
+// the unrolled Gauss-Jordan for small blocks, the rolled one (df.cuh) from 8 on
+template <class Ops, int DP, int W>
+__device__ __forceinline__ bool gj_inverse(typename Ops::C (&a)[DP], int c) {
+    if constexpr (DP >= 8) return warp_gj_inverse_rolled<Ops, DP, W>(a, c);
+    else return warp_gj_inverse_t<Ops, DP, W>(a, c);
+}
 
 template <int DP, int W>
 __device__ __forceinline__ double group_sum(double v) {
@@ -172,9 +179,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                     for (int a = 0; a < DP; a++) tS[a + c * DP] = sp[a];
                 }
             }
-            sing |= warp_gj_inverse_t<Ops, DP, W>(s, c);
+            sing |= gj_inverse<Ops, DP, W>(s, c);
             if ((MODE & S_BLOCK) && !G0E) {
-                sing |= warp_gj_inverse_t<Ops, DP, W>(s0, c);
+                sing |= gj_inverse<Ops, DP, W>(s0, c);
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     accG[a] = Ops::add(accG[a], s[a]);
