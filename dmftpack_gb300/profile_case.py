@@ -6,12 +6,15 @@ profiles/ are taken with.
     python -m dmftpack_gb300.profile_case dmft  [--k 32 --nfreq 4096 --ntau 8192 --iters 2 --mixed --newton]
     python -m dmftpack_gb300.profile_case lattice [--k 16 --nfreq 4096 --mixed --newton]
     python -m dmftpack_gb300.profile_case batched [--nprob 64 --mixed --graph --autotune]
+    python -m dmftpack_gb300.profile_case adjoint [--k 16 --nfreq 2048]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
        U' = 2.6 (the SC2PT workload's impurity sizes by default: d = 10, N_w = 4096, N_tau = 8192, beta = 40).
 batched: GreenFtn_w over the ragged batch (64 seeded problems: n in {1,3,5,10,14,28}, k^3 with k in
        {8,12,16,24,32}, N_freq in {512..4096}, beta in [10, 100]) in one batched call, timed over repeats.
+adjoint: one GreenFtn_w pass, one reverse-mode (VJP) and one forward-mode (JVP) pass of G_loc on the 56-orbital
+       SOC model (20 x 20 correlated block, k^3 grid, beta = 30), FP64.
 lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
@@ -61,6 +64,28 @@ def run_batched(ctx, dev, a):
     units = sum(w.nk * 2 * w.nfreq for w in wls)
     return {"nprob": len(wls), "units": units, "mixed": a.mixed, "graph": a.graph, "autotune": a.autotune,
             "seconds_per_call": times, "units_per_s_last": units / times[-1]}
+
+
+def run_adjoint(ctx, dev, a):
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.soc56(k=a.k, nfreq=a.nfreq or 2048)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, wl.D)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    S = torch.from_numpy(wl.sigma).to(dev)
+    rng = np.random.default_rng(1)
+    X = torch.from_numpy(rng.normal(size=wl.sigma.shape) + 1j * rng.normal(size=wl.sigma.shape)).to(dev)
+    out = {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq}
+    for name, fn in (("greenftn_w", lambda: ctx.GreenFtn_w(lat, Hd, S, 0.0, with_gwhf=False)),
+                     ("vjp", lambda: ctx.GreenFtn_w_vjp(lat, Hd, S, 0.0, X)),
+                     ("jvp", lambda: ctx.GreenFtn_w_jvp(lat, Hd, S, 0.0, X, 0.3))):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        out[name + "_seconds"] = time.perf_counter() - t0
+    return out
 
 
 def run_lattice(ctx, dev, a):
@@ -123,7 +148,7 @@ def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint"])
     ap.add_argument("--nprob", type=int, default=64)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--autotune", action="store_true")
@@ -164,8 +189,9 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case in ("dmft", "lattice", "batched"):
-        out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched}[a.case](ctx, dev, a))
+    if a.case in ("dmft", "lattice", "batched", "adjoint"):
+        out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched,
+                    "adjoint": run_adjoint}[a.case](ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
         return
