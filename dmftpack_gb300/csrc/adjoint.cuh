@@ -42,14 +42,14 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
     const int D = g.D, DD = D * D, m = g.m;
     C *sB = sm, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
     C *wla = sH + (size_t)g.kc * DD;                  // [NG][m]
-    C *tla = wla + (size_t)NG * m;                    // [NG][3][DP][DP]: S', G, input (Gbar or Sigma_dot)
+    C *tla = wla + (size_t)NG * m;                    // [NG][4][DP][DP]: S', G, input (Gbar or Sigma_dot), work
     const int c = threadIdx.x & (W - 1), grp = threadIdx.x / W;
     const int f_raw = blockIdx.x * NG + grp;
     const bool fvalid = f_raw < g.nf;
     const int f = fvalid ? f_raw : g.nf - 1;
     const int chunk = blockIdx.y;
     const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
-    C *tS = tla + (size_t)grp * 3 * DP * DP, *tG = tS + DP * DP, *tX = tG + DP * DP;
+    C *tS = tla + (size_t)grp * 4 * DP * DP, *tG = tS + DP * DP, *tX = tG + DP * DP, *tV = tX + DP * DP;
     C *wl = wla + (size_t)grp * m;
     const bool col = c < D;
     const double w = DG_PI * (2. * f + 1.) / g.beta;
@@ -111,59 +111,66 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
                 }
             }
             __syncwarp();
+            // the intermediate column v goes through the group's work tile, so only G(:, c), S'(:, c), Sigma(:, c)
+            // and the accumulator live in registers; the inner sums are rolled loops over shared memory
             if (MODE == AD_JVP) {
-                // column c of G (Sigma_dot - mu_dot S') G
-                C v[DP];
+                // column c of G (Sigma_dot - mu_dot S') G: v = (Sigma_dot - mu_dot S') G(:, c), then G v
+                if (c < DP)
+                    for (int a = 0; a < DP; a++) {
+                        C x = cmk(0, 0);
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++)
+                            x = cfma(csub(tX[a + b * DP], cscale(tS[a + b * DP], g.mu_dot)), tG[b + c * DP], x);
+                        tV[a + c * DP] = x;
+                    }
+                __syncwarp();
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     C x = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++)
-                        x = cfma(csub(tX[a + b * DP], cscale(tS[a + b * DP], g.mu_dot)), s[b], x);
-                    v[a] = x;
-                }
-#pragma unroll
-                for (int a = 0; a < DP; a++) {
-                    C x = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++) x = cfma(tG[a + b * DP], v[b], x);
+                    if (c < DP)
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++) x = cfma(tG[a + b * DP], tV[b + c * DP], x);
                     acc[a] = cadd(acc[a], x);
                 }
+                __syncwarp();
             } else {
                 // column c of G^H Gbar G^H: v = Gbar conj(G(c, :))^T, then G^H v
-                C v[DP];
+                if (c < DP)
+                    for (int a = 0; a < DP; a++) {
+                        C x = cmk(0, 0);
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++) x = cfma(tX[a + b * DP], cconj(tG[c + b * DP]), x);
+                        tV[a + c * DP] = x;
+                    }
+                __syncwarp();
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     C x = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++) x = cfma(tX[a + b * DP], cconj(tG[c + b * DP]), x);
-                    v[a] = x;
-                }
-#pragma unroll
-                for (int a = 0; a < DP; a++) {
-                    C x = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++) x = cfma(cconj(tG[b + a * DP]), v[b], x);
+                    if (c < DP)
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++) x = cfma(cconj(tG[b + a * DP]), tV[b + c * DP], x);
                     acc[a] = cadd(acc[a], x);
                 }
-                // Re Tr[(G S' G)^H Gbar], column c: y = G (S' G(:, c)), sum_a conj(y_a) Gbar(a, c)
-                C u[DP];
-#pragma unroll
-                for (int a = 0; a < DP; a++) {
-                    C x = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++) x = cfma(tS[a + b * DP], s[b], x);
-                    u[a] = x;
-                }
+                __syncwarp();
+                // Re Tr[(G S' G)^H Gbar], column c: u = S' G(:, c) in the work tile, y = G u, sum_a Re(Gbar(a,c) conj(y_a))
+                if (c < DP)
+                    for (int a = 0; a < DP; a++) {
+                        C x = cmk(0, 0);
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++) x = cfma(tS[a + b * DP], tG[b + c * DP], x);
+                        tV[a + c * DP] = x;
+                    }
+                __syncwarp();
                 double t = 0.0;
-#pragma unroll
-                for (int a = 0; a < DP; a++) {
-                    C y = cmk(0, 0);
-#pragma unroll
-                    for (int b = 0; b < DP; b++) y = cfma(tG[a + b * DP], u[b], y);
-                    if (col && a < D) t += cmulc(tX[a + c * DP], y).x;  // Re(Gbar(a,c) conj(y_a))
-                }
+                if (col)
+                    for (int a = 0; a < D; a++) {
+                        C y = cmk(0, 0);
+#pragma unroll 4
+                        for (int b = 0; b < DP; b++) y = cfma(tG[a + b * DP], tV[b + c * DP], y);
+                        t += cmulc(tX[a + c * DP], y).x;
+                    }
                 accmu += group_sum<DP, W>(t);
+                __syncwarp();
             }
         }
     }
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
 
 inline size_t ad_smem(int DP, int W, int kc, int D, int m) {
     const int NG = 128 / W;
-    return ((size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)NG * m + (size_t)NG * 3 * DP * DP) * 16;
+    return ((size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)NG * m + (size_t)NG * 4 * DP * DP) * 16;
 }
 
 typedef void (*AdKernel)(AdArgs);
