@@ -24,6 +24,7 @@
 // arithmetic type.  Per-chunk sums are reduced over chunks in a fixed order by a second kernel.
 // Ops = OpsD (FP64) or OpsF (double-float on the FP32 pipe; FP64 appears only when staging and storing).
 #pragma once
+#include <type_traits>
 #include "df.cuh"
 #include "linalg.cuh"
 
@@ -46,11 +47,14 @@ struct SchurArgs {
     int *status;
 };
 
-// the unrolled Gauss-Jordan for small blocks, the rolled one (df.cuh) from 8 on
+// the rolled Gauss-Jordan (df.cuh) for double-float at every width and for FP64 from 8 on (measured: double-float
+// kernels are instruction-fetch bound, FP64 ones FP64-pipe bound), the unrolled one otherwise
 template <class Ops, int DP, int W>
 __device__ __forceinline__ bool gj_inverse(typename Ops::C (&a)[DP], int c) {
-    if constexpr (DP >= 8) return warp_gj_inverse_rolled<Ops, DP, W>(a, c);
-    else return warp_gj_inverse_t<Ops, DP, W>(a, c);
+    if constexpr (DP >= 8 || (std::is_same<Ops, OpsF>::value && DP >= 2))
+        return warp_gj_inverse_rolled<Ops, DP, W>(a, c);
+    else
+        return warp_gj_inverse_t<Ops, DP, W>(a, c);
 }
 
 template <int DP, int W>
