@@ -86,6 +86,7 @@ struct OpsD {
     static __device__ __forceinline__ C fms(C a, C b, C acc) { return cfms(a, b, acc); }
     static __device__ __forceinline__ C rcp(C a) { return crcp(a); }
     static __device__ __forceinline__ double re(C a) { return a.x; }
+    static __device__ __forceinline__ double im(C a) { return a.y; }
     static __device__ __forceinline__ double mag2(C a) { return cabs2(a); }
     static __device__ __forceinline__ C shfl(C v, int src, int w) { return shfl2(v, src, w); }
 };
@@ -126,6 +127,7 @@ struct OpsF {
         return {df_mul(a.re, r), df_neg(df_mul(a.im, r))};
     }
     static __device__ __forceinline__ double re(C a) { return df_val(a.re); }
+    static __device__ __forceinline__ double im(C a) { return df_val(a.im); }
     static __device__ __forceinline__ float mag2(C a) {  // pivot choice only: FP32 magnitude suffices
         return __fmaf_rn(a.re.h, a.re.h, __fmul_rn(a.im.h, a.im.h));
     }

@@ -357,7 +357,38 @@ struct Prepared {
     double2 *sig, *mom, *UP, *m0, *B;
     double *eps, *epsQ;
     cudaEvent_t static_ready = nullptr;  // recorded on the side stream after the static eigen-decomposition
+    double e0 = 0, de = 0, eta = 0;      // real-axis grid (S_REAL passes)
 };
+
+// the per-k Schur data for a real-axis pass (no self-energy tail, no static spectrum): sig = Sigma(E) as given
+int prepare_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dSE, int nE,
+                 Prepared &P) {
+    P.n = L->n;
+    P.nk = L->nk;
+    P.Nf = nE;
+    P.ncl = L->ncl;
+    P.nh = L->nh;
+    P.D = L->ncl * L->nh;
+    P.mask = 0;
+    P.beta = L->beta;
+    P.H = dH;
+    P.sig = const_cast<double2 *>(dSE);
+    const int n = P.n, nk = P.nk, D = P.D, m = n - D;
+    if (n < 1 || nk < 1 || D < 1 || D > n || !pick_schur(D))
+        return dg_fail(ctx, DMFTGPU_BADARG, "gloc_real: unsupported sizes (need 1 <= ncl*nh <= min(n, 20))");
+    P.m0 = (double2 *)dg_buf(ctx, "real.m0", (size_t)D * D * sizeof(double2));
+    P.epsQ = (double *)dg_buf(ctx, "lat.epsQ", (size_t)nk * (m + 1) * sizeof(double));
+    P.B = (double2 *)dg_buf(ctx, "lat.B", (size_t)nk * (m + 1) * D * sizeof(double2));
+    if (!P.m0 || !P.epsQ || !P.B) return DMFTGPU_NOMEM;
+    DG_CUDA(cudaMemsetAsync(P.m0, 0, (size_t)D * D * sizeof(double2), ctx->stream));
+    if (m > 0) {
+        const size_t sm = eig_blk_smem(m);
+        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_schur_prep_blk<<<nk, EIG_THREADS, sm, ctx->stream>>>(n, D, P.H, P.epsQ, P.B, ctx->d_status);
+        DG_LAUNCH(ctx, "k_schur_prep_blk");
+    }
+    return DMFTGPU_OK;
+}
 
 int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P) {
     P.n = L->n;
@@ -482,17 +513,16 @@ int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid
 __global__ void k_schur_reduce(int nchunk, int nf2, int DD, int mode, const double2 *pblk, const double2 *pblk0,
                                const double2 *ptr, double2 *blk, double2 *blk0, double *tr, double *dtr) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (mode & dg::S_BLOCK) {
-        if (t >= (long long)nf2 * DD) return;
+    if ((mode & dg::S_BLOCK) && t < (long long)nf2 * DD) {
         double2 s = cmk(0, 0), s0 = cmk(0, 0);
         for (int q = 0; q < nchunk; q++) {
             s = cadd(s, pblk[(size_t)q * nf2 * DD + t]);
             s0 = cadd(s0, pblk0[(size_t)q * nf2 * DD + t]);
         }
         blk[t] = s;
-        blk0[t] = s0;
-    } else {
-        if (t >= nf2) return;
+        if (blk0) blk0[t] = s0;
+    }
+    if ((mode & dg::S_TRACE) && t < nf2) {
         double a = 0, b = 0;
         for (int q = 0; q < nchunk; q++) {
             a += ptr[(size_t)q * nf2 + t].x;
@@ -508,7 +538,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
               double *tr, double *dtr, bool mixed) {
     const SInst *in = pick_schur(P.D);
     SchurKernel kern = in->get(mode, mixed);
-    const int m = P.n - P.D, NG = 128 / in->W, nf2 = 2 * P.Nf, DD = P.D * P.D;
+    const int m = P.n - P.D, NG = 128 / in->W, DD = P.D * P.D;
+    const int nf2 = (mode & dg::S_REAL) ? P.Nf : 2 * P.Nf;  // the real axis has exactly the caller's points
     int kc = 16;
     while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n) > 96 * 1024) kc /= 2;
     const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n);
@@ -533,7 +564,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
         pblk = (double2 *)dg_buf(ctx, "schur.pblk", (size_t)nchunk_max * nf2 * DD * sizeof(double2));
         pblk0 = (double2 *)dg_buf(ctx, "schur.pblk0", (size_t)nchunk_max * nf2 * DD * sizeof(double2));
         if (!pblk || !pblk0) return DMFTGPU_NOMEM;
-    } else {
+    }
+    if (mode & dg::S_TRACE) {
         ptr = (double2 *)dg_buf(ctx, "schur.ptr", (size_t)nchunk_max * nf2 * sizeof(double2));
         if (!ptr) return DMFTGPU_NOMEM;
     }
@@ -553,6 +585,9 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.nf2 = nf2;
     g.D = P.D;
     g.wgrid = wgrid;
+    g.e0 = P.e0;
+    g.de = P.de;
+    g.eta = P.eta;
     g.kc = kc;
     g.kchunk = kchunk;
     g.beta = P.beta;
@@ -562,7 +597,7 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     g.ptr = ptr;
     g.status = ctx->d_status;
     // the TRACE passes read the static eigenvalues (Tr G0), computed on the side stream
-    if ((mode & dg::S_TRACE) || ((mode & dg::S_BLOCK) && in->DP >= 8))
+    if (!(mode & dg::S_REAL) && ((mode & dg::S_TRACE) || ((mode & dg::S_BLOCK) && in->DP >= 8)))
         DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     // autotuning: time 4, 8 and 16 CTAs per SM once per (width, mode, precision, N_k, points) and keep the fastest
     auto tuned = ctx->tuned.find(key);
@@ -601,7 +636,7 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
         kern<<<dim3(fblocks, nchunk), 128, smem, ctx->stream>>>(g);
     }
     DG_LAUNCH(ctx, "k_schur");
-    const long long nred = (mode & dg::S_BLOCK) ? (long long)nf2 * DD : nf2;
+    const long long nred = (mode & dg::S_BLOCK) ? std::max((long long)nf2 * DD, (long long)nf2) : nf2;
     k_schur_reduce<<<dg_ceil_div(nred, 256), 256, 0, ctx->stream>>>(nchunk, nf2, DD, mode, pblk, pblk0, ptr, blk, blk0,
                                                                      tr, dtr);
     DG_LAUNCH(ctx, "k_schur_reduce");
@@ -760,6 +795,14 @@ int greenftn_w_dev(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH
     k_nummat<<<(int)DD, 256, 0, ctx->stream>>>(Nf, L->nk, D, L->beta, blk, blk0, occ, dN);
     DG_LAUNCH(ctx, "k_nummat");
     return DMFTGPU_OK;
+}
+
+
+// the real-axis sums divided by N_k: G_PP blocks, and Tr G as (re, im)
+__global__ void k_real_finish(int nE, int DD, int nk, const double2 *blk, const double *tr, double2 *g, double2 *trace) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < (long long)nE * DD) g[t] = cscale(blk[t], 1.0 / nk);
+    if (t < nE) trace[t] = cmk(tr[t] / nk, tr[nE + t] / nk);
 }
 
 }  // namespace
@@ -938,6 +981,45 @@ int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattic
             if (flags & DMFTGPU_GRAPH) ctx->graph_key = "warm:" + key;
         }
     }
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// retarded lattice Green function on a real-energy grid (retarded_GreenFtn2, src/GreenFtn.cpp:425-466, as
+// summed over k by qs_spectra, src/qs_spectra.cpp:99-130): gloc[nE] = (1/N_k) sum_k G_PP(k, E) and trace[nE] =
+// (1/N_k) sum_k Tr G(k, E) over the whole model space, G = (E + mu + i eta - H - Sigma(E))^-1
+int dmftgpu_gloc_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma_e, int nE,
+                      double e0, double de, double eta, double mu, double *gloc, double *trace, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma_e || !gloc || !trace || nE < 1 || !(eta > 0)) return DMFTGPU_BADARG;
+    if (L->ncl != 1 || L->hartr) return dg_fail(ctx, DMFTGPU_BADARG, "gloc_real: one cluster, HartrIndex identity");
+    cudaSetDevice(ctx->device);
+    const int D = L->nh;
+    const size_t DD = (size_t)D * D;
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma_e, (size_t)nE * DD * sizeof(double2), flags, "io.sigma_e", &st);
+    if (st) return st;
+    double2 *dG = (double2 *)dg_out(ctx, gloc, (size_t)nE * DD * sizeof(double2), flags, "io.gloc_e", &st);
+    if (st) return st;
+    double2 *dT = (double2 *)dg_out(ctx, trace, (size_t)nE * sizeof(double2), flags, "io.trace_e", &st);
+    if (st) return st;
+    double2 *blk = (double2 *)dg_buf(ctx, "real.blk", (size_t)nE * DD * sizeof(double2));
+    double *tr = (double *)dg_buf(ctx, "real.tr", 2 * (size_t)nE * sizeof(double));
+    if (!blk || !tr) return DMFTGPU_NOMEM;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare_real(ctx, L, dH, dS, nE, P));
+    P.e0 = e0;
+    P.de = de;
+    P.eta = eta;
+    DG_TRY(run_schur(ctx, P, dg::S_BLOCK | dg::S_TRACE | dg::S_REAL, mu, 0, blk, nullptr, tr, tr + nE,
+                     (flags & DMFTGPU_MIXED) != 0));
+    k_real_finish<<<dg_ceil_div((long long)nE * DD, 256), 256, 0, ctx->stream>>>(nE, (int)DD, L->nk, blk, tr, dG, dT);
+    DG_LAUNCH(ctx, "k_real_finish");
+    DG_TRY(dg_out_done(ctx, gloc, dG, (size_t)nE * DD * sizeof(double2), flags));
+    DG_TRY(dg_out_done(ctx, trace, dT, (size_t)nE * sizeof(double2), flags));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;

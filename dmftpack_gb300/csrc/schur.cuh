@@ -30,7 +30,9 @@
 
 namespace dg {
 
-enum { S_BLOCK = 1, S_TRACE = 2, S_DERIV = 4 };
+// S_REAL: the real-axis grid z = mu + (e0 + n de) + i eta of the spectra (retarded_GreenFtn2, src/GreenFtn.cpp:
+// 425-466), with TRACE giving the complex Tr G(z) of the whole model space (no G0 term) and BLOCK G_PP only
+enum { S_BLOCK = 1, S_TRACE = 2, S_DERIV = 4, S_REAL = 8 };
 
 struct SchurArgs {
     const double2 *H;     // [nk][n][n] column-major, correlated orbitals first
@@ -41,6 +43,7 @@ struct SchurArgs {
     const double *eps0;   // [nk][n] eigenvalues of H + m0 (TRACE modes; BLOCK for DP >= 8)
     const double2 *UP;    // [nk][n][D] correlated rows of their eigenvectors (BLOCK for DP >= 8)
     int n, m, nk, nf2, D, wgrid, kc, kchunk;  // kc: k points staged per round; kchunk: k points per CTA
+    double e0, de, eta;                        // S_REAL grid
     double beta, mu;
     double2 *pblk, *pblk0;  // [nchunk][nf2][D][D]  per-chunk k sums (BLOCK)
     double2 *ptr;           // [nchunk][nf2]         per-chunk trace sums (x = tr, y = dtr)
@@ -95,8 +98,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     extern __shared__ double2 sm[];
     const int D = g.D, DD = D * D, m = g.m;
     constexpr bool TR = (MODE & S_TRACE) != 0;
-    constexpr bool G0E = (MODE & S_BLOCK) && DP >= 8;  // GwHF from the static eigen-decomposition
-    constexpr bool E0 = TR || G0E;
+    constexpr bool RE = (MODE & S_REAL) != 0;
+    constexpr bool G0E = (MODE & S_BLOCK) && DP >= 8 && !RE;  // GwHF from the static eigen-decomposition
+    constexpr bool E0 = (TR && !RE) || G0E;
     C *st = reinterpret_cast<C *>(sm);
     C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m;
     C *sE0 = sH + (size_t)g.kc * DD;                                      // [kc][n] (E0)
@@ -119,8 +123,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     for (int t = threadIdx.x; t < DD; t += blockDim.x) sM0[t] = Ops::from(g.m0[t]);
     // per-group frequency constants: iw (as a complex with zero real part), z = mu + iw, Sigma(:, c)
     const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
-    const C zc = Ops::from(cmk(g.mu, w));
-    const C iwc = Ops::from(cmk(0.0, w));
+    // iwc: z - mu (i w_n, or E + i eta on the real axis); zc = z
+    const C zc = RE ? Ops::from(cmk(g.mu + (g.e0 + f * g.de), g.eta)) : Ops::from(cmk(g.mu, w));
+    const C iwc = RE ? Ops::from(cmk(g.e0 + f * g.de, g.eta)) : Ops::from(cmk(0.0, w));
     C sgc[DP];
 #pragma unroll
     for (int a = 0; a < DP; a++) sgc[a] = (col && a < D) ? Ops::from(g.sig[(size_t)f * DD + a + (size_t)c * D]) : Ops::zero();
@@ -160,7 +165,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         if (a < D) s[a] = Ops::fms(bs[l * D + a], q, s[a]);
                 }
             }
-            if ((MODE & S_BLOCK) && !G0E) {
+            if ((MODE & S_BLOCK) && !G0E && !RE) {
 #pragma unroll
                 for (int a = 0; a < DP; a++)
                     s0[a] = (col && a < D) ? Ops::sub(Ops::add(s[a], sgc[a]), sM0[a + c * D]) : s[a];
@@ -184,7 +189,11 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                 }
             }
             sing |= gj_inverse<Ops, DP, W>(s, c);
-            if ((MODE & S_BLOCK) && !G0E) {
+            if (RE && (MODE & S_BLOCK)) {
+#pragma unroll
+                for (int a = 0; a < DP; a++) accG[a] = Ops::add(accG[a], s[a]);
+            }
+            if ((MODE & S_BLOCK) && !G0E && !RE) {
                 sing |= gj_inverse<Ops, DP, W>(s0, c);
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
@@ -215,10 +224,11 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                     acc1 = Ops::add(acc1, wl[l]);
                     if (MODE & S_DERIV) acc2 = Ops::sub(acc2, Ops::mul(wl[l], wl[l]));
                 }
-                for (int j = c; j < g.n; j += W) {
-                    acc1 = Ops::sub(acc1, rl[j]);
-                    if (MODE & S_DERIV) acc2 = Ops::add(acc2, Ops::mul(rl[j], rl[j]));
-                }
+                if (!RE)
+                    for (int j = c; j < g.n; j += W) {
+                        acc1 = Ops::sub(acc1, rl[j]);
+                        if (MODE & S_DERIV) acc2 = Ops::add(acc2, Ops::mul(rl[j], rl[j]));
+                    }
                 C y[DP];
                 if (MODE & S_DERIV) {
                     // Y = G S' G, column c: u = S' G(:,c), y = G u
@@ -268,6 +278,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                 }
                 acct1 += group_sum<DP, W>(Ops::re(acc1));
                 if (MODE & S_DERIV) acct2 += group_sum<DP, W>(Ops::re(acc2));
+                if (RE) acct2 += group_sum<DP, W>(Ops::im(acc1));  // complex Tr G on the real axis
             }
         }
     }
@@ -291,8 +302,8 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m, int n) {
     const int NG = 128 / W;
     size_t s = (size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D + (size_t)NG * m;
-    const bool g0e = (mode & S_BLOCK) && DP >= 8;
-    if ((mode & S_TRACE) || g0e) s += (size_t)kc * n + (size_t)NG * n;
+    const bool g0e = (mode & S_BLOCK) && DP >= 8 && !(mode & S_REAL);
+    if (((mode & S_TRACE) && !(mode & S_REAL)) || g0e) s += (size_t)kc * n + (size_t)NG * n;
     if (g0e) s += (size_t)kc * n * D;
     if (mode & S_DERIV) s += (size_t)NG * 2 * DP * DP;
     return s * 16;
@@ -306,6 +317,7 @@ SchurKernel schur_pick_ops(int mode) {
         case S_BLOCK: return k_schur<Ops, DP, W, S_BLOCK>;
         case S_TRACE: return k_schur<Ops, DP, W, S_TRACE>;
         case S_TRACE | S_DERIV: return k_schur<Ops, DP, W, S_TRACE | S_DERIV>;
+        case S_BLOCK | S_TRACE | S_REAL: return k_schur<Ops, DP, W, S_BLOCK | S_TRACE | S_REAL>;
         default: return nullptr;
     }
 }

@@ -31,7 +31,7 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -93,6 +93,8 @@ def load(require_built=True):
     lib.dmftgpu_greenftn_w.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _vp, C.c_int]
     lib.dmftgpu_greenftn_w_batched.argtypes = [_vp, C.c_int, P(_Lat), P(_vp), P(_vp), _dp, P(_vp), P(_vp), P(_vp),
                                                C.c_int]
+    lib.dmftgpu_gloc_real.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      _vp, _vp, C.c_int]
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
@@ -296,6 +298,26 @@ class Context:
             ptr(gwhf_cm) if gwhf_cm is not None else None, ptr(num_cm),
             self._flags(True, (MIXED if mixed else 0) | (GRAPH if graph else 0) | (AUTOTUNE if autotune else 0)))
         self._check("dmftgpu_greenftn_w_batched", st)
+
+    def retarded_GreenFtn(self, lat, H_k, SelfE_E, e0, de, eta, mu, mixed=False):
+        """Real-axis lattice sum on E_n = e0 + n de (n < len(SelfE_E)): returns (G_loc(E)[nE,D,D], Tr G(E)[nE])."""
+        dev = _is_torch(H_k)
+        h, s = _Arr(H_k, dev), _Arr(SelfE_E, dev)
+        nE, D = s.obj.shape[0], lat.D
+        g = _Arr.empty((nE, D, D), dev, like=h.obj)
+        if dev:
+            import torch
+            tr = torch.empty(nE, dtype=torch.complex128, device=h.obj.device)
+            trp = tr.data_ptr()
+        else:
+            tr = np.empty(nE, np.complex128)
+            trp = tr.ctypes.data
+        L = lat._c()
+        st = self.lib.dmftgpu_gloc_real(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), int(nE), float(e0), float(de),
+                                        float(eta), float(mu), _vp(g.ptr), _vp(trp),
+                                        self._flags(dev, MIXED if mixed else 0))
+        self._check("dmftgpu_gloc_real", st)
+        return g.result(), tr
 
     def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
         """Reverse mode of G_loc = GreenFtn_w(...)[0]: returns (Sigma_bar[nfreq,D,D], mu_bar) for the cotangent

@@ -118,6 +118,15 @@ int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattic
                                const double *const *sigma, const double *mu, double *const *gw, double *const *gwhf,
                                double *const *nummat, int flags);
 
+/* The retarded lattice Green function on a real-energy grid E_n = e0 + n de, n < nE (retarded_GreenFtn2,
+ * src/GreenFtn.cpp:425-466, summed over k as qs_spectra does, src/qs_spectra.cpp:99-130): with G(k, E) =
+ * (E + mu + i eta - H(k) - Sigma(E))^-1 and sigma_e[nE][D][D] the self-energy on the grid,
+ * gloc[nE][D][D] = (1/N_k) sum_k G_PP(k, E) and trace[nE] (complex) = (1/N_k) sum_k Tr G(k, E) over the whole
+ * model space, from which the spectral weights of qsdos follow (-Im/pi).  One cluster, HartrIndex the identity;
+ * FP64 or DMFTGPU_MIXED. */
+int dmftgpu_gloc_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma_e, int nE,
+                      double e0, double de, double eta, double mu, double *gloc, double *trace, int flags);
+
 /* Derivatives of GreenFtn_w's G_loc(iw_n) = (1/N_k) sum_k G_PP(k, iw_n), n < nfreq, for one correlated cluster
  * (no counterpart in the reference, which has no derivatives; they supply dN/dmu-style Newton steps and
  * Jacobian-vector products of the self-consistency residual).  dG_PP = G_PP dSigma G_PP - dmu (G^2)_PP, with G

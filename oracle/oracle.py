@@ -459,3 +459,21 @@ def dmft_iteration(H, state, p, it, pulay):
            np.linalg.norm(nummat - nm_imp) / np.linalg.norm(nummat), loops]
     new = dict(state, selfe=selfe, weiss=weiss, nummat=nummat, mu=mu, gloc=gloc)
     return new, gloc, gi, np.array(res)
+
+
+def retarded_gloc(H, sigma_e, e0, de, eta, mu, D):
+    """retarded_GreenFtn2 (src/GreenFtn.cpp:425-466) in the model basis (DF_CorrBase = I) summed over k as qs_spectra
+    does: G(k, E_n) = (E_n + mu + i eta - H(k) - Sigma(E_n) on the first D orbitals)^-1 by explicit inversion.
+    Returns ((1/N_k) sum_k G_PP, (1/N_k) sum_k Tr G)."""
+    nk, n = H.shape[0], H.shape[1]
+    nE = sigma_e.shape[0]
+    g = np.zeros((nE, D, D), np.complex128)
+    tr = np.zeros(nE, np.complex128)
+    for i in range(nE):
+        z = e0 + i * de + mu + 1j * eta
+        A = z * np.eye(n)[None] - H
+        A[:, :D, :D] -= sigma_e[i][None]
+        Gk = np.linalg.inv(A)
+        g[i] = Gk[:, :D, :D].mean(0)
+        tr[i] = np.trace(Gk, axis1=1, axis2=2).mean()
+    return g, tr

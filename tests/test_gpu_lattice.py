@@ -185,3 +185,26 @@ def test_hyb_delta_matches_oracle(ctx, orc):
     d_o = orc.hyb_delta(orb, wl.sigma, gw, himp, 0.2, wl.beta)
     d_g = ctx.Construct_hyb_delta(orb, wl.sigma, gw, 0.2, wl.beta, himp)
     assert rel_err(d_g, d_o) < TOL
+
+
+@pytest.mark.parametrize("case", ["t2g_p", "soc_small"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_retarded_gloc_real_axis(ctx, orc, case, mixed):
+    """Real-axis lattice sum (retarded_GreenFtn2 over a qs_spectra energy grid) against explicit inversion."""
+    if case == "t2g_p":
+        wl = models.t2g_p(k=3, nfreq=8, beta=10.0)
+    else:
+        wl = models.soc56(k=2, nfreq=8, beta=10.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    lat = lib.Lattice(wl.n, wl.nk, 8, wl.beta, 1, wl.D)
+    nE, e0, de, eta, mu = 40, -4.0, 0.2, 0.05, 0.3
+    rng = np.random.default_rng(2)
+    A = rng.normal(size=(wl.D, wl.D)) + 1j * rng.normal(size=(wl.D, wl.D))
+    Es = e0 + de * np.arange(nE)
+    # a causal self-energy on the grid: Hermitian static part - i Gamma(E) (PSD)
+    sig = 0.1 * (A + A.conj().T)[None] - 1j * (0.2 + 0.05 * Es[:, None, None] ** 2) * np.eye(wl.D)[None]
+    g_o, tr_o = orc.retarded_gloc(H, sig, e0, de, eta, mu, wl.D)
+    g, tr = ctx.retarded_GreenFtn(lat, H, sig, e0, de, eta, mu, mixed=mixed)
+    tol = 1e-9 if mixed else 1e-10
+    assert rel_err(g, g_o) < tol
+    assert rel_err(tr, tr_o) < tol
