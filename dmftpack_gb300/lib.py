@@ -31,7 +31,7 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -97,6 +97,7 @@ def load(require_built=True):
                                       _vp, _vp, C.c_int]
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
+    lib.dmftgpu_downfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
@@ -344,6 +345,34 @@ class Context:
                                        float(mu_dot), _vp(out.ptr), self._flags(dev))
         self._check("dmftgpu_gloc_jvp", st)
         return out.result()
+
+    def downfolding_ftn(self, H_k, HartrIndex_inDFT, S_overlap=None, with_df=False):
+        """Construct_Hk_Sk's generalized eigenproblem and downfolding_ftn over the full band window, per k: returns
+        (KS_eigenEnergy[nk,n], H_k_inModelSpace[nk,n,n], impurity_site_Hamiltonian[D,D]) and, with with_df,
+        DF_CorrBase[nk,n,n] as a fourth item.  H_k, S_overlap: (nk, n, n) numpy arrays or CUDA tensors (S_overlap
+        None: orthogonal basis); HartrIndex_inDFT: the D correlated orbitals."""
+        dev = _is_torch(H_k)
+        h = _Arr(H_k, dev)
+        s = _Arr(S_overlap, dev) if S_overlap is not None else None
+        nk, n = h.obj.shape[0], h.obj.shape[1]
+        hartr = np.ascontiguousarray(HartrIndex_inDFT, dtype=np.int32)
+        D = len(hartr)
+        hm = _Arr.empty((nk, n, n), dev, like=h.obj)
+        df = _Arr.empty((nk, n, n), dev, like=h.obj) if with_df else None
+        hi = _Arr.empty((D, D), dev, like=h.obj)
+        if dev:
+            import torch
+            eps = torch.empty((nk, n), dtype=torch.float64, device=h.obj.device)
+            ep = eps.data_ptr()
+        else:
+            eps = np.empty((nk, n))
+            ep = eps.ctypes.data
+        st = self.lib.dmftgpu_downfold(self.h, int(nk), int(n), int(D), hartr.ctypes.data_as(_ip), _vp(h.ptr),
+                                       _vp(s.ptr) if s else None, _vp(ep), _vp(hm.ptr), _vp(df.ptr) if df else None,
+                                       _vp(hi.ptr), self._flags(dev))
+        self._check("dmftgpu_downfold", st)
+        out = (eps, hm.result(), hi.result())
+        return out + (df.result(),) if with_df else out
 
     def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False):
         dev = _is_torch(H_k)

@@ -7,6 +7,7 @@ profiles/ are taken with.
     python -m dmftpack_gb300.profile_case lattice [--k 16 --nfreq 4096 --mixed --newton]
     python -m dmftpack_gb300.profile_case batched [--nprob 64 --mixed --graph --autotune]
     python -m dmftpack_gb300.profile_case adjoint [--k 16 --nfreq 2048]
+    python -m dmftpack_gb300.profile_case downfold [--k 16 --repeat 2]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
@@ -15,6 +16,9 @@ batched: GreenFtn_w over the ragged batch (64 seeded problems: n in {1,3,5,10,14
        {8,12,16,24,32}, N_freq in {512..4096}, beta in [10, 100]) in one batched call, timed over repeats.
 adjoint: one GreenFtn_w pass, one reverse-mode (VJP) and one forward-mode (JVP) pass of G_loc on the 56-orbital
        SOC model (20 x 20 correlated block, k^3 grid, beta = 30), FP64.
+downfold: the model Hamiltonian of the 56-orbital SOC model (20 correlated orbitals, k^3 grid) with a seeded
+       Hermitian positive-definite overlap S(k) = I + B B^H / 56: the generalized eigenproblem, the downfolding and
+       H_imp, device pointers, timed over repeats.
 lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
@@ -88,6 +92,26 @@ def run_adjoint(ctx, dev, a):
     return out
 
 
+def run_downfold(ctx, dev, a):
+    import torch
+    from dmftpack_gb300 import models
+    wl = models.soc56(k=a.k, nfreq=8)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    g = torch.Generator(device=dev).manual_seed(7)
+    B = 0.3 * torch.complex(torch.randn(wl.nk, wl.n, wl.n, device=dev, generator=g, dtype=torch.float64),
+                            torch.randn(wl.nk, wl.n, wl.n, device=dev, generator=g, dtype=torch.float64))
+    S = torch.eye(wl.n, dtype=torch.complex128, device=dev) + B @ B.conj().transpose(1, 2) / wl.n
+    hartr = list(range(wl.D))
+    times = []
+    for _ in range(a.repeat + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.downfolding_ftn(Hd, hartr, S)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    return {"nk": wl.nk, "n": wl.n, "D": wl.D, "seconds": times[1:], "k_per_second": wl.nk / min(times[1:])}
+
+
 def run_lattice(ctx, dev, a):
     import torch
     from dmftpack_gb300 import lib, models
@@ -148,7 +172,7 @@ def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint", "downfold"])
     ap.add_argument("--nprob", type=int, default=64)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--autotune", action="store_true")
@@ -189,9 +213,9 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case in ("dmft", "lattice", "batched", "adjoint"):
+    if a.case in ("dmft", "lattice", "batched", "adjoint", "downfold"):
         out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched,
-                    "adjoint": run_adjoint}[a.case](ctx, dev, a))
+                    "adjoint": run_adjoint, "downfold": run_downfold}[a.case](ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
         return

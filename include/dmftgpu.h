@@ -139,6 +139,18 @@ int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double 
 int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
                      const double *sigma_dot, double mu_dot, double *gloc_dot, int flags);
 
+/* The model Hamiltonian of a non-orthogonal tight-binding input, per k point: the generalized eigenproblem
+ * H(k) v = e S(k) v of Construct_Hk_Sk (src/ConstructModelHamiltonian.cpp:103-111) followed by downfolding_ftn
+ * over the full band window (src/downfolding.cpp:20-63) and the k-averaged impurity level
+ * (src/downfolding.cpp:85-104).  hk, sk: [nk][n][n] (sk NULL: identity overlap), hartr[D] the correlated rows
+ * (HartrIndex_inDFT, distinct, always a host pointer), n <= 56.  Outputs: eps[nk][n] ascending band energies; hmodel[nk][n][n] =
+ * DF diag(eps) DF^H with rows 0..D-1 the Loewdin-orthonormalised projected correlated orbitals; optional
+ * df[nk][n][n] (DF_CorrBase) and himp[D][D] = (1/nk) sum_k hmodel[k][0:D][0:D].  The ligand rows D..n-1 of DF
+ * are an orthonormal complement whose in-subspace rotation differs from Eigen's (see the kernel's header);
+ * FP64.  DMFTGPU_SINGULAR when S is not positive definite or the projected block is rank deficient. */
+int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const int *hartr, const double *hk, const double *sk,
+                     double *eps, double *hmodel, double *df, double *himp, int flags);
+
 /* Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119, declared src/TB.h:45-47):
  * delta[nfreq][dim][dim] = (iw+mu) I - himp[orb] - sigma[orb] - (gw[orb])^-1, orb[dim] indexes D. */
 int dmftgpu_hyb_delta(dmftgpu_ctx *ctx, int dim, const int *orb, int nfreq, double beta, int D,

@@ -477,3 +477,35 @@ def retarded_gloc(H, sigma_e, e0, de, eta, mu, D):
         g[i] = Gk[:, :D, :D].mean(0)
         tr[i] = np.trace(Gk, axis1=1, axis2=2).mean()
     return g, tr
+
+
+def downfold(H, S, hartr):
+    """Construct_Hk_Sk's generalized eigenproblem (src/ConstructModelHamiltonian.cpp:103-111) and downfolding_ftn over
+    the full band window (src/downfolding.cpp:20-63, NBAND = n, FromValToKS = identity), with the impurity level of
+    src/downfolding.cpp:85-104.  H, S: (nk, n, n) ordinary (k, i, j) arrays (S None: identity); hartr: the D
+    correlated orbitals (HartrIndex_inDFT).  Per k: H v = e S v with V^H S V = I (scipy.linalg.eigh), P = V[hartr],
+    P <- S_d^-1/2 P (S_d = P P^H), DF = Q^H from the complete QR of P^H with rows 0..D-1 replaced by P,
+    H_model = DF diag(e) DF^H.  Returns (eps (nk, n), H_model (nk, n, n), DF (nk, n, n), H_imp (D, D)).  LAPACK's
+    Householder and eigenvector phase conventions differ from Eigen's, so only quantities invariant under a unitary
+    rotation of DF's rows D..n-1 are comparable with the reference (and with the CUDA kernel)."""
+    import scipy.linalg as sla
+    H = np.asarray(H, np.complex128)
+    nk, n = H.shape[0], H.shape[1]
+    hartr = np.asarray(hartr, int)
+    D = len(hartr)
+    eps = np.zeros((nk, n))
+    Hm = np.zeros((nk, n, n), np.complex128)
+    DF = np.zeros((nk, n, n), np.complex128)
+    for k in range(nk):
+        Sk = np.eye(n) if S is None else np.asarray(S[k], np.complex128)
+        e, V = sla.eigh(H[k], Sk)
+        P = V[hartr, :]
+        w, W = np.linalg.eigh(P @ P.conj().T)
+        Pn = (W * w ** -0.5) @ W.conj().T @ P
+        Q, _ = np.linalg.qr(Pn.conj().T, mode="complete")
+        F = Q.conj().T
+        F[:D] = Pn
+        eps[k] = e
+        DF[k] = F
+        Hm[k] = (F * e) @ F.conj().T
+    return eps, Hm, DF, Hm[:, :D, :D].mean(0)

@@ -181,3 +181,38 @@ def test_oracle_scgf2_without_interaction_keeps_the_bare_green_function(orc):
     assert loops == 10
     assert np.abs(se).max() < 1e-9
     assert np.abs(g[:nf] - g0).max() < 1e-9
+
+
+def _overlap(rng, nk, n, scale=0.2):
+    B = scale * (rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n)))
+    return np.eye(n)[None] + (B @ B.conj().transpose(0, 2, 1)) / n
+
+
+def test_downfold_orthogonal_basis_keeps_the_correlated_block(orc):
+    # with S = I the eigenvectors are unitary, the projected rows are already orthonormal and the correlated block
+    # of H_model is H's own; the ligand block is a unitary rotation of H's, so H_PL H_LP and its spectrum survive
+    wl = models.t2g_p(k=3, nfreq=8)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    D = 3
+    eps, Hm, DF, himp = orc.downfold(H, None, np.arange(D))
+    assert np.abs(Hm[:, :D, :D] - H[:, :D, :D]).max() < 1e-12
+    assert np.abs(Hm[:, :D, D:] @ Hm[:, D:, :D] - H[:, :D, D:] @ H[:, D:, :D]).max() < 1e-12
+    assert np.abs(np.linalg.eigvalsh(Hm[:, D:, D:]) - np.linalg.eigvalsh(H[:, D:, D:])).max() < 1e-12
+    assert np.abs(himp - H[:, :D, :D].mean(0)).max() < 1e-12
+
+
+def test_downfold_generalized_eigenproblem_and_orthonormal_frame(orc):
+    rng = np.random.default_rng(11)
+    nk, n, hartr = 4, 9, [1, 4, 5, 7]
+    H = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (H + H.conj().transpose(0, 2, 1)) / 2
+    S = _overlap(rng, nk, n)
+    eps, Hm, DF, himp = orc.downfold(H, S, hartr)
+    # eps solves det(H - e S) = 0: the eigenvalues of S^-1/2 H S^-1/2
+    for k in range(nk):
+        w, W = np.linalg.eigh(S[k])
+        Si = (W * w ** -0.5) @ W.conj().T
+        assert np.abs(np.linalg.eigvalsh(Si @ H[k] @ Si) - eps[k]).max() < 1e-12
+    assert np.abs(DF @ DF.conj().transpose(0, 2, 1) - np.eye(n)[None]).max() < 1e-12
+    assert np.abs(np.linalg.eigvalsh(Hm) - eps).max() < 1e-12
+    assert np.abs(himp - Hm[:, :4, :4].mean(0)).max() < 1e-14
