@@ -23,6 +23,7 @@
 #include "schur.cuh"
 #include "smallmat.cuh"
 #include "adjoint.cuh"
+#include "density.cuh"
 
 namespace {
 
@@ -150,7 +151,7 @@ __device__ inline EigSmem eig_smem(double2 *sm, int n) {
 __global__ void __launch_bounds__(EIG_THREADS) k_static_eig_blk(int n, int D, int nh, int mask,
                                                                 const double2 *__restrict__ H,
                                                                 const double2 *__restrict__ m0, double *eps,
-                                                                double2 *UP, int *status) {
+                                                                double2 *UP, double2 *Uf, int *status) {
     extern __shared__ double2 esm[];
     const int k = blockIdx.x;
     const size_t nn = (size_t)n * n;
@@ -169,11 +170,13 @@ __global__ void __launch_bounds__(EIG_THREADS) k_static_eig_blk(int n, int D, in
         const int l = q / D, a = q % D;
         UP[((size_t)k * n + l) * D + a] = DG_AT(e.U, n, a, l);
     }
+    if (Uf)
+        for (int q = threadIdx.x; q < (int)nn; q += blockDim.x) Uf[(size_t)k * nn + q] = e.U[q];
     if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
 }
 
 __global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, const double2 *__restrict__ H,
-                                                                double *epsQ, double2 *B, int *status) {
+                                                                double *epsQ, double2 *B, double2 *Vq, int *status) {
     extern __shared__ double2 esm[];
     const int k = blockIdx.x, m = n - D;
     EigSmem e = eig_smem(esm, m);
@@ -191,6 +194,8 @@ __global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, co
         for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(e.U, m, j, l), s);
         B[((size_t)k * m + l) * D + a] = s;
     }
+    if (Vq)
+        for (int q = threadIdx.x; q < m * m; q += blockDim.x) Vq[(size_t)k * m * m + q] = e.U[q];
     if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
 }
 
@@ -358,6 +363,8 @@ struct Prepared {
     double *eps, *epsQ;
     cudaEvent_t static_ready = nullptr;  // recorded on the side stream after the static eigen-decomposition
     double e0 = 0, de = 0, eta = 0;      // real-axis grid (S_REAL passes)
+    const int *perm = nullptr;           // device orbital permutation (nullptr: identity)
+    double2 *Vq = nullptr, *Uf = nullptr;  // with `vectors`: V of H_QQ [nk][m][m], U of H + m0 [nk][n][n]
 };
 
 // the per-k Schur data for a real-axis pass (no self-energy tail, no static spectrum): sig = Sigma(E) as given
@@ -384,13 +391,14 @@ int prepare_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, 
     if (m > 0) {
         const size_t sm = eig_blk_smem(m);
         DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_schur_prep_blk<<<nk, EIG_THREADS, sm, ctx->stream>>>(n, D, P.H, P.epsQ, P.B, ctx->d_status);
+        k_schur_prep_blk<<<nk, EIG_THREADS, sm, ctx->stream>>>(n, D, P.H, P.epsQ, P.B, nullptr, ctx->d_status);
         DG_LAUNCH(ctx, "k_schur_prep_blk");
     }
     return DMFTGPU_OK;
 }
 
-int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P) {
+int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P,
+            bool vectors = false) {
     P.n = L->n;
     P.nk = L->nk;
     P.Nf = L->nfreq;
@@ -428,6 +436,7 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
         k_permute<<<dg_ceil_div(tot, 256), 256, 0, s>>>(nk, n, dperm, dH, Hp);
         DG_LAUNCH(ctx, "k_permute");
         P.H = Hp;
+        P.perm = dperm;
     }
     P.mom = (double2 *)dg_buf(ctx, "lat.mom", 4 * (size_t)D * D * sizeof(double2));
     P.sig = (double2 *)dg_buf(ctx, "lat.sig", 2 * (size_t)Nf * D * D * sizeof(double2));
@@ -440,6 +449,11 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     if (!P.m0 || !P.epsQ || !P.B) return DMFTGPU_NOMEM;
     if (n > EIG_NMAX) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: n > 64");
     if (!P.mom || !P.sig || !P.eps || !P.UP) return DMFTGPU_NOMEM;
+    if (vectors) {
+        P.Vq = (double2 *)dg_buf(ctx, "lat.Vq", (size_t)nk * (m * m + 1) * sizeof(double2));
+        P.Uf = (double2 *)dg_buf(ctx, "lat.Uf", (size_t)nk * n * n * sizeof(double2));
+        if (!P.Vq || !P.Uf) return DMFTGPU_NOMEM;
+    }
     DG_TRY(dg_moments_dev(ctx, D, Nf, P.beta, dS, 0, P.mom));
     long long tot = 2LL * Nf * D * D;
     k_sigall<<<dg_ceil_div(tot, 256), 256, 0, s>>>(Nf, D, P.nh, mask, P.beta, dS, P.mom, P.sig, P.m0);
@@ -450,7 +464,7 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     if (m > 0) {
         const size_t sm = eig_blk_smem(m);
         DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_schur_prep_blk<<<nk, EIG_THREADS, sm, s>>>(n, D, P.H, P.epsQ, P.B, ctx->d_status);
+        k_schur_prep_blk<<<nk, EIG_THREADS, sm, s>>>(n, D, P.H, P.epsQ, P.B, P.Vq, ctx->d_status);
         DG_LAUNCH(ctx, "k_schur_prep_blk");
     }
     DG_CUDA(cudaEventRecord(ctx->ev_fork, s));
@@ -458,7 +472,8 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     {
         const size_t sm = eig_blk_smem(n);
         DG_CUDA(cudaFuncSetAttribute(k_static_eig_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_static_eig_blk<<<nk, EIG_THREADS, sm, ctx->side>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, ctx->d_status);
+        k_static_eig_blk<<<nk, EIG_THREADS, sm, ctx->side>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, P.Uf,
+                                                             ctx->d_status);
     }
     DG_LAUNCH(ctx, "k_static_eig_blk");
     DG_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
@@ -798,6 +813,149 @@ int greenftn_w_dev(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH
 }
 
 
+// densityMatDFT, the second half (src/GreenFtn.cpp:311-319): per k, X' = sum over splits of Y + Y^H (the P-Q block is
+// already the Hermitian combination), X = T X' T^H with T = diag(I, V), then
+// dens = X / beta + U diag(f(e0) - R / beta) U^H (Fermi factors with the +-100 cut-offs), stored in the caller's
+// orbital order.  One block per k; two n x n tiles in shared memory.
+__global__ void __launch_bounds__(128) k_dens_finish(int nk, int n, int D, int nsplit, double beta, double mu,
+                                                     const double2 *__restrict__ Y, const double *__restrict__ R,
+                                                     const double2 *__restrict__ Vq, const double2 *__restrict__ Uf,
+                                                     const double *__restrict__ eps0, const int *__restrict__ perm,
+                                                     double2 *dens) {
+    extern __shared__ double2 fsm[];
+    const int k = blockIdx.x, m = n - D, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
+    double2 *X = fsm, *T = fsm + nn;
+    double *gw = (double *)(T + nn);
+    for (int q = tid; q < nn; q += nt) {
+        double2 v = cmk(0, 0);
+        for (int sp = 0; sp < nsplit; sp++) v = cadd(v, Y[((size_t)sp * nk + k) * nn + q]);
+        T[q] = v;
+    }
+    for (int j = tid; j < n; j += nt) {
+        double r = 0;
+        for (int sp = 0; sp < nsplit; sp++) r += R[((size_t)sp * nk + k) * n + j];
+        const double x = beta * (eps0[(size_t)k * n + j] - mu);
+        const double f = x > 100.0 ? 0.0 : (x < -100.0 ? 1.0 : 1. / (1. + exp(x)));
+        gw[j] = f - r / beta;
+    }
+    __syncthreads();
+    for (int q = tid; q < nn; q += nt) {
+        const int i = q % n, j = q / n;
+        if ((i < D) == (j < D)) X[q] = cadd(T[q], cconj(T[j + i * n]));
+        else if (i < D) X[q] = T[q];
+        else X[q] = cconj(T[j + i * n]);
+    }
+    __syncthreads();
+    if (m > 0) {
+        const double2 *V = Vq + (size_t)k * m * m;  // V(i, l) = V[i + l m]
+        for (int q = tid; q < nn; q += nt) {
+            const int i = q % n, j = q / n;
+            if (j < D) T[q] = X[q];
+            else {
+                double2 v = cmk(0, 0);
+                for (int l = 0; l < m; l++) v = cfma(X[i + (D + l) * n], cconj(V[(j - D) + (size_t)l * m]), v);
+                T[q] = v;
+            }
+        }
+        __syncthreads();
+        for (int q = tid; q < nn; q += nt) {
+            const int i = q % n, j = q / n;
+            if (i < D) X[q] = T[q];
+            else {
+                double2 v = cmk(0, 0);
+                for (int l = 0; l < m; l++) v = cfma(V[(i - D) + (size_t)l * m], T[(D + l) + j * n], v);
+                X[q] = v;
+            }
+        }
+        __syncthreads();
+    }
+    const double2 *U = Uf + (size_t)k * nn;
+    for (int q = tid; q < nn; q += nt) {
+        const int i = q % n, j = q / n;
+        double2 v = cscale(X[q], 1.0 / beta);
+        for (int l = 0; l < n; l++) v = cfma(cscale(U[i + (size_t)l * n], gw[l]), cconj(U[j + (size_t)l * n]), v);
+        const int pi = perm ? perm[i] : i, pj = perm ? perm[j] : j;
+        dens[(size_t)k * nn + pi + (size_t)pj * n] = v;
+    }
+}
+
+using dg::DensArgs;
+using dg::DensKernel;
+DensKernel pick_dens(int DP) {
+    switch (DP) {
+        case 1: return dg::dens_kernel_1();
+        case 2: return dg::dens_kernel_2();
+        case 3: return dg::dens_kernel_3();
+        case 4: return dg::dens_kernel_4();
+        case 6: return dg::dens_kernel_6();
+        case 8: return dg::dens_kernel_8();
+        case 10: return dg::dens_kernel_10();
+        case 12: return dg::dens_kernel_12();
+        case 16: return dg::dens_kernel_16();
+        case 20: return dg::dens_kernel_20();
+    }
+    return nullptr;
+}
+
+// densityMatDFT for a prepared lattice (prepare(..., vectors = true)): enqueue only
+int run_density(dmftgpu_ctx *ctx, const Prepared &P, double mu, double2 *dens) {
+    const int n = P.n, D = P.D, m = n - D, nk = P.nk, nf2 = 2 * P.Nf;
+    const SInst *si = pick_schur(D);
+    DensKernel kern = si ? pick_dens(si->DP) : nullptr;
+    if (!kern) return dg_fail(ctx, DMFTGPU_BADARG, "density: unsupported correlated block");
+    const int DP = si->DP, W = si->W;
+    // groups per CTA: the most resident warps per SM within 227 KB of shared memory per CTA
+    const size_t smem_cap = 227 * 1024, sm_per_sm = 228 * 1024;
+    int ng = 0, best = -1;
+    for (int g = 1; g * W <= 128; g++) {
+        const size_t sm = dg::dens_smem(DP, D, m, n, g);
+        if (sm > smem_cap) break;
+        const int ctas = std::min((int)(sm_per_sm / (sm + 1024)), 2048 / (g * W));
+        const int warps = ctas * ((g * W + 31) / 32);
+        if (warps >= best) {
+            best = warps;
+            ng = g;
+        }
+    }
+    if (!ng) return dg_fail(ctx, DMFTGPU_BADARG, "density: model too large for one k point's shared memory");
+    const size_t smem = dg::dens_smem(DP, D, m, n, ng);
+    const int ctas_per_sm = std::max(1, (int)(sm_per_sm / (smem + 1024)));
+    int nsplit = dg_ceil_div(2LL * 152 * ctas_per_sm, nk);
+    nsplit = std::max(1, std::min(nsplit, std::max(1, nf2 / (4 * ng))));
+    double2 *Y = (double2 *)dg_buf(ctx, "dens.Y", (size_t)nsplit * nk * n * n * sizeof(double2));
+    double *R = (double *)dg_buf(ctx, "dens.R", (size_t)nsplit * nk * n * sizeof(double));
+    if (!Y || !R) return DMFTGPU_NOMEM;
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    DensArgs g;
+    g.H = P.H;
+    g.B = P.B;
+    g.epsQ = P.epsQ;
+    g.eps0 = P.eps;
+    g.sig = P.sig;
+    g.n = n;
+    g.m = m;
+    g.nk = nk;
+    g.nf2 = nf2;
+    g.D = D;
+    g.ng = ng;
+    g.beta = P.beta;
+    g.mu = mu;
+    g.Y = Y;
+    g.R = R;
+    g.status = ctx->d_status;
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    {
+        DgTimer tm(ctx, "k_dens_sum");
+        kern<<<dim3(nk, nsplit), ng * W, smem, ctx->stream>>>(g);
+    }
+    DG_LAUNCH(ctx, "k_dens_sum");
+    const size_t fs = 2 * (size_t)n * n * sizeof(double2) + n * sizeof(double);
+    DG_CUDA(cudaFuncSetAttribute(k_dens_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
+    k_dens_finish<<<nk, 128, fs, ctx->stream>>>(nk, n, D, nsplit, P.beta, mu, Y, R, P.Vq, P.Uf, P.eps, P.perm, dens);
+    DG_LAUNCH(ctx, "k_dens_finish");
+    return DMFTGPU_OK;
+}
+
 // the real-axis sums divided by N_k: G_PP blocks, and Tr G as (re, im)
 __global__ void k_real_finish(int nE, int DD, int nk, const double2 *blk, const double *tr, double2 *g, double2 *trace) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1051,6 +1209,30 @@ int dmftgpu_gloc_vjp(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *h
     DG_TRY(dg_out_done(ctx, sigma_bar, dSb, Nf * DD * sizeof(double2), flags));
     DG_CUDA(cudaMemcpyAsync(mu_bar, dmu, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// densityMatDFT of GreenFtn_w: dens[nk][n][n]
+int dmftgpu_density_dft(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
+                        double *dens, int flags) {
+    if (!ctx || check_lat(L) || !hk || !sigma || !dens) return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    const int D = L->ncl * L->nh, Nf = L->nfreq;
+    const size_t DD = (size_t)D * D, nb = (size_t)L->nk * L->n * L->n * sizeof(double2);
+    int st;
+    const double2 *dH = (const double2 *)dg_in(ctx, hk, nb, flags, "io.hk_in", &st);
+    if (st) return st;
+    const double2 *dS = (const double2 *)dg_in(ctx, sigma, Nf * DD * sizeof(double2), flags, "io.sigma", &st);
+    if (st) return st;
+    double2 *dD = (double2 *)dg_out(ctx, dens, nb, flags, "io.dens", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    Prepared P;
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P, true));
+    DG_TRY(run_density(ctx, P, mu, dD));
+    DG_TRY(dg_out_done(ctx, dens, dD, nb, flags));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;

@@ -31,7 +31,7 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_density_dft", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -95,6 +95,7 @@ def load(require_built=True):
                                                C.c_int]
     lib.dmftgpu_gloc_real.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                       _vp, _vp, C.c_int]
+    lib.dmftgpu_density_dft.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_downfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
@@ -319,6 +320,17 @@ class Context:
                                         self._flags(dev, MIXED if mixed else 0))
         self._check("dmftgpu_gloc_real", st)
         return g.result(), tr
+
+    def densityMatDFT(self, lat, H_k, SelfE_w, mu):
+        """GreenFtn_w's per-k density matrix densityMatDFT[nk, n, n] (the full-model-space occupation at each k)."""
+        dev = _is_torch(H_k)
+        h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
+        out = _Arr.empty((lat.nk, lat.n, lat.n), dev, like=h.obj)
+        L = lat._c()
+        st = self.lib.dmftgpu_density_dft(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(out.ptr),
+                                          self._flags(dev))
+        self._check("dmftgpu_density_dft", st)
+        return out.result()
 
     def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
         """Reverse mode of G_loc = GreenFtn_w(...)[0]: returns (Sigma_bar[nfreq,D,D], mu_bar) for the cotangent

@@ -127,6 +127,14 @@ int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattic
 int dmftgpu_gloc_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma_e, int nE,
                       double e0, double de, double eta, double mu, double *gloc, double *trace, int flags);
 
+/* GreenFtn_w's per-k density matrix in the model basis, densityMatDFT (src/GreenFtn.cpp:170-172, 268-275,
+ * 311-319): dens[nk][n][n] = (1/beta) sum_{n < 2 nfreq} [G + G^H - G0 - G0^H](k, iw_n) + U f(e0) U^H, with G the full
+ * n x n lattice Green function (Sigma on the HartrIndex orbitals, its moment tail beyond nfreq), G0 the resolvent
+ * of the static H + m0 = U diag(e0) U^H and f the Fermi factors with the reference's +-100 cut-offs.  Computed
+ * from the correlated-block Schur form (no n x n inversion); rows and columns in the caller's orbital order.  FP64. */
+int dmftgpu_density_dft(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
+                        double *dens, int flags);
+
 /* Derivatives of GreenFtn_w's G_loc(iw_n) = (1/N_k) sum_k G_PP(k, iw_n), n < nfreq, for one correlated cluster
  * (no counterpart in the reference, which has no derivatives; they supply dN/dmu-style Newton steps and
  * Jacobian-vector products of the self-consistency residual).  dG_PP = G_PP dSigma G_PP - dmu (G^2)_PP, with G

@@ -509,3 +509,33 @@ def downfold(H, S, hartr):
         DF[k] = F
         Hm[k] = (F * e) @ F.conj().T
     return eps, Hm, DF, Hm[:, :D, :D].mean(0)
+
+
+def density_dft(H, sigma, mu, beta, hartr=None):
+    """densityMatDFT of GreenFtn_w (src/GreenFtn.cpp:170-172, 197-215, 268-275, 311-319) by explicit n x n inversion
+    of every (k, iw_n), n < 2 N_freq: sum_n [G + G^H - G0 - G0^H] / beta + U f(e0) U^H, with Sigma on the HartrIndex
+    orbitals (its moment tail beyond N_freq), G0 the resolvent of H + m0 = U diag(e0) U^H (m0 added on the HartrIndex
+    block, as GreenFtn_w's static Hamiltonian does for a downfolded layout) and the +-100 cut-offs of the Fermi
+    factors.  H: (nk, n, n), sigma: (nfreq, D, D) ordinary arrays; returns (nk, n, n)."""
+    H = np.asarray(H, np.complex128)
+    sigma = np.asarray(sigma, np.complex128)
+    nk, n = H.shape[0], H.shape[1]
+    nf, D = sigma.shape[0], sigma.shape[1]
+    hp = np.arange(D) if hartr is None else np.asarray(hartr, int)
+    mom = moments(sigma, beta)
+    Hs = H.copy()
+    Hs[:, hp[:, None], hp[None, :]] += mom[0]
+    e0, U = np.linalg.eigh(Hs)
+    dens = np.zeros((nk, n, n), np.complex128)
+    eye = np.eye(n)
+    for f in range(2 * nf):
+        iw = 1j * np.pi * (2 * f + 1) / beta
+        sw = sigma[f] if f < nf else mom[0] + mom[1] / iw + mom[2] / iw ** 2 + mom[3] / iw ** 3
+        A = (iw + mu) * eye[None] - H
+        A[:, hp[:, None], hp[None, :]] -= sw
+        G = np.linalg.inv(A)
+        G0 = (U / (iw + mu - e0)[:, None, :]) @ U.conj().transpose(0, 2, 1)
+        dens += G + G.conj().transpose(0, 2, 1) - G0 - G0.conj().transpose(0, 2, 1)
+    x = beta * (e0 - mu)
+    fr = np.where(x > 100.0, 0.0, np.where(x < -100.0, 1.0, 1.0 / (1.0 + np.exp(np.clip(x, -100, 100)))))
+    return dens / beta + (U * fr[:, None, :]) @ U.conj().transpose(0, 2, 1)

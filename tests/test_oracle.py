@@ -216,3 +216,25 @@ def test_downfold_generalized_eigenproblem_and_orthonormal_frame(orc):
     assert np.abs(DF @ DF.conj().transpose(0, 2, 1) - np.eye(n)[None]).max() < 1e-12
     assert np.abs(np.linalg.eigvalsh(Hm) - eps).max() < 1e-12
     assert np.abs(himp - Hm[:, :4, :4].mean(0)).max() < 1e-14
+
+
+def test_density_dft_is_consistent_with_nummatrix_and_nele(orc):
+    # the correlated block of densityMatDFT averaged over k is GreenFtn_w's NumMatrix, its mean trace N(mu)
+    wl = models.t2g_p(k=3, nfreq=32, beta=10.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    d = orc.density_dft(H, wl.sigma, 0.2, wl.beta)
+    _, _, num = orc.greenftn_w(H, wl.sigma, 0.2, wl.beta, wl.ncl, wl.nh)
+    assert np.abs(d[:, :3, :3].mean(0) - num).max() < 1e-12
+    N = orc.nele(H, wl.sigma, 0.2, wl.beta, wl.ncl, wl.nh)
+    N = N[0] if isinstance(N, tuple) else N
+    assert abs(np.trace(d, axis1=1, axis2=2).real.mean() - N) < 1e-11
+    assert np.abs(d - d.conj().transpose(0, 2, 1)).max() < 1e-13
+
+
+def test_density_dft_without_self_energy_is_the_fermi_function_of_h(orc):
+    wl = models.t2g_p(k=2, nfreq=16, beta=8.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    d = orc.density_dft(H, np.zeros_like(wl.sigma), 0.1, wl.beta)
+    e, U = np.linalg.eigh(H)
+    f = (U / (1 + np.exp(wl.beta * (e - 0.1)))[:, None, :]) @ U.conj().transpose(0, 2, 1)
+    assert np.abs(d - f).max() < 1e-12
