@@ -8,6 +8,7 @@ profiles/ are taken with.
     python -m dmftpack_gb300.profile_case batched [--nprob 64 --mixed --graph --autotune]
     python -m dmftpack_gb300.profile_case adjoint [--k 16 --nfreq 2048]
     python -m dmftpack_gb300.profile_case downfold [--k 16 --repeat 2]
+    python -m dmftpack_gb300.profile_case density [--k 16 --nfreq 4096]
 
 gloc:  one GreenFtn_w pass of the seeded t2g+p model (12 x 12 H(k), k^3 grid, beta = 40).
 scgf2: `loops` SCGF2 loop iterations of a seeded d-spin-orbital impurity with Kanamori U = 4, J = 0.7,
@@ -19,6 +20,8 @@ adjoint: one GreenFtn_w pass, one reverse-mode (VJP) and one forward-mode (JVP) 
 downfold: the model Hamiltonian of the 56-orbital SOC model (20 correlated orbitals, k^3 grid) with a seeded
        Hermitian positive-definite overlap S(k) = I + B B^H / 56: the generalized eigenproblem, the downfolding and
        H_imp, device pointers, timed over repeats.
+density: densityMatDFT (the per-k density matrix, FP64) and, for comparison, one FP64 GreenFtn_w pass on the d+p
+       model of the dmft case.
 lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
@@ -112,6 +115,25 @@ def run_downfold(ctx, dev, a):
     return {"nk": wl.nk, "n": wl.n, "D": wl.D, "seconds": times[1:], "k_per_second": wl.nk / min(times[1:])}
 
 
+def run_density(ctx, dev, a):
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.dp28(k=a.k, nfreq=a.nfreq or 4096, ntau=a.ntau, beta=40.0)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, wl.D)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    out = {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq}
+    for name, fn in (("density_dft", lambda: ctx.densityMatDFT(lat, Hd, sig, 0.0)),
+                     ("greenftn_w_fp64", lambda: ctx.GreenFtn_w(lat, Hd, sig, 0.0))):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        out[name + "_seconds"] = time.perf_counter() - t0
+    return out
+
+
 def run_lattice(ctx, dev, a):
     import torch
     from dmftpack_gb300 import lib, models
@@ -172,7 +194,8 @@ def main():
     import torch
     from dmftpack_gb300 import lib, models
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint", "downfold"])
+    ap.add_argument("case", choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint", "downfold",
+                                        "density"])
     ap.add_argument("--nprob", type=int, default=64)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--autotune", action="store_true")
@@ -213,9 +236,9 @@ def main():
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case in ("dmft", "lattice", "batched", "adjoint", "downfold"):
+    if a.case in ("dmft", "lattice", "batched", "adjoint", "downfold", "density"):
         out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched,
-                    "adjoint": run_adjoint, "downfold": run_downfold}[a.case](ctx, dev, a))
+                    "adjoint": run_adjoint, "downfold": run_downfold, "density": run_density}[a.case](ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
         return
