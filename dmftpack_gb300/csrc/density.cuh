@@ -116,33 +116,32 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
             for (int a = 0; a < DP; a++) tG[a + c * DP] = s[a];
         }
         __syncwarp();
-        // one l per lane: Z1(:, l) = w_l G b_l, Z3(l, :) = w_l b_l^H G; X_PQ(:, l) += Z1(:, l) + Z3(l, :)^H
-        for (int l = c; l < m; l += W) {
+        // entries (a, l) spread over the lanes: Z1(a, l) = w_l (G b_l)(a), Z3(l, a) = w_l (b_l^H G)(a);
+        // X_PQ(a, l) += Z1(a, l) + conj(Z3(l, a))
+        for (int q = c; q < D * m; q += W) {
+            const int a = q % D, l = q / D;
             const C wv = wl[l];
             const C *bl = sB + (size_t)l * D;
-            for (int a = 0; a < D; a++) {
-                C z1 = cmk(0, 0), z3 = cmk(0, 0);
-                for (int b = 0; b < D; b++) {
-                    z1 = cfma(tG[a + b * DP], bl[b], z1);
-                    z3 = cfma(cconj(bl[b]), tG[b + a * DP], z3);
-                }
-                z1 = cmul(z1, wv);
-                z3 = cmul(z3, wv);
-                Z3[l + (size_t)a * m] = z3;
-                if (valid) Xpq[a + (size_t)l * D] = cadd(Xpq[a + (size_t)l * D], cadd(z1, cconj(z3)));
+            C z1 = cmk(0, 0), z3 = cmk(0, 0);
+            for (int b = 0; b < D; b++) {
+                z1 = cfma(tG[a + b * DP], bl[b], z1);
+                z3 = cfma(cconj(bl[b]), tG[b + a * DP], z3);
             }
+            z1 = cmul(z1, wv);
+            z3 = cmul(z3, wv);
+            Z3[l + (size_t)a * m] = z3;
+            if (valid) Xpq[q] = cadd(Xpq[q], cadd(z1, cconj(z3)));
         }
         __syncwarp();
-        // one column l' per lane: Y_QQ(:, l') += Z3 b_l' w_l'
-        for (int lp = c; lp < m && valid; lp += W) {
-            const C wv = wl[lp];
-            const C *bl = sB + (size_t)lp * D;
-            for (int l = 0; l < m; l++) {
+        // entries (l, l') spread over the lanes: Y_QQ(l, l') += (Z3 b_l')(l) w_l'
+        if (valid)
+            for (int q = c; q < m * m; q += W) {
+                const int l = q % m, lp = q / m;
+                const C *bl = sB + (size_t)lp * D;
                 C y = cmk(0, 0);
                 for (int b = 0; b < D; b++) y = cfma(Z3[l + (size_t)b * m], bl[b], y);
-                Yqq[l + (size_t)lp * m] = cfma(y, wv, Yqq[l + (size_t)lp * m]);
+                Yqq[q] = cfma(y, wl[lp], Yqq[q]);
             }
-        }
     }
     __syncwarp();
     if (c < DP) {

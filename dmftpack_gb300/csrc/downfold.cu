@@ -52,10 +52,11 @@ __device__ DfSmem df_smem(double2 *sm, int n) {
     return s;
 }
 
-// H, S: [nk][n][n] column-major (S == nullptr: identity); eps: [nk][n] ascending; Hm, DF: [nk][n][n]
+// H, S: [nk][n][n] column-major (S == nullptr: identity); eps: [nk][n] ascending; Hm, DF, EV: [nk][n][n]
 __global__ void __launch_bounds__(DF_THREADS) k_downfold(int n, int D, const int *__restrict__ hartr,
                                                          const double2 *__restrict__ Hk, const double2 *__restrict__ Sk,
-                                                         double *eps, double2 *Hm, double2 *DF, int *status) {
+                                                         double *eps, double2 *Hm, double2 *DF, double2 *EV,
+                                                         int *status) {
     extern __shared__ double2 dsm[];
     const int k = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
     const size_t nn = (size_t)n * n;
@@ -117,6 +118,8 @@ __global__ void __launch_bounds__(DF_THREADS) k_downfold(int n, int D, const int
             DG_AT(s.A, n, i, c) = cscale(v, 1.0 / DG_AT(s.L, n, i, i).x);
         }
     __syncthreads();
+    if (EV)
+        for (int q = tid; q < (int)nn; q += nt) EV[(size_t)k * nn + q] = s.A[q];
     // 5. P = V(hartr, :) into X (D x n, ld D); S_d = P P^H into U (D x D, ld D)
     double2 *P = s.X, *Sd = s.U;
     for (int q = tid; q < D * n; q += nt) P[q] = DG_AT(s.A, n, hartr[q % D], q / D);
@@ -220,7 +223,8 @@ __global__ void k_himp_avg(int nk, int n, int D, const double2 *__restrict__ Hm,
 }  // namespace
 
 extern "C" int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const int *hartr, const double *hk,
-                                const double *sk, double *eps, double *hmodel, double *df, double *himp, int flags) {
+                                const double *sk, double *eps, double *hmodel, double *df, double *evec, double *himp,
+                                int flags) {
     if (!ctx || nk < 1 || n < 1 || n > DF_NMAX || D < 1 || D > n || !hartr || !hk || !eps || !hmodel)
         return DMFTGPU_BADARG;
     for (int a = 0; a < D; a++) {
@@ -241,6 +245,8 @@ extern "C" int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const in
     if (st) return st;
     double2 *dF = (double2 *)dg_out(ctx, df, mb, flags, "io.df_df", &st);
     if (st) return st;
+    double2 *dV = (double2 *)dg_out(ctx, evec, mb, flags, "io.df_ev", &st);
+    if (st) return st;
     double2 *dI = (double2 *)dg_out(ctx, himp, (size_t)D * D * sizeof(double2), flags, "io.df_himp", &st);
     if (st) return st;
     int *dh = (int *)dg_buf(ctx, "df.hartr", D * sizeof(int));
@@ -249,7 +255,7 @@ extern "C" int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const in
     DG_TRY(dg_status_reset(ctx));
     const size_t sm = df_smem_bytes(n);
     DG_CUDA(cudaFuncSetAttribute(k_downfold, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_downfold<<<nk, DF_THREADS, sm, ctx->stream>>>(n, D, dh, dH, dS, dE, dM, dF, ctx->d_status);
+    k_downfold<<<nk, DF_THREADS, sm, ctx->stream>>>(n, D, dh, dH, dS, dE, dM, dF, dV, ctx->d_status);
     DG_LAUNCH(ctx, "k_downfold");
     if (dI) {
         k_himp_avg<<<dg_ceil_div(D * D, 128), 128, 0, ctx->stream>>>(nk, n, D, dM, dI);
@@ -258,6 +264,7 @@ extern "C" int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const in
     DG_TRY(dg_out_done(ctx, eps, dE, (size_t)nk * n * sizeof(double), flags));
     DG_TRY(dg_out_done(ctx, hmodel, dM, mb, flags));
     DG_TRY(dg_out_done(ctx, df, dF, mb, flags));
+    DG_TRY(dg_out_done(ctx, evec, dV, mb, flags));
     DG_TRY(dg_out_done(ctx, himp, dI, (size_t)D * D * sizeof(double2), flags));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));

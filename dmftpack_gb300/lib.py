@@ -31,7 +31,7 @@ DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
            "dmftgpu_synchronize", "dmftgpu_last_error", "dmftgpu_launch_count", "dmftgpu_timing",
            "dmftgpu_kernel_time", "dmftgpu_kmesh", "dmftgpu_hk",
-           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_density_dft", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
+           "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_density_dft", "dmftgpu_upfold", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc"]
@@ -96,9 +96,11 @@ def load(require_built=True):
     lib.dmftgpu_gloc_real.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                       _vp, _vp, C.c_int]
     lib.dmftgpu_density_dft.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_int]
+    lib.dmftgpu_upfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int, _ip, _vp, _vp,
+                                   _vp, C.c_int]
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
-    lib.dmftgpu_downfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_downfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
@@ -332,6 +334,30 @@ class Context:
         self._check("dmftgpu_density_dft", st)
         return out.result()
 
+    def upfolding_density(self, densityMatDFT, DF_CorrBase, KS_eigenVectors, kgrid, H_Rindex, S_overlap=None):
+        """upfolding_density over the full band window: returns (dual_DMR_dual, dual_DM_direct_DFTR,
+        direct_DMR_direct), each complex [nnz] at the rows of H_Rindex [nnz, 5] = (Rx, Ry, Rz, i0, j0).  The (nk, n, n)
+        inputs are numpy arrays or CUDA tensors; kgrid = (kx, ky, kz) of the k mesh."""
+        dev = _is_torch(densityMatDFT)
+        d, f, v = _Arr(densityMatDFT, dev), _Arr(DF_CorrBase, dev), _Arr(KS_eigenVectors, dev)
+        s = _Arr(S_overlap, dev) if S_overlap is not None else None
+        n = d.obj.shape[1]
+        ri = np.ascontiguousarray(H_Rindex, dtype=np.int32)
+        nnz = ri.shape[0]
+        if dev:
+            import torch
+            outs = [torch.empty(nnz, dtype=torch.complex128, device=d.obj.device) for _ in range(3)]
+            ptrs = [o.data_ptr() for o in outs]
+        else:
+            outs = [np.empty(nnz, np.complex128) for _ in range(3)]
+            ptrs = [o.ctypes.data for o in outs]
+        kx, ky, kz = kgrid
+        st = self.lib.dmftgpu_upfold(self.h, int(n), int(kx), int(ky), int(kz), _vp(d.ptr), _vp(f.ptr), _vp(v.ptr),
+                                     _vp(s.ptr) if s else None, int(nnz), ri.ctypes.data_as(_ip), _vp(ptrs[0]),
+                                     _vp(ptrs[1]), _vp(ptrs[2]), self._flags(dev))
+        self._check("dmftgpu_upfold", st)
+        return tuple(outs)
+
     def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
         """Reverse mode of G_loc = GreenFtn_w(...)[0]: returns (Sigma_bar[nfreq,D,D], mu_bar) for the cotangent
         Gbar[nfreq,D,D] (torch's complex-autograd convention: x_bar = J^H y_bar)."""
@@ -361,7 +387,7 @@ class Context:
     def downfolding_ftn(self, H_k, HartrIndex_inDFT, S_overlap=None, with_df=False):
         """Construct_Hk_Sk's generalized eigenproblem and downfolding_ftn over the full band window, per k: returns
         (KS_eigenEnergy[nk,n], H_k_inModelSpace[nk,n,n], impurity_site_Hamiltonian[D,D]) and, with with_df,
-        DF_CorrBase[nk,n,n] as a fourth item.  H_k, S_overlap: (nk, n, n) numpy arrays or CUDA tensors (S_overlap
+        DF_CorrBase[nk,n,n] and KS_eigenVectors_orthoBasis[nk,n,n] as fourth and fifth items.  H_k, S_overlap: (nk, n, n) numpy arrays or CUDA tensors (S_overlap
         None: orthogonal basis); HartrIndex_inDFT: the D correlated orbitals."""
         dev = _is_torch(H_k)
         h = _Arr(H_k, dev)
@@ -371,6 +397,7 @@ class Context:
         D = len(hartr)
         hm = _Arr.empty((nk, n, n), dev, like=h.obj)
         df = _Arr.empty((nk, n, n), dev, like=h.obj) if with_df else None
+        ev = _Arr.empty((nk, n, n), dev, like=h.obj) if with_df else None
         hi = _Arr.empty((D, D), dev, like=h.obj)
         if dev:
             import torch
@@ -381,10 +408,10 @@ class Context:
             ep = eps.ctypes.data
         st = self.lib.dmftgpu_downfold(self.h, int(nk), int(n), int(D), hartr.ctypes.data_as(_ip), _vp(h.ptr),
                                        _vp(s.ptr) if s else None, _vp(ep), _vp(hm.ptr), _vp(df.ptr) if df else None,
-                                       _vp(hi.ptr), self._flags(dev))
+                                       _vp(ev.ptr) if ev else None, _vp(hi.ptr), self._flags(dev))
         self._check("dmftgpu_downfold", st)
         out = (eps, hm.result(), hi.result())
-        return out + (df.result(),) if with_df else out
+        return out + (df.result(), ev.result()) if with_df else out
 
     def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False):
         dev = _is_torch(H_k)

@@ -20,8 +20,8 @@ adjoint: one GreenFtn_w pass, one reverse-mode (VJP) and one forward-mode (JVP) 
 downfold: the model Hamiltonian of the 56-orbital SOC model (20 correlated orbitals, k^3 grid) with a seeded
        Hermitian positive-definite overlap S(k) = I + B B^H / 56: the generalized eigenproblem, the downfolding and
        H_imp, device pointers, timed over repeats.
-density: densityMatDFT (the per-k density matrix, FP64) and, for comparison, one FP64 GreenFtn_w pass on the d+p
-       model of the dmft case.
+density: densityMatDFT (the per-k density matrix, FP64), one FP64 GreenFtn_w pass for comparison, and the
+       upfolding (k -> R sums onto the hopping table) of a k-resolved matrix, on the d+p model of the dmft case.
 lattice: one mu search (GreenFtn_w_adjust_mu) and one GreenFtn_w pass on the d+p model of the dmft case.
 dmft:  `iters` DMFT iterations with the SC2PT solver on the seeded 28-orbital d+p model (10 correlated
        spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, k^3 grid, beta = 40), H(k) rebuilt every iteration.
@@ -122,9 +122,11 @@ def run_density(ctx, dev, a):
     lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, wl.D)
     Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
     sig = torch.from_numpy(wl.sigma).to(dev)
-    out = {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq}
+    out = {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq, "nnz": len(wl.rindex)}
+    eye = torch.eye(wl.n, dtype=torch.complex128, device=dev).expand(wl.nk, wl.n, wl.n).contiguous()
     for name, fn in (("density_dft", lambda: ctx.densityMatDFT(lat, Hd, sig, 0.0)),
-                     ("greenftn_w_fp64", lambda: ctx.GreenFtn_w(lat, Hd, sig, 0.0))):
+                     ("greenftn_w_fp64", lambda: ctx.GreenFtn_w(lat, Hd, sig, 0.0)),
+                     ("upfolding_density", lambda: ctx.upfolding_density(Hd, eye, eye, wl.kgrid, wl.rindex))):
         fn()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -127,6 +127,18 @@ int dmftgpu_greenftn_w_batched(dmftgpu_ctx *ctx, int nprob, const dmftgpu_lattic
 int dmftgpu_gloc_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma_e, int nE,
                       double e0, double de, double eta, double mu, double *gloc, double *trace, int flags);
 
+/* upfolding_density over the full band window (src/upfolding.cpp:10-35, 38-91): per k, D_DFT = V (DF^H dens DF) V^H
+ * with dens[nk][n][n] the model-basis densityMatDFT, df[nk][n][n] DF_CorrBase and evec[nk][n][n] the KS eigenvectors
+ * in the DFT basis ((transformMatrix_k^H)^-1 KS_eigenVectors_orthoBasis; KS_eigenVectors_orthoBasis itself for the
+ * identity transform of the generalized-eigensolve path), then the k -> R sums
+ * DM(R)(i0, j0) = (1/nk) sum_k M_k(i0, j0) exp(+i k.a R) at the rindex[nnz][5] = (Rx, Ry, Rz, i0, j0) entries for
+ * M = S^-1 D_DFT S^-1 (dm_dual_dual, DM_DFT_DMFT.HWR), S^-1 D_DFT (dm_dual_direct) and D_DFT (dm_direct); sk NULL:
+ * S = I.  The k mesh is TightBinding's kx x ky x kz grid; outputs nnz complex each (any may be NULL); rindex host.
+ * n <= 64, kx, ky, kz <= 256.  FP64. */
+int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens, const double *df,
+                   const double *evec, const double *sk, int nnz, const int *rindex, double *dm_dual_dual,
+                   double *dm_dual_direct, double *dm_direct, int flags);
+
 /* GreenFtn_w's per-k density matrix in the model basis, densityMatDFT (src/GreenFtn.cpp:170-172, 268-275,
  * 311-319): dens[nk][n][n] = (1/beta) sum_{n < 2 nfreq} [G + G^H - G0 - G0^H](k, iw_n) + U f(e0) U^H, with G the full
  * n x n lattice Green function (Sigma on the HartrIndex orbitals, its moment tail beyond nfreq), G0 the resolvent
@@ -153,11 +165,12 @@ int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double 
  * (src/downfolding.cpp:85-104).  hk, sk: [nk][n][n] (sk NULL: identity overlap), hartr[D] the correlated rows
  * (HartrIndex_inDFT, distinct, always a host pointer), n <= 56.  Outputs: eps[nk][n] ascending band energies; hmodel[nk][n][n] =
  * DF diag(eps) DF^H with rows 0..D-1 the Loewdin-orthonormalised projected correlated orbitals; optional
- * df[nk][n][n] (DF_CorrBase) and himp[D][D] = (1/nk) sum_k hmodel[k][0:D][0:D].  The ligand rows D..n-1 of DF
+ * df[nk][n][n] (DF_CorrBase), evec[nk][n][n] (KS_eigenVectors_orthoBasis: the S-orthonormal eigenvectors, column l
+ * for eps[l]) and himp[D][D] = (1/nk) sum_k hmodel[k][0:D][0:D].  The ligand rows D..n-1 of DF
  * are an orthonormal complement whose in-subspace rotation differs from Eigen's (see the kernel's header);
  * FP64.  DMFTGPU_SINGULAR when S is not positive definite or the projected block is rank deficient. */
 int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const int *hartr, const double *hk, const double *sk,
-                     double *eps, double *hmodel, double *df, double *himp, int flags);
+                     double *eps, double *hmodel, double *df, double *evec, double *himp, int flags);
 
 /* Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119, declared src/TB.h:45-47):
  * delta[nfreq][dim][dim] = (iw+mu) I - himp[orb] - sigma[orb] - (gw[orb])^-1, orb[dim] indexes D. */

@@ -539,3 +539,25 @@ def density_dft(H, sigma, mu, beta, hartr=None):
     x = beta * (e0 - mu)
     fr = np.where(x > 100.0, 0.0, np.where(x < -100.0, 1.0, 1.0 / (1.0 + np.exp(np.clip(x, -100, 100)))))
     return dens / beta + (U * fr[:, None, :]) @ U.conj().transpose(0, 2, 1)
+
+
+def upfold(dens, DF, V, S, kgrid, rindex):
+    """upfolding_density over the full band window (src/upfolding.cpp:10-35, 38-91): per k, D_DFT = V (DF^H D DF) V^H,
+    then (1/N_k) sum_k M_k(i0, j0) exp(+i k.a R) at the rows (Rx, Ry, Rz, i0, j0) of rindex for M = S^-1 D_DFT S^-1,
+    S^-1 D_DFT and D_DFT, with the k mesh of TightBinding (kmesh above) and a = pi.  Arrays (nk, n, n) ordinary;
+    S None: identity.  Returns the three complex [nnz] vectors."""
+    dens, DF, V = (np.asarray(x, np.complex128) for x in (dens, DF, V))
+    X = DF.conj().transpose(0, 2, 1) @ dens @ DF
+    Dd = V @ X @ V.conj().transpose(0, 2, 1)
+    if S is None:
+        Mdd = Md = Dd
+    else:
+        Si = np.linalg.inv(np.asarray(S, np.complex128))
+        Mdd = Si @ Dd @ Si
+        Md = Si @ Dd
+    km = kmesh(*kgrid)
+    ri = np.asarray(rindex)
+    ph = np.exp(1j * np.pi * (km @ ri[:, :3].T.astype(float)))  # (nk, nnz): a = pi
+    nk = km.shape[0]
+    i0, j0 = ri[:, 3], ri[:, 4]
+    return tuple((M[:, i0, j0] * ph).sum(0) / nk for M in (Mdd, Md, Dd))

@@ -56,8 +56,13 @@ def test_downfold_matches_oracle(ctx, orc, case):
     H = _model_hk(orc, wl)
     S = _overlap(np.random.default_rng(7), H.shape[0], wl.n) if overlap else None
     eps, Hm, DF, himp = orc.downfold(H, S, hartr)
-    eps_g, hm_g, hi_g, df_g = ctx.downfolding_ftn(H, hartr, S, with_df=True)
+    eps_g, hm_g, hi_g, df_g, ev_g = ctx.downfolding_ftn(H, hartr, S, with_df=True)
     _check(eps_g, hm_g, hi_g, df_g, eps, Hm, himp, len(hartr))
+    # the eigenvectors solve H v = e S v with V^H S V = I
+    Sm = np.eye(wl.n)[None] if S is None else S
+    sc = max(1.0, np.abs(eps).max())
+    assert np.abs(H @ ev_g - (Sm @ ev_g) * eps_g[:, None, :]).max() < TOL * sc
+    assert np.abs(ev_g.conj().transpose(0, 2, 1) @ Sm @ ev_g - np.eye(wl.n)[None]).max() < 1e-11
     # the correlated rows of DF are fixed up to the eigenvector phases, which cancel in DF_P diag(e) DF_P^H
     D = len(hartr)
     assert np.abs(hm_g[:, :D, :D] - (df_g[:, :D] * eps_g[:, None, :]) @ df_g[:, :D].conj().transpose(0, 2, 1)).max() \

@@ -238,3 +238,13 @@ def test_density_dft_without_self_energy_is_the_fermi_function_of_h(orc):
     e, U = np.linalg.eigh(H)
     f = (U / (1 + np.exp(wl.beta * (e - 0.1)))[:, None, :]) @ U.conj().transpose(0, 2, 1)
     assert np.abs(d - f).max() < 1e-12
+
+
+def test_upfold_inverts_the_hk_fourier_sum(orc):
+    # with DF = V = I and S = I the k -> R sum of H(k) returns the hopping table (k grid wider than the R range)
+    wl = models.t2g_p(k=6, nfreq=8)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    eye = np.broadcast_to(np.eye(wl.n, dtype=np.complex128), H.shape)
+    dd, d, direct = orc.upfold(H, eye, eye, None, wl.kgrid, wl.rindex)
+    for x in (dd, d, direct):
+        assert np.abs(x - wl.hr).max() < 1e-12
