@@ -552,12 +552,17 @@ __global__ void k_schur_reduce(int nchunk, int nf2, int DD, int mode, const doub
 int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
               double *tr, double *dtr, bool mixed) {
     const SInst *in = pick_schur(P.D);
-    SchurKernel kern = in->get(mode, mixed);
-    const int m = P.n - P.D, NG = 128 / in->W, DD = P.D * P.D;
+    // BLOCK passes of correlated blocks up to 3 x 3: one thread per frequency (k_schur_tpi)
+    const bool tpi = mode == dg::S_BLOCK && P.D <= 3;
+    SchurKernel kern = tpi ? dg::schur_tpi_kernel(P.D, mixed) : in->get(mode, mixed);
+    const int m = P.n - P.D, NG = tpi ? 128 : 128 / in->W, DD = P.D * P.D;
     const int nf2 = (mode & dg::S_REAL) ? P.Nf : 2 * P.Nf;  // the real axis has exactly the caller's points
+    auto smem_of = [&](int kc_) {
+        return tpi ? dg::schur_tpi_smem(kc_, P.D, m) : dg::schur_smem(in->DP, in->W, mode, kc_, P.D, m, P.n);
+    };
     int kc = 16;
-    while (kc > 1 && dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n) > 96 * 1024) kc /= 2;
-    const size_t smem = dg::schur_smem(in->DP, in->W, mode, kc, P.D, m, P.n);
+    while (kc > 1 && smem_of(kc) > 96 * 1024) kc /= 2;
+    const size_t smem = smem_of(kc);
     if (smem > 200 * 1024) return dg_fail(ctx, DMFTGPU_BADARG, "lattice: correlated block too large");
     DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // k chunks: enough CTAs for `cps` per SM (8 unless tuned), at least 64 k points per chunk
@@ -570,7 +575,7 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
         *kchunk_out = kch;
         return dg_ceil_div(P.nk, kch);
     };
-    const std::string key = "schur/" + std::to_string(in->DP) + "/" + std::to_string(mode) + "/" +
+    const std::string key = std::string(tpi ? "schur_tpi/" : "schur/") + std::to_string(in->DP) + "/" + std::to_string(mode) + "/" +
                             std::to_string((int)mixed) + "/" + std::to_string(P.nk) + "/" + std::to_string(nf2);
     int kch_max;
     const int nchunk_max = chunks(16, &kch_max);

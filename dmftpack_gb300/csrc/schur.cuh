@@ -298,6 +298,154 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     if ((MODE & S_TRACE) && c == 0) g.ptr[(size_t)chunk * g.nf2 + f] = cmk(acct1, acct2);
 }
 
+// In-place inverse of a D x D matrix held by one thread (D <= 3): Gauss-Jordan with partial pivoting whose row
+// swaps are predicated moves between compile-time indices (no local memory), undone as column swaps at the end.
+template <class Ops, int N>
+__device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
+    typedef typename Ops::C C;
+    typedef typename Ops::M M;
+    bool sing = false;
+    int perm[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        int p = j;
+        M best = Ops::mag2(a[j][j]);
+#pragma unroll
+        for (int r = j + 1; r < N; r++) {
+            const M v = Ops::mag2(a[r][j]);
+            if (v > best) {
+                best = v;
+                p = r;
+            }
+        }
+        perm[j] = p;
+#pragma unroll
+        for (int r = j + 1; r < N; r++) {
+            const bool sw = (p == r);
+#pragma unroll
+            for (int c = 0; c < N; c++) {
+                const C x = a[j][c], y = a[r][c];
+                a[j][c] = sw ? y : x;
+                a[r][c] = sw ? x : y;
+            }
+        }
+        sing |= !(best > M(0));
+        const C piv = Ops::rcp(a[j][j]);
+        a[j][j] = Ops::one();
+#pragma unroll
+        for (int c = 0; c < N; c++) a[j][c] = Ops::mul(a[j][c], piv);
+#pragma unroll
+        for (int r = 0; r < N; r++)
+            if (r != j) {
+                const C t = a[r][j];
+                a[r][j] = Ops::zero();
+#pragma unroll
+                for (int c = 0; c < N; c++) a[r][c] = Ops::fms(t, a[j][c], a[r][c]);
+            }
+    }
+#pragma unroll
+    for (int j = N - 1; j >= 0; j--)
+#pragma unroll
+        for (int c2 = j + 1; c2 < N; c2++) {
+            const bool sw = (perm[j] == c2);
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+                const C x = a[r][j], y = a[r][c2];
+                a[r][j] = sw ? y : x;
+                a[r][c2] = sw ? x : y;
+            }
+        }
+    return sing;
+}
+
+// BLOCK mode (G_loc and GwHF) for correlated blocks of D <= 3: one thread per Matsubara frequency, the whole
+// D x D S(z) and S0(z) of that thread's (k, iw) in its registers, inverted by thread_inverse.  A lane-group
+// k_schur at these widths leaves lanes idle (D < W) and spends its issue slots on the group's pivot broadcasts;
+// here every lane does useful work and nothing is exchanged.  Shared-memory staging as k_schur (schur_stage).
+template <class Ops, int D>
+__global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
+    typedef typename Ops::C C;
+    extern __shared__ double2 sm[];
+    constexpr int DD = D * D;
+    const int m = g.m;
+    C *st = reinterpret_cast<C *>(sm);
+    C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m, *sM0 = sH + (size_t)g.kc * DD;
+    const int f_raw = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool fvalid = f_raw < g.nf2;
+    const int f = fvalid ? f_raw : g.nf2 - 1;
+    const int chunk = blockIdx.y;
+    const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
+    for (int t = threadIdx.x; t < DD; t += blockDim.x) sM0[t] = Ops::from(g.m0[t]);
+    const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
+    const C zc = Ops::from(cmk(g.mu, w)), iwc = Ops::from(cmk(0.0, w));
+    C sg[D][D], aG[D][D], aG0[D][D];
+#pragma unroll
+    for (int a = 0; a < D; a++)
+#pragma unroll
+        for (int b = 0; b < D; b++) {
+            sg[a][b] = Ops::from(g.sig[(size_t)f * DD + a + b * D]);
+            aG[a][b] = aG0[a][b] = Ops::zero();
+        }
+    bool sing = false;
+    for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
+        const int nkc = min(g.kc, kend - k0);
+        __syncthreads();
+        schur_stage<Ops>(g, k0, nkc, st, false, false);
+        __syncthreads();
+        for (int kk = 0; kk < nkc; kk++) {
+            const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
+            C s[D][D];
+#pragma unroll
+            for (int a = 0; a < D; a++)
+#pragma unroll
+                for (int b = 0; b < D; b++) {
+                    s[a][b] = Ops::sub(hp[a + b * D], sg[a][b]);
+                    if (a == b) s[a][b] = Ops::add(s[a][b], zc);
+                }
+            for (int l = 0; l < m; l++) {
+                const C wl = Ops::rcp(Ops::add(es[l], iwc));
+                C q[D];
+#pragma unroll
+                for (int b = 0; b < D; b++) q[b] = Ops::mulc(wl, bs[l * D + b]);
+#pragma unroll
+                for (int a = 0; a < D; a++) {
+                    const C ba = bs[l * D + a];
+#pragma unroll
+                    for (int b = 0; b < D; b++) s[a][b] = Ops::fms(ba, q[b], s[a][b]);
+                }
+            }
+            C s0[D][D];
+#pragma unroll
+            for (int a = 0; a < D; a++)
+#pragma unroll
+                for (int b = 0; b < D; b++) s0[a][b] = Ops::sub(Ops::add(s[a][b], sg[a][b]), sM0[a + b * D]);
+            sing |= thread_inverse<Ops, D>(s);
+            sing |= thread_inverse<Ops, D>(s0);
+#pragma unroll
+            for (int a = 0; a < D; a++)
+#pragma unroll
+                for (int b = 0; b < D; b++) {
+                    aG[a][b] = Ops::add(aG[a][b], s[a][b]);
+                    aG0[a][b] = Ops::add(aG0[a][b], s0[a][b]);
+                }
+        }
+    }
+    if (sing && fvalid) dg_flag(g.status, DG_SINGULAR);
+    if (!fvalid) return;
+    const size_t o = ((size_t)chunk * g.nf2 + f) * DD;
+#pragma unroll
+    for (int a = 0; a < D; a++)
+#pragma unroll
+        for (int b = 0; b < D; b++) {
+            g.pblk[o + a + b * D] = Ops::to(aG[a][b]);
+            g.pblk0[o + a + b * D] = Ops::to(aG0[a][b]);
+        }
+}
+
+inline size_t schur_tpi_smem(int kc, int D, int m) {
+    return ((size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D) * 16;
+}
+
 // shared-memory bytes of one k_schur launch
 inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m, int n) {
     const int NG = 128 / W;
@@ -326,6 +474,9 @@ template <int DP, int W>
 SchurKernel schur_pick(int mode, bool mixed) {
     return mixed ? schur_pick_ops<OpsF, DP, W>(mode) : schur_pick_ops<OpsD, DP, W>(mode);
 }
+
+// the thread-per-frequency BLOCK kernels, D = 1 .. 3 (schur_tpi.cu)
+SchurKernel schur_tpi_kernel(int D, bool mixed);
 
 #define DG_SCHUR_INST(DP, W) \
     SchurKernel schur_kernel_##DP(int mode, bool mixed) { return schur_pick<DP, W>(mode, mixed); }
