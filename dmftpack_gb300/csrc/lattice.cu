@@ -199,6 +199,100 @@ __global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, co
     if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
 }
 
+// The same two decompositions with one warp per k point (warp_heig), four k points per CTA: for the matrix sizes
+// up to 32 a block-wide Jacobi spends most of its time in block barriers with idle threads.  Per-warp shared
+// region: three n x n complex matrices, eigenvalues [64], order [64], rotations [33].
+constexpr int EIG_WPB = 4;
+inline size_t warp_eig_bytes(int n) {
+    const size_t b = (size_t)3 * n * n * sizeof(double2) + EIG_NMAX * sizeof(double) + EIG_NMAX * sizeof(int) + 16 +
+                     (EIG_NMAX / 2 + 1) * sizeof(DgRot);
+    return (b + 15) & ~(size_t)15;
+}
+__device__ inline EigSmem warp_eig_smem(double2 *sm, int n) {
+    char *base = reinterpret_cast<char *>(sm) + (threadIdx.x >> 5) * warp_eig_bytes(n);
+    EigSmem e;
+    const size_t nn = (size_t)n * n;
+    e.A0 = reinterpret_cast<double2 *>(base);
+    e.A = e.A0 + nn;
+    e.U = e.A + nn;
+    e.w = (double *)(e.U + nn);
+    e.ord = (int *)(e.w + EIG_NMAX);
+    e.rot = (DgRot *)(((size_t)(e.ord + EIG_NMAX) + 15) & ~(size_t)15);
+    e.red = nullptr;
+    return e;
+}
+
+__global__ void __launch_bounds__(32 * EIG_WPB) k_static_eig_warp(int nk, int n, int D, int nh, int mask,
+                                                                  const double2 *__restrict__ H,
+                                                                  const double2 *__restrict__ m0, double *eps,
+                                                                  double2 *UP, double2 *Uf, int *status) {
+    extern __shared__ double2 esm[];
+    const int lane = threadIdx.x & 31, k = blockIdx.x * EIG_WPB + (threadIdx.x >> 5);
+    if (k >= nk) return;  // whole warps only
+    const size_t nn = (size_t)n * n;
+    EigSmem e = warp_eig_smem(esm, n);
+    const double2 *Hk = H + (size_t)k * nn;
+    for (int q = lane; q < (int)nn; q += 32) {
+        const int a = q % n, b = q / n;
+        double2 v = Hk[q];
+        if (a < D && b < D && (!mask || a / nh == b / nh)) v = cadd(v, m0[a + b * D]);
+        e.A0[q] = v;
+    }
+    __syncwarp();
+    const int st = warp_heig(n, e.A0, e.A, e.U, e.w, e.ord, e.rot);
+    for (int l = lane; l < n; l += 32) eps[(size_t)k * n + l] = e.w[l];
+    for (int q = lane; q < n * D; q += 32) {
+        const int l = q / D, a = q % D;
+        UP[((size_t)k * n + l) * D + a] = DG_AT(e.U, n, a, l);
+    }
+    if (Uf)
+        for (int q = lane; q < (int)nn; q += 32) Uf[(size_t)k * nn + q] = e.U[q];
+    if (st && lane == 0) dg_flag(status, DG_NONCONV);
+}
+
+__global__ void __launch_bounds__(32 * EIG_WPB) k_schur_prep_warp(int nk, int n, int D, const double2 *__restrict__ H,
+                                                                  double *epsQ, double2 *B, double2 *Vq, int *status) {
+    extern __shared__ double2 esm[];
+    const int lane = threadIdx.x & 31, k = blockIdx.x * EIG_WPB + (threadIdx.x >> 5), m = n - D;
+    if (k >= nk) return;  // whole warps only
+    EigSmem e = warp_eig_smem(esm, m);
+    const double2 *Hk = H + (size_t)k * n * n;
+    for (int q = lane; q < m * m; q += 32) {
+        const int i = q % m, j = q / m;
+        e.A0[q] = Hk[(D + i) + (size_t)(D + j) * n];
+    }
+    __syncwarp();
+    const int st = warp_heig(m, e.A0, e.A, e.U, e.w, e.ord, e.rot);
+    for (int l = lane; l < m; l += 32) epsQ[(size_t)k * m + l] = e.w[l];
+    for (int q = lane; q < m * D; q += 32) {
+        const int l = q / D, a = q % D;
+        double2 s = cmk(0, 0);
+        for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(e.U, m, j, l), s);
+        B[((size_t)k * m + l) * D + a] = s;
+    }
+    if (Vq)
+        for (int q = lane; q < m * m; q += 32) Vq[(size_t)k * m * m + q] = e.U[q];
+    if (st && lane == 0) dg_flag(status, DG_NONCONV);
+}
+
+// the Schur data of every k point (H_QQ = V diag(e) V^H, b_l = H_PQ V(:, l)), by warps for m <= 32
+int launch_schur_prep(dmftgpu_ctx *ctx, cudaStream_t s, int nk, int n, int D, const double2 *H, double *epsQ,
+                      double2 *B, double2 *Vq) {
+    const int m = n - D;
+    if (m <= 32) {
+        const size_t sm = EIG_WPB * warp_eig_bytes(m);
+        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_schur_prep_warp<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, s>>>(nk, n, D, H, epsQ, B, Vq, ctx->d_status);
+        DG_LAUNCH(ctx, "k_schur_prep_warp");
+    } else {
+        const size_t sm = eig_blk_smem(m);
+        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_schur_prep_blk<<<nk, EIG_THREADS, sm, s>>>(n, D, H, epsQ, B, Vq, ctx->d_status);
+        DG_LAUNCH(ctx, "k_schur_prep_blk");
+    }
+    return DMFTGPU_OK;
+}
+
 // Fermi parts: occ_k = P U f U^H P (with the +-100 cut-offs of src/GreenFtn.cpp:314-316) for NumMatrix,
 // and sum_l f, beta f (1-f) for N(mu) (src/GreenFtn.cpp:616-620, no cut-off there)
 __global__ void k_fermi(int nk, int n, int D, double beta, double mu, const double *__restrict__ eps,
@@ -388,12 +482,7 @@ int prepare_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, 
     P.B = (double2 *)dg_buf(ctx, "lat.B", (size_t)nk * (m + 1) * D * sizeof(double2));
     if (!P.m0 || !P.epsQ || !P.B) return DMFTGPU_NOMEM;
     DG_CUDA(cudaMemsetAsync(P.m0, 0, (size_t)D * D * sizeof(double2), ctx->stream));
-    if (m > 0) {
-        const size_t sm = eig_blk_smem(m);
-        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_schur_prep_blk<<<nk, EIG_THREADS, sm, ctx->stream>>>(n, D, P.H, P.epsQ, P.B, nullptr, ctx->d_status);
-        DG_LAUNCH(ctx, "k_schur_prep_blk");
-    }
+    if (m > 0) DG_TRY(launch_schur_prep(ctx, ctx->stream, nk, n, D, P.H, P.epsQ, P.B, nullptr));
     return DMFTGPU_OK;
 }
 
@@ -461,21 +550,22 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     // the Schur data (eigen-decomposition of H_QQ) is needed first, by k_schur, on the main stream; the
     // static eigen-decomposition of H + m0 feeds only the Fermi terms, so it runs on the side stream
     // (FP64-pipe work) while the lattice kernel (FP32 pipe in the mixed form) proceeds
-    if (m > 0) {
-        const size_t sm = eig_blk_smem(m);
-        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_schur_prep_blk<<<nk, EIG_THREADS, sm, s>>>(n, D, P.H, P.epsQ, P.B, P.Vq, ctx->d_status);
-        DG_LAUNCH(ctx, "k_schur_prep_blk");
-    }
+    if (m > 0) DG_TRY(launch_schur_prep(ctx, s, nk, n, D, P.H, P.epsQ, P.B, P.Vq));
     DG_CUDA(cudaEventRecord(ctx->ev_fork, s));
     DG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-    {
+    if (n <= 32) {
+        const size_t sm = EIG_WPB * warp_eig_bytes(n);
+        DG_CUDA(cudaFuncSetAttribute(k_static_eig_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_static_eig_warp<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, ctx->side>>>(nk, n, D, P.nh, mask, P.H, P.m0,
+                                                                                     P.eps, P.UP, P.Uf, ctx->d_status);
+        DG_LAUNCH(ctx, "k_static_eig_warp");
+    } else {
         const size_t sm = eig_blk_smem(n);
         DG_CUDA(cudaFuncSetAttribute(k_static_eig_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         k_static_eig_blk<<<nk, EIG_THREADS, sm, ctx->side>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, P.Uf,
                                                              ctx->d_status);
+        DG_LAUNCH(ctx, "k_static_eig_blk");
     }
-    DG_LAUNCH(ctx, "k_static_eig_blk");
     DG_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
     P.static_ready = ctx->ev_join;
     return DMFTGPU_OK;
