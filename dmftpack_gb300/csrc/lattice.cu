@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, co
 // up to 32 a block-wide Jacobi spends most of its time in block barriers with idle threads.  Per-warp shared
 // region: three n x n complex matrices, eigenvalues [64], order [64], rotations [33].
 constexpr int EIG_WPB = 4;
-inline size_t warp_eig_bytes(int n) {
+__host__ __device__ inline size_t warp_eig_bytes(int n) {
     const size_t b = (size_t)3 * n * n * sizeof(double2) + EIG_NMAX * sizeof(double) + EIG_NMAX * sizeof(int) + 16 +
                      (EIG_NMAX / 2 + 1) * sizeof(DgRot);
     return (b + 15) & ~(size_t)15;
