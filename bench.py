@@ -393,11 +393,27 @@ def run_ours(args, rank, world, local_rank):
     #   schur:    8 m D^2 (Schur sum over the m = n - D ligand poles) + 2 x 8 D^3 (G and G0 blocks)
     m_ = wl.n - wl.D
     per_unit = 8.0 * wl.n ** 3 if explicit else 8.0 * m_ * wl.D ** 2 + 16.0 * wl.D ** 3
+    # algorithmic DRAM bytes of one pass: H(k) (or its Schur data) once, Sigma and the 2 D x D outputs per point
+    #   (complex 16 B: b_l and H_PP per k, Sigma over the 2 N_freq points, G and G0 out; real 8 B: e_l per k)
+    alg_bytes = (wl.nk * (16 * (wl.n * wl.n if explicit else m_ * wl.D + wl.D * wl.D) + (0 if explicit else 8 * m_))
+                 + 16 * 3 * 2 * wl.nfreq * wl.D * wl.D)
     # the mixed kernel runs in double-float on the FP32 pipe: its roof is the FP32 peak
     peak = fp64_peak_tflops(torch, dev) if not mixed else fp32_peak_tflops(torch, dev)
     flops = per_unit * inv_per_step
     k_avg = (k_ms / 1e3) / max(k_cnt, 1)
     achieved = flops / k_avg / 1e12
+    # DRAM bytes of one launch of the dominant kernel, from the ncu capture of this exact workload (or null)
+    traffic, traffic_kernel = None, kname
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "traffic.json")) as fh:
+            measured = json.load(fh)
+        tname = ("k_schur_tpi<%s, %d>" % ("OpsF" if mixed else "OpsD", wl.D)) if (not explicit and wl.D <= 3) else None
+        rec = measured.get(tname) if tname else None
+        if rec and rec["workload"] == {"n": wl.n, "D": wl.D, "nk": wl.nk, "nfreq": wl.nfreq,
+                                       "precision": args.precision}:
+            traffic, traffic_kernel = rec["dram_bytes_per_launch"], tname
+    except (OSError, ValueError, KeyError):
+        pass
     cpu_v, cpu_d = cpu_rate(wl, Hd.cpu().numpy(), seconds=12.0)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
@@ -410,8 +426,9 @@ def run_ours(args, rank, world, local_rank):
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "fp64" if not mixed else "fp32", "achieved": achieved,
-                        "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                        "kernel": kname, "kernel_ms_avg": k_avg * 1e3, "flops_per_unit": per_unit,
+                        "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                        "algorithmic_bytes": alg_bytes, "kernel": traffic_kernel, "kernel_ms_avg": k_avg * 1e3, "flops_per_unit": per_unit,
                         "peak_source": ("cuBLAS DGEMM 4096^3" if not mixed else "cuBLAS SGEMM 8192^3 (no TF32)")
                                        + " measured in this run (not in MEASURED_PEAKS.json); the flops are "
                                          "double-float operations counted as one flop each" * bool(mixed),
