@@ -172,6 +172,138 @@ __device__ inline int block_heig(int n, const double2 *A0, double2 *a, double2 *
     return st;
 }
 
+// block_heig for one warp (n <= 64): the same rotations, order and stopping rule, synchronised with __syncwarp
+// (a butterfly reduction of the off-diagonal mass, the stopping decision taken from lane 0), so several small
+// matrices share a thread block without block-wide barriers.  All 32 lanes call it; a, u: n*n shared (this warp's),
+// w: n doubles, order: n ints, rot: n/2+1 DgRot, all this warp's.  Returns DG_OK or DG_NONCONV (warp-uniform).
+__device__ inline int warp_heig(int n, const double2 *A0, double2 *a, double2 *u, double *w, int *order, DgRot *rot) {
+    const int lane = threadIdx.x & 31;
+    for (int e = lane; e < n * n; e += 32) {
+        const int i = e % n, j = e / n;
+        double2 v;
+        if (i > j) v = DG_AT(A0, n, i, j);
+        else if (i < j) v = cconj(DG_AT(A0, n, j, i));
+        else v = cmk(DG_AT(A0, n, i, i).x, 0.0);
+        a[e] = v;
+        u[e] = cmk(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncwarp();
+    const int m = n + (n & 1), half = m / 2;
+    int st = DG_NONCONV;
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0, tot = 0;
+        for (int e = lane; e < n * n; e += 32) {
+            const double v = cabs2(a[e]);
+            tot += v;
+            if (e % n != e / n) off += v;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        }
+        const int conv = __shfl_sync(0xffffffffu, (int)(off == 0.0 || off <= 1e-28 * tot), 0);
+        if (conv) {
+            st = DG_OK;
+            break;
+        }
+        for (int r = 0; r < m - 1; r++) {
+            if (lane < half) {
+                int p, q;
+                if (lane == 0) {
+                    p = r;
+                    q = m - 1;
+                } else {
+                    p = (r + lane) % (m - 1);
+                    q = (r - lane + (m - 1)) % (m - 1);
+                }
+                if (p > q) {
+                    const int t = p;
+                    p = q;
+                    q = t;
+                }
+                DgRot R;
+                R.p = p;
+                R.q = q;
+                R.on = 0;
+                R.c = 1.0;
+                R.s = 0.0;
+                R.ph = cmk(1, 0);
+                if (q < n) {
+                    const double2 apq = DG_AT(a, n, p, q);
+                    const double rr = sqrt(cabs2(apq));
+                    if (rr != 0.0) {
+                        const double app = DG_AT(a, n, p, p).x, aqq = DG_AT(a, n, q, q).x;
+                        const double theta = (aqq - app) / (2.0 * rr);
+                        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                        R.c = 1.0 / sqrt(t * t + 1.0);
+                        R.s = t * R.c;
+                        R.ph = cmk(apq.x / rr, apq.y / rr);
+                        R.on = 1;
+                    }
+                }
+                rot[lane] = R;
+            }
+            __syncwarp();
+            for (int x = lane; x < half * n; x += 32) {
+                const DgRot R = rot[x / n];
+                if (!R.on) continue;
+                const int k = x % n;
+                const double2 phc = cconj(R.ph);
+                const double2 akp = DG_AT(a, n, k, R.p), akq = DG_AT(a, n, k, R.q);
+                DG_AT(a, n, k, R.p) = csub(cscale(akp, R.c), cscale(cmul(phc, akq), R.s));
+                DG_AT(a, n, k, R.q) = cadd(cscale(akp, R.s), cscale(cmul(phc, akq), R.c));
+                const double2 ukp = DG_AT(u, n, k, R.p), ukq = DG_AT(u, n, k, R.q);
+                DG_AT(u, n, k, R.p) = csub(cscale(ukp, R.c), cscale(cmul(phc, ukq), R.s));
+                DG_AT(u, n, k, R.q) = cadd(cscale(ukp, R.s), cscale(cmul(phc, ukq), R.c));
+            }
+            __syncwarp();
+            for (int x = lane; x < half * n; x += 32) {
+                const DgRot R = rot[x / n];
+                if (!R.on) continue;
+                const int k = x % n;
+                const double2 apk = DG_AT(a, n, R.p, k), aqk = DG_AT(a, n, R.q, k);
+                DG_AT(a, n, R.p, k) = csub(cscale(apk, R.c), cscale(cmul(R.ph, aqk), R.s));
+                DG_AT(a, n, R.q, k) = cadd(cscale(apk, R.s), cscale(cmul(R.ph, aqk), R.c));
+            }
+            __syncwarp();
+            if (lane < half) {
+                const DgRot R = rot[lane];
+                if (R.on) {
+                    DG_AT(a, n, R.p, R.q) = cmk(0, 0);
+                    DG_AT(a, n, R.q, R.p) = cmk(0, 0);
+                    DG_AT(a, n, R.p, R.p).y = 0.0;
+                    DG_AT(a, n, R.q, R.q).y = 0.0;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (lane == 0) {
+        for (int i = 0; i < n; i++) order[i] = i;
+        for (int i = 1; i < n; i++) {
+            const int v = order[i];
+            const double key = DG_AT(a, n, v, v).x;
+            int j = i - 1;
+            while (j >= 0 && DG_AT(a, n, order[j], order[j]).x > key) {
+                order[j + 1] = order[j];
+                j--;
+            }
+            order[j + 1] = v;
+        }
+        for (int i = 0; i < n; i++) w[i] = DG_AT(a, n, order[i], order[i]).x;
+    }
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) a[e] = u[e];
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {
+        const int k = e % n, i = e / n;
+        DG_AT(u, n, k, i) = DG_AT(a, n, k, order[i]);
+    }
+    __syncwarp();
+    return st;
+}
+
 // C = A B (n x n, all shared or global, C distinct from A and B); all threads call it; ends with a barrier
 __device__ inline void block_matmul(int n, const double2 *A, const double2 *B, double2 *C) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
