@@ -361,7 +361,9 @@ __device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
 // BLOCK mode (G_loc and GwHF) for correlated blocks of D <= 3: one thread per Matsubara frequency, the whole
 // D x D S(z) and S0(z) of that thread's (k, iw) in its registers, inverted by thread_inverse.  A lane-group
 // k_schur at these widths leaves lanes idle (D < W) and spends its issue slots on the group's pivot broadcasts;
-// here every lane does useful work and nothing is exchanged.  Shared-memory staging as k_schur (schur_stage).
+// here every lane does useful work and nothing is exchanged.  Per k point the CTA stages, for all its
+// frequencies, the pole outer products P_l = b_l b_l^H, the shifted poles mu - e_l and -H_PP - m0; each thread
+// forms S0 = z - H_PP - m0 - sum_l w_l P_l and S = S0 - (Sigma - m0), Sigma - m0 held in its registers.
 template <class Ops, int D>
 __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
     typedef typename Ops::C C;
@@ -369,56 +371,58 @@ __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
     constexpr int DD = D * D;
     const int m = g.m;
     C *st = reinterpret_cast<C *>(sm);
-    C *sB = st, *sE = sB + (size_t)g.kc * m * D, *sH = sE + (size_t)g.kc * m, *sM0 = sH + (size_t)g.kc * DD;
+    C *sP = st, *sE = sP + (size_t)g.kc * m * DD, *sH = sE + (size_t)g.kc * m;
     const int f_raw = blockIdx.x * blockDim.x + threadIdx.x;
     const bool fvalid = f_raw < g.nf2;
     const int f = fvalid ? f_raw : g.nf2 - 1;
     const int chunk = blockIdx.y;
     const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
-    for (int t = threadIdx.x; t < DD; t += blockDim.x) sM0[t] = Ops::from(g.m0[t]);
     const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
     const C zc = Ops::from(cmk(g.mu, w)), iwc = Ops::from(cmk(0.0, w));
-    C sg[D][D], aG[D][D], aG0[D][D];
+    C sd[D][D], aG[D][D], aG0[D][D];  // sd = Sigma(iw) - m0
 #pragma unroll
     for (int a = 0; a < D; a++)
 #pragma unroll
         for (int b = 0; b < D; b++) {
-            sg[a][b] = Ops::from(g.sig[(size_t)f * DD + a + b * D]);
+            sd[a][b] = Ops::from(csub(g.sig[(size_t)f * DD + a + b * D], g.m0[a + b * D]));
             aG[a][b] = aG0[a][b] = Ops::zero();
         }
     bool sing = false;
     for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
         const int nkc = min(g.kc, kend - k0);
         __syncthreads();
-        schur_stage<Ops>(g, k0, nkc, st, false, false);
+        for (int t = threadIdx.x; t < nkc * m * DD; t += blockDim.x) {
+            const int e = t % DD, a = e % D, b = e / D;
+            const double2 *bl = g.B + ((size_t)k0 * m + t / DD) * D;
+            sP[t] = Ops::from(cmulc(bl[a], bl[b]));
+        }
+        for (int t = threadIdx.x; t < nkc * m; t += blockDim.x)
+            sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k0 * m + t], 0.0));
+        for (int t = threadIdx.x; t < nkc * DD; t += blockDim.x) {
+            const int kk = t / DD, e = t % DD, a = e % D, b = e / D;
+            sH[t] = Ops::from(csub(cneg(g.H[(size_t)(k0 + kk) * g.n * g.n + a + (size_t)b * g.n]), g.m0[e]));
+        }
         __syncthreads();
         for (int kk = 0; kk < nkc; kk++) {
-            const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
-            C s[D][D];
-#pragma unroll
-            for (int a = 0; a < D; a++)
-#pragma unroll
-                for (int b = 0; b < D; b++) {
-                    s[a][b] = Ops::sub(hp[a + b * D], sg[a][b]);
-                    if (a == b) s[a][b] = Ops::add(s[a][b], zc);
-                }
-            for (int l = 0; l < m; l++) {
-                const C wl = Ops::rcp(Ops::add(es[l], iwc));
-                C q[D];
-#pragma unroll
-                for (int b = 0; b < D; b++) q[b] = Ops::mulc(wl, bs[l * D + b]);
-#pragma unroll
-                for (int a = 0; a < D; a++) {
-                    const C ba = bs[l * D + a];
-#pragma unroll
-                    for (int b = 0; b < D; b++) s[a][b] = Ops::fms(ba, q[b], s[a][b]);
-                }
-            }
+            const C *ps = sP + (size_t)kk * m * DD, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
             C s0[D][D];
 #pragma unroll
             for (int a = 0; a < D; a++)
 #pragma unroll
-                for (int b = 0; b < D; b++) s0[a][b] = Ops::sub(Ops::add(s[a][b], sg[a][b]), sM0[a + b * D]);
+                for (int b = 0; b < D; b++) s0[a][b] = (a == b) ? Ops::add(hp[a + b * D], zc) : hp[a + b * D];
+            for (int l = 0; l < m; l++) {
+                const C wl = Ops::rcp(Ops::add(es[l], iwc));
+                const C *pl = ps + (size_t)l * DD;
+#pragma unroll
+                for (int a = 0; a < D; a++)
+#pragma unroll
+                    for (int b = 0; b < D; b++) s0[a][b] = Ops::fms(wl, pl[a + b * D], s0[a][b]);
+            }
+            C s[D][D];
+#pragma unroll
+            for (int a = 0; a < D; a++)
+#pragma unroll
+                for (int b = 0; b < D; b++) s[a][b] = Ops::sub(s0[a][b], sd[a][b]);
             sing |= thread_inverse<Ops, D>(s);
             sing |= thread_inverse<Ops, D>(s0);
 #pragma unroll
@@ -442,8 +446,9 @@ __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
         }
 }
 
+// staged per k: P_l [m][D][D], mu - e_l [m], -H_PP - m0 [D][D]
 inline size_t schur_tpi_smem(int kc, int D, int m) {
-    return ((size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D) * 16;
+    return ((size_t)kc * m * D * D + (size_t)kc * m + (size_t)kc * D * D) * 16;
 }
 
 // shared-memory bytes of one k_schur launch
