@@ -18,6 +18,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -50,11 +51,11 @@ def cm(a):
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
-    def __init__(self, index):
+    def __init__(self, index, path=None):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/dmftgpu_clocks.csv"
+        # the raw samples go where --clocks-out says (kept beside the run's other outputs), else to a temp file
+        self.path = path or os.path.join(tempfile.gettempdir(), "dmftgpu_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
@@ -311,7 +312,7 @@ def run_ours(args, rank, world, local_rank):
     assert torch.isfinite(torch.view_as_real(gw)).all()
     if world > 1:
         torch.distributed.barrier()
-    clocks = Clocks(local_rank)
+    clocks = Clocks(local_rank, args.clocks_out)
     clocks.start()
     ctx.timing(True)
     launches0 = ctx.launches()
@@ -450,6 +451,7 @@ def main():
     ap.add_argument("--algo", default="schur", choices=["schur", "explicit"],
                     help="schur: exact correlated-block form (default); explicit: full n x n inversion per (k, iw)")
     ap.add_argument("--no-variants", action="store_true", help="skip the side measurement of the other algorithm")
+    ap.add_argument("--clocks-out", default=None, help="CSV file for the nvidia-smi samples of the timed region")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
