@@ -53,3 +53,18 @@ def test_gen_uijkl_matches_oracle(orc, nso, dd):
     ui, ut = models.gen_Uijkl(nso, 4.0, 2.6, 0.7, density_density=dd)
     oi, ot = orc.gen_uijkl(nso, 4.0, 2.6, 0.7, density_density=dd)
     assert np.array_equal(ui, oi) and np.array_equal(ut, ot)
+
+
+def test_new_entry_points_reject_a_null_context_without_a_device():
+    # argument validation happens before any CUDA call, so these run on a machine without a GPU
+    from dmftpack_gb300 import lib
+    L = lib.load()
+    dummy = (ctypes.c_double * 8)()
+    hartr = (ctypes.c_int * 1)(0)
+    rindex = (ctypes.c_int * 5)(0, 0, 0, 0, 0)
+    lat = lib.Lattice(2, 1, 4, 10.0)._c()
+    p = ctypes.cast(dummy, ctypes.c_void_p)
+    assert L.dmftgpu_downfold(None, 1, 2, 1, hartr, p, None, p, p, None, None, None, 0) == lib.BADARG
+    assert L.dmftgpu_density_dft(None, ctypes.byref(lat), p, p, 0.0, p, 0) == lib.BADARG
+    assert L.dmftgpu_upfold(None, 2, 1, 1, 1, p, p, p, None, 1, rindex, p, p, p, 0) == lib.BADARG
+    assert L.dmftgpu_gloc_real(None, ctypes.byref(lat), p, p, 1, 0.0, 0.1, 0.05, 0.0, p, p, 0) == lib.BADARG
