@@ -48,3 +48,32 @@ def write_hr(norb, rindex, hr):
         out.append("%+d %+d %+d %d %d %d %d  %.17g %.17g" % (rx, ry, rz, a1, a2, i0 - acc[a1 - 1] + 1,
                                                            j0 - acc[a2 - 1] + 1, v.real, v.imag))
     return "\n".join(out) + "\n"
+
+
+def write_density_hwr(norb, rindex, values):
+    """The R-space density files of upfolding_density (DM_DFT_DMFT.HWR, dual_DM_direct.HWR, direct_DM_direct.HWR;
+    src/upfolding.cpp:94-136): one row per H_Rindex entry, ``Rx Ry Rz atom1 atom2 i j Re Im`` with 1-based atoms
+    and local orbitals and the values in C's ``%e``, no header.  norb: spin-orbitals per atom (the read_HR
+    headers), rindex[nnz,5] and values[nnz] as dmftgpu_upfold takes and returns them."""
+    acc = np.concatenate([[0], np.cumsum(norb)]).astype(int)
+    out = []
+    for (rx, ry, rz, i0, j0), v in zip(np.asarray(rindex), np.asarray(values)):
+        a1 = int(np.searchsorted(acc, i0, side="right"))
+        a2 = int(np.searchsorted(acc, j0, side="right"))
+        out.append(" %+d %+d %+d %d %d %d %d      %e    %e  " % (rx, ry, rz, a1, a2, i0 - acc[a1 - 1] + 1,
+                                                               j0 - acc[a2 - 1] + 1, v.real, v.imag))
+    return "\n".join(out) + "\n"
+
+
+def read_density_hwr(text, norb):
+    """Inverse of :func:`write_density_hwr` (the rows read_DensityMat consumes): (rindex[nnz,5], values[nnz])."""
+    acc = np.concatenate([[0], np.cumsum(norb)]).astype(int)
+    rows, vals = [], []
+    for ln in text.splitlines():
+        f = ln.split()
+        if len(f) < 9:
+            continue
+        rx, ry, rz, a1, a2, oi, oj = (int(x) for x in f[:7])
+        rows.append((rx, ry, rz, acc[a1 - 1] + oi - 1, acc[a2 - 1] + oj - 1))
+        vals.append(complex(float(f[7]), float(f[8])))
+    return np.asarray(rows, np.int32).reshape(-1, 5), np.asarray(vals, np.complex128)

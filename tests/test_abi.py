@@ -68,3 +68,18 @@ def test_new_entry_points_reject_a_null_context_without_a_device():
     assert L.dmftgpu_density_dft(None, ctypes.byref(lat), p, p, 0.0, p, 0) == lib.BADARG
     assert L.dmftgpu_upfold(None, 2, 1, 1, 1, p, p, p, None, 1, rindex, p, p, p, 0) == lib.BADARG
     assert L.dmftgpu_gloc_real(None, ctypes.byref(lat), p, p, 1, 0.0, 0.1, 0.05, 0.0, p, p, 0) == lib.BADARG
+
+
+def test_density_hwr_round_trip(orc):
+    # the upfolded density of H(k) itself (DF = V = I) is the hopping table; written and read back at %e precision
+    from dmftpack_gb300 import hwr, models
+    wl = models.t2g_p(k=6, nfreq=8)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    eye = np.broadcast_to(np.eye(wl.n, dtype=np.complex128), H.shape)
+    dd, _, _ = orc.upfold(H, eye, eye, None, wl.kgrid, wl.rindex)
+    text = hwr.write_density_hwr([3, 9], wl.rindex, dd)
+    first = text.splitlines()[0].split()
+    assert len(first) == 9 and first[0][0] in "+-" and "e" in first[7]
+    r, v = hwr.read_density_hwr(text, [3, 9])
+    assert (r == wl.rindex).all()
+    assert np.abs(v - wl.hr).max() <= 1e-6 * np.abs(wl.hr).max()
