@@ -561,3 +561,53 @@ def upfold(dens, DF, V, S, kgrid, rindex):
     nk = km.shape[0]
     i0, j0 = ri[:, 3], ri[:, 4]
     return tuple((M[:, i0, j0] * ph).sum(0) / nk for M in (Mdd, Md, Dd))
+
+
+def downfold_window(H, S, hartr, from_val_to_ks):
+    """downfolding_ftn with a band window (src/downfolding.cpp:20-63): per k the model space is the NBAND[k] bands
+    listed in from_val_to_ks[k]; P = V[hartr][:, window], P <- S_d^-1/2 P, DF = Q^H (complete QR of P^H, NBAND x
+    NBAND) with rows 0..D-1 replaced by P, H_model = DF diag(e[window]) DF^H.  Returns lists (eps, H_model, DF, V)
+    per k (ragged) and H_imp (D, D)."""
+    import scipy.linalg as sla
+    H = np.asarray(H, np.complex128)
+    nk, n = H.shape[0], H.shape[1]
+    hartr = np.asarray(hartr, int)
+    D = len(hartr)
+    out_e, out_h, out_df, out_v = [], [], [], []
+    himp = np.zeros((D, D), np.complex128)
+    for k in range(nk):
+        Sk = np.eye(n) if S is None else np.asarray(S[k], np.complex128)
+        e, V = sla.eigh(H[k], Sk)
+        win = np.asarray(from_val_to_ks[k], int)
+        P = V[hartr][:, win]
+        w, W = np.linalg.eigh(P @ P.conj().T)
+        Pn = (W * w ** -0.5) @ W.conj().T @ P
+        Q, _ = np.linalg.qr(Pn.conj().T, mode="complete")
+        F = Q.conj().T
+        F[:D] = Pn
+        Hm = (F * e[win]) @ F.conj().T
+        out_e.append(e)
+        out_h.append(Hm)
+        out_df.append(F)
+        out_v.append(V)
+        himp += Hm[:D, :D]
+    return out_e, out_h, out_df, out_v, himp / nk
+
+
+def upfold_window(dens, DF, V, S, eps, from_val_to_ks, mu, beta, kgrid, rindex):
+    """upfolding_density with a band window (src/upfolding.cpp:10-35, 38-91): per k, X = DF^H D DF in the window's
+    KS bands; Matrix_KSBase = diag(f(e - mu)) (the +-100 cut-offs) with the window block replaced by X; D_DFT =
+    V Matrix_KSBase V^H; then the three k -> R sums of :func:`upfold`.  dens, DF: ragged lists (NBAND[k] square);
+    V, S, eps: (nk, n, n), (nk, n, n) or None, (nk, n)."""
+    nk = len(dens)
+    n = np.asarray(V).shape[1]
+    Dd = np.zeros((nk, n, n), np.complex128)
+    for k in range(nk):
+        x = beta * (np.asarray(eps[k]) - mu)
+        f = np.where(x > 100.0, 0.0, np.where(x < -100.0, 1.0, 1.0 / (1.0 + np.exp(np.clip(x, -100, 100)))))
+        M = np.diag(f).astype(np.complex128)
+        win = np.asarray(from_val_to_ks[k], int)
+        M[np.ix_(win, win)] = DF[k].conj().T @ dens[k] @ DF[k]
+        Dd[k] = V[k] @ M @ V[k].conj().T
+    eye = np.broadcast_to(np.eye(n, dtype=np.complex128), (nk, n, n))
+    return upfold(Dd, eye, eye, S, kgrid, rindex)

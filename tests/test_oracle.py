@@ -248,3 +248,61 @@ def test_upfold_inverts_the_hk_fourier_sum(orc):
     dd, d, direct = orc.upfold(H, eye, eye, None, wl.kgrid, wl.rindex)
     for x in (dd, d, direct):
         assert np.abs(x - wl.hr).max() < 1e-12
+
+
+def test_band_window_selection():
+    from dmftpack_gb300.window import low_energy_subspace_in_KS_basis as sel
+    e = np.array([[-5.0, -1.0, 0.2, 0.9, 3.0], [-4.0, -2.5, -0.5, 1.5, 2.5]])
+    nband, idx = sel(e, 0.1, -3.0, 2.0, n_corr=2)
+    assert list(nband) == [3, 3] and list(idx[0]) == [1, 2, 3] and list(idx[1]) == [1, 2, 3]
+    nband, idx = sel(e, 0.0, -10.0, 10.0, n_corr=2, downfolding=False)
+    assert list(nband) == [5, 5] and list(idx[1]) == [0, 1, 2, 3, 4]
+    with pytest.raises(ValueError):
+        sel(e, 0.0, 5.0, 6.0, n_corr=1)      # empty window
+    with pytest.raises(ValueError):
+        sel(e, 0.1, -3.0, 2.0, n_corr=4)     # fewer bands than correlated orbitals
+
+
+def test_windowed_downfold_and_upfold_reduce_to_the_full_window(orc):
+    rng = np.random.default_rng(21)
+    wl = models.t2g_p(k=3, nfreq=8)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    S = _overlap(rng, H.shape[0], wl.n)
+    full = [np.arange(wl.n)] * H.shape[0]
+    e_w, hm_w, df_w, v_w, himp_w = orc.downfold_window(H, S, [0, 1, 2], full)
+    eps, Hm, DF, himp = orc.downfold(H, S, [0, 1, 2])
+    assert np.abs(np.array(e_w) - eps).max() < 1e-12
+    assert np.abs(np.array(hm_w)[:, :3, :3] - Hm[:, :3, :3]).max() < 1e-12
+    assert np.abs(himp_w - himp).max() < 1e-12
+    dens = [(d * 0.3 + d.conj().T * 0.3) for d in hm_w]
+    got = orc.upfold_window(dens, df_w, np.array(v_w), S, e_w, full, 0.0, 10.0, wl.kgrid, wl.rindex)
+    ref = orc.upfold(np.array(dens), np.array(df_w), np.array(v_w), S, wl.kgrid, wl.rindex)
+    for g_, r_ in zip(got, ref):
+        assert np.abs(g_ - r_).max() < 1e-12
+
+
+def test_windowed_upfold_of_the_model_fermi_density_is_the_full_fermi_density(orc):
+    # inside the window the model-basis density DF f(e) DF^H maps back to f(e) on the window's bands; outside,
+    # upfolding_density fills in f(e), so the result is V f(e) V^H over every band
+    from dmftpack_gb300.window import low_energy_subspace_in_KS_basis as sel
+    rng = np.random.default_rng(22)
+    wl = models.t2g_p(k=3, nfreq=8)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    S = _overlap(rng, H.shape[0], wl.n)
+    beta, mu = 8.0, 0.0
+    eps_all = np.array([np.linalg.eigvalsh(np.linalg.solve(np.linalg.cholesky(S[k]), H[k])
+                                           @ np.linalg.inv(np.linalg.cholesky(S[k])).conj().T)
+                        for k in range(H.shape[0])])
+    lo, hi = np.quantile(eps_all, 0.2), np.quantile(eps_all, 0.95)
+    nband, win = sel(eps_all, mu, lo, hi, n_corr=3)
+    assert nband.min() < wl.n  # a genuine window
+    e_w, hm_w, df_w, v_w, _ = orc.downfold_window(H, S, [0, 1, 2], win)
+    fermi = lambda e: 1.0 / (1.0 + np.exp(beta * (e - mu)))
+    dens = [df_w[k] @ np.diag(fermi(e_w[k][win[k]])) @ df_w[k].conj().T for k in range(H.shape[0])]
+    got = orc.upfold_window(dens, df_w, np.array(v_w), S, e_w, win, mu, beta, wl.kgrid, wl.rindex)
+    V = np.array(v_w)
+    full = np.array([V[k] @ np.diag(fermi(e_w[k])) @ V[k].conj().T for k in range(H.shape[0])])
+    eye = np.broadcast_to(np.eye(wl.n, dtype=np.complex128), full.shape)
+    ref = orc.upfold(full, eye, eye, S, wl.kgrid, wl.rindex)
+    for g_, r_ in zip(got, ref):
+        assert np.abs(g_ - r_).max() < 1e-11
