@@ -83,3 +83,25 @@ def test_density_hwr_round_trip(orc):
     r, v = hwr.read_density_hwr(text, [3, 9])
     assert (r == wl.rindex).all()
     assert np.abs(v - wl.hr).max() <= 1e-6 * np.abs(wl.hr).max()
+
+
+def test_ctypes_structs_match_the_header_layout(tmp_path):
+    # the C compiler's sizeof / offsetof of the ABI structs against the ctypes mirrors the bindings pass
+    import subprocess
+    from dmftpack_gb300 import lib
+    structs = {"dmftgpu_lattice": lib._Lat, "dmftgpu_dmft_params": lib.DmftParams}
+    src = ['#include <stddef.h>', '#include <stdio.h>', '#include "dmftgpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        src.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            src.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    src.append("return 0; }")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)])
+    got = dict(line.rsplit(" ", 1) for line in subprocess.check_output([str(exe)], text=True).splitlines())
+    for cname, py in structs.items():
+        assert int(got["%s size" % cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got["%s %s" % (cname, fname)]) == getattr(py, fname).offset, (cname, fname)
