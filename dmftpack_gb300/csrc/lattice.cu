@@ -642,7 +642,9 @@ __global__ void k_schur_reduce(int nchunk, int nf2, int DD, int mode, const doub
 int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
               double *tr, double *dtr, bool mixed) {
     const SInst *in = pick_schur(P.D);
-    // BLOCK passes of correlated blocks up to 3 x 3: one thread per frequency (k_schur_tpi)
+    // BLOCK passes of correlated blocks up to 3 x 3: one thread per frequency (k_schur_tpi).  It stages the
+    // D x D pole products of each staged k; prepare() caps n at 64 (the static eigensolver), so one k needs at
+    // most (9*63 + 63 + 9)*16 B = 10 KB and the 200 KB check below never rejects a tpi pass.
     const bool tpi = mode == dg::S_BLOCK && P.D <= 3;
     SchurKernel kern = tpi ? dg::schur_tpi_kernel(P.D, mixed) : in->get(mode, mixed);
     const int m = P.n - P.D, NG = tpi ? 128 : 128 / in->W, DD = P.D * P.D;
@@ -1378,8 +1380,9 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, c
                      (flags & DMFTGPU_MIXED) != 0));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
+    if (code) return code;
     if (!std::isfinite(*nele)) return DMFTGPU_NAN;
-    return code;
+    return DMFTGPU_OK;
 }
 
 int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
@@ -1402,6 +1405,16 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
                          (flags & DMFTGPU_MIXED) != 0);
     };
     const double goal = n_target;
+    // every exit reads the status word the N(mu) kernels raise (DG_SINGULAR for a zero pivot ...): a flagged
+    // code takes precedence over the search's own outcome, so a singular inversion is never reported as OK.
+    auto finish = [&](int ret, double mu_final) {
+        *mu_out = mu_final;
+        if (n_eval) *n_eval = evals;
+        int code = 0;
+        int rs = dg_status_read(ctx, &code);
+        if (rs) return rs;
+        return code ? code : ret;
+    };
     if (flags & DMFTGPU_NEWTON) {
         // safeguarded Newton: keep a bracket [lo, hi] with N(lo) < goal < N(hi) once found.  The first step
         // uses dN/dmu from the derivative pass; later steps take the secant slope of the last two evaluations
@@ -1417,46 +1430,36 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
                 DG_TRY(N(mu, &Nv, nullptr));
                 dN = (Nv - pN) / (mu - pmu);
             }
-            if (!std::isfinite(Nv)) return DMFTGPU_NAN;
+            if (!std::isfinite(Nv)) return finish(DMFTGPU_NAN, mu);
             need_deriv = !(dN > 0) || !std::isfinite(dN);
             pmu = mu;
             pN = Nv;
             double r = Nv - goal;
             if (r < 0) lo = std::max(lo, mu);
             else hi = std::min(hi, mu);
-            if (std::fabs(r) <= 1e-11 * std::max(1.0, std::fabs(goal))) {
-                *mu_out = mu;
-                if (n_eval) *n_eval = evals;
-                return DMFTGPU_OK;
-            }
+            if (std::fabs(r) <= 1e-11 * std::max(1.0, std::fabs(goal))) return finish(DMFTGPU_OK, mu);
             double step = (dN > 0) ? -r / dN : (r < 0 ? std::fabs(dmu) : -std::fabs(dmu));
             double next = mu + step;
             if (!(next > lo && next < hi)) {
                 if (lo > -1e299 && hi < 1e299) next = 0.5 * (lo + hi);
                 else next = mu + (r < 0 ? std::fabs(dmu) : -std::fabs(dmu));
             }
-            if (std::fabs(next - mu) < 1e-15 * std::max(1.0, std::fabs(mu))) {
-                *mu_out = next;
-                if (n_eval) *n_eval = evals;
-                return DMFTGPU_OK;
-            }
+            if (std::fabs(next - mu) < 1e-15 * std::max(1.0, std::fabs(mu))) return finish(DMFTGPU_OK, next);
             mu = next;
         }
-        *mu_out = mu;
-        if (n_eval) *n_eval = evals;
-        return DMFTGPU_NONCONVERGED;
+        return finish(DMFTGPU_NONCONVERGED, mu);
     }
     // the reference's bracket expansion + bisection (src/GreenFtn.cpp:81-121)
     double Nele[2] = {-1, -1};
     DG_TRY(N(mu, &Nele[0], nullptr));
-    if (!std::isfinite(Nele[0])) return DMFTGPU_NAN;
+    if (!std::isfinite(Nele[0])) return finish(DMFTGPU_NAN, mu);
     double muUB = 0, muLB = 0, mu_next;
     int nearAns = 0;
     if (Nele[0] > goal) mu -= (dmu - dmu);
     else if (Nele[0] < goal) mu -= (dmu + dmu);
     int guard = 0;
     while ((Nele[0] != goal) && std::abs(dmu) > 1e-5) {
-        if (++guard > 10000) return DMFTGPU_NONCONVERGED;
+        if (++guard > 10000) return finish(DMFTGPU_NONCONVERGED, mu);
         mu += dmu;
         Nele[1] = Nele[0];
         DG_TRY(N(mu, &Nele[0], nullptr));
@@ -1472,7 +1475,7 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
                 else dmu = -1 * std::fabs(dmu);
             }
             if (Nele[0] == goal) break;
-            if (!(std::abs(mu) < 600)) return DMFTGPU_NONCONVERGED;
+            if (!(std::abs(mu) < 600)) return finish(DMFTGPU_NONCONVERGED, mu);
         } else {
             if (Nele[0] > goal) muUB = mu;
             else if (Nele[0] < goal) muLB = mu;
@@ -1480,11 +1483,7 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
             dmu = mu_next - mu;
         }
     }
-    *mu_out = mu;
-    if (n_eval) *n_eval = evals;
-    int code = 0;
-    DG_TRY(dg_status_read(ctx, &code));
-    return code;
+    return finish(DMFTGPU_OK, mu);
 }
 
 }  // extern "C"

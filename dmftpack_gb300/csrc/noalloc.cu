@@ -11,7 +11,9 @@
 // larger requests are rejected with DMFTGPU_BADARG.  All calls share the one array, so calls that overlap
 // on the GPU (different streams, or several host threads at once) race on it; serialise them.  The first
 // call on each device resolves the device address of the array (cudaGetSymbolAddress); make that first
-// call before any stream capture.
+// call before any stream capture.  The arrays belong to the device that is current when the call is made,
+// and cuda_stream must belong to that device too (else DMFTGPU_BADARG).  Every call is synchronous: it
+// reads the status word back and waits for cuda_stream to finish before it returns.
 #include <mutex>
 
 #include "linalg.cuh"
@@ -93,10 +95,17 @@ extern "C" int dmftgpu_hyb_delta_noalloc(int dim, const int *orb, int nfreq, dou
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return DMFTGPU_CUDA_ERROR;
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    if (s) {
+        // the scratch address resolved below belongs to the current device: a stream created on another
+        // device would run the kernel against the wrong device's array, so such a stream is rejected
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) return DMFTGPU_BADARG;
+        if (sdev != dev) return DMFTGPU_BADARG;
+    }
     DevSymbols *sym = nullptr;
     int st = resolve_symbols(dev, sym);
     if (st) return st;
-    cudaStream_t s = (cudaStream_t)cuda_stream;
     if (cudaMemsetAsync(sym->status, 0, sizeof(int), s) != cudaSuccess) return DMFTGPU_CUDA_ERROR;
     k_hyb_delta_static<<<(nfreq + 127) / 128, 128, 0, s>>>(dim, nfreq, D, beta, mu, ot, (const double2 *)sigma,
                                                            (const double2 *)gw, (const double2 *)himp, sym->scratch,

@@ -266,11 +266,12 @@ int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const d
 /* No counterpart in the reference.  Construct_hyb_delta for callers that cannot allocate device memory
  * (a driver whose HBM belongs to a pool allocator, or one that must not stall the device with a
  * non-stream-ordered cudaMalloc): no context, no allocation, every array argument a DEVICE pointer except
- * orb (host, dim <= 32); work is enqueued on cuda_stream, which is then synchronised to return the status.
- * Scratch is a static device array of 2^19 complex numbers (8 MiB) per GPU that loads the library, so
- * nfreq*dim*dim must not exceed 524288 (else DMFTGPU_BADARG).  The first call on a device resolves the
- * array's device address and should precede any stream capture; calls that overlap on the GPU share the
- * array and race. */
+ * orb (host, dim <= 32); work is enqueued on cuda_stream (NULL: the legacy default stream), which must belong
+ * to the current device (else DMFTGPU_BADARG).  The call is synchronous: it waits for cuda_stream to finish
+ * and returns the status its kernel raised.  Scratch is a static device array of 2^19 complex numbers
+ * (8 MiB) per GPU that loads the library, so nfreq*dim*dim must not exceed 524288 (else DMFTGPU_BADARG).
+ * The first call on a device resolves the array's device address and should precede any stream capture;
+ * calls that overlap on the GPU share the array and race. */
 int dmftgpu_hyb_delta_noalloc(int dim, const int *orb, int nfreq, double beta, int D, const double *sigma,
                               const double *gw, const double *himp, double mu, double *delta, void *cuda_stream);
 

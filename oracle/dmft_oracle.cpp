@@ -235,6 +235,10 @@ Mat op_sqrt(const Mat &A) {
     return mul(mul(V, D), adj(V));
 }
 
+// threads for the per-frequency / per-tau / per-window loops of the transforms and the moment fit; every
+// index is computed independently, so the results do not depend on the count (orc_set_threads)
+int g_nthreads = 1;
+
 template <class F>
 void parallel_for(int n, int nthreads, F f) {
     if (nthreads <= 1 || n < 2) {
@@ -263,7 +267,11 @@ int moments_fit(int Dim, int Nf, double beta, const std::vector<Mat> &F, bool gr
     std::vector<cd> mt((size_t)DD * R * ncol);  // momentstest[ab][w][col]
     auto MT = [&](int ab, int w, int col) -> cd & { return mt[((size_t)ab * R + w) * ncol + col]; };
     std::vector<std::vector<double>> trace(ncol, std::vector<double>(R, 0.0));
-    for (int w = 0; w < R; w++) {
+    // window w costs ~ (Nf - w): threads take the windows round-robin to balance the triangle
+    const int T = std::max(1, std::min(g_nthreads, R));
+    parallel_for(T, T, [&](int tb, int te, int) {
+    for (int t0 = tb; t0 < te; t0++)
+    for (int w = t0; w < R; w += T) {
         int ASlen = Nf - w;
         Mat KtK(ncol, ncol);
         auto krow = [&](int jj, int im, double *kr) {
@@ -312,6 +320,7 @@ int moments_fit(int Dim, int Nf, double beta, const std::vector<Mat> &F, bool gr
         for (int a = 0; a < Dim; a++)
             for (int i = 0; i < ncol; i++) trace[i][w] += std::real(MT(a * Dim + a, w, i));
     }
+    });
     // window averages of the fitted moments (src/FourierTransform.cpp:259-283)
     std::vector<std::vector<Mat>> avg(ncol, std::vector<Mat>(C, Mat(Dim, Dim)));
     for (int ci = 0; ci < C; ci++) {
@@ -476,6 +485,8 @@ void add_sigma_block(Mat &A, const Mat &S, const orc_lattice *L, bool within_clu
 extern "C" {
 
 int orc_version(void) { return 1; }
+
+void orc_set_threads(int n) { g_nthreads = n < 1 ? 1 : n; }
 
 /* src/TB.cpp:196-207 with ax=ay=az=pi (src/dmft_common.h:37-39). */
 void orc_kmesh(int kx, int ky, int kz, double *kmesh) {
@@ -793,9 +804,13 @@ int orc_w2tau(int dim, int nfreq, int ntau, double beta, const double *fw, const
     Tail T = make_tail(dim, M);
     std::vector<Mat> tails(nfreq);
     double dwl = (2 * PI) / beta, w0l = (PI / beta);
-    for (int i = 0; i < nfreq; i++) tails[i] = tail_w(T, w0l + i * dwl);
+    parallel_for(nfreq, g_nthreads, [&](int b, int e, int) {
+        for (int i = b; i < e; i++) tails[i] = tail_w(T, w0l + i * dwl);
+    });
     std::vector<Mat> out(ntau + 1);
-    for (int j = 0; j < ntau + 1; j++) out[j] = ft_tau(F, T, tails, nfreq, beta, j * beta / ntau);
+    parallel_for(ntau + 1, g_nthreads, [&](int b, int e, int) {
+        for (int j = b; j < e; j++) out[j] = ft_tau(F, T, tails, nfreq, beta, j * beta / ntau);
+    });
     int nfix = positivity_fixup(out, ntau, beta);
     if (fixups) *fixups = nfix;
     store_stack(out, ntau + 1, ft);
@@ -840,8 +855,9 @@ int orc_tau2w(int dim, int nfreq, int ntau, double beta, const double *ft, doubl
         at[t] = scal(sub(Dt[t + 1], Dt[t]), 1.0 / (tau1 - tau0));
         bt[t] = add(scal(at[t], -tau0), Dt[t]);
     }
-    int st = OK;
-    for (int nn = 0; nn < nfreq; nn++) {
+    std::vector<char> causal(nfreq, 0);
+    parallel_for(nfreq, g_nthreads, [&](int nb, int ne, int) {
+    for (int nn = nb; nn < ne; nn++) {
         double wn = (2 * nn + 1) * PI / beta;
         Mat W(dim, dim);
         for (int t = 0; t < Nseg; t++) {
@@ -853,10 +869,13 @@ int orc_tau2w(int dim, int nfreq, int ntau, double beta, const double *ft, doubl
             for (int k = 0; k < dim * dim; k++) W.a[k] += at[t].a[k] * ca + bt[t].a[k] * cb;
         }
         Mat test = scal(sub(W, adj(W)), 1.0 / (2.0 * I1));
-        if (max_eig(test) > 0) st = CAUSAL;
+        if (max_eig(test) > 0) causal[nn] = 1;
         store(W, fw + (size_t)2 * dim * dim * nn);
     }
-    return st;
+    });
+    for (int nn = 0; nn < nfreq; nn++)
+        if (causal[nn]) return CAUSAL;
+    return OK;
 }
 
 /* src/SCGF2_fullLoop.cpp:603-690  getStimp: second-order Sigma(tau) from G(tau), U_{ijkl} list. */
@@ -865,8 +884,9 @@ int orc_sigma2_tau(int dim, int ntau, double beta, int nu, const int *uidx, cons
     std::vector<Mat> G = load_stack(gt, ntau + 1, dim), S(ntau + 1);
     std::vector<cd> U(nu);
     for (int x = 0; x < nu; x++) U[x] = cd(ut[2 * x], ut[2 * x + 1]);
-    int status = OK;
-    for (int t = 0; t < ntau + 1; t++) {
+    std::vector<char> herm(ntau + 1, 0);
+    parallel_for(ntau + 1, g_nthreads, [&](int tb, int te, int) {
+    for (int t = tb; t < te; t++) {
         Mat Sn(dim, dim);
         const Mat &Gt = G[t], &Gm = G[ntau - t];
         for (int x1 = 0; x1 < nu; x1++) {
@@ -878,9 +898,13 @@ int orc_sigma2_tau(int dim, int ntau, double beta, int nu, const int *uidx, cons
             }
         }
         S[t] = Sn;
-        if (fnorm(scal(sub(Gt, adj(Gt)), 1.0 / (2.0 * I1))) > 1e-10) status = HERMIT;
-        if (fnorm(scal(sub(Sn, adj(Sn)), 1.0 / (2.0 * I1))) > 1e-5) status = HERMIT;
+        if (fnorm(scal(sub(Gt, adj(Gt)), 1.0 / (2.0 * I1))) > 1e-10) herm[t] = 1;
+        if (fnorm(scal(sub(Sn, adj(Sn)), 1.0 / (2.0 * I1))) > 1e-5) herm[t] = 1;
     }
+    });
+    int status = OK;
+    for (int t = 0; t < ntau + 1; t++)
+        if (herm[t]) status = HERMIT;
     int nfix = positivity_fixup(S, ntau, beta);
     if (fixups) *fixups = nfix;
     store_stack(S, ntau + 1, st);

@@ -38,6 +38,8 @@ typedef struct {
 } orc_lattice;
 
 int  orc_version(void);
+/* threads for the transforms, the moment fit and getStimp (results do not depend on the count) */
+void orc_set_threads(int n);
 void orc_kmesh(int kx, int ky, int kz, double *kmesh);
 int  orc_hk(int n, int nnz, const int *rindex, const double *hr, int nk, const double *kmesh,
             double *hk, int nthreads);

@@ -18,6 +18,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
+# host threads of the k sums (GreenFtn_w, GiwToNele, H(k)) and of the transforms; ORACLE_THREADS overrides
+NTHREADS = int(os.environ.get("ORACLE_THREADS", os.cpu_count() or 1))
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -65,6 +67,9 @@ def lib():
         _lib.orc_estimate_asymto.restype = None
         _lib.orc_hermitian_eig.argtypes = [C.c_int, _dp, _dp, _dp]
         _lib.orc_inverse.argtypes = [C.c_int, _dp, _dp]
+        _lib.orc_set_threads.argtypes = [C.c_int]
+        _lib.orc_set_threads.restype = None
+        _lib.orc_set_threads(NTHREADS)
     return _lib
 
 
@@ -105,8 +110,9 @@ def kmesh(kx, ky, kz):
     return out
 
 
-def hk(n, rindex, hr, km, nthreads=1):
+def hk(n, rindex, hr, km, nthreads=None):
     """rindex: (nnz,5) int (Rx,Ry,Rz,i0,j0); hr: (nnz,) complex; returns (nk, n, n) H(k) (i,j order)."""
+    nthreads = nthreads or NTHREADS
     rindex = np.ascontiguousarray(rindex, dtype=np.int32)
     hr = np.ascontiguousarray(hr, dtype=np.complex128)
     km = np.ascontiguousarray(km, dtype=np.float64)
@@ -143,8 +149,9 @@ def moments(fw, beta, green_asym=False):
     return from_cm(out)
 
 
-def greenftn_w(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1):
+def greenftn_w(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=None):
     """GreenFtn_w: hk_ (nk,n,n), sigma (nfreq,D,D); returns (Gw, GwHF, NumMatrix)."""
+    nthreads = nthreads or NTHREADS
     hk_c = to_cm(hk_)
     s_c = to_cm(sigma)
     nk, n = hk_c.shape[0], hk_c.shape[1]
@@ -161,7 +168,8 @@ def greenftn_w(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1):
     return from_cm(gw), from_cm(gwhf), from_cm(num)
 
 
-def nele(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1, deriv=False):
+def nele(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=None, deriv=False):
+    nthreads = nthreads or NTHREADS
     hk_c = to_cm(hk_)
     s_c = to_cm(sigma)
     nk, n = hk_c.shape[0], hk_c.shape[1]
@@ -176,7 +184,8 @@ def nele(hk_, sigma, mu, beta, ncl, nh, hartr=None, nthreads=1, deriv=False):
     return (N.value, dN.value) if deriv else N.value
 
 
-def adjust_mu(hk_, sigma, mu, beta, ncl, nh, n_target, dmu=1.0, hartr=None, nthreads=1):
+def adjust_mu(hk_, sigma, mu, beta, ncl, nh, n_target, dmu=1.0, hartr=None, nthreads=None):
+    nthreads = nthreads or NTHREADS
     hk_c = to_cm(hk_)
     s_c = to_cm(sigma)
     nk, n = hk_c.shape[0], hk_c.shape[1]

@@ -41,10 +41,21 @@ def test_hwr_round_trip_and_reference_example():
     norb, r2, h2 = hwr.read_hr(text)
     assert norb == [12]
     assert (r2 == wl.rindex).all() and (h2 == wl.hr).all()
-    ex = "/root/reference/example/Hubb_model/primitive_Cell_ipt/Hk.HWR"
-    if os.path.exists(ex):  # only in the build container
-        norb, r, h = hwr.read_hr(ex, num_atoms=1)
-        assert norb == [2] and r.shape == (8, 5) and np.allclose(h, -0.25)
+
+
+
+def test_reference_example_fixture_parses_to_the_square_lattice_band(orc):
+    """tests/golden/hubbard_example.json (made from the reference's Hubbard example by make_hubbard_example.py):
+    its Hk.HWR rows, read by read_HR's restatement, give H(k) = -0.5 (cos kx + cos ky) on both spin-orbitals with
+    the reference's e^{-ik.R} convention."""
+    import test_gpu_fullsize as fs
+    fx, n, rindex, hr = fs.reference_example()
+    assert n == 2 and rindex.shape == (8, 5) and np.allclose(hr, -0.25)
+    assert fx["k_points"] == [22, 22, 1] and fx["n_matsubara"] == 400 and fx["n_tau"] == 2400
+    km = orc.kmesh(*fx["k_points"])
+    H = orc.hk(n, rindex, hr, km)
+    band = -0.5 * (np.cos(km[:, 0] * np.pi) + np.cos(km[:, 1] * np.pi))
+    assert np.abs(H - band[:, None, None] * np.eye(2)[None]).max() < 1e-14
 
 
 @pytest.mark.parametrize("nso,dd", [(2, True), (2, False), (6, False), (10, True), (10, False)])

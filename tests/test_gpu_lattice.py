@@ -153,6 +153,22 @@ def test_adjust_mu_bisection_matches_oracle_and_newton_converges(ctx, orc):
     assert ne_n < ne_o
 
 
+@pytest.mark.parametrize("newton", [False, True])
+def test_adjust_mu_reports_singular_inversion(ctx, newton):
+    """A zero pivot inside the mu search is reported as SINGULAR by both search modes (the reference would
+    carry inf/nan on silently).  Flat band H(k) = 0 and Sigma(i w_0) = mu0 + i w_0 make z - H - Sigma exactly
+    zero at the first frequency for the first mu evaluated."""
+    nk, nf, beta, mu0 = 8, 16, 10.0, 0.3
+    H = np.zeros((nk, 1, 1), complex)
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = (-0.5j / (wn + 1.0)).reshape(nf, 1, 1).astype(complex)
+    S[0, 0, 0] = complex(mu0, np.pi / beta)
+    lat = lib.Lattice(1, nk, nf, beta, 1, 1)
+    with pytest.raises(lib.DmftGpuError) as e:
+        ctx.GreenFtn_w_adjust_mu(lat, H, S, mu0, 1.0, 0.5, newton=newton)
+    assert e.value.code == lib.SINGULAR
+
+
 TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
 
 

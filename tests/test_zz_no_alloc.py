@@ -1,7 +1,8 @@
 """dmftgpu_hyb_delta_noalloc: the hybridisation entry point for callers that cannot allocate device memory
 (pool-owned HBM, or code that must not stall the device with a cudaMalloc).  It is checked against the
 regular dmftgpu_hyb_delta through the C ABI on two calls in a row, which also exercises the reuse of its
-static scratch.  This file is collected last on purpose."""
+static scratch, and both against the FP64 oracle's Construct_hyb_delta.  This file is collected last on
+purpose."""
 import ctypes as C
 
 import numpy as np
@@ -29,7 +30,7 @@ def _inputs(seed, nf, D):
     return beta, S, G, himp
 
 
-def test_noalloc_matches_hyb_delta_on_two_calls():
+def test_noalloc_matches_hyb_delta_on_two_calls(orc):
     import torch
     from dmftpack_gb300 import lib
 
@@ -41,6 +42,7 @@ def test_noalloc_matches_hyb_delta_on_two_calls():
         for call, (seed, nf, D, orb, mu) in enumerate([(1, 256, 4, [0, 1, 2], 0.3), (2, 512, 5, [4, 0, 2, 1], -0.7)]):
             beta, S, G, himp = _inputs(seed, nf, D)
             ref = ctx.Construct_hyb_delta(orb, S, G, mu, beta, himp)
+            assert rel_err(ref, orc.hyb_delta(orb, S, G, himp, mu, beta)) < TOL, call
             cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
             dS, dG, dH = cm(S), cm(G), cm(himp[None])[0]
             dim = len(orb)
@@ -53,6 +55,7 @@ def test_noalloc_matches_hyb_delta_on_two_calls():
             assert st == 0, (call, st)
             got = np.swapaxes(out.cpu().numpy(), -1, -2)
             assert rel_err(got, ref) < TOL, call
+            assert rel_err(got, orc.hyb_delta(orb, S, G, himp, mu, beta)) < TOL, call
     finally:
         ctx.close()
 
