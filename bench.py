@@ -402,6 +402,29 @@ def run_lattice(ctx, dev, a):
             "n_passes": npass, "mu_search_seconds": t1 - t0, "greenftn_w_seconds": t2 - t1}
 
 
+def run_hk(ctx, dev, a):
+    """H(k) of the d+p model (28 orbitals, 729 R vectors, k^3 grid): FP64 k_hk and the tensor-core form (first
+    call builds the phase-slice image, the second reuses it); device output, host clock around synchronised
+    calls, and the tensor form's largest difference from FP64 relative to max |H|."""
+    import torch
+    from dmftpack_gb300 import models
+    wl = models.dp28(k=a.k, nfreq=8, ntau=16)
+    out = {"nk": wl.nk, "n": wl.n, "n_R": len({tuple(r[:3]) for r in wl.rindex})}
+    res = {}
+    for name, mixed in (("fp64", False), ("tensor", True)):
+        ts = []
+        for _ in range(max(2, a.repeat)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res[name] = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev, mixed=mixed)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        out[name + "_seconds"] = ts
+    out["tensor_vs_fp64"] = float((res["tensor"] - res["fp64"]).abs().max() / res["fp64"].abs().max())
+    out["h_bytes"] = wl.nk * wl.n * wl.n * 16
+    return out
+
+
 def run_dmft(ctx, dev, a):
     """DMFT iterations (SC2PT) on the d+p model: returns per-iteration seconds, SCGF2 loops and residuals."""
     import torch
@@ -486,8 +509,8 @@ def run_case(a):
                              mixed=a.mixed)
         out.update(d=a.d, nfreq=nfreq, ntau=a.ntau, loops=a.loops, nu=int(uidx.shape[0]), direct=a.direct,
                    mixed=a.mixed)
-    if a.case in ("dmft", "lattice", "batched", "adjoint", "downfold", "density"):
-        out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched,
+    if a.case in ("dmft", "lattice", "batched", "adjoint", "downfold", "density", "hk"):
+        out.update({"dmft": run_dmft, "lattice": run_lattice, "batched": run_batched, "hk": run_hk,
                     "adjoint": run_adjoint, "downfold": run_downfold, "density": run_density}[a.case](ctx, dev, a))
         print(json.dumps(out), flush=True)
         ctx.close()
@@ -705,7 +728,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="skip the side measurement of the other algorithm")
     ap.add_argument("--clocks-out", default=None, help="CSV file for the nvidia-smi samples of the timed region")
     ap.add_argument("--case", default=None, choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint",
-                                                     "downfold", "density"],
+                                                     "downfold", "density", "hk"],
                     help="run one named hot-path case on cuda:0 instead of the benchmark (profiling runs)")
     case_args(ap)
     args = ap.parse_args()

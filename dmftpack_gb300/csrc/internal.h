@@ -51,6 +51,7 @@ struct dmftgpu_ctx {
     cudaGraphExec_t graph = nullptr;  // the last captured batched pass
     std::string graph_key;
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
+    std::string hk_phase_key;         // (k mesh, R list) of the phase-slice image in workspace "hk.tc.A"
 };
 
 // sets ctx->ft_direct and ctx->imp_mixed from a call's flags for the call's duration
@@ -111,6 +112,10 @@ int dg_moments_dev(dmftgpu_ctx *ctx, int dim, int nfreq, double beta, const doub
 // history workspaces of this mixer instance
 int dg_pulay_mixing(dmftgpu_ctx *ctx, DgPulay &P, const char *tag, long long len, double2 *in, double2 *out,
                     double mixing, int it);
+
+// H(k) on the tensor cores (hk_tc.cu); all pointers device
+int dg_hk_tensor(dmftgpu_ctx *ctx, int n, int nR, const int *dR, const double2 *dT, int kx, int ky, int kz,
+                 double2 *dH, const std::string &mesh_key);
 
 #define DG_LAUNCH(ctx, what)                     \
     do {                                         \

@@ -1101,11 +1101,26 @@ int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double
     int st;
     double2 *dH = (double2 *)dg_out(ctx, hk, (size_t)nk * ne * sizeof(double2), flags, "io.hk", &st);
     if (st) return st;
-    dim3 grid(dg_ceil_div(nk, HK_KB), dg_ceil_div(ne, HK_EB));
-    k_hk<<<grid, HK_KB * HK_EB, 0, ctx->stream>>>(nk, (int)Rl.size(), ne, kx, ky, kz, dR, dT, dH);
-    DG_LAUNCH(ctx, "k_hk");
+    if (flags & DMFTGPU_MIXED) {
+        // split precision on the tensor cores (hk_tc.cu); the phase image is keyed by the mesh and the R list
+        std::string key = std::to_string(kx) + "x" + std::to_string(ky) + "x" + std::to_string(kz) + ":";
+        unsigned long long h = 1469598103934665603ull;
+        for (int v : Rv) h = (h ^ (unsigned long long)(unsigned)v) * 1099511628211ull;
+        key += std::to_string(Rl.size()) + ":" + std::to_string(h);
+        DG_TRY(dg_status_reset(ctx));
+        DG_TRY(dg_hk_tensor(ctx, n, (int)Rl.size(), dR, dT, kx, ky, kz, dH, key));
+    } else {
+        dim3 grid(dg_ceil_div(nk, HK_KB), dg_ceil_div(ne, HK_EB));
+        k_hk<<<grid, HK_KB * HK_EB, 0, ctx->stream>>>(nk, (int)Rl.size(), ne, kx, ky, kz, dR, dT, dH);
+        DG_LAUNCH(ctx, "k_hk");
+    }
     DG_TRY(dg_out_done(ctx, hk, dH, (size_t)nk * ne * sizeof(double2), flags));
     DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (flags & DMFTGPU_MIXED) {
+        int code = 0;
+        DG_TRY(dg_status_read(ctx, &code));
+        return code;
+    }
     return DMFTGPU_OK;
 }
 

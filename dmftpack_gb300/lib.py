@@ -241,8 +241,9 @@ class Context:
         return extra
 
     # ------------------------------------------------------------------ lattice stage
-    def Construct_Hk(self, n, rindex, hr, kgrid, device_out=None):
+    def Construct_Hk(self, n, rindex, hr, kgrid, device_out=None, mixed=False):
         """H(k) on the TightBinding mesh (Construct_Hk_Sk's Fourier sum); kgrid = (kx, ky, kz).
+        mixed=True computes it on the tensor cores (bf16 slices, FP64-exact level sums); the default is FP64.
         Returns (nk, n, n): numpy, or a CUDA tensor when device_out is a torch device."""
         rindex = np.ascontiguousarray(rindex, np.int32)
         hr = np.ascontiguousarray(hr, np.complex128)
@@ -257,7 +258,8 @@ class Context:
             out = np.empty((nk, n, n), np.complex128)
             ptr = out.ctypes.data
         st = self.lib.dmftgpu_hk(self.h, n, rindex.shape[0], rindex.ctypes.data_as(_ip),
-                                 hr.view(np.float64).ctypes.data_as(_dp), kx, ky, kz, _vp(ptr), self._flags(dev))
+                                 hr.view(np.float64).ctypes.data_as(_dp), kx, ky, kz, _vp(ptr),
+                                 self._flags(dev, MIXED if mixed else 0))
         self._check("dmftgpu_hk", st)
         # stored column-major per k: reinterpret
         return out.transpose(-1, -2) if dev else np.ascontiguousarray(np.swapaxes(out, -1, -2))

@@ -28,6 +28,19 @@ def test_hk_matches_oracle(ctx, orc):
     assert rel_err(Hd.cpu().numpy(), H) < 1e-13
 
 
+@pytest.mark.parametrize("case", ["t2g_p", "dp28", "soc56", "hubbard"])
+def test_hk_tensor_cores_match_oracle(ctx, orc, case):
+    """H(k) as a tcgen05 GEMM (bf16 slices, exact level sums): k counts and 2 n^2 that are not multiples of the
+    128 x 48 tile, N_R = 9 .. 729, against the FP64 oracle at the plain form's tolerance; a second call reuses
+    the cached phase image."""
+    wl = {"t2g_p": lambda: models.t2g_p(k=5, nfreq=8), "dp28": lambda: models.dp28(k=3, nfreq=8, ntau=16),
+          "soc56": lambda: models.soc56(k=3, nfreq=8), "hubbard": lambda: models.hubbard_2d(kx=11, ky=13, nfreq=8)}[case]()
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    for _ in range(2):
+        Ht = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, mixed=True)
+        assert rel_err(Ht, H) < TOL
+
+
 @pytest.mark.parametrize("green", [False, True])
 def test_moments_match_oracle(ctx, orc, green):
     wl = models.t2g_p(k=2, nfreq=200, beta=20.0)
