@@ -32,7 +32,7 @@ constexpr int TN = 48;        // real output columns per tile (MMA N)
 constexpr int KC = 64;        // K per chunk: 4 MMA steps of 16
 constexpr int NS = 5;         // slices per operand
 constexpr int NL = NS;        // levels L = 2 .. NS+1
-constexpr int TMEM_COLS = 256;  // >= NL * TN, a power of two
+constexpr int TMEM_COLS_PIPE = 512;  // two accumulator sets of NL * TN = 240 columns, a power of two
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
 // element offset in the smem image of one operand chunk: [slice][k step][row group][k group][8 rows][8 elems]
@@ -124,94 +124,165 @@ __global__ void k_hk_hop_img(int nR, int ne, int nchunk, const double2 *__restri
     }
 }
 
-// one (128 k points) x (48 real columns) tile of H(k): per K chunk, load both slice images into shared memory,
-// one thread issues the 4 x 15 MMAs into the five level accumulators, every thread then drains its lane (k point)
-__global__ void __launch_bounds__(128) k_hk_tc(int nk, int ne, int nchunk, const __nv_bfloat16 *__restrict__ Aimg,
-                                               const __nv_bfloat16 *__restrict__ Bimg, const double *__restrict__ g,
-                                               double2 *__restrict__ hk, int *status) {
+// double-float helpers for the drain (FP32 pipe): a + b with b a float, and the FP64 value of hi + lo
+struct dfs {
+    float h, l;
+};
+__device__ __forceinline__ dfs dfs_add(dfs a, float b) {
+    const float s = __fadd_rn(a.h, b);
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b, bb)), a.l);
+    const float t = __fadd_rn(s, e);
+    return {t, __fsub_rn(e, __fsub_rn(t, s))};
+}
+
+constexpr int NSTAGE = 2;      // shared-memory ring of chunk images
+constexpr int GROUP = 4;       // chunks accumulated in TMEM between drains: K = 256 keeps the top levels exact
+constexpr int NBUF = 2;        // TMEM accumulator sets (NBUF * NL * TN <= 512 columns)
+constexpr uint32_t A_BYTES = (uint32_t)(img_elems(TM) * 2), B_BYTES = (uint32_t)(img_elems(TN) * 2);
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int NTHREADS = 192;  // warps 0-3: drain (TMEM lane quarters 0-3); warp 4: bulk copies; warp 5: MMA
+
+struct TcBars {
+    uint64_t full[NSTAGE], empty[NSTAGE], tfull[NBUF], tempty[NBUF];
+    uint32_t tslot;
+    int err;
+};
+// the shared error flag is written by one role and polled by the others: read it through a volatile access
+__device__ __forceinline__ bool tc_failed(TcBars *b) { return *reinterpret_cast<volatile int *>(&b->err) != 0; }
+
+// One (128 k points) x (48 real columns) tile of H(k), warp-specialised: warp 4 streams the chunk images
+// into a two-stage shared-memory ring with 1-D bulk copies (mbarrier transaction counts); warp 5 issues the
+// 4 x 15 MMAs of each chunk into one of two TMEM accumulator sets and hands a set over every GROUP chunks;
+// warps 0-3 drain a set (their lane = k point) into double-float registers while the next set fills.
+__global__ void __launch_bounds__(NTHREADS, 1) k_hk_tc(int nk, int ne, int nchunk,
+                                                      const __nv_bfloat16 *__restrict__ Aimg,
+                                                      const __nv_bfloat16 *__restrict__ Bimg,
+                                                      const double *__restrict__ g, double2 *__restrict__ hk,
+                                                      int *status) {
     extern __shared__ __align__(1024) unsigned char smraw[];
-    __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
-    __nv_bfloat16 *sB = sA + img_elems(TM);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sB + img_elems(TN));
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
-    const int warp = threadIdx.x >> 5;
-    const int mt = blockIdx.x, nt = blockIdx.y;
+    TcBars *bar = reinterpret_cast<TcBars *>(smraw + NSTAGE * STAGE_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nt = blockIdx.x, mt = blockIdx.y;  // CTAs resident together share mt: its phase tiles stay in L2
+    const int ngroup = (nchunk + GROUP - 1) / GROUP;
     if (warp == 0) {
-        tc::tmem_alloc(tslot, TMEM_COLS);
+        tc::tmem_alloc(&bar->tslot, TMEM_COLS_PIPE);
         tc::tmem_relinquish();
     }
-    if (threadIdx.x == 0) tc::mbar_init(mbar, 1);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NSTAGE; i++) {
+            tc::mbar_init(&bar->full[i], 1);
+            tc::mbar_init(&bar->empty[i], 1);
+        }
+        for (int i = 0; i < NBUF; i++) {
+            tc::mbar_init(&bar->tfull[i], 1);
+            tc::mbar_init(&bar->tempty[i], 128);
+        }
+        bar->err = 0;
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = *tslot;
-    const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
-    constexpr uint32_t IDESC = tc::idesc_bf16_f32(TM, TN);
-    const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
-    double acc[TN];
-#pragma unroll
-    for (int c = 0; c < TN; c++) acc[c] = 0.0;
-    bool ok = true;
-    int kc = 0;
-    for (; kc < nchunk; kc++) {
-        const uint4 *ga = reinterpret_cast<const uint4 *>(Aimg + ((size_t)mt * nchunk + kc) * img_elems(TM));
-        const uint4 *gb = reinterpret_cast<const uint4 *>(Bimg + ((size_t)nt * nchunk + kc) * img_elems(TN));
-        uint4 *da = reinterpret_cast<uint4 *>(sA), *db = reinterpret_cast<uint4 *>(sB);
-        for (int i = threadIdx.x; i < (int)(img_elems(TM) * 2 / 16); i += blockDim.x) da[i] = ga[i];
-        for (int i = threadIdx.x; i < (int)(img_elems(TN) * 2 / 16); i += blockDim.x) db[i] = gb[i];
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (threadIdx.x == 0) {
-            int started = 0;  // bit L: level L's accumulator has been written in this chunk
-#pragma unroll 1
-            for (int q = 0; q < 4; q++)
-#pragma unroll 1
-                for (int i = 0; i < NS; i++)
-#pragma unroll 1
-                    for (int j = 0; j < NS - i; j++) {  // level L = i + j (0-based): L <= NS - 1
-                        const int L = i + j;
-                        const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((i * 4 + q) * TM * 16 * 2), 128, 256);
-                        const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((j * 4 + q) * TN * 16 * 2), 128, 256);
-                        tc::mma_bf16(tbase + (uint32_t)(L * TN), ad, bd, IDESC, (started >> L) & 1);
-                        started |= 1 << L;
-                    }
-            tc::mma_commit(mbar);
-        }
-        // every thread waits (bounded); the CTA goes on only if all of them saw the completion
-        ok = __syncthreads_and(tc::mbar_wait(mbar, kc & 1, WAIT_LIMIT)) != 0;
-        if (!ok) break;
-        tc::fence_after_sync();
-        // drain: level L (products of slice levels summing to L + 2) weighs 2^{-8(L+2)}
-#pragma unroll
-        for (int cg = 0; cg < TN / 16; cg++) {
-#pragma unroll
-            for (int L = 0; L < NL; L++) {
-                float v[16];
-                tc::tmem_ld16(lane_addr + (uint32_t)(L * TN + cg * 16), v);
-                const double w = ldexp(1.0, -8 * (L + 2));
-#pragma unroll
-                for (int c = 0; c < 16; c++) acc[cg * 16 + c] = fma((double)v[c], w, acc[cg * 16 + c]);
+    const uint32_t tbase = bar->tslot;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int c = 0; c < nchunk; c++) {
+                const int st = c & 1;
+                if (c >= NSTAGE && !tc::mbar_wait(&bar->empty[st], ((c >> 1) - 1) & 1, WAIT_LIMIT)) {
+                    atomicExch(&bar->err, 1);
+                    break;
+                }
+                unsigned char *dst = smraw + st * STAGE_BYTES;
+                tc::mbar_arrive_expect_tx(&bar->full[st], STAGE_BYTES);
+                tc::bulk_g2s(dst, Aimg + ((size_t)mt * nchunk + c) * img_elems(TM), A_BYTES, &bar->full[st]);
+                tc::bulk_g2s(dst + A_BYTES, Bimg + ((size_t)nt * nchunk + c) * img_elems(TN), B_BYTES,
+                             &bar->full[st]);
+                issued = c + 1;
+            }
+            if (tc_failed(bar)) {
+                // let the copies already in flight land before the CTA's shared memory goes away
+                for (int c = (issued > NSTAGE ? issued - NSTAGE : 0); c < issued; c++)
+                    tc::mbar_wait(&bar->full[c & 1], (c >> 1) & 1, WAIT_LIMIT);
             }
         }
-        tc::fence_before_sync();
-        __syncthreads();
-    }
-    if (!ok) {
-        // a tensor-core completion did not arrive in time: record it, give the in-flight MMAs a bounded
-        // chance to finish, then release TMEM and leave without writing
-        if (threadIdx.x == 0) atomicMax(status, (int)DMFTGPU_CUDA_ERROR);
-        tc::mbar_wait(mbar, kc & 1, WAIT_LIMIT);
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr uint32_t IDESC = tc::idesc_bf16_f32(TM, TN);
+            for (int gi = 0; gi < ngroup && !tc_failed(bar); gi++) {
+                const int b = gi & 1;
+                if (gi >= NBUF && !tc::mbar_wait(&bar->tempty[b], ((gi >> 1) - 1) & 1, WAIT_LIMIT)) {
+                    atomicExch(&bar->err, 1);
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t acc0 = tbase + (uint32_t)(b * NL * TN);
+                int started = 0;  // bit L: level L of this set has been written in this group
+                const int c1 = min(nchunk, (gi + 1) * GROUP);
+                for (int c = gi * GROUP; c < c1; c++) {
+                    const int st = c & 1;
+                    if (!tc::mbar_wait(&bar->full[st], (c >> 1) & 1, WAIT_LIMIT)) {
+                        atomicExch(&bar->err, 1);
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const uint32_t a0 = tc::smem_u32(smraw + st * STAGE_BYTES), b0 = a0 + A_BYTES;
+#pragma unroll 1
+                    for (int q = 0; q < 4; q++)
+#pragma unroll 1
+                        for (int i = 0; i < NS; i++)
+#pragma unroll 1
+                            for (int j = 0; j < NS - i; j++) {
+                                const int L = i + j;
+                                const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((i * 4 + q) * TM * 16 * 2), 128, 256);
+                                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((j * 4 + q) * TN * 16 * 2), 128, 256);
+                                tc::mma_bf16(acc0 + (uint32_t)(L * TN), ad, bd, IDESC, (started >> L) & 1);
+                                started |= 1 << L;
+                            }
+                    tc::mma_commit(&bar->empty[st]);  // this stage's images may be overwritten once these finish
+                }
+                tc::mma_commit(&bar->tfull[b]);        // the set is complete once every MMA issued so far is
+            }
+        }
     } else {
+        // drain: level L (slice levels summing to L + 2) weighs 2^{-8(L+2)}, an exact power-of-two scaling
+        dfs acc[TN];
+#pragma unroll
+        for (int c = 0; c < TN; c++) acc[c] = {0.f, 0.f};
+        const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+        bool ok = true;
+        for (int gi = 0; gi < ngroup; gi++) {
+            const int b = gi & 1;
+            if (!tc::mbar_wait(&bar->tfull[b], (gi >> 1) & 1, WAIT_LIMIT) || tc_failed(bar)) {
+                ok = false;
+                atomicExch(&bar->err, 1);
+                break;
+            }
+            tc::fence_after_sync();
+#pragma unroll
+            for (int cg = 0; cg < TN / 16; cg++) {
+#pragma unroll
+                for (int L = 0; L < NL; L++) {
+                    float v[16];
+                    tc::tmem_ld16(lane_addr + (uint32_t)(b * NL * TN + L * TN + cg * 16), v);
+                    const float w = __int_as_float((127 - 8 * (L + 2)) << 23);  // 2^{-8(L+2)}
+#pragma unroll
+                    for (int c = 0; c < 16; c++) acc[cg * 16 + c] = dfs_add(acc[cg * 16 + c], v[c] * w);
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&bar->tempty[b]);
+        }
         const int k = mt * TM + threadIdx.x;
-        if (k < nk) {
+        if (ok && k < nk) {
 #pragma unroll
             for (int c = 0; c < TN; c += 2) {
                 const int e = (nt * TN + c) >> 1;
                 if (e < ne) {
-                    const double s = g[e];
-                    hk[(size_t)k * ne + e] = make_double2(acc[c] * s, acc[c + 1] * s);
+                    const double sc = g[e];
+                    hk[(size_t)k * ne + e] = make_double2(((double)acc[c].h + (double)acc[c].l) * sc,
+                                                          ((double)acc[c + 1].h + (double)acc[c + 1].l) * sc);
                 }
             }
         }
@@ -219,10 +290,11 @@ __global__ void __launch_bounds__(128) k_hk_tc(int nk, int ne, int nchunk, const
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (warp == 0) tc::tmem_dealloc(tbase, TMEM_COLS);
+    if (threadIdx.x == 0 && tc_failed(bar)) atomicMax(status, (int)DMFTGPU_CUDA_ERROR);
+    if (warp == 0) tc::tmem_dealloc(tbase, TMEM_COLS_PIPE);
 }
 
-size_t tc_smem_bytes() { return (img_elems(TM) + img_elems(TN)) * sizeof(__nv_bfloat16) + 16; }
+size_t tc_smem_bytes() { return (size_t)NSTAGE * STAGE_BYTES + sizeof(TcBars); }
 
 }  // namespace
 
@@ -255,7 +327,7 @@ int dg_hk_tensor(dmftgpu_ctx *ctx, int n, int nR, const int *dR, const double2 *
     DG_CUDA(cudaFuncSetAttribute(k_hk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     {
         DgTimer tm(ctx, "k_hk_tc");
-        k_hk_tc<<<dim3(nmt, nnt), 128, smem, ctx->stream>>>(nk, ne, nchunk, Aimg, Bimg, g, dH, ctx->d_status);
+        k_hk_tc<<<dim3(nnt, nmt), NTHREADS, smem, ctx->stream>>>(nk, ne, nchunk, Aimg, Bimg, g, dH, ctx->d_status);
     }
     DG_LAUNCH(ctx, "k_hk_tc");
     return DMFTGPU_OK;

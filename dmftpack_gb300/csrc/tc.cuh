@@ -63,6 +63,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// arrive on the mbarrier and raise its expected transaction byte count by `bytes` (the bulk copies that
+// complete_tx on it then finish the phase)
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+// plain arrive (count 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// ---- 1-D bulk asynchronous copy global -> shared (the TMA engine, no tensor map): both addresses 16-byte
+// aligned, size a multiple of 16 bytes; completion is signalled to the mbarrier as transaction bytes ----
+__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, uint32_t bytes, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src_gmem), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // ---- descriptors ----
 // shared-memory matrix descriptor: start address, LBO and SBO in 16-byte units, bits 46-48 = 0b001 (the
 // descriptor version of tcgen05), base offset 0, LBO mode 0, layout type 0 (no swizzle, bits 61-63)
