@@ -255,3 +255,62 @@ __device__ __forceinline__ bool warp_gj_inverse_rolled(typename Ops::C (&a)[N], 
     }
     return singular;
 }
+
+// warp_gj_inverse_rolled for lane groups of any width N that need not divide 32: the group is lanes
+// base .. base+N-1 of the warp (lane c of the group holds column c), so 32/N groups share a warp with no idle
+// padding lanes inside a group.  Every shuffle names an absolute source lane (width 32) and runs with the
+// full mask under warp-uniform control flow; lanes outside any group take part with base past the last
+// group and compute values that are never used.
+template <class Ops, int N>
+__device__ __forceinline__ bool group_gj_inverse(typename Ops::C (&a)[N], const int c, const int base) {
+    typedef typename Ops::C C;
+    typedef typename Ops::M M;
+    bool singular = false;
+    int perm[N];
+#pragma unroll 1
+    for (int j = 0; j < N; j++) {
+        M best = M(-1);
+        int pp = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const M v = Ops::mag2(a[i]);
+            if (i <= N - 1 - j && v > best) {
+                best = v;
+                pp = i;
+            }
+        }
+        pp = __shfl_sync(0xffffffffu, pp, base + j, 32);
+        best = __shfl_sync(0xffffffffu, best, base + j, 32);
+        singular |= !(best > M(0));
+        perm[j] = pp + j;
+#pragma unroll
+        for (int i = 1; i < N; i++)
+            if (i == pp) {
+                const C t = a[0];
+                a[0] = a[i];
+                a[i] = t;
+            }
+        const C piv = Ops::shfl(a[0], base + j, 32);
+        const C ipiv = Ops::rcp(piv);
+        const C t = Ops::mul(a[0], ipiv);
+        const bool is_piv_col = (c == j);
+#pragma unroll
+        for (int i = 1; i < N; i++) {
+            const C f = Ops::shfl(a[i], base + j, 32);
+            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+        }
+        a[0] = is_piv_col ? ipiv : t;
+        const C r0 = a[0];
+#pragma unroll
+        for (int i = 0; i < N - 1; i++) a[i] = a[i + 1];
+        a[N - 1] = r0;
+    }
+#pragma unroll 1
+    for (int j = N - 1; j >= 0; j--) {
+        const int p = perm[j];
+        const int src = base + ((c == j) ? p : ((c == p) ? j : c));
+#pragma unroll
+        for (int i = 0; i < N; i++) a[i] = Ops::shfl(a[i], src, 32);
+    }
+    return singular;
+}

@@ -106,8 +106,9 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
         return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: correlated block must be <= 32 spin-orbital pairs");
     cudaSetDevice(ctx->device);
     DgFtMode ftm(ctx, flags);
+    DgTensorMode tmode(ctx, flags);
     cudaStream_t s = ctx->stream;
-    const int dflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NEWTON));
+    const int dflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NEWTON | DMFTGPU_NO_TENSOR));
     double2 *dSE = (double2 *)selfe, *dW = (double2 *)weiss, *dN = (double2 *)nummat, *dG = (double2 *)gloc,
             *dGI = (double2 *)gimp;
     DgUList Ul;

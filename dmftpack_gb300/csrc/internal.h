@@ -52,6 +52,15 @@ struct dmftgpu_ctx {
     std::string graph_key;
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
     std::string hk_phase_key;         // (k mesh, R list) of the phase-slice image in workspace "hk.tc.A"
+    bool tensor = true;               // tensor-core contractions allowed in the mixed form (!DMFTGPU_NO_TENSOR)
+};
+
+// sets ctx->tensor from a call's flags for the call's duration
+struct DgTensorMode {
+    dmftgpu_ctx *ctx;
+    bool saved;
+    DgTensorMode(dmftgpu_ctx *c, int flags) : ctx(c), saved(c->tensor) { ctx->tensor = !(flags & DMFTGPU_NO_TENSOR); }
+    ~DgTensorMode() { ctx->tensor = saved; }
 };
 
 // sets ctx->ft_direct and ctx->imp_mixed from a call's flags for the call's duration

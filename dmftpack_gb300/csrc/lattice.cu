@@ -24,6 +24,7 @@
 #include "smallmat.cuh"
 #include "adjoint.cuh"
 #include "density.cuh"
+#include "trace_tc.h"
 
 namespace {
 
@@ -459,6 +460,7 @@ struct Prepared {
     double e0 = 0, de = 0, eta = 0;      // real-axis grid (S_REAL passes)
     const int *perm = nullptr;           // device orbital permutation (nullptr: identity)
     double2 *Vq = nullptr, *Uf = nullptr;  // with `vectors`: V of H_QQ [nk][m][m], U of H + m0 [nk][n][n]
+    mutable bool tc_ready = false;         // the tensor-core N(mu) pass's per-k operand images are built
 };
 
 // the per-k Schur data for a real-axis pass (no self-energy tail, no static spectrum): sig = Sigma(E) as given
@@ -764,9 +766,30 @@ int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double
     double *fs = (double *)dg_buf(ctx, "nele.fs", 2 * (size_t)P.nk * sizeof(double));
     if (!tr || !dtr || !fs) return DMFTGPU_NOMEM;
     if (explicit_inv && mixed) return dg_fail(ctx, DMFTGPU_BADARG, "nele: the explicit form is FP64 only");
-    if (explicit_inv) DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
-    else DG_TRY(run_schur(ctx, P, deriv ? (dg::S_TRACE | dg::S_DERIV) : dg::S_TRACE, mu, 1, nullptr, nullptr, tr, dtr,
-                          mixed));
+    if (explicit_inv) {
+        DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+    } else if (mixed && !deriv && ctx->tensor && !ctx->capturing && dg_trace_tc_supported(P.n, P.D)) {
+        // the pole sums on the tensor cores (trace_tc.cu)
+        DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
+        TraceTcArgs a;
+        a.H = P.H;
+        a.B = P.B;
+        a.epsQ = P.epsQ;
+        a.sig = P.sig;
+        a.eps0 = P.eps;
+        a.n = P.n;
+        a.m = P.n - P.D;
+        a.nk = P.nk;
+        a.nf2 = nf2;
+        a.D = P.D;
+        a.wgrid = 1;
+        a.beta = P.beta;
+        a.mu = mu;
+        DG_TRY(dg_trace_tc(ctx, a, &P.tc_ready, tr));
+    } else {
+        DG_TRY(run_schur(ctx, P, deriv ? (dg::S_TRACE | dg::S_DERIV) : dg::S_TRACE, mu, 1, nullptr, nullptr, tr, dtr,
+                         mixed));
+    }
     DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     k_fermi<<<dg_ceil_div(P.nk, 128), 128, 0, ctx->stream>>>(P.nk, P.n, P.D, P.beta, mu, P.eps, P.UP, nullptr, fs);
     DG_LAUNCH(ctx, "k_fermi");
@@ -1101,7 +1124,7 @@ int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double
     int st;
     double2 *dH = (double2 *)dg_out(ctx, hk, (size_t)nk * ne * sizeof(double2), flags, "io.hk", &st);
     if (st) return st;
-    if (flags & DMFTGPU_MIXED) {
+    if ((flags & DMFTGPU_MIXED) && !(flags & DMFTGPU_NO_TENSOR)) {
         // split precision on the tensor cores (hk_tc.cu); the phase image is keyed by the mesh and the R list
         std::string key = std::to_string(kx) + "x" + std::to_string(ky) + "x" + std::to_string(kz) + ":";
         unsigned long long h = 1469598103934665603ull;
@@ -1116,7 +1139,7 @@ int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double
     }
     DG_TRY(dg_out_done(ctx, hk, dH, (size_t)nk * ne * sizeof(double2), flags));
     DG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (flags & DMFTGPU_MIXED) {
+    if ((flags & DMFTGPU_MIXED) && !(flags & DMFTGPU_NO_TENSOR)) {
         int code = 0;
         DG_TRY(dg_status_read(ctx, &code));
         return code;
@@ -1382,6 +1405,7 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, c
                  double *nele, double *dnele, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !nele) return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgTensorMode tmode(ctx, flags);
     const size_t DD = (size_t)L->ncl * L->nh * L->ncl * L->nh;
     int st;
     const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);
@@ -1404,6 +1428,7 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
                       double dmu, double n_target, double *mu_out, int *n_eval, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !mu_out) return DMFTGPU_BADARG;
     cudaSetDevice(ctx->device);
+    DgTensorMode tmode(ctx, flags);
     const size_t DD = (size_t)L->ncl * L->nh * L->ncl * L->nh;
     int st;
     const double2 *dH = (const double2 *)dg_in(ctx, hk, (size_t)L->nk * L->n * L->n * sizeof(double2), flags, "io.hk_in", &st);

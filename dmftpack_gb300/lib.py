@@ -25,7 +25,7 @@ _vp = C.c_void_p
 OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
 STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
                 6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
-DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40
+DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE, NO_TENSOR = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40, 0x80
 
 # every symbol include/dmftgpu.h declares
 EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_stream", "dmftgpu_get_stream",
@@ -241,7 +241,7 @@ class Context:
         return extra
 
     # ------------------------------------------------------------------ lattice stage
-    def Construct_Hk(self, n, rindex, hr, kgrid, device_out=None, mixed=False):
+    def Construct_Hk(self, n, rindex, hr, kgrid, device_out=None, mixed=False, tensor=True):
         """H(k) on the TightBinding mesh (Construct_Hk_Sk's Fourier sum); kgrid = (kx, ky, kz).
         mixed=True computes it on the tensor cores (bf16 slices, FP64-exact level sums); the default is FP64.
         Returns (nk, n, n): numpy, or a CUDA tensor when device_out is a torch device."""
@@ -259,7 +259,7 @@ class Context:
             ptr = out.ctypes.data
         st = self.lib.dmftgpu_hk(self.h, n, rindex.shape[0], rindex.ctypes.data_as(_ip),
                                  hr.view(np.float64).ctypes.data_as(_dp), kx, ky, kz, _vp(ptr),
-                                 self._flags(dev, MIXED if mixed else 0))
+                                 self._flags(dev, (MIXED if mixed else 0) | (0 if tensor else NO_TENSOR)))
         self._check("dmftgpu_hk", st)
         # stored column-major per k: reinterpret
         return out.transpose(-1, -2) if dev else np.ascontiguousarray(np.swapaxes(out, -1, -2))
@@ -415,24 +415,28 @@ class Context:
         out = (eps, hm.result(), hi.result())
         return out + (df.result(), ev.result()) if with_df else out
 
-    def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False):
+    def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False, tensor=True):
+        """N(mu) (and dN/dmu with deriv).  In the mixed form the N(mu) pass of correlated blocks of 4 .. 10 orbitals
+        runs its pole sums on the tensor cores unless tensor=False."""
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         N, dN = C.c_double(), C.c_double()
         L = lat._c()
         st = self.lib.dmftgpu_nele(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), C.byref(N),
                                    C.byref(dN) if deriv else None,
-                                   self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)))
+                                   self._flags(dev, (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)
+                                               | (0 if tensor else NO_TENSOR)))
         self._check("dmftgpu_nele", st)
         return (N.value, dN.value) if deriv else N.value
 
-    def GreenFtn_w_adjust_mu(self, lat, H_k, SelfE_w, mu, dmu, n_target, newton=False, mixed=False, explicit=False):
+    def GreenFtn_w_adjust_mu(self, lat, H_k, SelfE_w, mu, dmu, n_target, newton=False, mixed=False, explicit=False,
+                             tensor=True):
         """Returns (mu, number of N(mu) passes)."""
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         out, ne = C.c_double(), C.c_int()
         L = lat._c()
-        fl = (NEWTON if newton else 0) | (MIXED if mixed else 0) | (EXPLICIT if explicit else 0)
+        fl = (NEWTON if newton else 0) | (MIXED if mixed else 0) | (EXPLICIT if explicit else 0) | (0 if tensor else NO_TENSOR)
         st = self.lib.dmftgpu_adjust_mu(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), float(dmu),
                                         float(n_target), C.byref(out), C.byref(ne), self._flags(dev, fl))
         self._check("dmftgpu_adjust_mu", st)
@@ -573,7 +577,7 @@ class Context:
 
     # ------------------------------------------------------------------ DMFT iteration
     def DMFT_iteration(self, lat, Hk_cm, params, iteration, selfe_cm, weiss_cm, nummat_cm, gloc_cm, mu,
-                       mixed=False, newton=False, direct=False):
+                       mixed=False, newton=False, direct=False, tensor=True):
         """One dmft_main loop iteration on device state kept in the library's column-major layout (CUDA
         tensors, updated in place: SelfEnergy_w, weiss_fieldTB, NumMatrix, G_loc).  params: dict(solver ("IPT" or
         "SC2PT"), ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype, nominal_charge, uidx, ut,
@@ -592,7 +596,8 @@ class Context:
         m = C.c_double(mu)
         res = np.zeros(5)
         L = lat._c()
-        fl = self._flags(True, (MIXED if mixed else 0) | (NEWTON if newton else 0) | (DIRECT_DFT if direct else 0))
+        fl = self._flags(True, (MIXED if mixed else 0) | (NEWTON if newton else 0) | (DIRECT_DFT if direct else 0)
+                         | (0 if tensor else NO_TENSOR))
         st = self.lib.dmftgpu_dmft_iteration(self.h, C.byref(L), _vp(Hk_cm.data_ptr()), C.byref(P), int(iteration),
                                              _vp(selfe_cm.data_ptr()), _vp(weiss_cm.data_ptr()),
                                              _vp(nummat_cm.data_ptr()), C.byref(m), _vp(gloc_cm.data_ptr()),

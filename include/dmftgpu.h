@@ -41,6 +41,8 @@ enum {
                                    reference does (default: the exact correlated-block Schur form) */
 #define DMFTGPU_GRAPH 0x20     /* dmftgpu_greenftn_w_batched: replay the batched pass as one CUDA graph */
 #define DMFTGPU_AUTOTUNE 0x40  /* dmftgpu_greenftn_w_batched: tune each Schur kernel's k chunking on first use */
+#define DMFTGPU_NO_TENSOR 0x80 /* with DMFTGPU_MIXED: keep the contractions (H(k), the N(mu) pole sums) on the
+                                  CUDA cores instead of the tensor cores */
 #define DMFTGPU_DIRECT_DFT 0x10 /* iw <-> tau transforms by the reference's direct per-point sums (default: the
                                    same sums by FFT when N_tau is a power of two <= 8192) */
 

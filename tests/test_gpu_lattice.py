@@ -185,6 +185,43 @@ def test_adjust_mu_reports_singular_inversion(ctx, newton):
 TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
 
 
+@pytest.mark.parametrize("n,D,nf", [(12, 4, 40), (16, 6, 33), (20, 8, 48), (28, 10, 64), (19, 9, 40), (40, 10, 24),
+                                    (11, 5, 16)])
+def test_nele_tensor_cores_match_oracle(ctx, orc, n, D, nf):
+    """N(mu) with the pole sums on the tensor cores (bf16 slices, exact top levels) and the inversions in
+    double-float: block widths 4 .. 10 (padded ones included), m = n - D up to 30, frequency counts that leave a
+    partial 32-frequency tile; against the FP64 oracle and the CUDA-core mixed pass."""
+    rng = np.random.default_rng(100 * n + D)
+    nk, beta = 27, 8.0
+    A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (A + np.conj(np.swapaxes(A, 1, 2))) / 3
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = np.zeros((nf, D, D), complex)
+    for d in range(D):
+        S[:, d, d] = 0.1 * d - 0.6j / (wn + 0.4)
+    S[:, 0, 1] = S[:, 1, 0] = 0.05 / (1j * wn + 1.0)
+    lat = lib.Lattice(n, nk, nf, beta, 1, D)
+    for mu in (-0.4, 0.3):
+        N = orc.nele(H, S, mu, beta, 1, D)
+        gN = ctx.GiwToNele(lat, H, S, mu, mixed=True)
+        gC = ctx.GiwToNele(lat, H, S, mu, mixed=True, tensor=False)
+        assert abs(gN - N) < TOL_MIXED * max(1.0, abs(N)), (gN, N)
+        assert abs(gN - gC) < TOL_MIXED * max(1.0, abs(N))
+
+
+def test_newton_mu_through_tensor_core_passes(ctx, orc):
+    """The mixed Newton mu search on the 28-orbital d+p model (D = 10): its secant passes run on the tensor cores;
+    the mu it returns gives the target occupation in the FP64 oracle."""
+    wl = models.dp28(k=3, nfreq=64, ntau=256, beta=10.0)
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, wl.D)
+    mu_n, ne = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, wl.n_electrons, newton=True, mixed=True)
+    assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, 1, wl.D) - wl.n_electrons) < 1e-9
+    mu_c, _ = ctx.GreenFtn_w_adjust_mu(lat, H, wl.sigma, 0.0, 1.0, wl.n_electrons, newton=True, mixed=True,
+                                       tensor=False)
+    assert abs(mu_n - mu_c) < 1e-9
+
+
 @pytest.mark.parametrize("case", list(CASES))
 def test_mixed_precision_lattice_sum(ctx, orc, case):
     wl = CASES[case]()
