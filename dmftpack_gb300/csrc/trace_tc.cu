@@ -14,10 +14,11 @@
 // FP64-level accuracy from bf16: each row is scaled by a power of two to |x| <= 1 and split into 5 slices
 // x = sum_s v_s 2^{-8s} (v_s integers, |v_1| <= 256, |v_s| <= 128 after), each stored pre-weighted
 // (v_s 2^{-8s}, exact in bf16); the dof columns likewise (per k and column).  Products of slices (i, j) carry
-// their true weight 2^{-8(i+j)}.  Level i + j = 2 (one product) and level 3 (two) accumulate exactly in their
-// own FP32 accumulators (integer sums below 2^21 in their units); the 12 products of levels >= 4 share a third
-// one, whose FP32 rounding (~2^-40 of the row x column scale) is far below the 1e-9 bar of the mixed form.  The
-// residual of 5 slices is 2^-41.  Three accumulators x NP columns stay within TMEM's 512.
+// their true weight 2^{-8(i+j)}.  Levels i + j = 2, 3 and 4 (one, two and three products) accumulate exactly in
+// their own FP32 accumulators (sums of at most 32 poles stay below 2^22 in their units); the 9 products of levels
+// >= 5 share a fourth one, whose values are below 2^-23 of the row x column scale, so its FP32 rounding adds
+// ~2^-42 of it.  (Merging level 4 as well would leave ~5e-10 of it: level 4 reaches 2^-16 of the scale.)  The
+// residual of 5 slices is 2^-41.  Four accumulators x NP columns stay within TMEM's 512.
 //
 // The D x D inversion of M and the trace run on the FP32 pipe in double-float, one frequency per group of DP
 // lanes (32/DP groups per warp, group_gj_inverse), after the drain has assembled S and R from the dofs.
@@ -64,7 +65,8 @@ struct TT {
     static constexpr int NT = NW * 32;
     static constexpr int A_EL = NS * KSTEPS * ROWS * 16;
     static constexpr int B_EL = NS * KSTEPS * NP * 16;
-    static constexpr int TMEM = pow2_at_least(3 * NP);
+    static constexpr int NACC = 4;                       // TMEM accumulators: levels 2, 3, 4 exact, >= 5 merged
+    static constexpr int TMEM = pow2_at_least(NACC * NP);
     // shared memory layout (bytes)
     static constexpr int O_A = 0;
     static constexpr int O_B = O_A + A_EL * 2;
@@ -78,7 +80,7 @@ struct TT {
     static constexpr int O_EQ = O_E0 + NE0 * 8;                        // KP float2: mu - e_l
     static constexpr int O_BAR = (O_EQ + KP * 8 + 15) / 16 * 16;       // 2 mbarriers + the TMEM slot
     static constexpr int SMEM = O_BAR + 32;
-    static_assert(3 * NP <= 512, "accumulators exceed TMEM");
+    static_assert(NACC * NP <= 512, "accumulators exceed TMEM");
     static_assert(NP <= 256 && NP % 16 == 0, "MMA N");
     static_assert(O_B % 16 == 0 && O_COL % 16 == 0 && O_BAR % 16 == 0, "alignment");
 };
@@ -173,7 +175,7 @@ struct TcKArgs {
 
 // CTA = 32 Matsubara frequencies x one chunk of k points.  Per k: stage H_PP, e_l, e0_j; build the A image
 // (w_l and w_l^2 of the 32 frequencies, sliced per row); one thread issues the bulk copy of the k's B image and the
-// 30 MMAs; warps 0-3 drain the three accumulators into the dofs of S and R (warp = channel, lane = frequency);
+// 30 MMAs; warps 0-3 drain the four accumulators into the dofs of S and R (warp = channel, lane = frequency);
 // every inversion warp forms M column by column, inverts it and adds Re[Tr M^-1 (I + R) + sum w - sum r0].
 template <int DP>
 __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        // 4. MMAs: accumulator 0 <- level 2, 1 <- level 3, 2 <- levels >= 4
+        // 4. MMAs: accumulators 0, 1, 2 <- levels 2, 3, 4; accumulator 3 <- levels >= 5
         if (tid == issuer) {
             if (tc::mbar_wait(barB, it & 1, WAIT_LIMIT)) {
                 tc::fence_after_sync();
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
                     for (int i = 0; i < NS; i++)
 #pragma unroll 1
                         for (int j = 0; j < NS - i; j++) {
-                            const int L = min(i + j, 2);
+                            const int L = min(i + j, 3);
                             const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((i * KSTEPS + q) * ROWS * 16 * 2), 128, 256);
                             const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((j * KSTEPS + q) * T::NP * 16 * 2), 128, 256);
                             tc::mma_bf16(tbase + (uint32_t)(L * T::NP), ad, bd, IDESC, (started >> L) & 1);
@@ -322,23 +324,25 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
         ok = __syncthreads_and(tc::mbar_wait(barM, it & 1, WAIT_LIMIT)) != 0;
         if (!ok) break;
         tc::fence_after_sync();
-        // 5. drain: warp = channel, lane = frequency; dof p = a0 + a1 + a2, scaled back by row and column scales
+        // 5. drain: warp = channel, lane = frequency; dof p = a0 + a1 + a2 + a3, scaled back by row and column scales
         if (warp < 4) {
             const float rs = rowsc[warp * FT + lane];
             float2 *dst = dofs + (size_t)(warp * FT + lane) * T::NDOF;
             const uint32_t la = tbase + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
             for (int qg = 0; qg < T::NP / 16; qg++) {
-                float v0[16], v1[16], v2[16];
+                float v0[16], v1[16], v2[16], v3[16];
                 tc::tmem_ld16(la + (uint32_t)(0 * T::NP + qg * 16), v0);
                 tc::tmem_ld16(la + (uint32_t)(1 * T::NP + qg * 16), v1);
                 tc::tmem_ld16(la + (uint32_t)(2 * T::NP + qg * 16), v2);
+                tc::tmem_ld16(la + (uint32_t)(3 * T::NP + qg * 16), v3);
 #pragma unroll
                 for (int cc = 0; cc < 16; cc++) {
                     const int p = qg * 16 + cc;
                     if (p < D * D) {
                         dfl s = two_sum(v0[cc], v1[cc]);
                         s = df_add(s, {v2[cc], 0.f});
+                        s = df_add(s, {v3[cc], 0.f});
                         const float sc = rs * sCol[p];
                         dst[p] = make_float2(s.h * sc, s.l * sc);
                     }
