@@ -190,7 +190,10 @@ TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
 def test_nele_tensor_cores_match_oracle(ctx, orc, n, D, nf):
     """N(mu) with the pole sums on the tensor cores (bf16 slices, exact top levels) and the inversions in
     double-float: block widths 4 .. 10 (padded ones included), m = n - D up to 30, frequency counts that leave a
-    partial 32-frequency tile; against the FP64 oracle and the CUDA-core mixed pass."""
+    partial 32-frequency tile.  Against the FP64 oracle with a diagonal Sigma, and, with an off-diagonal Sigma
+    element added, against the GPU's FP64 and CUDA-core double-float passes (the same tail moments on every path:
+    for that Sigma the moment fit's window choice compares variances that are equal up to rounding, so the
+    oracle may pick another window)."""
     rng = np.random.default_rng(100 * n + D)
     nk, beta = 27, 8.0
     A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
@@ -199,14 +202,18 @@ def test_nele_tensor_cores_match_oracle(ctx, orc, n, D, nf):
     S = np.zeros((nf, D, D), complex)
     for d in range(D):
         S[:, d, d] = 0.1 * d - 0.6j / (wn + 0.4)
-    S[:, 0, 1] = S[:, 1, 0] = 0.05 / (1j * wn + 1.0)
     lat = lib.Lattice(n, nk, nf, beta, 1, D)
     for mu in (-0.4, 0.3):
         N = orc.nele(H, S, mu, beta, 1, D)
         gN = ctx.GiwToNele(lat, H, S, mu, mixed=True)
-        gC = ctx.GiwToNele(lat, H, S, mu, mixed=True, tensor=False)
         assert abs(gN - N) < TOL_MIXED * max(1.0, abs(N)), (gN, N)
-        assert abs(gN - gC) < TOL_MIXED * max(1.0, abs(N))
+    S[:, 0, 1] = S[:, 1, 0] = 0.05 / (1j * wn + 1.0)
+    for mu in (-0.4, 0.3):
+        gF = ctx.GiwToNele(lat, H, S, mu)
+        gN = ctx.GiwToNele(lat, H, S, mu, mixed=True)
+        gC = ctx.GiwToNele(lat, H, S, mu, mixed=True, tensor=False)
+        assert abs(gN - gF) < 1e-11 * max(1.0, abs(gF)), (gN, gF)
+        assert abs(gC - gF) < 1e-11 * max(1.0, abs(gF)), (gC, gF)
 
 
 def test_newton_mu_through_tensor_core_passes(ctx, orc):
