@@ -59,6 +59,8 @@ template <int DP>
 struct TT {
     static constexpr int NP = np_of(DP);                 // MMA N: dofs padded to a multiple of 16
     static constexpr int NDOF = DP * DP;
+    static constexpr int NDS = NDOF | 1;                 // dof stride per (channel, frequency): odd in 8-byte words,
+                                                          // so 16 lanes' float2 accesses at this stride hit distinct banks
     static constexpr int GPW = 32 / DP;                  // frequency groups per warp
     static constexpr int NGW = (FT + GPW - 1) / GPW;     // inversion warps (the first 4 also drain TMEM)
     static constexpr int NW = (NGW > 4 ? NGW : 4) + 1;   // + the warp that issues the copies and the MMAs
@@ -71,8 +73,8 @@ struct TT {
     static constexpr int O_A = 0;
     static constexpr int O_B = O_A + A_EL * 2;
     static constexpr int O_COL = O_B + B_EL * 2;                       // NP floats: dof column scales of k
-    static constexpr int O_DOF = O_COL + NP * 4;                       // [4][FT][NDOF] float2 (double-float)
-    static constexpr int DOF_BYTES = 4 * FT * (NDOF > KP ? NDOF : KP) * 8;  // also the A build's [4][FT][KP]
+    static constexpr int O_DOF = O_COL + NP * 4;                       // [4][FT][NDS] float2 (double-float)
+    static constexpr int DOF_BYTES = 4 * FT * (NDS > KP ? NDS : KP) * 8;   // also the A build's [4][FT][KP]
     static constexpr int O_ROW = O_DOF + DOF_BYTES;                    // ROWS floats: row scales
     static constexpr int O_SUMW = O_ROW + ROWS * 4;                    // FT cdf: sum_l w_l
     static constexpr int O_H = O_SUMW + FT * 16;                       // DP x DP cdf: H_PP(a, c) at a + c DP
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(sm + T::O_A);
     __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(sm + T::O_B);
     float *sCol = reinterpret_cast<float *>(sm + T::O_COL);
-    float2 *dofs = reinterpret_cast<float2 *>(sm + T::O_DOF);   // [4][FT][NDOF]
+    float2 *dofs = reinterpret_cast<float2 *>(sm + T::O_DOF);   // [4][FT][NDS]
     float2 *vals = dofs;                                          // [4][FT][KP] during the A build (aliased)
     float *rowsc = reinterpret_cast<float *>(sm + T::O_ROW);
     cdf *sumw = reinterpret_cast<cdf *>(sm + T::O_SUMW);
@@ -269,17 +271,25 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
             vals[(3 * FT + ff) * KP + l] = f2_of(w2.im);
         }
         __syncthreads();
-        if (tid < ROWS) {
-            float mx = 0.f;
-            for (int l = 0; l < m; l++) mx = fmaxf(mx, fabsf(vals[tid * KP + l].x));
-            int ex = 0;
-            frexpf(mx, &ex);
-            rowsc[tid] = (mx > 0.f) ? ldexpf(1.f, ex) : 1.f;
-        } else if (tid < ROWS + FT) {
-            const int ff = tid - ROWS;
-            cdf s = Ops::zero();
-            for (int l = 0; l < m; l++) s = Ops::add(s, cdf{dfl_of(vals[ff * KP + l]), dfl_of(vals[(FT + ff) * KP + l])});
-            sumw[ff] = s;
+        // row scales and sum_l w_l, one row per warp at a time with the lanes across the poles (KP = 32 = a warp):
+        // consecutive lanes read consecutive values, and the reductions are shuffles
+        for (int row = warp; row < ROWS + FT; row += T::NW) {
+            if (row < ROWS) {
+                float mx = (lane < m) ? fabsf(vals[row * KP + lane].x) : 0.f;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                if (lane == 0) {
+                    int ex = 0;
+                    frexpf(mx, &ex);
+                    rowsc[row] = (mx > 0.f) ? ldexpf(1.f, ex) : 1.f;
+                }
+            } else {
+                const int ff = row - ROWS;
+                cdf sw = (lane < m) ? cdf{dfl_of(vals[ff * KP + lane]), dfl_of(vals[(FT + ff) * KP + lane])} : Ops::zero();
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sw = Ops::add(sw, Ops::shfl(sw, lane ^ o, 32));
+                if (lane == 0) sumw[ff] = sw;
+            }
         }
         __syncthreads();
         for (int t = tid; t < ROWS * KP; t += T::NT) {
@@ -324,13 +334,15 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
         ok = __syncthreads_and(tc::mbar_wait(barM, it & 1, WAIT_LIMIT)) != 0;
         if (!ok) break;
         tc::fence_after_sync();
-        // 5. drain: warp = channel, lane = frequency; dof p = a0 + a1 + a2 + a3, scaled back by row and column scales
-        if (warp < 4) {
-            const float rs = rowsc[warp * FT + lane];
-            float2 *dst = dofs + (size_t)(warp * FT + lane) * T::NDOF;
-            const uint32_t la = tbase + ((uint32_t)(warp * 32) << 16);
+        // 5. drain: TMEM lane quarter = channel (warp % 4), lane = frequency; the warps sharing a quarter split its
+        // column groups.  dof p = a0 + a1 + a2 + a3, scaled back by the row and column scales
+        if (warp < 4 * (T::NW / 4)) {
+            const int ch = warp & 3, part = warp >> 2, nparts = T::NW / 4;
+            const float rs = rowsc[ch * FT + lane];
+            float2 *dst = dofs + (size_t)(ch * FT + lane) * T::NDS;
+            const uint32_t la = tbase + ((uint32_t)(ch * 32) << 16);
 #pragma unroll 1
-            for (int qg = 0; qg < T::NP / 16; qg++) {
+            for (int qg = part; qg < T::NP / 16; qg += nparts) {
                 float v0[16], v1[16], v2[16], v3[16];
                 tc::tmem_ld16(la + (uint32_t)(0 * T::NP + qg * 16), v0);
                 tc::tmem_ld16(la + (uint32_t)(1 * T::NP + qg * 16), v1);
@@ -353,8 +365,8 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
         __syncthreads();
         // 6. inversion and trace (inversion warps; lanes outside a group compute unused values)
         if (warp < T::NGW) {
-            const float2 *d0 = dofs + (size_t)(0 * FT + fl) * T::NDOF, *d1 = dofs + (size_t)(1 * FT + fl) * T::NDOF;
-            const float2 *d2 = dofs + (size_t)(2 * FT + fl) * T::NDOF, *d3 = dofs + (size_t)(3 * FT + fl) * T::NDOF;
+            const float2 *d0 = dofs + (size_t)(0 * FT + fl) * T::NDS, *d1 = dofs + (size_t)(1 * FT + fl) * T::NDS;
+            const float2 *d2 = dofs + (size_t)(2 * FT + fl) * T::NDS, *d3 = dofs + (size_t)(3 * FT + fl) * T::NDS;
             cdf col[DP];
 #pragma unroll
             for (int r = 0; r < DP; r++) {
