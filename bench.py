@@ -257,6 +257,56 @@ def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
     return out
 
 
+def dmft_iteration_cfg5(ctx, dev, stream, k=16):
+    """The spec comparison on the SC2PT workload (28-orbital d+p model, 729 R vectors, 10 correlated
+    spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, beta = 40, N_freq = 4096, N_tau = 8192) on a k^3 grid: one
+    full DMFT iteration (H(k), mu search, G_loc, Delta, SCGF2 to its stopping test, Pulay) in the plain form (FP64
+    on the CUDA cores, the reference's bisection) and in the mixed form (double-float, tensor-core H(k) and N(mu)
+    pole sums, Newton mu from the derivative pass), both from the same initial TightBinding state; seconds per
+    iteration by CUDA events on the launching stream, and the mixed form's largest relative differences after the
+    iteration (G_loc, NumMatrix, Delta, Sigma, mu) from FP64 with the same Newton mu search."""
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.dp28(k=k, nfreq=4096, ntau=8192, beta=40.0)
+    D = wl.D
+    uidx, ut = models.gen_Uijkl(D, 4.0, 2.6, 0.7)
+    p = dict(solver="SC2PT", ntau=wl.ntau, n_electrons=wl.n_electrons, U=4.0, Uprime=2.6, J=0.7, mixing=0.5,
+             magnetism=0, dctype=1, nominal_charge=2.0, uidx=uidx, ut=ut, scgf_max_iter=0)
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, D)
+    tcm = lambda t: t.transpose(-1, -2).contiguous()
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    mu0, _ = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, wl.n_electrons)
+    gl0, _, nm0 = ctx.GreenFtn_w(lat, Hd, sig, mu0, with_gwhf=False)
+    we0 = ctx.Construct_hyb_delta(list(range(D)), sig, gl0, mu0, wl.beta, Hd[:, :D, :D].mean(0))
+    init = [tcm(sig), tcm(we0), tcm(nm0), tcm(gl0)]
+    out, states = {}, {}
+    for arm, mixed, newton in (("fp64_bisection", False, False), ("fp64_newton", False, True),
+                               ("mixed_tensor_newton", True, True)):
+        se, we, nm, gl = (t.clone() for t in init)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        Hk = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev, mixed=mixed)  # TightBinding's H(k)
+        mu, gi, res = ctx.DMFT_iteration(lat, tcm(Hk), p, 1, se, we, nm, gl, mu0, mixed=mixed, newton=newton)
+        e.record(stream)
+        e.synchronize()
+        out[arm] = {"s_per_iter": s.elapsed_time(e) / 1e3, "scgf2_loops": int(res[4]), "mu": mu,
+                    "residuals": {"GwRD": float(res[0]), "NumMatRD": float(res[3])}}
+        states[arm] = (se, we, nm, gl, mu)
+    # precision: the mixed form against FP64 with the same mu search (the bisection's mu differs by up to its 1e-5
+    # resolution, which would dominate the comparison)
+    a, b = states["fp64_newton"], states["mixed_tensor_newton"]
+    rel = lambda x, y: float((x - y).abs().max() / y.abs().max())
+    out["mixed_vs_fp64"] = {"G_loc": rel(b[3], a[3]), "NumMatrix": rel(b[2], a[2]), "Delta": rel(b[1], a[1]),
+                            "Sigma": rel(b[0], a[0]), "mu": abs(b[4] - a[4])}
+    out["speedup"] = out["fp64_bisection"]["s_per_iter"] / out["mixed_tensor_newton"]["s_per_iter"]
+    out["workload"] = ("SC2PT d+p model: n=28 (729 R vectors), 10 correlated spin-orbitals, Kanamori U=4 J=0.7 "
+                       "U'=2.6, k grid %dx%dx%d, beta=40, N_freq=4096, N_tau=8192; one DMFT iteration from the same "
+                       "initial state" % (k, k, k))
+    return out
+
+
 def scgf2_timing(ctx, dev, loops=4):
     """Seconds per SCGF2 loop on a seeded 10 spin-orbital impurity with the SC2PT workload's sizes (N_freq = 4096,
     N_tau = 8192, beta = 40, Kanamori U = 4, J = 0.7, U' = 2.6), FP64 and mixed (double-float getStimp)."""
@@ -652,6 +702,7 @@ def run_ours(args, rank, world, local_rank):
             variants[name] = {"value": inv_per_step / t_o, "unit": UNIT, "ms_per_step": t_o * 1e3}
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     scgf2 = None if args.no_variants else scgf2_timing(ctx, dev)
+    cfg5 = None if args.no_variants else dmft_iteration_cfg5(ctx, dev, stream, k=args.cfg5_k)
     if rank != 0:
         return
     # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
@@ -696,7 +747,7 @@ def run_ours(args, rank, world, local_rank):
                           l2="1 GiB buffer written between timed steps", replicas=world),
            "variants": variants, "vs_reference_same_algorithm": same_alg, "peaks": peaks,
            "error_vs_fp64": err, "dmft_iteration": dmft_iter,
-           "scgf2_loop": scgf2,
+           "scgf2_loop": scgf2, "dmft_iteration_cfg5": cfg5,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
                    "timing": "host clock around the C-ABI call with pinned host buffers, %d steps, the same L2 "
@@ -726,6 +777,7 @@ def main():
     ap.add_argument("--algo", default="schur", choices=["schur", "explicit"],
                     help="schur: exact correlated-block form (default); explicit: full n x n inversion per (k, iw)")
     ap.add_argument("--no-variants", action="store_true", help="skip the side measurement of the other algorithm")
+    ap.add_argument("--cfg5-k", type=int, default=16, help="k grid (k^3) of the SC2PT DMFT-iteration comparison")
     ap.add_argument("--clocks-out", default=None, help="CSV file for the nvidia-smi samples of the timed region")
     ap.add_argument("--case", default=None, choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint",
                                                      "downfold", "density", "hk"],

@@ -176,11 +176,13 @@ __device__ __forceinline__ bool warp_gj_inverse_t(typename Ops::C (&a)[N], const
         const C ipiv = Ops::rcp(piv);
         const C t = Ops::mul(a[j], ipiv);
         const bool is_piv_col = (c == j);
+        // the pivot column's entries become -f ipiv = fms(f, ipiv, 0): one fms per entry on every lane
+        const C tu = is_piv_col ? ipiv : t;
 #pragma unroll
         for (int i = 0; i < N; i++) {
             if (i == j) continue;
             const C f = Ops::shfl(a[i], j, W);
-            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+            a[i] = Ops::fms(f, tu, is_piv_col ? Ops::zero() : a[i]);
         }
         a[j] = is_piv_col ? ipiv : t;
     }
@@ -234,10 +236,11 @@ __device__ __forceinline__ bool warp_gj_inverse_rolled(typename Ops::C (&a)[N], 
         const C ipiv = Ops::rcp(piv);
         const C t = Ops::mul(a[0], ipiv);
         const bool is_piv_col = (c == j);
+        const C tu = is_piv_col ? ipiv : t;  // the pivot column's entries become fms(f, ipiv, 0) = -f ipiv
 #pragma unroll
         for (int i = 1; i < N; i++) {
             const C f = Ops::shfl(a[i], j, W);
-            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+            a[i] = Ops::fms(f, tu, is_piv_col ? Ops::zero() : a[i]);
         }
         a[0] = is_piv_col ? ipiv : t;
         // rotate: the finished pivot row moves to the end
@@ -294,10 +297,11 @@ __device__ __forceinline__ bool group_gj_inverse(typename Ops::C (&a)[N], const 
         const C ipiv = Ops::rcp(piv);
         const C t = Ops::mul(a[0], ipiv);
         const bool is_piv_col = (c == j);
+        const C tu = is_piv_col ? ipiv : t;  // the pivot column's entries become fms(f, ipiv, 0) = -f ipiv
 #pragma unroll
         for (int i = 1; i < N; i++) {
             const C f = Ops::shfl(a[i], base + j, 32);
-            a[i] = is_piv_col ? Ops::neg(Ops::mul(f, ipiv)) : Ops::fms(f, t, a[i]);
+            a[i] = Ops::fms(f, tu, is_piv_col ? Ops::zero() : a[i]);
         }
         a[0] = is_piv_col ? ipiv : t;
         const C r0 = a[0];

@@ -48,11 +48,12 @@ __device__ __forceinline__ bool warp_gj_inverse(double2 (&a)[N], const int c) {
         const double2 ipiv = crcp(piv);
         const double2 t = cmul(a[j], ipiv);  // new row-j entry of this lane's column
         const bool is_piv_col = (c == j);
+        const double2 tu = is_piv_col ? ipiv : t;  // the pivot column's entries become cfms(f, ipiv, 0) = -f ipiv
 #pragma unroll
         for (int i = 0; i < N; i++) {
             if (i == j) continue;
             const double2 f = shfl2(a[i], j, W);  // a_ij before the update (lane j's register i)
-            a[i] = is_piv_col ? cneg(cmul(f, ipiv)) : cfms(f, t, a[i]);
+            a[i] = cfms(f, tu, is_piv_col ? cmk(0.0, 0.0) : a[i]);
         }
         a[j] = is_piv_col ? ipiv : t;
     }

@@ -80,7 +80,8 @@ struct TT {
     static constexpr int O_H = O_SUMW + FT * 16;                       // DP x DP cdf: H_PP(a, c) at a + c DP
     static constexpr int O_E0 = O_H + DP * DP * 16;                    // NE0 float2: mu - e0_j
     static constexpr int O_EQ = O_E0 + NE0 * 8;                        // KP float2: mu - e_l
-    static constexpr int O_BAR = (O_EQ + KP * 8 + 15) / 16 * 16;       // 2 mbarriers + the TMEM slot
+    static constexpr int O_WF = O_EQ + KP * 8;                         // FT float2: the CTA's Matsubara frequencies
+    static constexpr int O_BAR = (O_WF + FT * 8 + 15) / 16 * 16;       // 2 mbarriers + the TMEM slot
     static constexpr int SMEM = O_BAR + 32;
     static_assert(NACC * NP <= 512, "accumulators exceed TMEM");
     static_assert(NP <= 256 && NP % 16 == 0, "MMA N");
@@ -194,6 +195,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
     cdf *hH = reinterpret_cast<cdf *>(sm + T::O_H);
     float2 *sE0 = reinterpret_cast<float2 *>(sm + T::O_E0);
     float2 *sEq = reinterpret_cast<float2 *>(sm + T::O_EQ);
+    float2 *sWf = reinterpret_cast<float2 *>(sm + T::O_WF);
     uint64_t *barB = reinterpret_cast<uint64_t *>(sm + T::O_BAR), *barM = barB + 1;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(barB + 2);
     const TraceTcArgs &a = g.a;
@@ -210,6 +212,12 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
     if (tid == 0) {
         tc::mbar_init(barB, 1);
         tc::mbar_init(barM, 1);
+    }
+    if (tid < FT) {
+        // the tile's frequencies once, as double-float (the same FP64 expression as the lane-group kernels)
+        const int ff = min(blockIdx.x * FT + tid, a.nf2 - 1);
+        const double wv = a.wgrid ? (DG_PI / a.beta + ff * ((2 * DG_PI) / a.beta)) : (DG_PI * (2. * ff + 1.) / a.beta);
+        sWf[tid] = f2_of(df_make(wv));
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -260,8 +268,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
             const int ff = t / KP, l = t % KP;
             cdf w = Ops::zero(), w2 = Ops::zero();
             if (l < m) {
-                const double wv = wfreq(min(f0 + ff, a.nf2 - 1));
-                const cdf x = {dfl_of(sEq[l]), df_make(wv)};
+                const cdf x = {dfl_of(sEq[l]), dfl_of(sWf[ff])};
                 w = Ops::rcp(x);
                 w2 = Ops::mul(w, w);
             }
