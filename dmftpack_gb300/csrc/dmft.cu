@@ -9,6 +9,7 @@
 //   TightBinding (src/TB.cpp:97-369): mu search, GreenFtn_w, Construct_hyb_delta, impurity_site_Hamiltonian
 //     (k average of the correlated block, src/downfolding.cpp:86-121)
 //   dmft_scf_check residuals (src/dmft_main.cpp:902-1014) on the in-memory G_imp and G_loc
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -83,6 +84,86 @@ __global__ void k_scf_terms(int nfreq, int d, const double2 *gimp, const double2
     nrm[n] = b;
 }
 
+// out[n] = B^H X[n] B (to_solver) or B X[n] B^H (back), n < nmat, every D x D column-major; one thread per entry
+__global__ void k_rotate(int nmat, int D, const double2 *__restrict__ B, const double2 *__restrict__ X,
+                         double2 *__restrict__ out, int to_solver) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t DD = (size_t)D * D;
+    if (t >= (long long)nmat * DD) return;
+    const int n = (int)(t / DD), e = (int)(t % DD), i = e % D, j = e / D;
+    const double2 *x = X + (size_t)n * DD;
+    double2 acc = cmk(0, 0);
+    for (int b = 0; b < D; b++) {
+        double2 xb = cmk(0, 0);  // (X B)(:, j)_a or (X B^H)(:, j)_a, contracted with row i of the left factor below
+        for (int a = 0; a < D; a++) {
+            const double2 l = to_solver ? cconj(DG_AT(B, D, a, i)) : DG_AT(B, D, i, a);  // (B^H)_ia or B_ia
+            xb = cfma(l, DG_AT(x, D, a, b), xb);
+        }
+        const double2 r = to_solver ? DG_AT(B, D, b, j) : cconj(DG_AT(B, D, j, b));  // B_bj or (B^H)_bj
+        acc = cfma(xb, r, acc);
+    }
+    out[t] = acc;
+}
+
+// Hermitian eigen-decomposition of a small matrix on the host by cyclic Jacobi rotations: eigenvalues ascending
+// (the order of Eigen's SelfAdjointEigenSolver), V column-major with a fixed gauge: each eigenvector's first
+// component of largest modulus is made real and positive.
+void host_heig(int n, std::vector<double2> A, std::vector<double> &w, std::vector<double2> &V) {
+    auto at = [&](std::vector<double2> &M, int i, int j) -> double2 & { return M[i + (size_t)j * n]; };
+    V.assign((size_t)n * n, make_double2(0, 0));
+    for (int i = 0; i < n; i++) at(V, i, i) = make_double2(1, 0);
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) off += cabs2(at(A, p, q));
+        if (off < 1e-30) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                const double2 apq = at(A, p, q);
+                const double mag = std::sqrt(cabs2(apq));
+                if (mag < 1e-300) continue;
+                const double2 ph = cmk(apq.x / mag, apq.y / mag);  // e^{i phi}
+                const double tau = (at(A, q, q).x - at(A, p, p).x) / (2 * mag);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
+                const double c = 1 / std::sqrt(1 + t * t), sn = t * c;
+                // J = [[c, s e^{i phi}], [-s e^{-i phi}, c]] on columns (p, q); A <- J^H A J, V <- V J
+                for (int k = 0; k < n; k++) {  // columns p, q of A and V
+                    const double2 akp = at(A, k, p), akq = at(A, k, q);
+                    at(A, k, p) = csub(cscale(akp, c), cscale(cmul(akq, cconj(ph)), sn));
+                    at(A, k, q) = cadd(cscale(akq, c), cscale(cmul(akp, ph), sn));
+                    const double2 vkp = at(V, k, p), vkq = at(V, k, q);
+                    at(V, k, p) = csub(cscale(vkp, c), cscale(cmul(vkq, cconj(ph)), sn));
+                    at(V, k, q) = cadd(cscale(vkq, c), cscale(cmul(vkp, ph), sn));
+                }
+                for (int k = 0; k < n; k++) {  // rows p, q of A
+                    const double2 apk = at(A, p, k), aqk = at(A, q, k);
+                    at(A, p, k) = csub(cscale(apk, c), cscale(cmul(aqk, ph), sn));
+                    at(A, q, k) = cadd(cscale(aqk, c), cscale(cmul(apk, cconj(ph)), sn));
+                }
+            }
+    }
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return at(A, x, x).x < at(A, y, y).x; });
+    w.resize(n);
+    std::vector<double2> Vs((size_t)n * n);
+    for (int j = 0; j < n; j++) {
+        w[j] = at(A, ord[j], ord[j]).x;
+        int big = 0;
+        double bm = -1;
+        for (int i = 0; i < n; i++)
+            if (cabs2(at(V, i, ord[j])) > bm * (1 + 1e-12)) {
+                bm = cabs2(at(V, i, ord[j]));
+                big = i;
+            }
+        const double2 v = at(V, big, ord[j]);
+        const double m = std::sqrt(cabs2(v));
+        const double2 g = cmk(v.x / m, -v.y / m);  // conj(v)/|v|
+        for (int i = 0; i < n; i++) Vs[i + (size_t)j * n] = cmul(at(V, i, ord[j]), g);
+    }
+    V = Vs;
+}
+
 double2 *buf2(dmftgpu_ctx *ctx, const char *name, size_t count) {
     return (double2 *)dg_buf(ctx, name, count * sizeof(double2));
 }
@@ -131,11 +212,15 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     k_himp<<<DD, 256, 0, s>>>(L->nk, L->n, D, dhartr, (const double2 *)hk, himp);
     DG_LAUNCH(ctx, "k_himp");
     {
-        const int Nh = D;  // N_peratom_HartrOrbit
-        const double averU = (Nh * p->U + Nh * (Nh - 1) * p->Uprime) / (double)(Nh * Nh);
-        const double v = averU * (p->nominal_charge - 0.5) - p->J * (p->nominal_charge / 2.0 - 0.5);
-        std::vector<double2> h(DD, make_double2(0, 0));
-        for (int i = 0; i < D; i++) h[i + i * D] = make_double2(p->dctype == DMFTGPU_DC_NOMINAL ? v : 0.0, 0.0);
+        // dc_for_dmft from the NumMatrix of the last TightBinding (the state this iteration starts from)
+        if ((p->dctype & 0xff) == DMFTGPU_DC_SIGMA0)
+            return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: sigma0 double counting needs dmftgpu_double_counting");
+        std::vector<double2> nm(DD), h(DD, make_double2(0, 0));
+        DG_CUDA(cudaMemcpyAsync(nm.data(), dN, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+        const int st = dmftgpu_double_counting(p->dctype, 1, D, p->U, p->Uprime, p->J, p->nominal_charge,
+                                               (const double *)nm.data(), nullptr, 0, (double *)h.data());
+        if (st) return dg_fail(ctx, st, "dmft_iteration: double counting");
         DG_CUDA(cudaMemcpyAsync(dc, h.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
         DG_CUDA(cudaStreamSynchronize(s));
     }
@@ -143,15 +228,51 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     k_sub<<<dg_ceil_div(DD, 64), 64, 0, s>>>(DD, himp, dc, hdc);
     DG_LAUNCH(ctx, "k_sub");
     DG_TRY(dg_status_reset(ctx));
+    // impurityBasisSwitch (proj_to_site, src/SOLVER.cpp:541-595): H_imp - DC, Delta and NumMatrix go to the solver
+    // basis B; Sigma and G_imp (w < N_freq) and the occupation come back (src/SOLVER.cpp:426-434)
+    const double2 *sH = hdc, *sW = dW, *sN = dN;
+    double2 *Bd = nullptr;
+    const int rgrid = 128;
+    if (p->basis_switch) {
+        std::vector<double2> hh(DD), d0(DD), Bh(DD);
+        DG_CUDA(cudaMemcpyAsync(hh.data(), hdc, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        DG_CUDA(cudaMemcpyAsync(d0.data(), dW, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+        DG_TRY(dmftgpu_impurity_basis(D, p->magnetism, (const double *)hh.data(), (const double *)d0.data(),
+                                      (double *)Bh.data()));
+        Bd = buf2(ctx, "dmft.basis", DD);
+        double2 *hR = buf2(ctx, "dmft.hrot", DD), *wR = buf2(ctx, "dmft.wrot", (size_t)Nf * DD);
+        double2 *nR = buf2(ctx, "dmft.nrot", DD);
+        if (!Bd || !hR || !wR || !nR) return DMFTGPU_NOMEM;
+        DG_CUDA(cudaMemcpyAsync(Bd, Bh.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, hdc, hR, 1);
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, dW, wR, 1);
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, dN, nR, 1);
+        DG_LAUNCH(ctx, "k_rotate");
+        sH = hR;
+        sW = wR;
+        sN = nR;
+    }
     int loops = 0;
     if (p->solver == DMFTGPU_SOLVER_IPT) {
-        DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, hdc, dW, dN, Ul, seimp, dGI, occ));
+        DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, sH, sW, sN, Ul, seimp, dGI, occ));
     } else {
-        // Gw_strong: the lattice G_loc of the last TightBinding call starts the SCGF2 loop
+        // Gw_strong: the lattice G_loc of the last TightBinding call starts the SCGF2 loop (as given, unrotated)
         DG_CUDA(cudaMemcpyAsync(dGI, dG, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        DG_TRY(dg_scgf2_dev(ctx, D, Nf, p->ntau, L->beta, *mu, p->mixing, hdc, dW, dGI, Ul,
+        DG_TRY(dg_scgf2_dev(ctx, D, Nf, p->ntau, L->beta, *mu, p->mixing, sH, sW, dGI, Ul,
                             p->scgf_max_iter > 0 ? p->scgf_max_iter : 2000, seimp, &loops));
-        DG_CUDA(cudaMemcpyAsync(occ, dN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_CUDA(cudaMemcpyAsync(occ, sN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    }
+    if (p->basis_switch) {
+        double2 *tmp = buf2(ctx, "dmft.rtmp", (size_t)Nf * DD);
+        if (!tmp) return DMFTGPU_NOMEM;
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, seimp, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(seimp, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, dGI, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(dGI, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, occ, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(occ, tmp, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_LAUNCH(ctx, "k_rotate");
     }
     if (p->magnetism == 0) {
         k_spin_average<<<dg_ceil_div((long long)(Nf + 6) * (D / 2), 128), 128, 0, s>>>(D, Nf + 5, seimp, occ);
@@ -211,5 +332,126 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     resid[2] = std::sqrt(GwRD_max);
     resid[3] = std::sqrt(dn) / std::sqrt(nn);
     resid[4] = loops;
+    return DMFTGPU_OK;
+}
+
+// dc_for_dmft (src/dmft_main.cpp:593-707), host arithmetic; see include/dmftgpu.h
+extern "C" int dmftgpu_double_counting(int dctype, int natoms, int nso, double U, double Uprime, double J,
+                                       double nominal_charge, const double *nummat, const double *sigma0, int initial,
+                                       double *dc) {
+    const int base = dctype & 0xff;
+    const bool uprime = (dctype & DMFTGPU_DC_UPRIME) != 0;
+    if (natoms < 1 || nso < 1 || !dc || base < DMFTGPU_DC_NONE || base > DMFTGPU_DC_SIGMA0) return DMFTGPU_BADARG;
+    const bool sigma0_step = base == DMFTGPU_DC_SIGMA0 && initial;
+    if ((base == DMFTGPU_DC_FLL || base == DMFTGPU_DC_AMF || (base == DMFTGPU_DC_SIGMA0 && !initial)) && !nummat)
+        return DMFTGPU_BADARG;
+    if (sigma0_step && !sigma0) return DMFTGPU_BADARG;
+    if ((base == DMFTGPU_DC_NOMINAL || base == DMFTGPU_DC_FLL || base == DMFTGPU_DC_SIGMA0) && (nso % 2))
+        return DMFTGPU_BADARG;  // spin-orbital pairs (i, i+1)
+    const int N = natoms * nso;
+    auto at = [&](const double *m, int i, int j) { return make_double2(m[2 * (i + (size_t)j * N)], m[2 * (i + (size_t)j * N) + 1]); };
+    std::vector<double2> out((size_t)N * N, make_double2(0, 0));
+    double averU = (nso * U + nso * (nso - 1) * Uprime) / (double)(nso * nso);
+    const double averJ = J;
+    for (int a = 0; a < natoms; a++) {
+        const int o = a * nso;
+        double up = 0, down = 0;
+        if (nummat)
+            for (int n = 0; n < nso; n += 2) {
+                up += at(nummat, o + n, o + n).x;
+                if (n + 1 < nso) down += at(nummat, o + n + 1, o + n + 1).x;
+            }
+        auto set = [&](int i, int j, double2 v) { out[(o + i) + (size_t)(o + j) * N] = v; };
+        if (sigma0_step) {
+            double tr = 0;
+            for (int i = 0; i < nso; i++) tr += at(sigma0, o + i, o + i).x;
+            const double temp = tr / nso;
+            for (int i = 0; i < nso; i++)
+                for (int j = 0; j < nso; j++) {
+                    double2 v = at(dc, o + i, o + j);
+                    if (i == j) v.x += temp;
+                    set(i, j, v);
+                }
+        } else if (base == DMFTGPU_DC_FLL || base == DMFTGPU_DC_SIGMA0) {
+            const double u = uprime ? Uprime : averU;
+            for (int i = 0; i < nso; i += 2) {
+                set(i, i, make_double2(u * (down + up - 0.5) - averJ * (up - 0.5), 0));
+                set(i + 1, i + 1, make_double2(u * (down + up - 0.5) - averJ * (down - 0.5), 0));
+            }
+        } else if (base == DMFTGPU_DC_AMF) {
+            const double n0 = (down + down) / nso;  // the reference's expression (src/dmft_main.cpp:653)
+            for (int i = 0; i < nso; i++)
+                set(i, i, make_double2(averU * n0 * (nso - 1) - averJ * n0 * (nso / 2 - 1), 0));
+        } else if (base == DMFTGPU_DC_NOMINAL) {
+            const double u = uprime ? Uprime : averU;
+            const double v = u * (nominal_charge - 0.5) - averJ * (nominal_charge / 2.0 - 0.5);
+            for (int i = 0; i < nso; i += 2) {
+                set(i, i, make_double2(v, 0));
+                set(i + 1, i + 1, make_double2(v, 0));
+            }
+        }
+    }
+    std::memcpy(dc, out.data(), out.size() * sizeof(double2));
+    return DMFTGPU_OK;
+}
+
+// proj_to_site's solver basis (src/SOLVER.cpp:541-586), host arithmetic; see include/dmftgpu.h
+extern "C" int dmftgpu_impurity_basis(int dim, int magnetism, const double *himp, const double *delta0,
+                                      double *basis) {
+    if (dim < 1 || dim > 64 || !himp || !delta0 || !basis) return DMFTGPU_BADARG;
+    const int n = dim;
+    auto H = [&](int i, int j) { return make_double2(himp[2 * (i + (size_t)j * n)], himp[2 * (i + (size_t)j * n) + 1]); };
+    auto W = [&](int i, int j) { return make_double2(delta0[2 * (i + (size_t)j * n)], delta0[2 * (i + (size_t)j * n) + 1]); };
+    std::vector<double2> B((size_t)n * n, make_double2(0, 0));
+    double imn = 0;
+    for (int e = 0; e < n * n; e++) imn += himp[2 * e + 1] * himp[2 * e + 1];
+    std::vector<double> w;
+    std::vector<double2> V;
+    if (std::sqrt(imn) < 1e-5 && (magnetism == 0 || magnetism == 1) && n % 2 == 0) {
+        // the spin-averaged real problem: Re[(Delta(iw_0) + H_imp) averaged over the spin pair, Hermitian part]
+        const int h = n / 2;
+        std::vector<double2> M((size_t)h * h);
+        for (int i = 0; i < n; i += 2)
+            for (int j = 0; j < n; j += 2)
+                M[i / 2 + (size_t)(j / 2) * h] = cscale(cadd(cadd(W(i, j), W(i + 1, j + 1)), cadd(H(i, j), H(i + 1, j + 1))), 0.5);
+        std::vector<double2> R((size_t)h * h);
+        for (int i = 0; i < h; i++)
+            for (int j = 0; j < h; j++)
+                R[i + (size_t)j * h] = make_double2(0.5 * (M[i + (size_t)j * h].x + M[j + (size_t)i * h].x), 0.0);
+        host_heig(h, R, w, V);
+        for (int i = 0; i < n; i += 2)
+            for (int j = 0; j < n; j += 2) {
+                const double v = V[i / 2 + (size_t)(j / 2) * h].x;
+                B[i + (size_t)j * n] = make_double2(v, 0);
+                B[(i + 1) + (size_t)(j + 1) * n] = make_double2(v, 0);
+            }
+    } else {
+        // eigenbasis of H_imp, then of the real part of (H_imp + the Hermitian part of Delta(iw_0)) in it
+        std::vector<double2> Hm((size_t)n * n);
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) Hm[i + (size_t)j * n] = H(i, j);
+        std::vector<double2> V1;
+        host_heig(n, Hm, w, V1);
+        std::vector<double2> X((size_t)n * n), T((size_t)n * n, make_double2(0, 0));
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++)
+                X[i + (size_t)j * n] = cadd(H(i, j), cscale(cadd(W(i, j), cconj(W(j, i))), 0.5));
+        for (int i = 0; i < n; i++)  // T = V1^H X V1, real part
+            for (int j = 0; j < n; j++) {
+                double2 acc = make_double2(0, 0);
+                for (int a = 0; a < n; a++)
+                    for (int b = 0; b < n; b++)
+                        acc = cadd(acc, cmul(cmul(cconj(V1[a + (size_t)i * n]), X[a + (size_t)b * n]), V1[b + (size_t)j * n]));
+                T[i + (size_t)j * n] = make_double2(acc.x, 0.0);
+            }
+        host_heig(n, T, w, V);
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double2 acc = make_double2(0, 0);
+                for (int a = 0; a < n; a++) acc = cadd(acc, cmul(V1[i + (size_t)a * n], make_double2(V[a + (size_t)j * n].x, 0.0)));
+                B[i + (size_t)j * n] = acc;
+            }
+    }
+    std::memcpy(basis, B.data(), B.size() * sizeof(double2));
     return DMFTGPU_OK;
 }

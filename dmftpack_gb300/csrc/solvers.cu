@@ -5,6 +5,8 @@
 //   SCGF2 (src/SCGF2_fullLoop.cpp:392-533): the self-consistent second-order (SC2PT) loop on G_imp with Pulay
 //   mixing.  The host reads back two residual norms and the status word per loop iteration (the loop's
 //   stopping test).
+//   weak_solver (src/SOLVER.cpp:72-102): the one-shot low-level solvers of the weakly correlated subspace,
+//   HF (on_shot_HF, src/SCGF2_fullLoop.cpp:218-250) and 2PT / SC2PT (SC2PT_weak, src/SCGF2_fullLoop.cpp:49-133).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -293,6 +295,78 @@ extern "C" int dmftgpu_ipt(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, doubl
     DG_TRY(dg_out_done(ctx, se_out, dSE, (nfreq + 5) * dd * sizeof(double2), flags));
     if (gimp_out) DG_TRY(dg_out_done(ctx, gimp_out, dGI, (nfreq + 5) * dd * sizeof(double2), flags));
     DG_TRY(dg_out_done(ctx, nummat_out, dNO, dd * sizeof(double2), flags));
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    return code;
+}
+
+// weak_solver on device pointers.  gw: nfreq slots (Gw_weak); gwhf: nfreq slots (GwHF_weak, read by 2PT only);
+// se_out: nfreq+5 slots (SE_out in ImgFreqFtn order).
+//   HF:     occ = getoccMat(G), F = getFockOperator(occ), Sigma^(2) = 0
+//   2PT:    as SC2PT with G0 = GwHF;  SC2PT: G0 = G
+//   (SC)2PT: occ and F from G; G0(iw) -> G0(tau) (green tail, m1 = I); Sigma^(2)(tau) = getStimp(G0(tau));
+//           Sigma^(2)(iw) = FT_t_to_w; the two tail estimates; writeResults
+int dg_weak_solver_dev(dmftgpu_ctx *ctx, int solver, int d, int nfreq, int ntau, double beta, const double2 *gw,
+                       const double2 *gwhf, const DgUList &Ul, double2 *se_out) {
+    const size_t dd = (size_t)d * d;
+    cudaStream_t s = ctx->stream;
+    double2 *G = (double2 *)dg_buf(ctx, "weak.g", (size_t)(nfreq + 4) * dd * sizeof(double2));
+    double2 *s2 = (double2 *)dg_buf(ctx, "weak.s2", (size_t)(nfreq + 3) * dd * sizeof(double2));
+    double2 *occ = (double2 *)dg_buf(ctx, "weak.occ", dd * sizeof(double2));
+    double2 *fock = (double2 *)dg_buf(ctx, "weak.fock", dd * sizeof(double2));
+    if (!G || !s2 || !occ || !fock) return DMFTGPU_NOMEM;
+    DG_CUDA(cudaMemsetAsync(G, 0, (size_t)(nfreq + 4) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemsetAsync(s2, 0, (size_t)(nfreq + 3) * dd * sizeof(double2), s));
+    DG_CUDA(cudaMemcpyAsync(G, gw, (size_t)nfreq * dd * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    k_set_identity<<<1, 32 * (int)((dd + 31) / 32), 0, s>>>(d, G + (size_t)nfreq * dd);  // Gwimp[N_freq] = I
+    DG_LAUNCH(ctx, "k_set_identity");
+    DG_TRY(dg_occ_dev(ctx, d, nfreq, beta, G, occ));
+    DG_TRY(dg_fock_dev(ctx, d, Ul, occ, fock));
+    if (solver != DMFTGPU_WEAK_HF) {
+        double2 *gt = (double2 *)dg_buf(ctx, "weak.gt", (size_t)(ntau + 1) * dd * sizeof(double2));
+        double2 *st = (double2 *)dg_buf(ctx, "weak.st", (size_t)(ntau + 1) * dd * sizeof(double2));
+        double2 *T = (double2 *)dg_buf(ctx, "weak.tail", 9 * dd * sizeof(double2));
+        double2 *Dw = (double2 *)dg_buf(ctx, "weak.Dw", (size_t)nfreq * dd * sizeof(double2));
+        if (!gt || !st || !T || !Dw) return DMFTGPU_NOMEM;
+        // FourierTransform(G0, Gt0, G0[N_freq] = I, true): the green-tail fit of G0
+        const double2 *g0 = (solver == DMFTGPU_WEAK_SC2PT) ? G : gwhf;
+        DG_TRY(dg_green_tail_dev(ctx, d, nfreq, beta, g0, T, Dw));
+        DG_TRY(dg_w2tau_tail_dev(ctx, d, nfreq, ntau, beta, T, Dw, gt));
+        DG_TRY(dg_sigma2_dev(ctx, d, ntau, beta, Ul, gt, st));
+        DG_TRY(dg_tau2w_dev(ctx, d, nfreq, ntau, beta, st, s2, true));
+    }
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 1));
+    DG_TRY(dg_estimate_asymto_dev(ctx, d, nfreq, beta, s2, 2));
+    k_write_results<<<dg_ceil_div((long long)(nfreq + 5) * dd, 128), 128, 0, s>>>(d, nfreq, s2, fock, G, se_out,
+                                                                                  nullptr);
+    DG_LAUNCH(ctx, "k_write_results");
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_weak_solver(dmftgpu_ctx *ctx, int solver, int dim, int nfreq, int ntau, double beta,
+                                   const double *gw, const double *gwhf, int nu, const int *uidx, const double *ut,
+                                   double *se_out, int flags) {
+    if (!ctx || dim < 1 || dim > 32 || nfreq < 8 || ntau < 2 || !gw || !se_out || nu < 0 || !(beta > 0) ||
+        solver < DMFTGPU_WEAK_HF || solver > DMFTGPU_WEAK_SC2PT || (solver == DMFTGPU_WEAK_2PT && !gwhf))
+        return DMFTGPU_BADARG;
+    cudaSetDevice(ctx->device);
+    DgFtMode ftm(ctx, flags);
+    const size_t dd = (size_t)dim * dim;
+    int st;
+    DgUList Ul;
+    DG_TRY(dg_ulist(ctx, dim, nu, uidx, ut, Ul));
+    const double2 *dG = (const double2 *)dg_in(ctx, gw, nfreq * dd * sizeof(double2), flags, "io.weak_g", &st);
+    if (st) return st;
+    const double2 *dGHF = nullptr;
+    if (solver == DMFTGPU_WEAK_2PT) {
+        dGHF = (const double2 *)dg_in(ctx, gwhf, nfreq * dd * sizeof(double2), flags, "io.weak_ghf", &st);
+        if (st) return st;
+    }
+    double2 *dSE = (double2 *)dg_out(ctx, se_out, (nfreq + 5) * dd * sizeof(double2), flags, "io.weak_se", &st);
+    if (st) return st;
+    DG_TRY(dg_status_reset(ctx));
+    DG_TRY(dg_weak_solver_dev(ctx, solver, dim, nfreq, ntau, beta, dG, dGHF, Ul, dSE));
+    DG_TRY(dg_out_done(ctx, se_out, dSE, (nfreq + 5) * dd * sizeof(double2), flags));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;

@@ -34,7 +34,7 @@ EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_
            "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_density_dft", "dmftgpu_upfold", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
-           "dmftgpu_hyb_delta_noalloc"]
+           "dmftgpu_hyb_delta_noalloc", "dmftgpu_weak_solver", "dmftgpu_double_counting", "dmftgpu_impurity_basis"]
 
 
 class DmftGpuError(RuntimeError):
@@ -48,7 +48,7 @@ class DmftParams(C.Structure):
     _fields_ = [("solver", C.c_int), ("ntau", C.c_int), ("n_electrons", C.c_double), ("U", C.c_double),
                 ("Uprime", C.c_double), ("J", C.c_double), ("mixing", C.c_double), ("magnetism", C.c_int),
                 ("dctype", C.c_int), ("nominal_charge", C.c_double), ("nu", C.c_int), ("uidx", _ip), ("ut", _dp),
-                ("scgf_max_iter", C.c_int)]
+                ("scgf_max_iter", C.c_int), ("basis_switch", C.c_int)]
 
 
 class _Lat(C.Structure):
@@ -119,6 +119,11 @@ def load(require_built=True):
                                   C.c_int, _ip, _dp, C.c_int, _vp, P(C.c_int), C.c_int]
     lib.dmftgpu_dmft_iteration.argtypes = [_vp, P(_Lat), _vp, P(DmftParams), C.c_int, _vp, _vp, _vp, _dp, _vp, _vp,
                                            _dp, C.c_int]
+    lib.dmftgpu_impurity_basis.argtypes = [C.c_int, C.c_int, _vp, _vp, _vp]
+    lib.dmftgpu_double_counting.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                            _vp, _vp, C.c_int, _vp]
+    lib.dmftgpu_weak_solver.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, C.c_int, _ip,
+                                        _dp, _vp, C.c_int]
     lib.dmftgpu_hyb_delta_noalloc.argtypes = [C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
                                               C.c_double, _vp, _vp]
     _lib = lib
@@ -575,6 +580,24 @@ class Context:
         self._check("dmftgpu_scgf2", st)
         return se.result(), g.result(), loops.value
 
+    WEAK_SOLVERS = {"HF": 0, "2PT": 1, "SC2PT": 2}
+
+    def weak_solver(self, solver, gw, gwhf, uidx, ut, beta, ntau, direct=False, mixed=False):
+        """weak_solver (Lowlevel_SOLVERTYPE "HF", "2PT" or "SC2PT") on Gw_weak (nfreq slots) and, for "2PT", GwHF_weak:
+        returns SE_out[nfreq+5]."""
+        dev = _is_torch(gw)
+        g = _Arr(gw, dev)
+        ghf = _Arr(gwhf, dev) if gwhf is not None else None
+        nf, d = g.obj.shape[0], g.obj.shape[1]
+        uidx, ut, nu = self._ulist(uidx, ut)
+        se = _Arr.empty((nf + 5, d, d), dev, like=g.obj)
+        st = self.lib.dmftgpu_weak_solver(self.h, self.WEAK_SOLVERS[solver], d, nf, int(ntau), float(beta), _vp(g.ptr),
+                                          _vp(ghf.ptr) if ghf else None, nu, uidx.ctypes.data_as(_ip),
+                                          ut.view(np.float64).ctypes.data_as(_dp), _vp(se.ptr),
+                                          self._flags(dev, (DIRECT_DFT if direct else 0) | (MIXED if mixed else 0)))
+        self._check("dmftgpu_weak_solver", st)
+        return se.result()
+
     # ------------------------------------------------------------------ DMFT iteration
     def DMFT_iteration(self, lat, Hk_cm, params, iteration, selfe_cm, weiss_cm, nummat_cm, gloc_cm, mu,
                        mixed=False, newton=False, direct=False, tensor=True):
@@ -591,7 +614,8 @@ class Context:
         P = DmftParams(solver, params["ntau"], params["n_electrons"], params["U"], params["Uprime"], params["J"],
                        params["mixing"], params.get("magnetism", 0), params.get("dctype", 1),
                        params.get("nominal_charge", 1.0), uidx.shape[0], uidx.ctypes.data_as(_ip),
-                       ut.view(np.float64).ctypes.data_as(_dp), params.get("scgf_max_iter", 0))
+                       ut.view(np.float64).ctypes.data_as(_dp), params.get("scgf_max_iter", 0),
+                       int(bool(params.get("basis_switch", False))))
         gimp = torch.empty((nf + 5, D, D), dtype=torch.complex128, device=selfe_cm.device)
         m = C.c_double(mu)
         res = np.zeros(5)
@@ -604,6 +628,38 @@ class Context:
                                              _vp(gimp.data_ptr()), res.ctypes.data_as(_dp), fl)
         self._check("dmftgpu_dmft_iteration", st)
         return m.value, gimp, res
+
+
+DC_NONE, DC_NOMINAL, DC_FLL, DC_AMF, DC_SIGMA0, DC_UPRIME = 0, 1, 2, 3, 4, 0x100
+
+
+def double_counting(dctype, natoms, nso, U, Uprime, J, nominal_charge, nummat=None, sigma0=None, initial=0,
+                    dc_prev=None):
+    """dc_for_dmft: the double-counting self-energy, (natoms nso) x (natoms nso) (host arithmetic; no device)."""
+    N = natoms * nso
+    cmo = lambda a: np.ascontiguousarray(np.asarray(a, np.complex128).T) if a is not None else None
+    nm, s0 = cmo(nummat), cmo(sigma0)
+    dc = cmo(dc_prev) if dc_prev is not None else np.zeros((N, N), np.complex128)
+    dc = np.ascontiguousarray(dc)
+    st = load().dmftgpu_double_counting(int(dctype), natoms, nso, float(U), float(Uprime), float(J),
+                                        float(nominal_charge), _vp(nm.ctypes.data) if nm is not None else None,
+                                        _vp(s0.ctypes.data) if s0 is not None else None, int(initial),
+                                        _vp(dc.ctypes.data))
+    if st != OK:
+        raise DmftGpuError("dmftgpu_double_counting", st)
+    return np.ascontiguousarray(dc.T)
+
+
+def impurity_basis(himp, delta0, magnetism=0):
+    """proj_to_site's solver basis (impurityBasisSwitch) for H_imp - DC and Delta(i w_0) (d x d): returns B (d x d)."""
+    d = np.asarray(himp).shape[0]
+    cmo = lambda a: np.ascontiguousarray(np.asarray(a, np.complex128).T)
+    h, w0 = cmo(himp), cmo(delta0)
+    out = np.zeros((d, d), np.complex128)
+    st = load().dmftgpu_impurity_basis(d, int(magnetism), _vp(h.ctypes.data), _vp(w0.ctypes.data), _vp(out.ctypes.data))
+    if st != OK:
+        raise DmftGpuError("dmftgpu_impurity_basis", st)
+    return np.ascontiguousarray(out.T)
 
 
 def kmesh(kx, ky, kz):

@@ -228,6 +228,37 @@ int dmftgpu_scgf2(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, d
                   const double *himp, const double *weiss, double *gimp, int nu, const int *uidx, const double *ut,
                   int max_iter, double *se_out, int *loops, int flags);
 
+/* dc_for_dmft (src/dmft_main.cpp:593-707): the double-counting self-energy of every correlated atom, host
+ * arithmetic only (no device, no context).  natoms = NumCorrAtom, nso = N_peratom_HartrOrbit; nummat, sigma0 and
+ * dc are (natoms nso) x (natoms nso) complex column-major host arrays: nummat the NumMatrix the DC is built from
+ * (NelectronDFT), sigma0 = SelfEnergy_w at the first Matsubara frequency (read by DMFTGPU_DC_SIGMA0 with
+ * initial != 0 only, may be NULL otherwise), dc: in, the previous Sw_doublecounting (SIGMA0, initial != 0); out,
+ * the new one.  initial is the reference's initial_dc (0 on the first call, 1 in the DMFT loop). */
+int dmftgpu_double_counting(int dctype, int natoms, int nso, double U, double Uprime, double J, double nominal_charge,
+                            const double *nummat, const double *sigma0, int initial, double *dc);
+
+/* proj_to_site's solver basis for impurityBasisSwitch (src/SOLVER.cpp:541-586), host arithmetic: with a real H_imp
+ * and magnetism 0 or 1, the eigenvectors of the spin-pair-averaged real symmetric Re[H_imp + Delta(i w_0)] on both
+ * spins of each pair; otherwise the eigenvectors of H_imp times those of the real part of (H_imp + the Hermitian part
+ * of Delta(i w_0)) in that basis.  himp, delta0: dim x dim (H_imp - DC and Delta(i w_0)), basis: out, all complex
+ * column-major host arrays.  Eigenvectors are ordered by ascending eigenvalue with each one's first component of
+ * largest modulus made real and positive (the reference takes Eigen's phases; for the Kanamori and density-density
+ * interactions, whose terms pair every index, a spin-pair-averaged basis gives the same self-energy whatever the
+ * phases). */
+int dmftgpu_impurity_basis(int dim, int magnetism, const double *himp, const double *delta0, double *basis);
+
+/* weak_solver (src/SOLVER.cpp:72-102, Lowlevel_SOLVERTYPE): the one-shot solver of the weakly correlated
+ * subspace (the Hartree orbitals beyond the correlated ones), run by dmft_main when NumHartrOrbit_per_cluster >
+ * NSpinOrbit_per_atom (src/dmft_main.cpp:420-454).  DMFTGPU_WEAK_HF: on_shot_HF (src/SCGF2_fullLoop.cpp:218-250),
+ * the Fock term of getoccMat(gw); DMFTGPU_WEAK_2PT / _SC2PT: SC2PT_weak (src/SCGF2_fullLoop.cpp:49-133), the Fock
+ * term plus the second-order Sigma from G0 = gwhf (2PT) or G0 = gw (SC2PT).  gw, gwhf: nfreq slots (Gw_weak,
+ * GwHF_weak; gwhf may be NULL except for 2PT); se_out[nfreq+5] in ImgFreqFtn order (writeResults). */
+#define DMFTGPU_WEAK_HF 0
+#define DMFTGPU_WEAK_2PT 1
+#define DMFTGPU_WEAK_SC2PT 2
+int dmftgpu_weak_solver(dmftgpu_ctx *ctx, int solver, int dim, int nfreq, int ntau, double beta, const double *gw,
+                        const double *gwhf, int nu, const int *uidx, const double *ut, double *se_out, int flags);
+
 /* ---------------------------------------------------------------------------------------------
  * One DMFT self-consistency iteration: the body of the loop of src/dmft_main.cpp:343-570 for one correlated
  * cluster solved by IPT (two spin-orbitals, the example model of the reference) or by SC2PT (SCGF2, up to 32
@@ -237,6 +268,12 @@ int dmftgpu_scgf2(dmftgpu_ctx *ctx, int dim, int nfreq, int ntau, double beta, d
 #define DMFTGPU_SOLVER_SC2PT 1 /* SCGF2 */
 #define DMFTGPU_DC_NONE 0
 #define DMFTGPU_DC_NOMINAL 1 /* dc_for_dmft "nominal" (src/dmft_main.cpp:665-677) */
+#define DMFTGPU_DC_FLL 2     /* "fll" (src/dmft_main.cpp:621-640): from the spin-resolved occupation of NumMatrix */
+#define DMFTGPU_DC_AMF 3     /* "amf" (src/dmft_main.cpp:641-660) */
+#define DMFTGPU_DC_SIGMA0 4  /* "sigma0" (src/dmft_main.cpp:606-618): FLL on the first call, then the previous DC
+                                plus Re Tr Sigma(i w_0) / N per atom (dmftgpu_double_counting only) */
+#define DMFTGPU_DC_UPRIME 0x100 /* with NOMINAL or FLL: U' instead of the orbital-averaged U ("nominal_Uprime",
+                                   "fll_Uprime") */
 typedef struct {
     int solver;            /* DMFTGPU_SOLVER_IPT or DMFTGPU_SOLVER_SC2PT */
     int ntau;              /* N_TAU */
@@ -244,12 +281,14 @@ typedef struct {
     double U, Uprime, J;   /* U, U', J */
     double mixing;         /* MIXING (Pulay, history 2, start 5) */
     int magnetism;         /* MAGNETISM (0: spin-averaged self-energy and occupation) */
-    int dctype;            /* DMFTGPU_DC_* */
+    int dctype;            /* DMFTGPU_DC_NONE, _NOMINAL, _FLL, _AMF, optionally | DMFTGPU_DC_UPRIME; FLL and AMF use
+                              the nummat the iteration starts from (the NumMatrix of the last TightBinding) */
     double nominal_charge; /* N_d */
     int nu;                /* U_{ijkl} list of the correlated space (gen_Uijkl), host pointers */
     const int *uidx;
     const double *ut;
     int scgf_max_iter;     /* SCGF2 loop limit (0: the reference's 2000) */
+    int basis_switch;      /* impurityBasisSwitch: solve in the basis of dmftgpu_impurity_basis (src/SOLVER.cpp:541-595) */
 } dmftgpu_dmft_params;
 
 /* SOLVER (IPT or SCGF2) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing

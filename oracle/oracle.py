@@ -425,6 +425,103 @@ def scgf2(himp, weiss, gimp_init, uidx, ut, mu, beta, ntau, mixing, max_iter=200
     return se, go, loop
 
 
+DC_NONE, DC_NOMINAL, DC_FLL, DC_AMF, DC_SIGMA0, DC_UPRIME = 0, 1, 2, 3, 4, 0x100
+
+
+def double_counting(dctype, natoms, nso, U, Up, J, nominal_charge, nummat=None, sigma0=None, initial=0, dc_prev=None):
+    """dc_for_dmft (src/dmft_main.cpp:593-707): the (natoms nso) x (natoms nso) double-counting matrix.  dctype:
+    DC_NOMINAL / DC_FLL (optionally | DC_UPRIME: averU = U'), DC_AMF, DC_SIGMA0 (with initial: the previous DC plus
+    Re Tr Sigma(i w_0) / nso per atom, :606-618; else FLL)."""
+    base, uprime = dctype & 0xFF, bool(dctype & DC_UPRIME)
+    N = natoms * nso
+    out = np.zeros((N, N), np.complex128)
+    averU = (nso * U + nso * (nso - 1) * Up) / (nso * nso)
+    for at in range(natoms):
+        o = at * nso
+        if nummat is not None:
+            up = sum(nummat[o + n, o + n].real for n in range(0, nso, 2))
+            down = sum(nummat[o + n + 1, o + n + 1].real for n in range(0, nso, 2) if n + 1 < nso)
+        if base == DC_SIGMA0 and initial:
+            temp = sum(sigma0[o + i, o + i].real for i in range(nso)) / nso
+            out[o:o + nso, o:o + nso] = dc_prev[o:o + nso, o:o + nso] + temp * np.eye(nso)
+        elif base in (DC_FLL, DC_SIGMA0):
+            u = Up if uprime else averU
+            for i in range(0, nso, 2):
+                out[o + i, o + i] = u * (down + up - 0.5) - J * (up - 0.5)
+                out[o + i + 1, o + i + 1] = u * (down + up - 0.5) - J * (down - 0.5)
+        elif base == DC_AMF:
+            n0 = (down + down) / nso  # as written at :653
+            for i in range(nso):
+                out[o + i, o + i] = averU * n0 * (nso - 1) - J * n0 * (nso // 2 - 1)
+        elif base == DC_NOMINAL:
+            u = Up if uprime else averU
+            v = u * (nominal_charge - 0.5) - J * (nominal_charge / 2.0 - 0.5)
+            for i in range(0, nso, 2):
+                out[o + i, o + i] = v
+                out[o + i + 1, o + i + 1] = v
+    return out
+
+
+def _eigh_gauged(a):
+    """numpy eigh with eigenvalues ascending and each eigenvector's first component of largest modulus made real
+    and positive."""
+    w, v = np.linalg.eigh(a)
+    for j in range(v.shape[1]):
+        mags = np.abs(v[:, j]) ** 2
+        big = 0
+        for i in range(len(mags)):
+            if mags[i] > mags[big] * (1 + 1e-12):
+                big = i
+        v[:, j] *= np.conj(v[big, j]) / abs(v[big, j])
+    return w, v
+
+
+def impurity_basis(himp, delta0, magnetism=0):
+    """proj_to_site's solver basis for impurityBasisSwitch (src/SOLVER.cpp:541-586) from H_imp - DC and
+    Delta(i w_0), with the eigenvector gauge of _eigh_gauged."""
+    n = himp.shape[0]
+    B = np.zeros((n, n), np.complex128)
+    if np.linalg.norm(himp.imag) < 1e-5 and magnetism in (0, 1) and n % 2 == 0:
+        M = 0.5 * (delta0[0::2, 0::2] + delta0[1::2, 1::2]) + 0.5 * (himp[0::2, 0::2] + himp[1::2, 1::2])
+        M = 0.5 * (M + M.conj().T)
+        _, v = _eigh_gauged(M.real.astype(np.complex128))
+        B[0::2, 0::2] = v.real
+        B[1::2, 1::2] = v.real
+    else:
+        _, V1 = _eigh_gauged(himp)
+        X = himp + 0.5 * (delta0 + delta0.conj().T)
+        T = (V1.conj().T @ X @ V1).real
+        _, v = _eigh_gauged(T.astype(np.complex128))
+        B = V1 @ v.real
+    return B
+
+
+def weak_solver(solver, gw, gwhf, uidx, ut, beta, ntau):
+    """weak_solver (src/SOLVER.cpp:72-102): "HF" is on_shot_HF (src/SCGF2_fullLoop.cpp:218-250), "2PT" / "SC2PT" is
+    SC2PT_weak (src/SCGF2_fullLoop.cpp:49-133) with G0 = gwhf / gw.  gw, gwhf: nfreq slots.  Returns
+    SE_out[nfreq+5] (writeResults, src/SCGF2_fullLoop.cpp:696-720)."""
+    nf, d = gw.shape[0], gw.shape[1]
+    eye = np.eye(d, dtype=np.complex128)
+    F = fock(occ(gw, beta), uidx, ut)
+    s2 = np.zeros((nf + 3, d, d), np.complex128)
+    if solver != "HF":
+        g0 = gw if solver == "SC2PT" else gwhf
+        gt, _ = fourier(g0, beta, ntau, True, eye)
+        st, _, stat = sigma2_tau(gt, uidx, ut, beta)
+        _check(stat, "sigma2_tau")
+        s2w, stat = tau2w(st, beta, nf)
+        _check(stat, "tau2w")
+        s2[:nf] = s2w
+    s2 = estimate_asymto(s2, nf, beta, 1)
+    s2 = estimate_asymto(s2, nf, beta, 2)
+    se = np.zeros((nf + 5, d, d), np.complex128)
+    se[:nf] = s2[:nf] + F
+    se[nf] = F
+    se[nf + 1] = s2[nf]
+    se[nf + 2] = s2[nf + 1]
+    return se
+
+
 def dmft_iteration(H, state, p, it, pulay):
     """The dmft_main loop body for one correlated cluster (the first D orbitals) with IPT (D = 2) or SC2PT
     (SCGF2) (src/dmft_main.cpp:343-570): state = dict(selfe, weiss, nummat, mu, beta, gloc, scgf_static);
@@ -433,19 +530,30 @@ def dmft_iteration(H, state, p, it, pulay):
     beta = state["beta"]
     nf, D = state["selfe"].shape[0], state["selfe"].shape[1]
     himp = H[:, :D, :D].mean(0)
-    averU = (D * p["U"] + D * (D - 1) * p["Uprime"]) / (D * D)
-    dc = (averU * (p["nominal_charge"] - 0.5) - p["J"] * (p["nominal_charge"] / 2 - 0.5)) * np.eye(D)
+    dc = double_counting(p.get("dctype", DC_NOMINAL), 1, D, p["U"], p["Uprime"], p["J"], p["nominal_charge"],
+                         nummat=state["nummat"])
     loops = 0
+    hdc, wS, nS = himp - dc, state["weiss"], state["nummat"]
+    B = None
+    if p.get("basis_switch"):
+        # impurityBasisSwitch (src/SOLVER.cpp:541-595); the results come back at w < N_freq (:426-434)
+        B = impurity_basis(hdc, state["weiss"][0], p.get("magnetism", 0))
+        hdc = B.conj().T @ hdc @ B
+        wS = B.conj().T[None] @ wS @ B[None]
+        nS = B.conj().T @ nS @ B
     if p.get("solver", "IPT") == "SC2PT":
-        se, gi, loops = scgf2(himp - dc, state["weiss"], state["gloc"], p["uidx"], p["ut"], state["mu"], beta,
+        se, gi, loops = scgf2(hdc, wS, state["gloc"], p["uidx"], p["ut"], state["mu"], beta,
                               p["ntau"], p["mixing"], max_iter=p.get("scgf_max_iter", 0) or 2000,
                               static=state.setdefault("scgf_static", {"prev": 0.0}))
-        nm = state["nummat"].copy()
+        nm = nS.copy()
     else:
-        se, gi, nm, st = ipt(himp - dc, state["weiss"], state["nummat"], p["uidx"], p["ut"], p["U"], state["mu"],
-                             beta, p["ntau"])
+        se, gi, nm, st = ipt(hdc, wS, nS, p["uidx"], p["ut"], p["U"], state["mu"], beta, p["ntau"])
         if st != 0:
             raise RuntimeError("oracle IPT status %d" % st)
+    if B is not None:
+        se[:nf] = B[None] @ se[:nf] @ B.conj().T[None]
+        gi[:nf] = B[None] @ gi[:nf] @ B.conj().T[None]
+        nm = B @ nm @ B.conj().T
     for M in list(se) + [nm]:
         for n in range(0, D, 2):
             avg = (M[n, n] + M[n + 1, n + 1]) / 2

@@ -295,3 +295,105 @@ def test_scgf2_density_density_two_orbitals(orc):
         c2.close()
     assert loops == loops_o
     assert rel_err(se, se_o) < 1e-9 and rel_err(g, g_o) < 1e-9
+
+
+@pytest.mark.parametrize("solver", ["HF", "2PT", "SC2PT"])
+@pytest.mark.parametrize("d,nfreq,ntau", [(6, 64, 256), (10, 200, 600)])
+def test_weak_solver_matches_oracle(orc, solver, d, nfreq, ntau):
+    """weak_solver (the low-level solver of the weakly correlated subspace): HF, 2PT (second order from GwHF) and
+    SC2PT (from Gw) on a Kanamori U list, FFT (power-of-two N_tau) and direct transform paths."""
+    himp, weiss, g0, uidx, ut, mu, beta, _ = _scgf_case(orc, d=d, nfreq=nfreq, seed=d + nfreq)
+    rng = np.random.default_rng(d)
+    wn = np.pi * (2 * np.arange(nfreq) + 1) / beta
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    h2 = 0.2 * (A + A.conj().T) / 2
+    ghf = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - h2[None] - weiss)
+    se_o = orc.weak_solver(solver, g0, ghf, uidx, ut, beta, ntau)
+    c2 = lib.Context(0)
+    try:
+        se = c2.weak_solver(solver, g0, ghf, uidx, ut, beta, ntau)
+    finally:
+        c2.close()
+    assert rel_err(se[:nfreq + 3], se_o[:nfreq + 3]) < 1e-10
+
+
+@pytest.mark.parametrize("dctype", ["fll", "amf", "nominal_Uprime"])
+def test_dmft_iterations_double_counting_types(orc, dctype):
+    """Three IPT iterations with the FLL, AMF and nominal-U' double counting (built from the NumMatrix each
+    iteration starts from, as dc_for_dmft is in the reference's loop) against the oracle."""
+    import torch
+    wl, H, p, state = _dmft_setup(orc)
+    p = dict(p, dctype={"fll": lib.DC_FLL, "amf": lib.DC_AMF, "nominal_Uprime": lib.DC_NOMINAL | lib.DC_UPRIME}[dctype],
+             Uprime=0.8 * p["U"])
+    dev = torch.device("cuda:0")
+    cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
+    back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
+    Hd, se, we, gl = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["gloc"])
+    nm = cm(state["nummat"][None])[0].contiguous()
+    mu_g = state["mu"]
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
+    pulay = orc.Pulay()
+    c2 = lib.Context(0)
+    try:
+        for it in range(1, 4):
+            state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
+            mu_g, gimp_g, res_g = c2.DMFT_iteration(lat, Hd, p, it, se, we, nm, gl, mu_g)
+            torch.cuda.synchronize()
+            assert abs(mu_g - state["mu"]) < 1e-12, it
+            assert rel_err(back(se), state["selfe"]) < 1e-9, it
+            assert rel_err(back(gl), gloc) < 1e-9, it
+    finally:
+        c2.close()
+
+
+@pytest.mark.parametrize("solver", ["IPT", "SC2PT"])
+def test_dmft_iterations_with_basis_switch(orc, solver):
+    """impurityBasisSwitch: the impurity problem solved in the eigenbasis of Re[H_imp + Delta(i w_0)] and rotated
+    back, IPT on the 2-spin-orbital model and SC2PT on a 4-spin-orbital block of a seeded lattice, against the oracle
+    with the same basis gauge."""
+    import torch
+    if solver == "IPT":
+        wl, H, p, state = _dmft_setup(orc)
+        D = 2
+    else:
+        rng = np.random.default_rng(12)
+        n, D, nk, nf, beta = 8, 4, 27, 48, 8.0
+        A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+        H = (A + np.conj(np.swapaxes(A, 1, 2))) / 4
+        wn = np.pi * (2 * np.arange(nf) + 1) / beta
+        sig = np.zeros((nf, D, D), complex)
+        for d in range(D):
+            sig[:, d, d] = -0.4j / (wn + 0.6)
+        uidx, ut = orc.gen_uijkl(D, 2.0, 1.4, 0.3)
+        p = dict(solver="SC2PT", ntau=4 * nf, n_electrons=4.0, U=2.0, Uprime=1.4, J=0.3, mixing=0.5, magnetism=0,
+                 dctype=1, nominal_charge=1.0, uidx=uidx, ut=ut, scgf_max_iter=30)
+        mu, _ = orc.adjust_mu(H, sig, 0.0, beta, 1, D, 4.0)
+        gloc, _, num = orc.greenftn_w(H, sig, mu, beta, 1, D)
+        weiss = orc.hyb_delta(list(range(D)), sig, gloc, H[:, :D, :D].mean(0), mu, beta)
+        state = dict(selfe=sig.copy(), weiss=weiss, nummat=num, mu=mu, beta=beta, gloc=gloc)
+
+        class W:
+            pass
+        wl = W()
+        wl.n, wl.nk, wl.nfreq, wl.beta = n, nk, nf, beta
+    p = dict(p, basis_switch=True)
+    dev = torch.device("cuda:0")
+    cm = lambda a: torch.from_numpy(np.ascontiguousarray(np.swapaxes(a, -1, -2))).to(dev)
+    back = lambda t: np.swapaxes(t.cpu().numpy(), -1, -2)
+    Hd, se, we, gl = cm(H), cm(state["selfe"]), cm(state["weiss"]), cm(state["gloc"])
+    nm = cm(state["nummat"][None])[0].contiguous()
+    mu_g = state["mu"]
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, D)
+    pulay = orc.Pulay()
+    c2 = lib.Context(0)
+    try:
+        for it in range(1, 3):
+            state, gloc, gimp, res = orc.dmft_iteration(H, state, p, it, pulay)
+            mu_g, gimp_g, res_g = c2.DMFT_iteration(lat, Hd, p, it, se, we, nm, gl, mu_g)
+            torch.cuda.synchronize()
+            assert abs(mu_g - state["mu"]) < 1e-10, it
+            assert rel_err(back(se), state["selfe"]) < 1e-9, it
+            assert rel_err(back(gl), gloc) < 1e-9, it
+            assert rel_err(back(gimp_g)[:wl.nfreq], gimp[:wl.nfreq]) < 1e-9, it
+    finally:
+        c2.close()

@@ -306,3 +306,23 @@ def test_windowed_upfold_of_the_model_fermi_density_is_the_full_fermi_density(or
     ref = orc.upfold(full, eye, eye, S, wl.kgrid, wl.rindex)
     for g_, r_ in zip(got, ref):
         assert np.abs(g_ - r_).max() < 1e-11
+
+
+def test_weak_solver_hf_is_the_fock_term(orc):
+    """on_shot_HF: Sigma = F at every frequency and in the static slot, no 1/iw tail; SC2PT adds a causal second-order
+    part whose static slot is still F."""
+    d, nf, beta = 4, 48, 8.0
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    h = 0.3 * (A + A.conj().T) / 2
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    g = np.linalg.inv(1j * wn[:, None, None] * np.eye(d)[None] - h[None])
+    uidx, ut = orc.gen_uijkl(d, 2.0, 1.4, 0.3)
+    F = orc.fock(orc.occ(g, beta), uidx, ut)
+    se = orc.weak_solver("HF", g, None, uidx, ut, beta, 192)
+    assert np.abs(se[:nf] - F[None]).max() < 1e-14 and np.abs(se[nf] - F).max() < 1e-14
+    assert np.abs(se[nf + 1:]).max() < 1e-14
+    se2 = orc.weak_solver("SC2PT", g, None, uidx, ut, beta, 192)
+    assert np.abs(se2[nf] - F).max() < 1e-14
+    # second-order part: Im Sigma^(2)(iw) <= 0 on the diagonal (causal)
+    assert (np.einsum("nii->ni", se2[:nf] - F[None]).imag <= 1e-12).all()
