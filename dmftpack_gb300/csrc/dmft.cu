@@ -284,7 +284,11 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     DG_LAUNCH(ctx, "k_se_combine");
     // ---- Pulay mixing of SelfEnergy_w (w < N_freq)
     if (!ctx->pulay) ctx->pulay = new DgPulay();
-    if (iteration <= 1) *ctx->pulay = DgPulay();
+    if (iteration <= 1) {
+        *ctx->pulay = DgPulay();  // pulayMixing(2, 5, ...) of dmft_main (src/dmft_main.cpp:342) unless set
+        if (p->pulay_history > 0) ctx->pulay->hist = p->pulay_history;
+        if (p->pulay_start > 0) ctx->pulay->start = p->pulay_start;
+    }
     DG_TRY(dg_pulay_mixing(ctx, *ctx->pulay, "pulay", (long long)Nf * DD, dSE, seout, p->mixing, iteration));
     DG_CUDA(cudaMemcpyAsync(dSE, seout, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     int code = 0;

@@ -48,7 +48,8 @@ class DmftParams(C.Structure):
     _fields_ = [("solver", C.c_int), ("ntau", C.c_int), ("n_electrons", C.c_double), ("U", C.c_double),
                 ("Uprime", C.c_double), ("J", C.c_double), ("mixing", C.c_double), ("magnetism", C.c_int),
                 ("dctype", C.c_int), ("nominal_charge", C.c_double), ("nu", C.c_int), ("uidx", _ip), ("ut", _dp),
-                ("scgf_max_iter", C.c_int), ("basis_switch", C.c_int)]
+                ("scgf_max_iter", C.c_int), ("basis_switch", C.c_int), ("pulay_history", C.c_int),
+                ("pulay_start", C.c_int)]
 
 
 class _Lat(C.Structure):
@@ -604,8 +605,8 @@ class Context:
         """One dmft_main loop iteration on device state kept in the library's column-major layout (CUDA
         tensors, updated in place: SelfEnergy_w, weiss_fieldTB, NumMatrix, G_loc).  params: dict(solver ("IPT" or
         "SC2PT"), ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype, nominal_charge, uidx, ut,
-        scgf_max_iter).  Returns (mu, gimp_cm[nfreq+5], residuals[5] = GwRD, GwRD_low, GwRD_max, NumMatRD,
-        SCGF2 loops)."""
+        scgf_max_iter, basis_switch, pulay_history, pulay_start).  Returns (mu, gimp_cm[nfreq+5], residuals[5] = GwRD,
+        GwRD_low, GwRD_max, NumMatRD, SCGF2 loops)."""
         import torch
         nf, D = lat.nfreq, lat.D
         uidx = np.ascontiguousarray(params["uidx"], np.int32).reshape(-1, 4)
@@ -615,7 +616,8 @@ class Context:
                        params["mixing"], params.get("magnetism", 0), params.get("dctype", 1),
                        params.get("nominal_charge", 1.0), uidx.shape[0], uidx.ctypes.data_as(_ip),
                        ut.view(np.float64).ctypes.data_as(_dp), params.get("scgf_max_iter", 0),
-                       int(bool(params.get("basis_switch", False))))
+                       int(bool(params.get("basis_switch", False))), int(params.get("pulay_history", 0)),
+                       int(params.get("pulay_start", 0)))
         gimp = torch.empty((nf + 5, D, D), dtype=torch.complex128, device=selfe_cm.device)
         m = C.c_double(mu)
         res = np.zeros(5)

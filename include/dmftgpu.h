@@ -289,6 +289,8 @@ typedef struct {
     const double *ut;
     int scgf_max_iter;     /* SCGF2 loop limit (0: the reference's 2000) */
     int basis_switch;      /* impurityBasisSwitch: solve in the basis of dmftgpu_impurity_basis (src/SOLVER.cpp:541-595) */
+    int pulay_history;     /* Pulay (DIIS) history of the SelfEnergy_w mixer (0: the reference's 2) */
+    int pulay_start;       /* first iteration of the DIIS step; simple mixing before it (0: the reference's 5) */
 } dmftgpu_dmft_params;
 
 /* SOLVER (IPT or SCGF2) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing
