@@ -257,6 +257,50 @@ def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
     return out
 
 
+def dmft_convergence_cfg1(ctx, dev, max_iter=40):
+    """DMFT iterations to a self-consistency residual GwRD < 1e-6 (dmft_scf_check's measure, src/dmft_main.cpp:
+    902-1014) on the single-band Hubbard workload (64x64 k, beta = 50, N_freq = 2048, N_tau = 8192, U = 2, IPT,
+    Sigma seeded U^2/(4 iw)): the plain form (FP64, the reference's bisection mu to |dmu| <= 1e-5 and its
+    pulayMixing(2, 5)) against the adjoint-driven form (double-float lattice sums, Newton mu from the derivative
+    pass, Pulay history 3 from iteration 3), both from the same initial TightBinding state, at most max_iter
+    iterations each.  The bisection's mu resolution leaves a residual floor near 7e-6 on this workload."""
+    import torch
+    from dmftpack_gb300 import lib, models
+    wl = models.hubbard_2d(kx=64, ky=64, beta=50.0, nfreq=2048, ntau=8192)
+    U = wl.extra["U"]
+    uidx, ut = models.gen_Uijkl(2, U, U, 0.0, density_density=True)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    Hcm = Hd.transpose(-1, -2).contiguous()
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, 2)
+    tcm = lambda t: t.transpose(-1, -2).contiguous()
+    sig = torch.from_numpy(wl.sigma).to(dev)
+    mu0, _ = ctx.GreenFtn_w_adjust_mu(lat, Hd, sig, 0.0, 1.0, 1.0)
+    gl0, _, nm0 = ctx.GreenFtn_w(lat, Hd, sig, mu0, with_gwhf=False)
+    we0 = ctx.Construct_hyb_delta([0, 1], sig, gl0, mu0, wl.beta, Hd[:, :2, :2].mean(0))
+    init = [tcm(sig), tcm(we0), tcm(nm0), tcm(gl0)]
+    out = {}
+    for arm, mixed, newton, hist, start in (("fp64_bisection_pulay2", False, False, 2, 5),
+                                            ("mixed_newton_pulay3", True, True, 3, 3)):
+        p = dict(ntau=wl.ntau, n_electrons=1.0, U=U, Uprime=U, J=0.0, mixing=0.5, magnetism=0, dctype=1,
+                 nominal_charge=1.0, uidx=uidx, ut=ut, pulay_history=hist, pulay_start=start)
+        se, we, nm, gl = (t.clone() for t in init)
+        mu, resid, n_conv = mu0, [], None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for it in range(1, max_iter + 1):
+            mu, _, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, gl, mu, mixed=mixed, newton=newton)
+            resid.append(float(res[0]))
+            if res[0] < 1e-6:
+                n_conv = it
+                break
+        torch.cuda.synchronize()
+        out[arm] = {"iterations_to_1e-6": n_conv, "iterations_run": len(resid), "seconds": time.perf_counter() - t0,
+                    "final_GwRD": resid[-1], "GwRD_last5": resid[-5:]}
+    out["workload"] = ("single-band Hubbard, 2D square lattice, k grid 64x64, beta=50, N_freq=2048, N_tau=8192, U=2, "
+                       "IPT, Sigma seeded U^2/(4 iw); iterations until GwRD < 1e-6 (at most %d)" % max_iter)
+    return out
+
+
 def dmft_iteration_cfg5(ctx, dev, stream, k=16):
     """The spec comparison on the SC2PT workload (28-orbital d+p model, 729 R vectors, 10 correlated
     spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, beta = 40, N_freq = 4096, N_tau = 8192) on a k^3 grid: one
@@ -703,6 +747,7 @@ def run_ours(args, rank, world, local_rank):
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     scgf2 = None if args.no_variants else scgf2_timing(ctx, dev)
     cfg5 = None if args.no_variants else dmft_iteration_cfg5(ctx, dev, stream, k=args.cfg5_k)
+    conv = None if args.no_variants else dmft_convergence_cfg1(ctx, dev)
     if rank != 0:
         return
     # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
@@ -747,7 +792,7 @@ def run_ours(args, rank, world, local_rank):
                           l2="1 GiB buffer written between timed steps", replicas=world),
            "variants": variants, "vs_reference_same_algorithm": same_alg, "peaks": peaks,
            "error_vs_fp64": err, "dmft_iteration": dmft_iter,
-           "scgf2_loop": scgf2, "dmft_iteration_cfg5": cfg5,
+           "scgf2_loop": scgf2, "dmft_iteration_cfg5": cfg5, "dmft_convergence": conv,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
                    "timing": "host clock around the C-ABI call with pinned host buffers, %d steps, the same L2 "
