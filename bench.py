@@ -750,23 +750,23 @@ def run_ours(args, rank, world, local_rank):
     conv = None if args.no_variants else dmft_convergence_cfg1(ctx, dev)
     if rank != 0:
         return
-    # roofline of the dominant kernel, counted on the arithmetic the kernel performs:
-    #   explicit: 8 n^3 real flops per (k, iw) inversion (zgetrf+zgetri convention)
-    #   schur:    8 m D^2 (Schur sum over the m = n - D ligand poles) + 2 x 8 D^3 (G and G0 blocks)
+    # roofline of the dominant kernel.  FP64 forms: the FP64 flops of the algorithm (explicit: 8 n^3 per (k, iw)
+    # inversion, the zgetrf+zgetri convention; Schur: 8 m D^2 for the pole sum + 2 x 8 D^3 for the G and G0 blocks)
+    # against cuBLAS DGEMM.  Double-float form: the FP32 flops its algorithm executes per (k, iw) point
+    # (2 FFMA + FADD + FMUL, counted once by ncu on this kernel and recorded in profiles/traffic.json: the count
+    # does not depend on the data) against cuBLAS SGEMM, both peaks measured in this run (MEASURED_PEAKS.json has
+    # only HBM and bf16 figures).
     m_ = wl.n - wl.D
-    per_unit = 8.0 * wl.n ** 3 if explicit else 8.0 * m_ * wl.D ** 2 + 16.0 * wl.D ** 3
     # algorithmic DRAM bytes of one pass: H(k) (or its Schur data) once, Sigma and the 2 D x D outputs per point
     #   (complex 16 B: b_l and H_PP per k, Sigma over the 2 N_freq points, G and G0 out; real 8 B: e_l per k)
     alg_bytes = (wl.nk * (16 * (wl.n * wl.n if explicit else m_ * wl.D + wl.D * wl.D) + (0 if explicit else 8 * m_))
                  + 16 * 3 * 2 * wl.nfreq * wl.D * wl.D)
-    # the mixed kernel runs in double-float on the FP32 pipe: its roof is the FP32 peak; both roofs are measured
     peaks = {"fp64_dgemm_tflops": fp64_peak_tflops(torch, dev), "fp32_sgemm_tflops": fp32_peak_tflops(torch, dev)}
     peak = peaks["fp32_sgemm_tflops"] if mixed else peaks["fp64_dgemm_tflops"]
-    flops = per_unit * inv_per_step
     k_avg = (k_ms / 1e3) / max(k_cnt, 1)
-    achieved = flops / k_avg / 1e12
-    # DRAM bytes of one launch of the dominant kernel, from the ncu capture of this exact workload (or null)
-    traffic, traffic_kernel = None, kname
+    per_unit = 8.0 * wl.n ** 3 if explicit else 8.0 * m_ * wl.D ** 2 + 16.0 * wl.D ** 3
+    per_unit_kind = "FP64 flops of the algorithm"
+    traffic, traffic_kernel, counts = None, kname, None
     try:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "traffic.json")) as fh:
             measured = json.load(fh)
@@ -775,8 +775,15 @@ def run_ours(args, rank, world, local_rank):
         if rec and rec["workload"] == {"n": wl.n, "D": wl.D, "nk": wl.nk, "nfreq": wl.nfreq,
                                        "precision": args.precision}:
             traffic, traffic_kernel = rec["dram_bytes_per_launch"], tname
+            counts = rec.get("fp32_per_point")
     except (OSError, ValueError, KeyError):
         pass
+    if mixed and counts:
+        per_unit = float(counts["flops"])
+        per_unit_kind = ("FP32 flops the double-float algorithm executes per (k, iw) point (2 FFMA + FADD + FMUL, "
+                         "ncu count in profiles/traffic.json)")
+    flops = per_unit * inv_per_step
+    achieved = flops / k_avg / 1e12
     cpu_v, cpu_d = cpu_rate(wl, Hd.cpu().numpy(), seconds=12.0)
     # the same algorithm on both sides: the GPU's explicit n x n inversion (the reference's method) over the CPU
     # arm; the headline ratio also carries the exact Schur-complement reformulation
@@ -800,10 +807,10 @@ def run_ours(args, rank, world, local_rank):
            "roofline": {"bound": "fp64" if not mixed else "fp32", "achieved": achieved,
                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                        "algorithmic_bytes": alg_bytes, "kernel": traffic_kernel, "kernel_ms_avg": k_avg * 1e3, "flops_per_unit": per_unit,
+                        "algorithmic_bytes": alg_bytes, "kernel": traffic_kernel, "kernel_ms_avg": k_avg * 1e3,
+                        "flops_per_unit": per_unit, "flops_counted": per_unit_kind,
                         "peak_source": ("cuBLAS DGEMM 4096^3" if not mixed else "cuBLAS SGEMM 8192^3 (no TF32)")
-                                       + " measured in this run (not in MEASURED_PEAKS.json); the flops are "
-                                         "double-float operations counted as one flop each" * bool(mixed),
+                                       + " measured in this run (MEASURED_PEAKS.json has HBM and bf16 figures only)",
                         "flops_per_launch": flops},
            "cpu_baseline": dict(cpu_d, value=cpu_v, unit=UNIT, kind="port"),
            "clocks": clk, "gpu_launches": launches}
