@@ -262,8 +262,9 @@ def dmft_convergence_cfg1(ctx, dev, max_iter=40):
     902-1014) on the single-band Hubbard workload (64x64 k, beta = 50, N_freq = 2048, N_tau = 8192, U = 2, IPT,
     Sigma seeded U^2/(4 iw)): the plain form (FP64, the reference's bisection mu to |dmu| <= 1e-5 and its
     pulayMixing(2, 5)) against the adjoint-driven form (double-float lattice sums, Newton mu from the derivative
-    pass, Pulay history 3 from iteration 3), both from the same initial TightBinding state, at most max_iter
-    iterations each.  The bisection's mu resolution leaves a residual floor near 7e-6 on this workload."""
+    pass, Pulay history 3 from iteration 3) and the same with the Newton-Krylov Sigma mixer from iteration 3
+    (Jacobian-vector products from the lattice tangent pass), all from the same initial TightBinding state, at most
+    max_iter iterations each.  The bisection's mu resolution leaves a residual floor near 7e-6 on this workload."""
     import torch
     from dmftpack_gb300 import lib, models
     wl = models.hubbard_2d(kx=64, ky=64, beta=50.0, nfreq=2048, ntau=8192)
@@ -279,23 +280,26 @@ def dmft_convergence_cfg1(ctx, dev, max_iter=40):
     we0 = ctx.Construct_hyb_delta([0, 1], sig, gl0, mu0, wl.beta, Hd[:, :2, :2].mean(0))
     init = [tcm(sig), tcm(we0), tcm(nm0), tcm(gl0)]
     out = {}
-    for arm, mixed, newton, hist, start in (("fp64_bisection_pulay2", False, False, 2, 5),
-                                            ("mixed_newton_pulay3", True, True, 3, 3)):
+    for arm, mixed, newton, hist, start, mixer in (("fp64_bisection_pulay2", False, False, 2, 5, "pulay"),
+                                                   ("mixed_newton_pulay3", True, True, 3, 3, "pulay"),
+                                                   ("mixed_newton_krylov", True, True, 3, 3, "newton_krylov")):
         p = dict(ntau=wl.ntau, n_electrons=1.0, U=U, Uprime=U, J=0.0, mixing=0.5, magnetism=0, dctype=1,
-                 nominal_charge=1.0, uidx=uidx, ut=ut, pulay_history=hist, pulay_start=start)
+                 nominal_charge=1.0, uidx=uidx, ut=ut, pulay_history=hist, pulay_start=start, mixer=mixer,
+                 newton_start=3)
         se, we, nm, gl = (t.clone() for t in init)
-        mu, resid, n_conv = mu0, [], None
+        mu, resid, n_conv, jvps = mu0, [], None, 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for it in range(1, max_iter + 1):
             mu, _, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, gl, mu, mixed=mixed, newton=newton)
+            jvps += ctx.mixer_stats()[0]
             resid.append(float(res[0]))
             if res[0] < 1e-6:
                 n_conv = it
                 break
         torch.cuda.synchronize()
         out[arm] = {"iterations_to_1e-6": n_conv, "iterations_run": len(resid), "seconds": time.perf_counter() - t0,
-                    "final_GwRD": resid[-1], "GwRD_last5": resid[-5:]}
+                    "jacobian_vector_products": jvps, "final_GwRD": resid[-1], "GwRD_last5": resid[-5:]}
     out["workload"] = ("single-band Hubbard, 2D square lattice, k grid 64x64, beta=50, N_freq=2048, N_tau=8192, U=2, "
                        "IPT, Sigma seeded U^2/(4 iw); iterations until GwRD < 1e-6 (at most %d)" % max_iter)
     return out

@@ -170,6 +170,193 @@ double2 *buf2(dmftgpu_ctx *ctx, const char *name, size_t count) {
 
 }  // namespace
 
+namespace {
+
+// What every SOLVER call of one iteration shares
+struct DmftSolve {
+    const dmftgpu_dmft_params *p;
+    int D, Nf, DD;
+    double beta;
+    const DgUList *Ul;
+    const double2 *himp;  // k average of the correlated block of H(k)
+};
+
+// SOLVER of the loop body (src/SOLVER.cpp:105-502, src/dmft_main.cpp:489-525) from (weiss, nm_in, mu): the double
+// counting from nm_in (dc_for_dmft), proj_to_site (H_imp - DC and, with basis_switch, the rotation to the solver
+// basis; the basis is computed when *basis_ready is false and reused otherwise), IPT or SCGF2 (started from gstart),
+// the rotation back, the magnetism == 0 spin average.  Outputs: seout[Nf] = SE_out - DC, gimp[Nf+5], occ (IPT's
+// occupation; nm_in for SCGF2), dc, *loops.
+int dmft_solver(dmftgpu_ctx *ctx, const DmftSolve &S, const double2 *weiss, const double2 *nm_in, double mu,
+                const double2 *gstart, double2 *seout, double2 *gimp, double2 *occ, double2 *dc, double2 *basis,
+                bool *basis_ready, int *loops) {
+    const dmftgpu_dmft_params *p = S.p;
+    const int D = S.D, Nf = S.Nf, DD = S.DD;
+    cudaStream_t s = ctx->stream;
+    double2 *hdc = buf2(ctx, "dmft.hdc", DD), *seimp = buf2(ctx, "dmft.seimp", (size_t)(Nf + 5) * DD);
+    if (!hdc || !seimp) return DMFTGPU_NOMEM;
+    {
+        // dc_for_dmft from the NumMatrix of the last TightBinding (the state this iteration starts from)
+        if ((p->dctype & 0xff) == DMFTGPU_DC_SIGMA0)
+            return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: sigma0 double counting needs dmftgpu_double_counting");
+        std::vector<double2> nm(DD), h(DD, make_double2(0, 0));
+        DG_CUDA(cudaMemcpyAsync(nm.data(), nm_in, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+        const int st = dmftgpu_double_counting(p->dctype, 1, D, p->U, p->Uprime, p->J, p->nominal_charge,
+                                               (const double *)nm.data(), nullptr, 0, (double *)h.data());
+        if (st) return dg_fail(ctx, st, "dmft_iteration: double counting");
+        DG_CUDA(cudaMemcpyAsync(dc, h.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
+        DG_CUDA(cudaStreamSynchronize(s));
+    }
+    k_sub<<<dg_ceil_div(DD, 64), 64, 0, s>>>(DD, S.himp, dc, hdc);
+    DG_LAUNCH(ctx, "k_sub");
+    // impurityBasisSwitch (proj_to_site, src/SOLVER.cpp:541-595): H_imp - DC, Delta and NumMatrix go to the solver
+    // basis B; Sigma and G_imp (w < N_freq) and the occupation come back (src/SOLVER.cpp:426-434)
+    const double2 *sH = hdc, *sW = weiss, *sN = nm_in;
+    const int rgrid = 128;
+    if (p->basis_switch) {
+        if (!*basis_ready) {
+            std::vector<double2> hh(DD), d0(DD), Bh(DD);
+            DG_CUDA(cudaMemcpyAsync(hh.data(), hdc, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            DG_CUDA(cudaMemcpyAsync(d0.data(), weiss, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            DG_CUDA(cudaStreamSynchronize(s));
+            DG_TRY(dmftgpu_impurity_basis(D, p->magnetism, (const double *)hh.data(), (const double *)d0.data(),
+                                          (double *)Bh.data()));
+            DG_CUDA(cudaMemcpyAsync(basis, Bh.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
+            *basis_ready = true;
+        }
+        double2 *hR = buf2(ctx, "dmft.hrot", DD), *wR = buf2(ctx, "dmft.wrot", (size_t)Nf * DD);
+        double2 *nR = buf2(ctx, "dmft.nrot", DD);
+        if (!hR || !wR || !nR) return DMFTGPU_NOMEM;
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, basis, hdc, hR, 1);
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, basis, weiss, wR, 1);
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, basis, nm_in, nR, 1);
+        DG_LAUNCH(ctx, "k_rotate");
+        sH = hR;
+        sW = wR;
+        sN = nR;
+    }
+    *loops = 0;
+    if (p->solver == DMFTGPU_SOLVER_IPT) {
+        DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, S.beta, p->U, mu, sH, sW, sN, *S.Ul, seimp, gimp, occ));
+    } else {
+        // Gw_strong: SCGF2 starts from gstart (the lattice G_loc of the last TightBinding call, as given, unrotated)
+        if (gstart != gimp)
+            DG_CUDA(cudaMemcpyAsync(gimp, gstart, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_scgf2_dev(ctx, D, Nf, p->ntau, S.beta, mu, p->mixing, sH, sW, gimp, *S.Ul,
+                            p->scgf_max_iter > 0 ? p->scgf_max_iter : 2000, seimp, loops));
+        DG_CUDA(cudaMemcpyAsync(occ, sN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    }
+    if (p->basis_switch) {
+        double2 *tmp = buf2(ctx, "dmft.rtmp", (size_t)Nf * DD);
+        if (!tmp) return DMFTGPU_NOMEM;
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, basis, seimp, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(seimp, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, basis, gimp, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(gimp, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, basis, occ, tmp, 0);
+        DG_CUDA(cudaMemcpyAsync(occ, tmp, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_LAUNCH(ctx, "k_rotate");
+    }
+    if (p->magnetism == 0) {
+        k_spin_average<<<dg_ceil_div((long long)(Nf + 6) * (D / 2), 128), 128, 0, s>>>(D, Nf + 5, seimp, occ);
+        DG_LAUNCH(ctx, "k_spin_average");
+    }
+    k_se_combine<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, s>>>(Nf, D, seimp, dc, seout);
+    DG_LAUNCH(ctx, "k_se_combine");
+    return DMFTGPU_OK;
+}
+
+// NumMatrix moved along a G_loc tangent: out = nm + h (1/beta) sum_{n < Nf} (dG_n + dG_n^H), the Matsubara sum's
+// first-order change without the tail beyond N_freq (one block per entry, fixed-order reduction)
+__global__ void k_nummat_tangent(int nfreq, int D, double beta, double h, const double2 *__restrict__ dG,
+                                 const double2 *__restrict__ nm, double2 *__restrict__ out) {
+    __shared__ double2 red[128];
+    const int e = blockIdx.x, a = e % D, b = e / D, DD = D * D;
+    double2 s = cmk(0, 0);
+    for (int n = threadIdx.x; n < nfreq; n += blockDim.x)
+        s = cadd(s, cadd(dG[(size_t)n * DD + a + b * D], cconj(dG[(size_t)n * DD + b + a * D])));
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + k]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[e] = cadd(nm[e], cscale(red[0], h / beta));
+}
+
+// One Newton-Krylov step of the self-energy mixer: with x = SelfEnergy_w, Phi(x) = SE_out of SOLVER on the
+// TightBinding state of x and F = Phi(x) - x, solve (J_Phi - I) dx = -F by GMRES and return x + dx in xnew.
+// J_Phi v: the lattice part exactly, by the tangent kernel (dmftgpu_gloc_jvp at fixed mu) with mu's first-order
+// change from the electron count (dN/dSigma.v by a directional difference of the N(mu) pass, dN/dmu from the
+// derivative pass); NumMatrix along the same tangent; then the small D x D stages (Construct_hyb_delta and SOLVER)
+// by a directional difference at the tangent point.  SCGF2's perturbed solves start from the unperturbed G_imp.
+int dmft_newton_step(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const DmftSolve &S, int lflags,
+                     const double2 *x, const double2 *seout0, const double2 *gimp0, const double2 *weiss,
+                     const double2 *nm, const double2 *gloc, double mu, double2 *basis, bool basis_ready,
+                     double2 *xnew, int *krylov, double *relres) {
+    const dmftgpu_dmft_params *p = S.p;
+    const int D = S.D, Nf = S.Nf, DD = S.DD;
+    const long long n = (long long)Nf * DD;
+    cudaStream_t s = ctx->stream;
+    double2 *b = buf2(ctx, "nk.b", n), *xp = buf2(ctx, "nk.xp", n), *dG = buf2(ctx, "nk.dG", n);
+    double2 *Gp = buf2(ctx, "nk.Gp", n), *Wp = buf2(ctx, "nk.Wp", n), *nmp = buf2(ctx, "nk.nmp", DD);
+    double2 *sop = buf2(ctx, "nk.sop", n), *gip = buf2(ctx, "nk.gip", (size_t)(Nf + 5) * DD);
+    double2 *occp = buf2(ctx, "nk.occp", DD), *dcp = buf2(ctx, "nk.dcp", DD), *dx = buf2(ctx, "nk.dx", n);
+    if (!b || !xp || !dG || !Gp || !Wp || !nmp || !sop || !gip || !occp || !dcp || !dx) return DMFTGPU_NOMEM;
+    // b = -F = x - Phi(x)
+    DG_CUDA(cudaMemcpyAsync(b, x, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    DG_TRY(dg_vaxpby(ctx, n, -1.0, seout0, 1.0, b));
+    double N0 = 0, dNdmu = 0, dummy = 0, xx = 0;
+    DG_TRY(dmftgpu_nele(ctx, L, hk, (const double *)x, mu, &N0, nullptr, lflags));
+    DG_TRY(dmftgpu_nele(ctx, L, hk, (const double *)x, mu, &dummy, &dNdmu, lflags));
+    if (!(dNdmu > 0)) return dg_fail(ctx, DMFTGPU_NONCONVERGED, "dmft_iteration: dN/dmu <= 0 at the Newton point");
+    DG_TRY(dg_vdot(ctx, n, x, x, &xx));
+    // directional-difference step: SCGF2's own stopping test leaves ~1e-6 of noise in its solution
+    const double eps = p->solver == DMFTGPU_SOLVER_SC2PT ? 1e-4 : 1e-6;
+    const double scgf_prev = ctx->scgf_prev_norm;
+    std::vector<int> orb(D);
+    for (int i = 0; i < D; i++) orb[i] = i;
+    auto apply = [&](const double2 *v, double2 *Av) -> int {
+        double vv = 0;
+        DG_TRY(dg_vdot(ctx, n, v, v, &vv));
+        const double h = eps * std::max(1.0, std::sqrt(xx)) / std::sqrt(vv);
+        DG_CUDA(cudaMemcpyAsync(xp, x, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_vaxpby(ctx, n, h, v, 1.0, xp));
+        double Np = 0;
+        DG_TRY(dmftgpu_nele(ctx, L, hk, (const double *)xp, mu, &Np, nullptr, lflags));
+        const double dmu = -(Np - N0) / h / dNdmu;
+        DG_TRY(dmftgpu_gloc_jvp(ctx, L, hk, (const double *)x, mu, (const double *)v, dmu, (double *)dG,
+                                DMFTGPU_DEVICE_PTRS));
+        DG_CUDA(cudaMemcpyAsync(Gp, gloc, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_vaxpby(ctx, n, h, dG, 1.0, Gp));
+        k_nummat_tangent<<<DD, 128, 0, s>>>(Nf, D, S.beta, h, dG, nm, nmp);
+        DG_LAUNCH(ctx, "k_nummat_tangent");
+        const double mup = mu + h * dmu;
+        DG_TRY(dmftgpu_hyb_delta(ctx, D, orb.data(), Nf, S.beta, D, (const double *)xp, (const double *)Gp,
+                                 (const double *)S.himp, mup, (double *)Wp, DMFTGPU_DEVICE_PTRS));
+        bool ready = basis_ready;
+        int loops = 0;
+        DG_TRY(dmft_solver(ctx, S, Wp, nmp, mup, gimp0, sop, gip, occp, dcp, basis, &ready, &loops));
+        ctx->scgf_prev_norm = scgf_prev;
+        int code = 0;
+        DG_TRY(dg_status_read(ctx, &code));
+        if (code) return code;
+        // Av = (Phi(x + h v) - Phi(x)) / h - v
+        DG_CUDA(cudaMemcpyAsync(Av, sop, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_vaxpby(ctx, n, -1.0 / h, seout0, 1.0 / h, Av));
+        DG_TRY(dg_vaxpby(ctx, n, -1.0, v, 1.0, Av));
+        return DMFTGPU_OK;
+    };
+    const int m = p->krylov_dim > 0 ? p->krylov_dim : 8;
+    const double tol = p->krylov_tol > 0 ? p->krylov_tol : 1e-3;
+    DG_TRY(dg_gmres(ctx, n, b, m, tol, apply, dx, krylov, relres));
+    DG_CUDA(cudaMemcpyAsync(xnew, x, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    DG_TRY(dg_vaxpby(ctx, n, 1.0, dx, 1.0, xnew));
+    return DMFTGPU_OK;
+}
+
+}  // namespace
+
 extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk,
                                       const dmftgpu_dmft_params *p, int iteration, double *selfe, double *weiss,
                                       double *nummat, double *mu, double *gloc, double *gimp, double *resid,
@@ -179,6 +366,10 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
     if (!(flags & DMFTGPU_DEVICE_PTRS)) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: device pointers only");
     if (p->solver != DMFTGPU_SOLVER_IPT && p->solver != DMFTGPU_SOLVER_SC2PT)
         return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: solver");
+    if (p->mixer != DMFTGPU_MIXER_PULAY && p->mixer != DMFTGPU_MIXER_NEWTON_KRYLOV)
+        return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: mixer");
+    if (p->krylov_dim < 0 || p->krylov_dim > 64 || p->krylov_tol < 0 || p->newton_start < 0)
+        return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: Newton-Krylov settings");
     const int D = L->ncl * L->nh, Nf = L->nfreq, DD = D * D;
     if (L->ncl != 1) return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: one correlated cluster");
     if (p->solver == DMFTGPU_SOLVER_IPT && D != 2)
@@ -194,12 +385,13 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
             *dGI = (double2 *)gimp;
     DgUList Ul;
     DG_TRY(dg_ulist(ctx, D, p->nu, p->uidx, p->ut, Ul));
-    double2 *himp = buf2(ctx, "dmft.himp", DD), *hdc = buf2(ctx, "dmft.hdc", DD), *dc = buf2(ctx, "dmft.dc", DD);
-    double2 *seimp = buf2(ctx, "dmft.seimp", (size_t)(Nf + 5) * DD), *seout = buf2(ctx, "dmft.seout", (size_t)Nf * DD);
+    double2 *himp = buf2(ctx, "dmft.himp", DD), *dc = buf2(ctx, "dmft.dc", DD);
+    double2 *seout = buf2(ctx, "dmft.seout", (size_t)Nf * DD);
     double2 *occ = buf2(ctx, "dmft.occ", DD), *nm_imp = buf2(ctx, "dmft.nmimp", DD);
+    double2 *basis = buf2(ctx, "dmft.basis", DD);
     double *rd = (double *)dg_buf(ctx, "dmft.rd", 2 * (size_t)Nf * sizeof(double));
     int *dhartr = (int *)dg_buf(ctx, "dmft.hartr", D * sizeof(int));
-    if (!himp || !hdc || !dc || !seimp || !seout || !occ || !nm_imp || !rd || !dhartr) return DMFTGPU_NOMEM;
+    if (!himp || !dc || !seout || !occ || !nm_imp || !basis || !rd || !dhartr) return DMFTGPU_NOMEM;
     {
         std::vector<int> h(D);
         for (int i = 0; i < D; i++) h[i] = L->hartr ? L->hartr[i] : i;
@@ -208,90 +400,54 @@ extern "C" int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *L
         DG_CUDA(cudaMemcpyAsync(dhartr, h.data(), D * sizeof(int), cudaMemcpyHostToDevice, s));
         DG_CUDA(cudaStreamSynchronize(s));
     }
-    // impurity_site_Hamiltonian (k average of H_PP) and the double counting (dc_for_dmft, nominal)
+    // impurity_site_Hamiltonian (k average of H_PP)
     k_himp<<<DD, 256, 0, s>>>(L->nk, L->n, D, dhartr, (const double2 *)hk, himp);
     DG_LAUNCH(ctx, "k_himp");
-    {
-        // dc_for_dmft from the NumMatrix of the last TightBinding (the state this iteration starts from)
-        if ((p->dctype & 0xff) == DMFTGPU_DC_SIGMA0)
-            return dg_fail(ctx, DMFTGPU_BADARG, "dmft_iteration: sigma0 double counting needs dmftgpu_double_counting");
-        std::vector<double2> nm(DD), h(DD, make_double2(0, 0));
-        DG_CUDA(cudaMemcpyAsync(nm.data(), dN, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
-        DG_CUDA(cudaStreamSynchronize(s));
-        const int st = dmftgpu_double_counting(p->dctype, 1, D, p->U, p->Uprime, p->J, p->nominal_charge,
-                                               (const double *)nm.data(), nullptr, 0, (double *)h.data());
-        if (st) return dg_fail(ctx, st, "dmft_iteration: double counting");
-        DG_CUDA(cudaMemcpyAsync(dc, h.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
-        DG_CUDA(cudaStreamSynchronize(s));
-    }
-    // ---- SOLVER: proj_to_site, IPT or SCGF2, spin average, NumMatrix
-    k_sub<<<dg_ceil_div(DD, 64), 64, 0, s>>>(DD, himp, dc, hdc);
-    DG_LAUNCH(ctx, "k_sub");
     DG_TRY(dg_status_reset(ctx));
-    // impurityBasisSwitch (proj_to_site, src/SOLVER.cpp:541-595): H_imp - DC, Delta and NumMatrix go to the solver
-    // basis B; Sigma and G_imp (w < N_freq) and the occupation come back (src/SOLVER.cpp:426-434)
-    const double2 *sH = hdc, *sW = dW, *sN = dN;
-    double2 *Bd = nullptr;
-    const int rgrid = 128;
-    if (p->basis_switch) {
-        std::vector<double2> hh(DD), d0(DD), Bh(DD);
-        DG_CUDA(cudaMemcpyAsync(hh.data(), hdc, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
-        DG_CUDA(cudaMemcpyAsync(d0.data(), dW, DD * sizeof(double2), cudaMemcpyDeviceToHost, s));
-        DG_CUDA(cudaStreamSynchronize(s));
-        DG_TRY(dmftgpu_impurity_basis(D, p->magnetism, (const double *)hh.data(), (const double *)d0.data(),
-                                      (double *)Bh.data()));
-        Bd = buf2(ctx, "dmft.basis", DD);
-        double2 *hR = buf2(ctx, "dmft.hrot", DD), *wR = buf2(ctx, "dmft.wrot", (size_t)Nf * DD);
-        double2 *nR = buf2(ctx, "dmft.nrot", DD);
-        if (!Bd || !hR || !wR || !nR) return DMFTGPU_NOMEM;
-        DG_CUDA(cudaMemcpyAsync(Bd, Bh.data(), DD * sizeof(double2), cudaMemcpyHostToDevice, s));
-        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, hdc, hR, 1);
-        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, dW, wR, 1);
-        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, dN, nR, 1);
-        DG_LAUNCH(ctx, "k_rotate");
-        sH = hR;
-        sW = wR;
-        sN = nR;
-    }
+    // ---- SOLVER: proj_to_site, IPT or SCGF2, spin average
+    const DmftSolve S{p, D, Nf, DD, L->beta, &Ul, himp};
+    bool basis_ready = false;
     int loops = 0;
-    if (p->solver == DMFTGPU_SOLVER_IPT) {
-        DG_TRY(dg_ipt_dev(ctx, D, Nf, p->ntau, L->beta, p->U, *mu, sH, sW, sN, Ul, seimp, dGI, occ));
-    } else {
-        // Gw_strong: the lattice G_loc of the last TightBinding call starts the SCGF2 loop (as given, unrotated)
-        DG_CUDA(cudaMemcpyAsync(dGI, dG, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        DG_TRY(dg_scgf2_dev(ctx, D, Nf, p->ntau, L->beta, *mu, p->mixing, sH, sW, dGI, Ul,
-                            p->scgf_max_iter > 0 ? p->scgf_max_iter : 2000, seimp, &loops));
-        DG_CUDA(cudaMemcpyAsync(occ, sN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-    }
-    if (p->basis_switch) {
-        double2 *tmp = buf2(ctx, "dmft.rtmp", (size_t)Nf * DD);
-        if (!tmp) return DMFTGPU_NOMEM;
-        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, seimp, tmp, 0);
-        DG_CUDA(cudaMemcpyAsync(seimp, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        k_rotate<<<dg_ceil_div((long long)Nf * DD, rgrid), rgrid, 0, s>>>(Nf, D, Bd, dGI, tmp, 0);
-        DG_CUDA(cudaMemcpyAsync(dGI, tmp, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        k_rotate<<<dg_ceil_div((long long)DD, rgrid), rgrid, 0, s>>>(1, D, Bd, occ, tmp, 0);
-        DG_CUDA(cudaMemcpyAsync(occ, tmp, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        DG_LAUNCH(ctx, "k_rotate");
-    }
-    if (p->magnetism == 0) {
-        k_spin_average<<<dg_ceil_div((long long)(Nf + 6) * (D / 2), 128), 128, 0, s>>>(D, Nf + 5, seimp, occ);
-        DG_LAUNCH(ctx, "k_spin_average");
-    }
-    DG_CUDA(cudaMemcpyAsync(dN, occ, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    DG_TRY(dmft_solver(ctx, S, dW, dN, *mu, dG, seout, dGI, occ, dc, basis, &basis_ready, &loops));
     DG_CUDA(cudaMemcpyAsync(nm_imp, occ, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-    k_se_combine<<<dg_ceil_div((long long)Nf * DD, 256), 256, 0, s>>>(Nf, D, seimp, dc, seout);
-    DG_LAUNCH(ctx, "k_se_combine");
-    // ---- Pulay mixing of SelfEnergy_w (w < N_freq)
+    int code = 0;
+    DG_TRY(dg_status_read(ctx, &code));
+    if (code) return code;
+    // ---- the self-energy mixer: Pulay (src/dmft_main.cpp:529-533) or a Newton-Krylov step
     if (!ctx->pulay) ctx->pulay = new DgPulay();
     if (iteration <= 1) {
         *ctx->pulay = DgPulay();  // pulayMixing(2, 5, ...) of dmft_main (src/dmft_main.cpp:342) unless set
         if (p->pulay_history > 0) ctx->pulay->hist = p->pulay_history;
         if (p->pulay_start > 0) ctx->pulay->start = p->pulay_start;
     }
-    DG_TRY(dg_pulay_mixing(ctx, *ctx->pulay, "pulay", (long long)Nf * DD, dSE, seout, p->mixing, iteration));
-    DG_CUDA(cudaMemcpyAsync(dSE, seout, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-    int code = 0;
+    ctx->nk_krylov = 0;
+    ctx->nk_relres = 0;
+    {
+        // the fixed-point residual |SE_out - SelfEnergy_w| / |SelfEnergy_w| that both mixers reduce
+        double2 *fr = buf2(ctx, "dmft.fres", (size_t)Nf * DD);
+        if (!fr) return DMFTGPU_NOMEM;
+        DG_CUDA(cudaMemcpyAsync(fr, seout, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        DG_TRY(dg_vaxpby(ctx, (long long)Nf * DD, -1.0, dSE, 1.0, fr));
+        double ff = 0, xx = 0;
+        DG_TRY(dg_vdot(ctx, (long long)Nf * DD, fr, fr, &ff));
+        DG_TRY(dg_vdot(ctx, (long long)Nf * DD, dSE, dSE, &xx));
+        ctx->mix_resid = xx > 0 ? std::sqrt(ff / xx) : std::sqrt(ff);
+    }
+    const int nstart = p->newton_start > 0 ? p->newton_start : 3;
+    if (p->mixer == DMFTGPU_MIXER_NEWTON_KRYLOV && iteration >= nstart) {
+        // the Jacobian is taken at the state this call starts from (NumMatrix of its TightBinding, not IPT's)
+        double2 *nm_tb = buf2(ctx, "dmft.nmtb", DD), *xnew = buf2(ctx, "dmft.xnew", (size_t)Nf * DD);
+        if (!nm_tb || !xnew) return DMFTGPU_NOMEM;
+        DG_CUDA(cudaMemcpyAsync(nm_tb, dN, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        const int lflags = DMFTGPU_DEVICE_PTRS | (flags & (DMFTGPU_MIXED | DMFTGPU_NO_TENSOR));
+        DG_TRY(dmft_newton_step(ctx, L, hk, S, lflags, dSE, seout, dGI, dW, nm_tb, dG, *mu, basis, basis_ready, xnew,
+                                &ctx->nk_krylov, &ctx->nk_relres));
+        DG_CUDA(cudaMemcpyAsync(dSE, xnew, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    } else {
+        DG_TRY(dg_pulay_mixing(ctx, *ctx->pulay, "pulay", (long long)Nf * DD, dSE, seout, p->mixing, iteration));
+        DG_CUDA(cudaMemcpyAsync(dSE, seout, (size_t)Nf * DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    }
+    DG_CUDA(cudaMemcpyAsync(dN, occ, DD * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     DG_TRY(dg_status_read(ctx, &code));
     if (code) return code;
     // ---- TightBinding: mu search, GreenFtn_w, Construct_hyb_delta
@@ -457,5 +613,13 @@ extern "C" int dmftgpu_impurity_basis(int dim, int magnetism, const double *himp
             }
     }
     std::memcpy(basis, B.data(), B.size() * sizeof(double2));
+    return DMFTGPU_OK;
+}
+
+extern "C" int dmftgpu_mixer_stats(dmftgpu_ctx *ctx, int *krylov, double *relres, double *residual) {
+    if (!ctx || !krylov || !relres || !residual) return DMFTGPU_BADARG;
+    *krylov = ctx->nk_krylov;
+    *relres = ctx->nk_relres;
+    *residual = ctx->mix_resid;
     return DMFTGPU_OK;
 }

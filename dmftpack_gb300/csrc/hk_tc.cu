@@ -10,10 +10,12 @@
 // column's power-of-two scale g_c is split into S = 5 integer slices, x = sum_s x_s 2^{-8s}, x_1 in [-256, 256]
 // and x_s in [-128, 128] for s > 1 (each an integer, exact in bf16), leaving |x - sum| <= 2^-41.  A product of
 // slices (i, j) is an exact integer of at most 16 bits with weight 2^{-8(i+j)}; the products of one "level"
-// L = i + j (L <= S + 1 = 6: 15 products) accumulate in their own FP32 TMEM accumulator, and over a K chunk of 64
-// every partial sum stays below 2^24, so each accumulator holds an exact integer.  After each chunk the five
-// accumulators are read into FP64 registers with their weights; the result carries ~2^-41 of the operands'
-// magnitude, well inside the 1e-10 relative bar of the plain FP64 form.
+// L = i + j (L <= S + 1 = 6: 15 products) accumulate in their own FP32 TMEM accumulator.  Per K index a level
+// adds at most 2^16 (L = 2, 3), 1.25 x 2^16 (L = 4), 1.5 x 2^16 (L = 5) or 1.75 x 2^16 (L = 6), so over K = 128
+// (two chunks of 64) every partial sum stays below 2^24 and each accumulator holds an exact integer.  Every two
+// chunks the five accumulators are drained into double-float registers with their weights (exact power-of-two
+// scalings); the result carries ~2^-41 of the operands' magnitude, well inside the 1e-10 relative bar of the
+// plain FP64 form.
 //
 // Work per launch: 15 x 2 x N_k x 2n^2 x 2N_R bf16 flops; HBM: the N_k n^2 complex H(k) written once (the
 // phase-slice image is built once per (k mesh, R list) and kept in the context's workspace).
@@ -137,7 +139,7 @@ __device__ __forceinline__ dfs dfs_add(dfs a, float b) {
 }
 
 constexpr int NSTAGE = 2;      // shared-memory ring of chunk images
-constexpr int GROUP = 4;       // chunks accumulated in TMEM between drains: K = 256 keeps the top levels exact
+constexpr int GROUP = 2;       // chunks accumulated in TMEM between drains: K = 128 keeps every level exact
 constexpr int NBUF = 2;        // TMEM accumulator sets (NBUF * NL * TN <= 512 columns)
 constexpr uint32_t A_BYTES = (uint32_t)(img_elems(TM) * 2), B_BYTES = (uint32_t)(img_elems(TN) * 2);
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_hk_tc(int nk, int ne, int nchun
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (threadIdx.x == 0 && tc_failed(bar)) atomicMax(status, (int)DMFTGPU_CUDA_ERROR);
+    if (threadIdx.x == 0 && tc_failed(bar)) atomicMax(status, (int)DMFTGPU_TIMEOUT);
     if (warp == 0) tc::tmem_dealloc(tbase, TMEM_COLS_PIPE);
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <string>
 #include <utility>
@@ -53,6 +54,9 @@ struct dmftgpu_ctx {
     std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
     std::string hk_phase_key;         // (k mesh, R list) of the phase-slice image in workspace "hk.tc.A"
     bool tensor = true;               // tensor-core contractions allowed in the mixed form (!DMFTGPU_NO_TENSOR)
+    int nk_krylov = 0;                // Jacobian-vector products of the last Newton-Krylov mixer step (0: none)
+    double nk_relres = 0.0;           // its linear solve's relative residual
+    double mix_resid = 0.0;           // |SE_out - SelfEnergy_w| / |SelfEnergy_w| of the last DMFT iteration
 };
 
 // sets ctx->tensor from a call's flags for the call's duration
@@ -125,6 +129,14 @@ int dg_pulay_mixing(dmftgpu_ctx *ctx, DgPulay &P, const char *tag, long long len
 // H(k) on the tensor cores (hk_tc.cu); all pointers device
 int dg_hk_tensor(dmftgpu_ctx *ctx, int n, int nR, const int *dR, const double2 *dT, int kx, int ky, int kz,
                  double2 *dH, const std::string &mesh_key);
+
+// Newton-Krylov support (nk.cu): real inner product of complex device vectors (a synchronous fixed-order
+// reduction), y = a x + b y, and GMRES with at most m Arnoldi vectors on `apply` (x = the solution of
+// apply(x) = b, *relres = |b - apply(x)| / |b| of the Arnoldi least-squares problem)
+int dg_vdot(dmftgpu_ctx *ctx, long long n, const double2 *a, const double2 *b, double *out);
+int dg_vaxpby(dmftgpu_ctx *ctx, long long n, double a, const double2 *x, double b, double2 *y);
+int dg_gmres(dmftgpu_ctx *ctx, long long n, const double2 *b, int m, double tol,
+             const std::function<int(const double2 *, double2 *)> &apply, double2 *x, int *iters, double *relres);
 
 #define DG_LAUNCH(ctx, what)                     \
     do {                                         \

@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(TT<DP>::NT, 1) k_trace_tc(TcKArgs g) {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid == 0 && !ok) atomicMax(g.status, (int)DMFTGPU_CUDA_ERROR);
+    if (tid == 0 && !ok) atomicMax(g.status, (int)DMFTGPU_TIMEOUT);
     if (warp == 0) tc::tmem_dealloc(tbase, T::TMEM);
 }
 

@@ -65,24 +65,34 @@ def read_full(path, nfreq, norbit, beta, beta_prev):
     rows = _rows(path)
     wmax = max(r[0] for r in rows) + 1
     S = np.zeros((wmax, norbit, norbit), np.complex128)
+    mats = np.zeros(wmax)  # as in the reference, a frequency with no line keeps grid point 0
     for w, m, n, re, im in rows:
         if w >= 0:
             S[w, m, n] = re + 1j * im
-    mats = (2 * np.arange(wmax) + 1) * np.pi / beta_prev
+            mats[w] = (2 * w + 1) * np.pi / beta_prev
     F = np.zeros((nfreq + 5, norbit, norbit), np.complex128)
     dw_prev = 2 * np.pi / beta_prev
+    # complex-by-real products and quotients act on the real and imaginary parts separately, as std::complex's
+    # operators do (numpy's vectorised complex arithmetic can differ in the last bit)
+    Sr, Si = S.real.copy(), S.imag.copy()
+
+    def line(a, b, t):
+        return ((Sr[b] - Sr[a]) / dw_prev * t + Sr[a]) + 1j * ((Si[b] - Si[a]) / dw_prev * t + Si[a])
+
     wp = 0
     for w in range(nfreq):
         x = (2 * w + 1) * np.pi / beta
         if x <= mats[0]:
-            F[w] = (S[1] - S[0]) / dw_prev * (x - mats[0]) + S[0]
+            F[w] = line(0, 1, x - mats[0])
         elif x <= mats[wmax - 1]:
-            while not (mats[wp] < x <= mats[wp + 1]):
+            while wp + 1 < wmax and not (mats[wp] < x <= mats[wp + 1]):
                 wp += 1
-            F[w] = (S[wp + 1] - S[wp]) / dw_prev * (x - mats[wp]) + S[wp]
+            if wp + 1 >= wmax:
+                raise ValueError("%s: no bracketing pair of Matsubara points for w_%d" % (path, w))
+            F[w] = line(wp, wp + 1, x - mats[wp])
         else:
-            last = S[wmax - 1]
-            re_part = (last + last.conj().T) / 2.0
-            im_part = (last - last.conj().T) / 2j
-            F[w] = re_part + mats[wmax - 1] * im_part / x
+            lr, li = Sr[wmax - 1], Si[wmax - 1]
+            rr, ri = (lr + lr.T) / 2.0, (li - li.T) / 2.0     # R = (F + F^H)/2
+            jr, ji = (li + li.T) / 2.0, -((lr - lr.T) / 2.0)  # J = (F - F^H)/(2i)
+            F[w] = (rr + mats[wmax - 1] * jr / x) + 1j * (ri + mats[wmax - 1] * ji / x)
     return F

@@ -22,9 +22,9 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 
-OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM = range(9)
+OK, SINGULAR, NONCONVERGED, NAN, BADARG, CAUSALITY, HERMITICITY, CUDA_ERROR, NOMEM, TIMEOUT, IO = range(11)
 STATUS_NAMES = {0: "OK", 1: "SINGULAR", 2: "NONCONVERGED", 3: "NAN", 4: "BADARG", 5: "CAUSALITY",
-                6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM"}
+                6: "HERMITICITY", 7: "CUDA_ERROR", 8: "NOMEM", 9: "TIMEOUT", 10: "IO"}
 DEVICE_PTRS, MIXED, NEWTON, EXPLICIT, DIRECT_DFT, GRAPH, AUTOTUNE, NO_TENSOR = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40, 0x80
 
 # every symbol include/dmftgpu.h declares
@@ -34,7 +34,8 @@ EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_
            "dmftgpu_moments", "dmftgpu_greenftn_w", "dmftgpu_greenftn_w_batched", "dmftgpu_gloc_real", "dmftgpu_density_dft", "dmftgpu_upfold", "dmftgpu_gloc_vjp", "dmftgpu_gloc_jvp", "dmftgpu_downfold", "dmftgpu_nele", "dmftgpu_adjust_mu", "dmftgpu_hyb_delta",
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
-           "dmftgpu_hyb_delta_noalloc", "dmftgpu_weak_solver", "dmftgpu_double_counting", "dmftgpu_impurity_basis"]
+           "dmftgpu_hyb_delta_noalloc", "dmftgpu_weak_solver", "dmftgpu_double_counting", "dmftgpu_impurity_basis",
+           "dmftgpu_mixer_stats", "dmftgpu_imgfreq_write", "dmftgpu_imgfreq_update", "dmftgpu_imgfreq_read"]
 
 
 class DmftGpuError(RuntimeError):
@@ -49,7 +50,8 @@ class DmftParams(C.Structure):
                 ("Uprime", C.c_double), ("J", C.c_double), ("mixing", C.c_double), ("magnetism", C.c_int),
                 ("dctype", C.c_int), ("nominal_charge", C.c_double), ("nu", C.c_int), ("uidx", _ip), ("ut", _dp),
                 ("scgf_max_iter", C.c_int), ("basis_switch", C.c_int), ("pulay_history", C.c_int),
-                ("pulay_start", C.c_int)]
+                ("pulay_start", C.c_int), ("mixer", C.c_int), ("newton_start", C.c_int), ("krylov_dim", C.c_int),
+                ("krylov_tol", C.c_double)]
 
 
 class _Lat(C.Structure):
@@ -121,6 +123,10 @@ def load(require_built=True):
     lib.dmftgpu_dmft_iteration.argtypes = [_vp, P(_Lat), _vp, P(DmftParams), C.c_int, _vp, _vp, _vp, _dp, _vp, _vp,
                                            _dp, C.c_int]
     lib.dmftgpu_impurity_basis.argtypes = [C.c_int, C.c_int, _vp, _vp, _vp]
+    lib.dmftgpu_mixer_stats.argtypes = [_vp, _ip, _dp, _dp]
+    lib.dmftgpu_imgfreq_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _vp]
+    lib.dmftgpu_imgfreq_update.argtypes = [C.c_char_p, C.c_int, C.c_int, _vp]
+    lib.dmftgpu_imgfreq_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, _vp]
     lib.dmftgpu_double_counting.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                             _vp, _vp, C.c_int, _vp]
     lib.dmftgpu_weak_solver.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, C.c_int, _ip,
@@ -605,8 +611,9 @@ class Context:
         """One dmft_main loop iteration on device state kept in the library's column-major layout (CUDA
         tensors, updated in place: SelfEnergy_w, weiss_fieldTB, NumMatrix, G_loc).  params: dict(solver ("IPT" or
         "SC2PT"), ntau, n_electrons, U, Uprime, J, mixing, magnetism, dctype, nominal_charge, uidx, ut,
-        scgf_max_iter, basis_switch, pulay_history, pulay_start).  Returns (mu, gimp_cm[nfreq+5], residuals[5] = GwRD,
-        GwRD_low, GwRD_max, NumMatRD, SCGF2 loops)."""
+        scgf_max_iter, basis_switch, pulay_history, pulay_start, mixer ("pulay" or "newton_krylov"), newton_start,
+        krylov_dim, krylov_tol).  Returns (mu, gimp_cm[nfreq+5], residuals[5] = GwRD, GwRD_low, GwRD_max, NumMatRD,
+        SCGF2 loops)."""
         import torch
         nf, D = lat.nfreq, lat.D
         uidx = np.ascontiguousarray(params["uidx"], np.int32).reshape(-1, 4)
@@ -617,7 +624,9 @@ class Context:
                        params.get("nominal_charge", 1.0), uidx.shape[0], uidx.ctypes.data_as(_ip),
                        ut.view(np.float64).ctypes.data_as(_dp), params.get("scgf_max_iter", 0),
                        int(bool(params.get("basis_switch", False))), int(params.get("pulay_history", 0)),
-                       int(params.get("pulay_start", 0)))
+                       int(params.get("pulay_start", 0)), self.MIXERS[params.get("mixer", "pulay")],
+                       int(params.get("newton_start", 0)), int(params.get("krylov_dim", 0)),
+                       float(params.get("krylov_tol", 0.0)))
         gimp = torch.empty((nf + 5, D, D), dtype=torch.complex128, device=selfe_cm.device)
         m = C.c_double(mu)
         res = np.zeros(5)
@@ -630,6 +639,17 @@ class Context:
                                              _vp(gimp.data_ptr()), res.ctypes.data_as(_dp), fl)
         self._check("dmftgpu_dmft_iteration", st)
         return m.value, gimp, res
+
+    MIXERS = {"pulay": 0, "newton_krylov": 1}
+
+    def mixer_stats(self):
+        """(Jacobian-vector products, linear-solve relative residual, fixed-point residual |SE_out - Sigma| / |Sigma|)
+        of the last DMFT_iteration's mixer; the first two are (0, 0.0) after a Pulay step."""
+        k = C.c_int()
+        r = C.c_double()
+        f = C.c_double()
+        self._check("dmftgpu_mixer_stats", self.lib.dmftgpu_mixer_stats(self.h, C.byref(k), C.byref(r), C.byref(f)))
+        return k.value, r.value, f.value
 
 
 DC_NONE, DC_NOMINAL, DC_FLL, DC_AMF, DC_SIGMA0, DC_UPRIME = 0, 1, 2, 3, 4, 0x100
@@ -670,3 +690,36 @@ def kmesh(kx, ky, kz):
     if st != OK:
         raise DmftGpuError("dmftgpu_kmesh", st)
     return out
+
+
+def _imgfreq_cm(F):
+    return np.ascontiguousarray(np.swapaxes(np.asarray(F, np.complex128), -1, -2))
+
+
+def imgfreq_write(path, F):
+    """dataOut_full through the library: F is an (N_freq + 5, N, N) stack."""
+    F = np.asarray(F, np.complex128)
+    cm = _imgfreq_cm(F)
+    st = load().dmftgpu_imgfreq_write(os.fsencode(path), F.shape[0] - 5, F.shape[1], _vp(cm.ctypes.data))
+    if st:
+        raise DmftGpuError("dmftgpu_imgfreq_write", st, path)
+
+
+def imgfreq_update(path, nfreq, norbit, into=None):
+    """update_full through the library: the file's w < N_freq entries overwrite `into` (zeros if None)."""
+    F = np.zeros((nfreq + 5, norbit, norbit), np.complex128) if into is None else np.asarray(into, np.complex128)
+    cm = _imgfreq_cm(F)
+    st = load().dmftgpu_imgfreq_update(os.fsencode(path), nfreq, norbit, _vp(cm.ctypes.data))
+    if st:
+        raise DmftGpuError("dmftgpu_imgfreq_update", st, path)
+    return np.swapaxes(cm, -1, -2).copy()
+
+
+def imgfreq_read(path, nfreq, norbit, beta, beta_prev):
+    """read_full through the library: the file re-gridded from beta_prev's Matsubara points to beta's."""
+    cm = np.zeros((nfreq + 5, norbit, norbit), np.complex128)
+    st = load().dmftgpu_imgfreq_read(os.fsencode(path), nfreq, norbit, float(beta), float(beta_prev),
+                                     _vp(cm.ctypes.data))
+    if st:
+        raise DmftGpuError("dmftgpu_imgfreq_read", st, path)
+    return np.swapaxes(cm, -1, -2).copy()

@@ -31,7 +31,10 @@ enum {
     DMFTGPU_CAUSALITY = 5,    /* an eigenvalue of Im G or Im Delta has the wrong sign (reference: assert) */
     DMFTGPU_HERMITICITY = 6,  /* G(tau) or Sigma(tau) not Hermitian (reference: assert) */
     DMFTGPU_CUDA_ERROR = 7,
-    DMFTGPU_NOMEM = 8
+    DMFTGPU_NOMEM = 8,
+    DMFTGPU_TIMEOUT = 9,      /* a bounded wait inside a tensor-core kernel ran out (the kernel freed its TMEM and
+                                 returned; the context stays usable) */
+    DMFTGPU_IO = 10           /* a restart file could not be opened, read or written */
 };
 
 #define DMFTGPU_DEVICE_PTRS 0x1 /* array arguments live in device memory */
@@ -291,7 +294,19 @@ typedef struct {
     int basis_switch;      /* impurityBasisSwitch: solve in the basis of dmftgpu_impurity_basis (src/SOLVER.cpp:541-595) */
     int pulay_history;     /* Pulay (DIIS) history of the SelfEnergy_w mixer (0: the reference's 2) */
     int pulay_start;       /* first iteration of the DIIS step; simple mixing before it (0: the reference's 5) */
+    int mixer;             /* DMFTGPU_MIXER_PULAY (the reference's) or DMFTGPU_MIXER_NEWTON_KRYLOV */
+    int newton_start;      /* Newton-Krylov: first iteration of Newton steps, the Pulay mixer before it (0: 3) */
+    int krylov_dim;        /* Newton-Krylov: Jacobian-vector products per step at most (0: 8, at most 64) */
+    double krylov_tol;     /* Newton-Krylov: relative residual of each step's linear solve (0: 1e-3) */
 } dmftgpu_dmft_params;
+
+/* Self-energy mixers of dmftgpu_dmft_iteration.  NEWTON_KRYLOV (no counterpart in the reference): with x =
+ * SelfEnergy_w and Phi(x) the SOLVER output on the TightBinding state of x, each step solves
+ * (dPhi/dx - I) dx = x - Phi(x) by GMRES and sets x <- x + dx.  Its Jacobian-vector products take the lattice
+ * part from the tangent pass of dmftgpu_gloc_jvp (mu's first-order change from the electron count) and the
+ * D x D stages (Construct_hyb_delta, SOLVER) by directional differences; the fixed point is the Pulay mixer's. */
+#define DMFTGPU_MIXER_PULAY 0
+#define DMFTGPU_MIXER_NEWTON_KRYLOV 1
 
 /* SOLVER (IPT or SCGF2) with proj_to_site and the magnetism == 0 averaging (src/SOLVER.cpp:105-502), the Pulay mixing
  * of SelfEnergy_w (src/dmft_main.cpp:529-533), TightBinding's mu search, GreenFtn_w and Construct_hyb_delta
@@ -305,6 +320,26 @@ typedef struct {
 int dmftgpu_dmft_iteration(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk,
                            const dmftgpu_dmft_params *params, int iteration, double *selfe, double *weiss,
                            double *nummat, double *mu, double *gloc, double *gimp, double *resid, int flags);
+
+/* The last dmftgpu_dmft_iteration's mixer: *krylov = Jacobian-vector products of its Newton-Krylov step (0 when the
+ * call used the Pulay mixer), *relres = the relative residual of that step's linear solve, *residual = the
+ * fixed-point residual |SE_out - SelfEnergy_w| / |SelfEnergy_w| (w < N_freq) the mixer was given. */
+int dmftgpu_mixer_stats(dmftgpu_ctx *ctx, int *krylov, double *relres, double *residual);
+
+/* ---------------------------------------------------------------------------------------------
+ * Restart files: ImgFreqFtn's text format ("w m n Re Im" lines, printf "%d %d %d %+0.8f %+0.8f"), host only (no
+ * context, no device).  f: nfreq + 5 ImgFreqFtn slots of column-major norbit x norbit complex matrices.
+ * dmftgpu_imgfreq_write: dataOut_full (src/ImgTimeFtn.cpp:330-355): elements with |F| > 1e-7 for w < nfreq, then
+ *   every tail slot as w = -1 .. -5.
+ * dmftgpu_imgfreq_update: update_full (src/ImgTimeFtn.cpp:624-670): the file's w in [0, nfreq) entries overwrite f,
+ *   the rest of f is kept; DMFTGPU_BADARG for an orbital index outside [0, norbit) (the reference exits).
+ * dmftgpu_imgfreq_read: read_full (src/ImgTimeFtn.cpp:673-751): a file written at beta_prev re-gridded to beta's
+ *   Matsubara points (linear interpolation, linear extrapolation below the file's first point, R + w_last J / w
+ *   above its last); the tail slots of f are zeroed.
+ * DMFTGPU_IO when the file cannot be opened, read or written. */
+int dmftgpu_imgfreq_write(const char *path, int nfreq, int norbit, const double *f);
+int dmftgpu_imgfreq_update(const char *path, int nfreq, int norbit, double *f);
+int dmftgpu_imgfreq_read(const char *path, int nfreq, int norbit, double beta, double beta_prev, double *f);
 
 /* No counterpart in the reference.  Construct_hyb_delta for callers that cannot allocate device memory
  * (a driver whose HBM belongs to a pool allocator, or one that must not stall the device with a

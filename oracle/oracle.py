@@ -522,10 +522,22 @@ def weak_solver(solver, gw, gwhf, uidx, ut, beta, ntau):
     return se
 
 
+def newton_mu(H, sigma, mu, beta, D, n_target, tol=1e-12, max_iter=50):
+    """The root of N(mu) = n_target to |N - n_target| <= tol by Newton steps on dN/dmu from the derivative pass,
+    started from mu (the bisection's result): the mu that the library's DMFTGPU_NEWTON search converges to, for the
+    DMFT loop's fixed point without the bisection's |dmu| <= 1e-5 resolution (src/GreenFtn.cpp:66-139)."""
+    for _ in range(max_iter):
+        N, dN = nele(H, sigma, mu, beta, 1, D, deriv=True)
+        if abs(N - n_target) <= tol or not dN > 0:
+            break
+        mu += (n_target - N) / dN
+    return mu
+
+
 def dmft_iteration(H, state, p, it, pulay):
     """The dmft_main loop body for one correlated cluster (the first D orbitals) with IPT (D = 2) or SC2PT
     (SCGF2) (src/dmft_main.cpp:343-570): state = dict(selfe, weiss, nummat, mu, beta, gloc, scgf_static);
-    p = dict(solver, ntau, n_electrons, U, Uprime, J, mixing, uidx, ut, nominal_charge, scgf_max_iter).
+    p = dict(solver, ntau, n_electrons, U, Uprime, J, mixing, uidx, ut, nominal_charge, scgf_max_iter, newton_mu).
     Returns (new state, gloc, gimp, residuals[5])."""
     beta = state["beta"]
     nf, D = state["selfe"].shape[0], state["selfe"].shape[1]
@@ -563,6 +575,8 @@ def dmft_iteration(H, state, p, it, pulay):
     seout = se[:nf] - dc[None]
     selfe = pulay.mixing(state["selfe"], seout, p["mixing"], it)
     mu, nev = adjust_mu(H, selfe, state["mu"], beta, 1, D, p["n_electrons"])
+    if p.get("newton_mu"):
+        mu = newton_mu(H, selfe, mu, beta, D, p["n_electrons"])
     gloc, _, nummat = greenftn_w(H, selfe, mu, beta, 1, D)
     weiss = hyb_delta(list(range(D)), selfe, gloc, himp, mu, beta)
     wn = np.pi * (2 * np.arange(nf) + 1) / beta

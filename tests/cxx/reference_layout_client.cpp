@@ -8,9 +8,14 @@
 //   IN : int32 n, nk, nfreq, D; float64 beta, mu0, n_target; then H_k (nk n x n, column-major complex) and
 //        SelfE_w (nfreq D x D), both as interleaved re/im float64
 //   OUT: float64 mu (adjusted), then Gw (nfreq D x D), NumMatrix (D x D), weiss_fieldTB (nfreq D x D)
+//
+//   reference_layout_client restart IN OUT N_freq Norbit beta beta_prev
+//   an ImgFreqFtn restart file IN (written at beta_prev) read with read_full on beta's grid, written with
+//   dataOut_full to OUT (host only: no device is touched)
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "dmftgpu.h"
@@ -92,7 +97,38 @@ static void Construct_hyb_delta(dmftgpu_ctx *ctx, const Globals &g, int impurity
     unpack(out, g.N_freq, impurityDim, weiss_fieldTB);
 }
 
+// ImgFreqFtn's restart-file methods (src/ImgTimeFtn.cpp:330-355, 624-670, 673-751) over the library's host calls:
+// Ftn_ holds N_freq + 5 column-major Norbit x Norbit matrices
+struct ImgFreqFtn {
+    int Nfreq_, Norbit;
+    std::vector<Mat> Ftn_;
+    ImgFreqFtn(int nfreq, int norbit) : Nfreq_(nfreq), Norbit(norbit), Ftn_(nfreq + 5, Mat((size_t)norbit * norbit)) {}
+    void dataOut_full(const char *filename) {
+        std::vector<cmplx> flat = pack(Ftn_);
+        check(dmftgpu_imgfreq_write(filename, Nfreq_, Norbit, (const double *)flat.data()), "dmftgpu_imgfreq_write",
+              nullptr);
+    }
+    void update_full(const char *filename) {
+        std::vector<cmplx> flat = pack(Ftn_);
+        check(dmftgpu_imgfreq_update(filename, Nfreq_, Norbit, (double *)flat.data()), "dmftgpu_imgfreq_update",
+              nullptr);
+        unpack(flat, Nfreq_ + 5, Norbit, Ftn_);
+    }
+    void read_full(const char *filename, double beta, double beta_prev) {
+        std::vector<cmplx> flat((size_t)(Nfreq_ + 5) * Norbit * Norbit);
+        check(dmftgpu_imgfreq_read(filename, Nfreq_, Norbit, beta, beta_prev, (double *)flat.data()),
+              "dmftgpu_imgfreq_read", nullptr);
+        unpack(flat, Nfreq_ + 5, Norbit, Ftn_);
+    }
+};
+
 int main(int argc, char **argv) {
+    if (argc == 8 && std::string(argv[1]) == "restart") {
+        ImgFreqFtn SelfE_w(std::atoi(argv[4]), std::atoi(argv[5]));
+        SelfE_w.read_full(argv[2], std::atof(argv[6]), std::atof(argv[7]));
+        SelfE_w.dataOut_full(argv[3]);
+        return 0;
+    }
     if (argc != 3) {
         std::fprintf(stderr, "usage: %s IN OUT\n", argv[0]);
         return 1;

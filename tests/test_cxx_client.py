@@ -33,6 +33,26 @@ def test_reference_layout_client_compiles_and_links(tmp_path):
     assert os.access(_compile(tmp_path), os.X_OK)
 
 
+def test_reference_layout_client_restart_files(tmp_path):
+    """The compiled caller's ImgFreqFtn::read_full / dataOut_full shims (host only) against the module restatement:
+    a file written at beta_prev, re-gridded to beta and written again, byte for byte."""
+    from dmftpack_gb300 import imgfreq_io as io
+    exe = _compile(tmp_path)
+    nf, N, beta_prev, beta = 64, 3, 12.0, 16.0
+    rng = np.random.default_rng(4)
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta_prev
+    A = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+    F = np.zeros((nf + 5, N, N), np.complex128)
+    F[:nf] = (A + A.conj().T)[None] / 2 + 1.0 / (1j * wn[:, None, None] - rng.normal(size=(N, N))[None])
+    src, out, ref = tmp_path / "Sw.full.dat", tmp_path / "client.dat", tmp_path / "module.dat"
+    io.write_full(src, F)
+    r = subprocess.run([exe, "restart", str(src), str(out), "80", str(N), str(beta), str(beta_prev)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    io.write_full(ref, io.read_full(src, 80, N, beta, beta_prev))
+    assert out.read_bytes() == ref.read_bytes()
+
+
 @pytest.mark.gpu
 def test_reference_layout_client_matches_oracle(tmp_path, orc):
     from dmftpack_gb300 import models

@@ -61,3 +61,42 @@ def test_read_full_regrids_to_a_new_temperature(tmp_path):
     R, J = (last + last.conj().T) / 2, (last - last.conj().T) / 2j
     for w in np.where(wn_new > wn[-1])[0]:
         assert np.abs(G[w] - (R + wn[-1] * J / wn_new[w])).max() < 1e-7
+
+
+# ---- the same formats through the C ABI (dmftgpu_imgfreq_*: host code, no device), against this module ----
+
+def test_c_abi_writes_the_same_bytes(tmp_path):
+    from dmftpack_gb300 import lib
+    F = _sample(nf=40, N=4, seed=3)
+    a, b = tmp_path / "py.dat", tmp_path / "c.dat"
+    io.write_full(a, F)
+    lib.imgfreq_write(b, F)
+    assert a.read_bytes() == b.read_bytes()
+
+
+def test_c_abi_update_and_read_match_the_restatement(tmp_path):
+    from dmftpack_gb300 import lib
+    nf, N = 120, 3
+    F = _sample(nf=nf, N=N, beta=15.0, seed=5)
+    F[7] = 0   # a frequency with no line in the file
+    p = tmp_path / "Sw_SOLVER.full.dat"
+    io.write_full(p, F)
+    base = np.full_like(F, 2.0 - 1.0j)
+    assert np.array_equal(lib.imgfreq_update(p, nf, N, into=base), io.update_full(p, nf, N, into=base))
+    for beta, beta_prev in ((15.0, 15.0), (20.0, 15.0), (11.0, 15.0)):
+        assert np.array_equal(lib.imgfreq_read(p, 90, N, beta, beta_prev), io.read_full(p, 90, N, beta, beta_prev))
+
+
+def test_c_abi_errors(tmp_path):
+    import pytest
+    from dmftpack_gb300 import lib
+    with pytest.raises(lib.DmftGpuError) as e:
+        lib.imgfreq_update(tmp_path / "missing.dat", 8, 2)
+    assert e.value.code == lib.IO
+    p = tmp_path / "bad.dat"
+    p.write_text("0 0 5 +1.00000000 +0.00000000\n")
+    with pytest.raises(lib.DmftGpuError) as e:
+        lib.imgfreq_update(p, 8, 2)
+    assert e.value.code == lib.BADARG
+    with pytest.raises(ValueError):
+        io.update_full(p, 8, 2)
