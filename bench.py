@@ -727,13 +727,15 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     err = {"G_loc": float((gw_b - gw).abs().max() / gw.abs().max()),
            "NumMatrix": float((nm_b - nm).abs().max() / nm.abs().max())}
+    gw_ref = gw.clone()
     # side measurement: the other algorithm on the same inputs (one timed step)
     variants = {}
     if not args.no_variants:
-        # the other forms on the same inputs, one timed step each: FP64 Schur, FP64 explicit (the reference's
-        # algorithm), and the mixed Schur form when the headline is FP64
+        # the other forms on the same inputs, one timed step each: FP64 Schur, the explicit inversion (the
+        # reference's algorithm) in FP64 and in double-float, and the mixed Schur form when the headline is FP64
         others = {"schur_fp64": flags & ~(lib.MIXED | lib.EXPLICIT),
-                  "explicit_fp64": (flags & ~lib.MIXED) | lib.EXPLICIT}
+                  "explicit_fp64": (flags & ~lib.MIXED) | lib.EXPLICIT,
+                  "explicit_mixed": flags | lib.MIXED | lib.EXPLICIT}
         if not mixed:
             others["schur_mixed"] = (flags & ~lib.EXPLICIT) | lib.MIXED
         for name, fl in others.items():
@@ -747,7 +749,8 @@ def run_ours(args, rank, world, local_rank):
             e.record(stream)
             e.synchronize()
             t_o = s.elapsed_time(e) / 1e3
-            variants[name] = {"value": inv_per_step / t_o, "unit": UNIT, "ms_per_step": t_o * 1e3}
+            variants[name] = {"value": inv_per_step / t_o, "unit": UNIT, "ms_per_step": t_o * 1e3,
+                              "G_loc_vs_fp64": float((gw - gw_ref).abs().max() / gw_ref.abs().max())}
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     scgf2 = None if args.no_variants else scgf2_timing(ctx, dev)
     cfg5 = None if args.no_variants else dmft_iteration_cfg5(ctx, dev, stream, k=args.cfg5_k)
@@ -795,6 +798,9 @@ def run_ours(args, rank, world, local_rank):
     if "explicit_fp64" in variants:
         same_alg = {"value": variants["explicit_fp64"]["value"] / cpu_v, "gpu": "explicit_fp64",
                     "cpu": "oracle GreenFtn_w (explicit inversion, threads over k)"}
+        if "explicit_mixed" in variants:
+            same_alg["value_mixed"] = variants["explicit_mixed"]["value"] / cpu_v
+            same_alg["gpu_mixed"] = "explicit_mixed (double-float explicit inversion)"
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32x2 (double-float)",

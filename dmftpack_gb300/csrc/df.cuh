@@ -89,6 +89,19 @@ struct OpsD {
     static __device__ __forceinline__ double im(C a) { return a.y; }
     static __device__ __forceinline__ double mag2(C a) { return cabs2(a); }
     static __device__ __forceinline__ C shfl(C v, int src, int w) { return shfl2(v, src, w); }
+    // real parts (R) for the Hermitian split of the pole sums
+    typedef double R;
+    static __device__ __forceinline__ R rzero() { return 0.0; }
+    static __device__ __forceinline__ R rfrom(double x) { return x; }
+    static __device__ __forceinline__ R rfma(R a, R b, R acc) { return ::fma(a, b, acc); }
+    static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
+    static __device__ __forceinline__ R radd(R a, R b) { return a + b; }
+    static __device__ __forceinline__ R rsub(R a, R b) { return a - b; }
+    static __device__ __forceinline__ R rneg(R a) { return -a; }
+    static __device__ __forceinline__ R rrcp(R a) { return 1.0 / a; }
+    static __device__ __forceinline__ C mk(R re, R im) { return cmk(re, im); }
+    static __device__ __forceinline__ R cre(C a) { return a.x; }
+    static __device__ __forceinline__ R cim(C a) { return a.y; }
 };
 
 struct OpsF {
@@ -131,6 +144,18 @@ struct OpsF {
     static __device__ __forceinline__ float mag2(C a) {  // pivot choice only: FP32 magnitude suffices
         return __fmaf_rn(a.re.h, a.re.h, __fmul_rn(a.im.h, a.im.h));
     }
+    typedef dfl R;
+    static __device__ __forceinline__ R rzero() { return {0.f, 0.f}; }
+    static __device__ __forceinline__ R rfrom(double x) { return df_make(x); }
+    static __device__ __forceinline__ R rfma(R a, R b, R acc) { return df_fma(a, b, acc); }
+    static __device__ __forceinline__ R rmul(R a, R b) { return df_mul(a, b); }
+    static __device__ __forceinline__ R radd(R a, R b) { return df_add(a, b); }
+    static __device__ __forceinline__ R rsub(R a, R b) { return df_sub(a, b); }
+    static __device__ __forceinline__ R rneg(R a) { return df_neg(a); }
+    static __device__ __forceinline__ R rrcp(R a) { return df_rcp(a); }
+    static __device__ __forceinline__ C mk(R re, R im) { return {re, im}; }
+    static __device__ __forceinline__ R cre(C a) { return a.re; }
+    static __device__ __forceinline__ R cim(C a) { return a.im; }
     static __device__ __forceinline__ C shfl(C v, int src, int w) {
         C o;
         o.re.h = __shfl_sync(0xffffffffu, v.re.h, src, w);

@@ -415,7 +415,7 @@ using dg::M_TRACE;
 
 struct Inst {
     int N, W;
-    GlocKernel (*get)(int);
+    GlocKernel (*get)(int, bool);
 };
 const Inst kInst[] = {
     {1, 1, dg::gloc_kernel_1},    {2, 2, dg::gloc_kernel_2},    {3, 4, dg::gloc_kernel_3},
@@ -574,16 +574,13 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
 }
 
 int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid, double2 *blk, double2 *blk0,
-             double *tr, double *dtr) {
+             double *tr, double *dtr, bool mixed) {
     const Inst *in = pick_inst(P.n);
     if (!in) return dg_fail(ctx, DMFTGPU_BADARG, "explicit inversion: n > 28 not instantiated");
-    GlocKernel kern = in->get(mode);
-    const int NG = 128 / in->W, DD = P.D * P.D;
+    GlocKernel kern = in->get(mode, mixed);
     int fpb = 4;
     auto smem_for = [&](int f) {
-        size_t s = (size_t)NG * f * DD * 2 + (size_t)NG * in->N * P.D + (size_t)NG * f;
-        if (mode & M_DERIV) s += (size_t)NG * in->N * in->N;
-        return s * sizeof(double2);
+        return dg::gloc_smem(in->N, in->W, mode, f, P.D, mixed ? sizeof(cdf) : sizeof(double2));
     };
     while (fpb > 1 && smem_for(fpb) > 160 * 1024) fpb--;
     size_t smem = smem_for(fpb);
@@ -607,6 +604,9 @@ int run_gloc(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgrid
     g.tr = tr;
     g.dtr = dtr;
     g.status = ctx->d_status;
+    // every mode reads the static spectrum (e_l for Tr G0 and the G0 block, U for the G0 block), computed on the
+    // side stream
+    DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     {
         DgTimer tm(ctx, "k_gloc");
         kern<<<dg_ceil_div(g.nf2, fpb), 128, smem, ctx->stream>>>(g);
@@ -645,8 +645,8 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
               double *tr, double *dtr, bool mixed) {
     const SInst *in = pick_schur(P.D);
     // BLOCK passes of correlated blocks up to 3 x 3: one thread per frequency (k_schur_tpi).  It stages the
-    // D x D pole products of each staged k; prepare() caps n at 64 (the static eigensolver), so one k needs at
-    // most (9*63 + 63 + 9)*16 B = 10 KB and the 200 KB check below never rejects a tpi pass.
+    // Hermitian pole products of each staged k; prepare() caps n at 64 (the static eigensolver), so one k needs
+    // at most 63 * (3 * 16 + 3 * 8 + 8) + 9 * 16 B = 5.2 KB and the 200 KB check below never rejects a tpi pass.
     const bool tpi = mode == dg::S_BLOCK && P.D <= 3;
     SchurKernel kern = tpi ? dg::schur_tpi_kernel(P.D, mixed) : in->get(mode, mixed);
     const int m = P.n - P.D, NG = tpi ? 128 : 128 / in->W, DD = P.D * P.D;
@@ -765,9 +765,8 @@ int nele_pass(dmftgpu_ctx *ctx, const Prepared &P, double mu, bool deriv, double
     double *dtr = (double *)dg_buf(ctx, "nele.dtr", nf2 * sizeof(double));
     double *fs = (double *)dg_buf(ctx, "nele.fs", 2 * (size_t)P.nk * sizeof(double));
     if (!tr || !dtr || !fs) return DMFTGPU_NOMEM;
-    if (explicit_inv && mixed) return dg_fail(ctx, DMFTGPU_BADARG, "nele: the explicit form is FP64 only");
     if (explicit_inv) {
-        DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr));
+        DG_TRY(run_gloc(ctx, P, deriv ? (M_TRACE | M_DERIV) : M_TRACE, mu, 1, nullptr, nullptr, tr, dtr, mixed));
     } else if (mixed && !deriv && ctx->tensor && !ctx->capturing && dg_trace_tc_supported(P.n, P.D)) {
         // the pole sums on the tensor cores (trace_tc.cu)
         DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
@@ -920,7 +919,8 @@ int greenftn_w_dev(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH
     double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
     double *fs = (double *)dg_buf(ctx, "gloc.fs", 2 * (size_t)L->nk * sizeof(double));
     if (!blk || !blk0 || !occ || !fs) return DMFTGPU_NOMEM;
-    if (flags & DMFTGPU_EXPLICIT) DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr));
+    if (flags & DMFTGPU_EXPLICIT)
+        DG_TRY(run_gloc(ctx, P, M_BLOCK, mu, 0, blk, blk0, nullptr, nullptr, (flags & DMFTGPU_MIXED) != 0));
     else DG_TRY(run_schur(ctx, P, dg::S_BLOCK, mu, 0, blk, blk0, nullptr, nullptr, (flags & DMFTGPU_MIXED) != 0));
     DG_CUDA(cudaStreamWaitEvent(ctx->stream, P.static_ready, 0));
     k_fermi<<<dg_ceil_div(L->nk, 128), 128, 0, ctx->stream>>>(L->nk, L->n, D, L->beta, mu, P.eps, P.UP, occ, fs);
@@ -1150,8 +1150,6 @@ int dmftgpu_hk(dmftgpu_ctx *ctx, int n, int nnz, const int *rindex, const double
 int dmftgpu_greenftn_w(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, const double *sigma, double mu,
                        double *gw, double *gwhf, double *nummat, int flags) {
     if (!ctx || check_lat(L) || !hk || !sigma || !gw || !nummat) return DMFTGPU_BADARG;
-    if ((flags & DMFTGPU_MIXED) && (flags & DMFTGPU_EXPLICIT))
-        return dg_fail(ctx, DMFTGPU_BADARG, "greenftn_w: the explicit form is FP64 only");
     cudaSetDevice(ctx->device);
     const int D = L->ncl * L->nh, Nf = L->nfreq;
     const size_t DD = (size_t)D * D;

@@ -362,23 +362,34 @@ __device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
 // D x D S(z) and S0(z) of that thread's (k, iw) in its registers, inverted by thread_inverse.  A lane-group
 // k_schur at these widths leaves lanes idle (D < W) and spends its issue slots on the group's pivot broadcasts;
 // here every lane does useful work and nothing is exchanged.  Per k point the CTA stages, for all its
-// frequencies, the pole outer products P_l = b_l b_l^H, the shifted poles mu - e_l and -H_PP - m0; each thread
-// forms S0 = z - H_PP - m0 - sum_l w_l P_l and S = S0 - (Sigma - m0), Sigma - m0 held in its registers.
+// frequencies, the pole outer products P_l = b_l b_l^H (Hermitian: the real diagonal and the upper triangle), the
+// shifted poles mu - e_l and -H_PP - m0; each thread forms S0 = z - H_PP - m0 - sum_l w_l P_l and
+// S = S0 - (Sigma - m0), Sigma - m0 held in its registers.
+//
+// The pole sum in Hermitian parts: with w_l = 1/(z - e_l) = (x_l - i w)/(x_l^2 + w^2), x_l = mu - e_l,
+// sum_l w_l P_l = A + i B with A = sum_l Re(w_l) P_l and B = sum_l Im(w_l) P_l both Hermitian, so only the
+// diagonal (real) and the upper triangle of A and B are accumulated: 2 D + 4 D(D-1)/2 real multiply-adds per pole
+// instead of 4 D^2, and the lower triangle follows as A_ba + i B_ba = conj(A_ab) + i conj(B_ab).
 template <class Ops, int D>
 __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
     typedef typename Ops::C C;
+    typedef typename Ops::R R;
     extern __shared__ double2 sm[];
-    constexpr int DD = D * D;
+    constexpr int DD = D * D, NP = D * (D - 1) / 2;
     const int m = g.m;
-    C *st = reinterpret_cast<C *>(sm);
-    C *sP = st, *sE = sP + (size_t)g.kc * m * DD, *sH = sE + (size_t)g.kc * m;
+    // staged per k: P_l off-diagonal pairs [m][NP] (C), -H_PP - m0 [DD] (C), P_l diagonal [m][D] (R), mu - e_l [m] (R)
+    C *sPo = reinterpret_cast<C *>(sm);
+    C *sH = sPo + (size_t)g.kc * m * NP;
+    R *sPd = reinterpret_cast<R *>(sH + (size_t)g.kc * DD);
+    R *sE = sPd + (size_t)g.kc * m * D;
     const int f_raw = blockIdx.x * blockDim.x + threadIdx.x;
     const bool fvalid = f_raw < g.nf2;
     const int f = fvalid ? f_raw : g.nf2 - 1;
     const int chunk = blockIdx.y;
     const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
     const double w = g.wgrid ? (DG_PI / g.beta + f * ((2 * DG_PI) / g.beta)) : (DG_PI * (2. * f + 1.) / g.beta);
-    const C zc = Ops::from(cmk(g.mu, w)), iwc = Ops::from(cmk(0.0, w));
+    const C zc = Ops::from(cmk(g.mu, w));
+    const R wr = Ops::rfrom(w), w2 = Ops::rmul(wr, wr);
     C sd[D][D], aG[D][D], aG0[D][D];  // sd = Sigma(iw) - m0
 #pragma unroll
     for (int a = 0; a < D; a++)
@@ -391,32 +402,69 @@ __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
     for (int k0 = kbeg; k0 < kend; k0 += g.kc) {
         const int nkc = min(g.kc, kend - k0);
         __syncthreads();
-        for (int t = threadIdx.x; t < nkc * m * DD; t += blockDim.x) {
-            const int e = t % DD, a = e % D, b = e / D;
-            const double2 *bl = g.B + ((size_t)k0 * m + t / DD) * D;
-            sP[t] = Ops::from(cmulc(bl[a], bl[b]));
+        for (int t = threadIdx.x; t < nkc * m * D; t += blockDim.x) {
+            const double2 b = g.B[((size_t)k0 * m + t / D) * D + t % D];
+            sPd[t] = Ops::rfrom(b.x * b.x + b.y * b.y);
         }
-        for (int t = threadIdx.x; t < nkc * m; t += blockDim.x)
-            sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k0 * m + t], 0.0));
+        if (NP > 0)
+            for (int t = threadIdx.x; t < nkc * m * NP; t += blockDim.x) {
+                int q = t % NP, a = 0;  // pair q in row-major order over the strict upper triangle
+                while (q >= D - 1 - a) {
+                    q -= D - 1 - a;
+                    a++;
+                }
+                const double2 *bl = g.B + ((size_t)k0 * m + t / NP) * D;
+                sPo[t] = Ops::from(cmulc(bl[a], bl[a + 1 + q]));
+            }
+        for (int t = threadIdx.x; t < nkc * m; t += blockDim.x) sE[t] = Ops::rfrom(g.mu - g.epsQ[(size_t)k0 * m + t]);
         for (int t = threadIdx.x; t < nkc * DD; t += blockDim.x) {
             const int kk = t / DD, e = t % DD, a = e % D, b = e / D;
             sH[t] = Ops::from(csub(cneg(g.H[(size_t)(k0 + kk) * g.n * g.n + a + (size_t)b * g.n]), g.m0[e]));
         }
         __syncthreads();
         for (int kk = 0; kk < nkc; kk++) {
-            const C *ps = sP + (size_t)kk * m * DD, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
+            const C *po = sPo + (size_t)kk * m * NP, *hp = sH + (size_t)kk * DD;
+            const R *pd = sPd + (size_t)kk * m * D, *es = sE + (size_t)kk * m;
+            R Ad[D], Bd[D], Ar[NP ? NP : 1], Ai[NP ? NP : 1], Br[NP ? NP : 1], Bi[NP ? NP : 1];
+#pragma unroll
+            for (int a = 0; a < D; a++) Ad[a] = Bd[a] = Ops::rzero();
+#pragma unroll
+            for (int q = 0; q < NP; q++) Ar[q] = Ai[q] = Br[q] = Bi[q] = Ops::rzero();
+            for (int l = 0; l < m; l++) {
+                const R x = es[l];
+                const R r = Ops::rrcp(Ops::rfma(x, x, w2));
+                const R re = Ops::rmul(x, r), im = Ops::rneg(Ops::rmul(wr, r));  // w_l
+#pragma unroll
+                for (int a = 0; a < D; a++) {
+                    const R p = pd[(size_t)l * D + a];
+                    Ad[a] = Ops::rfma(re, p, Ad[a]);
+                    Bd[a] = Ops::rfma(im, p, Bd[a]);
+                }
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    const C p = po[(size_t)l * NP + q];
+                    Ar[q] = Ops::rfma(re, Ops::cre(p), Ar[q]);
+                    Ai[q] = Ops::rfma(re, Ops::cim(p), Ai[q]);
+                    Br[q] = Ops::rfma(im, Ops::cre(p), Br[q]);
+                    Bi[q] = Ops::rfma(im, Ops::cim(p), Bi[q]);
+                }
+            }
             C s0[D][D];
 #pragma unroll
-            for (int a = 0; a < D; a++)
-#pragma unroll
-                for (int b = 0; b < D; b++) s0[a][b] = (a == b) ? Ops::add(hp[a + b * D], zc) : hp[a + b * D];
-            for (int l = 0; l < m; l++) {
-                const C wl = Ops::rcp(Ops::add(es[l], iwc));
-                const C *pl = ps + (size_t)l * DD;
+            for (int a = 0; a < D; a++) {
+                const C h = Ops::add(hp[a + a * D], zc);
+                s0[a][a] = Ops::sub(h, Ops::mk(Ad[a], Bd[a]));
+            }
+            {
+                int q = 0;
 #pragma unroll
                 for (int a = 0; a < D; a++)
 #pragma unroll
-                    for (int b = 0; b < D; b++) s0[a][b] = Ops::fms(wl, pl[a + b * D], s0[a][b]);
+                    for (int b = a + 1; b < D; b++, q++) {
+                        // S_ab = (Ar - Bi) + i (Ai + Br), S_ba = (Ar + Bi) + i (Br - Ai)
+                        s0[a][b] = Ops::sub(hp[a + b * D], Ops::mk(Ops::rsub(Ar[q], Bi[q]), Ops::radd(Ai[q], Br[q])));
+                        s0[b][a] = Ops::sub(hp[b + a * D], Ops::mk(Ops::radd(Ar[q], Bi[q]), Ops::rsub(Br[q], Ai[q])));
+                    }
             }
             C s[D][D];
 #pragma unroll
@@ -446,9 +494,10 @@ __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
         }
 }
 
-// staged per k: P_l [m][D][D], mu - e_l [m], -H_PP - m0 [D][D]
+// staged per k: P_l off-diagonal pairs [m][D(D-1)/2] and -H_PP - m0 [D][D] (16 B complex), P_l diagonal [m][D] and
+// mu - e_l [m] (8 B real; double and double-float alike)
 inline size_t schur_tpi_smem(int kc, int D, int m) {
-    return ((size_t)kc * m * D * D + (size_t)kc * m + (size_t)kc * D * D) * 16;
+    return ((size_t)kc * m * (D * (D - 1) / 2) + (size_t)kc * D * D) * 16 + ((size_t)kc * m * D + (size_t)kc * m) * 8;
 }
 
 // shared-memory bytes of one k_schur launch

@@ -14,6 +14,7 @@
 // reference.  With the full window the Fermi-diagonal part of Matrix_KSBase (:17-22) is overwritten entirely by
 // the model-basis block (NBAND = n).
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "internal.h"
@@ -55,10 +56,15 @@ __device__ void sm_chol_solve(int n, const double2 *L, const double2 *X, bool tx
     __syncthreads();
 }
 
-// out: [3][nk][n][n] = (M_dd, M_d, M) per k
+// out: [3][nk][n][n] = (M_dd, M_d, M) per k.  Band window (nband != nullptr, src/upfolding.cpp:10-35): X lives in the
+// leading nband[k] x nband[k] block (the padding of a windowed downfolding beyond it); Matrix_KSBase is the Fermi
+// diagonal f(e - mu) of every band (the +-100 cut-offs of the reference) with the window's rows and columns
+// win[k][0 .. nband[k]-1] replaced by X.
 __global__ void __launch_bounds__(128) k_upfold_k(int nk, int n, const double2 *__restrict__ dens,
                                                   const double2 *__restrict__ DF, const double2 *__restrict__ EV,
-                                                  const double2 *__restrict__ S, double2 *out, int *status) {
+                                                  const double2 *__restrict__ S, const int *__restrict__ nband,
+                                                  const int *__restrict__ win, const double *__restrict__ eps,
+                                                  double mu, double beta, double2 *out, int *status) {
     extern __shared__ double2 usm[];
     const int k = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
     const size_t nn = (size_t)n * n, ko = (size_t)k * nn;
@@ -70,6 +76,26 @@ __global__ void __launch_bounds__(128) k_upfold_k(int nk, int n, const double2 *
     __syncthreads();
     sm_mm(n, A, false, B, false, C);  // D DF
     sm_mm(n, B, true, C, false, A);   // X = DF^H D DF
+    if (nband) {
+        const int nb = nband[k];
+        for (int q = tid; q < (int)nn; q += nt) {  // Matrix_KSBase into C
+            const int i = q % n, j = q / n;
+            double f = 0;
+            if (i == j) {
+                const double x = beta * (eps[(size_t)k * n + i] - mu);
+                f = x > 100.0 ? 0.0 : (x < -100.0 ? 1.0 : 1.0 / (1.0 + exp(x)));
+            }
+            C[q] = cmk(f, 0.0);
+        }
+        __syncthreads();
+        for (int q = tid; q < nb * nb; q += nt) {
+            const int a = q % nb, b = q / nb;
+            C[win[(size_t)k * n + a] + (size_t)win[(size_t)k * n + b] * n] = A[a + (size_t)b * n];
+        }
+        __syncthreads();
+        for (int q = tid; q < (int)nn; q += nt) A[q] = C[q];
+        __syncthreads();
+    }
     for (int q = tid; q < (int)nn; q += nt) B[q] = EV[ko + q];
     __syncthreads();
     sm_mm(n, A, false, B, true, C);   // X V^H
@@ -148,9 +174,12 @@ __global__ void k_upfold_gather(int nnz, int n, int nk, const int *__restrict__ 
 
 }  // namespace
 
-extern "C" int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens, const double *df,
-                              const double *evec, const double *sk, int nnz, const int *rindex, double *dm_dual_dual,
-                              double *dm_dual_direct, double *dm_direct, int flags) {
+namespace {
+
+int upfold_impl(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens, const double *df,
+                const double *evec, const double *sk, const double *eps, const int *nband, const int *win, double mu,
+                double beta, int nnz, const int *rindex, double *dm_dual_dual, double *dm_dual_direct,
+                double *dm_direct, int flags) {
     if (!ctx || n < 1 || n > UF_NMAX || kx < 1 || ky < 1 || kz < 1 || kx > UF_NMAX * 4 || ky > UF_NMAX * 4 ||
         kz > UF_NMAX * 4 || !dens || !df || !evec || nnz < 1 || !rindex)
         return DMFTGPU_BADARG;
@@ -167,8 +196,19 @@ extern "C" int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, c
     }
     const int nr[3] = {hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1};
     if (nr[0] > 4096 || nr[1] > 4096 || nr[2] > 4096) return dg_fail(ctx, DMFTGPU_BADARG, "upfold: R range too wide");
-    DG_CUDA(cudaSetDevice(ctx->device));
     const int nk = kx * ky * kz;
+    if (nband) {
+        if (!eps || !win || !(beta > 0) || !std::isfinite(mu)) return DMFTGPU_BADARG;
+        for (int k = 0; k < nk; k++) {
+            if (nband[k] < 1 || nband[k] > n) return dg_fail(ctx, DMFTGPU_BADARG, "upfold: NBAND[k] outside [1, n]");
+            for (int j = 0; j < nband[k]; j++) {
+                const int b = win[(size_t)k * n + j];
+                if (b < 0 || b >= n || (j > 0 && b <= win[(size_t)k * n + j - 1]))
+                    return dg_fail(ctx, DMFTGPU_BADARG, "upfold: FromValToKS not ascending band indices");
+            }
+        }
+    }
+    DG_CUDA(cudaSetDevice(ctx->device));
     const size_t nn = (size_t)n * n, mb = (size_t)nk * nn * sizeof(double2);
     int st;
     const double2 *dD = (const double2 *)dg_in(ctx, dens, mb, flags, "io.uf_dens", &st);
@@ -194,10 +234,21 @@ extern "C" int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, c
     int *dR = (int *)dg_buf(ctx, "uf.rindex", (size_t)nnz * 5 * sizeof(int));
     if (!M || !A1 || !A2 || !A3 || !dR) return DMFTGPU_NOMEM;
     DG_CUDA(cudaMemcpyAsync(dR, rindex, (size_t)nnz * 5 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    const double *dE = nullptr;
+    int *dnb = nullptr, *dwin = nullptr;
+    if (nband) {
+        dE = (const double *)dg_in(ctx, eps, (size_t)nk * n * sizeof(double), flags, "io.uf_eps", &st);
+        if (st) return st;
+        dnb = (int *)dg_buf(ctx, "uf.nband", (size_t)nk * sizeof(int));
+        dwin = (int *)dg_buf(ctx, "uf.win", (size_t)nk * n * sizeof(int));
+        if (!dnb || !dwin) return DMFTGPU_NOMEM;
+        DG_CUDA(cudaMemcpyAsync(dnb, nband, (size_t)nk * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        DG_CUDA(cudaMemcpyAsync(dwin, win, (size_t)nk * n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    }
     DG_TRY(dg_status_reset(ctx));
     const size_t sm = 3 * nn * sizeof(double2);
     DG_CUDA(cudaFuncSetAttribute(k_upfold_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_upfold_k<<<nk, 128, sm, ctx->stream>>>(nk, n, dD, dF, dV, dS, M, ctx->d_status);
+    k_upfold_k<<<nk, 128, sm, ctx->stream>>>(nk, n, dD, dF, dV, dS, dnb, dwin, dE, mu, beta, M, ctx->d_status);
     DG_LAUNCH(ctx, "k_upfold_k");
     // x: [3 kz ky][kx][n n] -> [3 kz ky][nrx][n n]; y: [3 kz][ky][nrx n n] -> [3 kz][nry][nrx n n];
     // z: [3][kz][nry nrx n n] -> [3][nrz][nry nrx n n]
@@ -225,4 +276,23 @@ extern "C" int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, c
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
     return code;
+}
+
+}  // namespace
+
+extern "C" int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens, const double *df,
+                              const double *evec, const double *sk, int nnz, const int *rindex, double *dm_dual_dual,
+                              double *dm_dual_direct, double *dm_direct, int flags) {
+    return upfold_impl(ctx, n, kx, ky, kz, dens, df, evec, sk, nullptr, nullptr, nullptr, 0.0, 1.0, nnz, rindex,
+                       dm_dual_dual, dm_dual_direct, dm_direct, flags);
+}
+
+extern "C" int dmftgpu_upfold_window(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens,
+                                     const double *df, const double *evec, const double *sk, const double *eps,
+                                     const int *nband, const int *from_val_to_ks, double mu, double beta, int nnz,
+                                     const int *rindex, double *dm_dual_dual, double *dm_dual_direct,
+                                     double *dm_direct, int flags) {
+    if (!nband || !from_val_to_ks || !eps) return DMFTGPU_BADARG;
+    return upfold_impl(ctx, n, kx, ky, kz, dens, df, evec, sk, eps, nband, from_val_to_ks, mu, beta, nnz, rindex,
+                       dm_dual_dual, dm_dual_direct, dm_direct, flags);
 }

@@ -35,7 +35,8 @@ EXPORTS = ["dmftgpu_version", "dmftgpu_create", "dmftgpu_destroy", "dmftgpu_set_
            "dmftgpu_fourier_w2tau", "dmftgpu_fourier_tau2w", "dmftgpu_sigma2_tau", "dmftgpu_fock", "dmftgpu_dyson",
            "dmftgpu_occupation", "dmftgpu_estimate_asymto", "dmftgpu_ipt", "dmftgpu_scgf2", "dmftgpu_dmft_iteration",
            "dmftgpu_hyb_delta_noalloc", "dmftgpu_weak_solver", "dmftgpu_double_counting", "dmftgpu_impurity_basis",
-           "dmftgpu_mixer_stats", "dmftgpu_imgfreq_write", "dmftgpu_imgfreq_update", "dmftgpu_imgfreq_read"]
+           "dmftgpu_mixer_stats", "dmftgpu_imgfreq_write", "dmftgpu_imgfreq_update", "dmftgpu_imgfreq_read",
+           "dmftgpu_downfold_window", "dmftgpu_upfold_window"]
 
 
 class DmftGpuError(RuntimeError):
@@ -104,6 +105,10 @@ def load(require_built=True):
     lib.dmftgpu_gloc_vjp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, _vp, _dp, C.c_int]
     lib.dmftgpu_gloc_jvp.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _vp, C.c_double, _vp, C.c_int]
     lib.dmftgpu_downfold.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_downfold_window.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _ip, _vp, _vp, C.c_double, C.c_double,
+                                            C.c_double, C.c_double, _ip, _ip, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    lib.dmftgpu_upfold_window.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _ip, _ip,
+                                          C.c_double, C.c_double, C.c_int, _ip, _vp, _vp, _vp, C.c_int]
     lib.dmftgpu_nele.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, _dp, _dp, C.c_int]
     lib.dmftgpu_adjust_mu.argtypes = [_vp, P(_Lat), _vp, _vp, C.c_double, C.c_double, C.c_double, _dp, _ip, C.c_int]
     lib.dmftgpu_hyb_delta.argtypes = [_vp, C.c_int, _ip, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, C.c_double,
@@ -348,10 +353,12 @@ class Context:
         self._check("dmftgpu_density_dft", st)
         return out.result()
 
-    def upfolding_density(self, densityMatDFT, DF_CorrBase, KS_eigenVectors, kgrid, H_Rindex, S_overlap=None):
-        """upfolding_density over the full band window: returns (dual_DMR_dual, dual_DM_direct_DFTR,
-        direct_DMR_direct), each complex [nnz] at the rows of H_Rindex [nnz, 5] = (Rx, Ry, Rz, i0, j0).  The (nk, n, n)
-        inputs are numpy arrays or CUDA tensors; kgrid = (kx, ky, kz) of the k mesh."""
+    def upfolding_density(self, densityMatDFT, DF_CorrBase, KS_eigenVectors, kgrid, H_Rindex, S_overlap=None,
+                          window=None):
+        """upfolding_density: returns (dual_DMR_dual, dual_DM_direct_DFTR, direct_DMR_direct), each complex [nnz] at
+        the rows of H_Rindex [nnz, 5] = (Rx, Ry, Rz, i0, j0).  The (nk, n, n) inputs are numpy arrays or CUDA
+        tensors; kgrid = (kx, ky, kz) of the k mesh.  window = (KS_eigenEnergy[nk, n], NBAND, FromValToKS, mu, beta)
+        for a windowed downfolding (dens and DF padded beyond NBAND[k]); None: the full band window."""
         dev = _is_torch(densityMatDFT)
         d, f, v = _Arr(densityMatDFT, dev), _Arr(DF_CorrBase, dev), _Arr(KS_eigenVectors, dev)
         s = _Arr(S_overlap, dev) if S_overlap is not None else None
@@ -366,10 +373,31 @@ class Context:
             outs = [np.empty(nnz, np.complex128) for _ in range(3)]
             ptrs = [o.ctypes.data for o in outs]
         kx, ky, kz = kgrid
-        st = self.lib.dmftgpu_upfold(self.h, int(n), int(kx), int(ky), int(kz), _vp(d.ptr), _vp(f.ptr), _vp(v.ptr),
-                                     _vp(s.ptr) if s else None, int(nnz), ri.ctypes.data_as(_ip), _vp(ptrs[0]),
-                                     _vp(ptrs[1]), _vp(ptrs[2]), self._flags(dev))
-        self._check("dmftgpu_upfold", st)
+        if window is None:
+            st = self.lib.dmftgpu_upfold(self.h, int(n), int(kx), int(ky), int(kz), _vp(d.ptr), _vp(f.ptr),
+                                         _vp(v.ptr), _vp(s.ptr) if s else None, int(nnz), ri.ctypes.data_as(_ip),
+                                         _vp(ptrs[0]), _vp(ptrs[1]), _vp(ptrs[2]), self._flags(dev))
+            self._check("dmftgpu_upfold", st)
+        else:
+            eps, nband, fvk, mu, beta = window
+            if dev:
+                import torch
+                e_obj = torch.as_tensor(eps, dtype=torch.float64, device=d.obj.device).contiguous()
+                e_ptr = e_obj.data_ptr()
+            else:
+                e_obj = np.ascontiguousarray(eps, dtype=np.float64)
+                e_ptr = e_obj.ctypes.data
+            nb = np.ascontiguousarray(nband, np.int32)
+            nk = nb.shape[0]
+            win = np.full((nk, n), -1, np.int32)
+            for k in range(nk):
+                win[k, :nb[k]] = fvk[k]
+            st = self.lib.dmftgpu_upfold_window(self.h, int(n), int(kx), int(ky), int(kz), _vp(d.ptr), _vp(f.ptr),
+                                                _vp(v.ptr), _vp(s.ptr) if s else None, _vp(e_ptr),
+                                                nb.ctypes.data_as(_ip), win.ctypes.data_as(_ip), float(mu),
+                                                float(beta), int(nnz), ri.ctypes.data_as(_ip), _vp(ptrs[0]),
+                                                _vp(ptrs[1]), _vp(ptrs[2]), self._flags(dev))
+            self._check("dmftgpu_upfold_window", st)
         return tuple(outs)
 
     def GreenFtn_w_vjp(self, lat, H_k, SelfE_w, mu, Gbar):
@@ -398,11 +426,13 @@ class Context:
         self._check("dmftgpu_gloc_jvp", st)
         return out.result()
 
-    def downfolding_ftn(self, H_k, HartrIndex_inDFT, S_overlap=None, with_df=False):
-        """Construct_Hk_Sk's generalized eigenproblem and downfolding_ftn over the full band window, per k: returns
-        (KS_eigenEnergy[nk,n], H_k_inModelSpace[nk,n,n], impurity_site_Hamiltonian[D,D]) and, with with_df,
-        DF_CorrBase[nk,n,n] and KS_eigenVectors_orthoBasis[nk,n,n] as fourth and fifth items.  H_k, S_overlap: (nk, n, n) numpy arrays or CUDA tensors (S_overlap
-        None: orthogonal basis); HartrIndex_inDFT: the D correlated orbitals."""
+    def downfolding_ftn(self, H_k, HartrIndex_inDFT, S_overlap=None, with_df=False, window=None, pad_energy=1e4):
+        """Construct_Hk_Sk's generalized eigenproblem and downfolding_ftn, per k: returns (KS_eigenEnergy[nk,n],
+        H_k_inModelSpace[nk,n,n], impurity_site_Hamiltonian[D,D]) and, with with_df, DF_CorrBase[nk,n,n] and
+        KS_eigenVectors_orthoBasis[nk,n,n] as fourth and fifth items; with window = (muDFT, lower, upper) the band
+        window of low_energy_subspace_in_KS_basis, and (NBAND[nk], FromValToKS list) follow as the last two items
+        (H_model and DF padded beyond NBAND[k] as dmftgpu_downfold_window describes).  H_k, S_overlap: (nk, n, n)
+        numpy arrays or CUDA tensors (S_overlap None: orthogonal basis); HartrIndex_inDFT: the D correlated orbitals."""
         dev = _is_torch(H_k)
         h = _Arr(H_k, dev)
         s = _Arr(S_overlap, dev) if S_overlap is not None else None
@@ -420,12 +450,29 @@ class Context:
         else:
             eps = np.empty((nk, n))
             ep = eps.ctypes.data
-        st = self.lib.dmftgpu_downfold(self.h, int(nk), int(n), int(D), hartr.ctypes.data_as(_ip), _vp(h.ptr),
-                                       _vp(s.ptr) if s else None, _vp(ep), _vp(hm.ptr), _vp(df.ptr) if df else None,
-                                       _vp(ev.ptr) if ev else None, _vp(hi.ptr), self._flags(dev))
-        self._check("dmftgpu_downfold", st)
+        if window is None:
+            st = self.lib.dmftgpu_downfold(self.h, int(nk), int(n), int(D), hartr.ctypes.data_as(_ip), _vp(h.ptr),
+                                           _vp(s.ptr) if s else None, _vp(ep), _vp(hm.ptr),
+                                           _vp(df.ptr) if df else None, _vp(ev.ptr) if ev else None, _vp(hi.ptr),
+                                           self._flags(dev))
+            self._check("dmftgpu_downfold", st)
+        else:
+            nband = np.zeros(nk, np.int32)
+            win = np.zeros((nk, n), np.int32)
+            mu_dft, lower, upper = (float(x) for x in window)
+            st = self.lib.dmftgpu_downfold_window(self.h, int(nk), int(n), int(D), hartr.ctypes.data_as(_ip),
+                                                  _vp(h.ptr), _vp(s.ptr) if s else None, mu_dft, lower, upper,
+                                                  float(pad_energy), nband.ctypes.data_as(_ip),
+                                                  win.ctypes.data_as(_ip), _vp(ep), _vp(hm.ptr),
+                                                  _vp(df.ptr) if df else None, _vp(ev.ptr) if ev else None,
+                                                  _vp(hi.ptr), self._flags(dev))
+            self._check("dmftgpu_downfold_window", st)
         out = (eps, hm.result(), hi.result())
-        return out + (df.result(), ev.result()) if with_df else out
+        if with_df:
+            out = out + (df.result(), ev.result())
+        if window is not None:
+            out = out + (nband, [win[k, :nband[k]].copy() for k in range(nk)])
+        return out
 
     def GiwToNele(self, lat, H_k, SelfE_w, mu, deriv=False, mixed=False, explicit=False, tensor=True):
         """N(mu) (and dN/dmu with deriv).  In the mixed form the N(mu) pass of correlated blocks of 4 .. 10 orbitals

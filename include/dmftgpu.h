@@ -41,7 +41,8 @@ enum {
 #define DMFTGPU_MIXED 0x2       /* double-float (FP32-pair) arithmetic on the FP32 pipe: lattice sums and getStimp */
 #define DMFTGPU_NEWTON 0x4      /* dmftgpu_adjust_mu: Newton steps on dN/dmu from the same pass */
 #define DMFTGPU_EXPLICIT 0x8    /* lattice sums by explicit n x n inversion of every (k, iw) matrix, as the
-                                   reference does (default: the exact correlated-block Schur form) */
+                                   reference does (default: the exact correlated-block Schur form); FP64, or
+                                   double-float with DMFTGPU_MIXED */
 #define DMFTGPU_GRAPH 0x20     /* dmftgpu_greenftn_w_batched: replay the batched pass as one CUDA graph */
 #define DMFTGPU_AUTOTUNE 0x40  /* dmftgpu_greenftn_w_batched: tune each Schur kernel's k chunking on first use */
 #define DMFTGPU_NO_TENSOR 0x80 /* with DMFTGPU_MIXED: keep the contractions (H(k), the N(mu) pole sums) on the
@@ -144,6 +145,15 @@ int dmftgpu_upfold(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double
                    const double *evec, const double *sk, int nnz, const int *rindex, double *dm_dual_dual,
                    double *dm_dual_direct, double *dm_direct, int flags);
 
+/* dmftgpu_upfold with a band window (src/upfolding.cpp:10-35): dens and df as dmftgpu_downfold_window leaves them
+ * (the window in the leading NBAND[k] x NBAND[k] block), eps[nk][n] the band energies, nband / from_val_to_ks (host)
+ * its window; Matrix_KSBase is the Fermi diagonal f(e - mu) (beta, the reference's +-100 cut-offs) with the window's
+ * rows and columns replaced by DF^H dens DF, then D_DFT = V Matrix_KSBase V^H and the three k -> R sums. */
+int dmftgpu_upfold_window(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const double *dens, const double *df,
+                          const double *evec, const double *sk, const double *eps, const int *nband,
+                          const int *from_val_to_ks, double mu, double beta, int nnz, const int *rindex,
+                          double *dm_dual_dual, double *dm_dual_direct, double *dm_direct, int flags);
+
 /* GreenFtn_w's per-k density matrix in the model basis, densityMatDFT (src/GreenFtn.cpp:170-172, 268-275,
  * 311-319): dens[nk][n][n] = (1/beta) sum_{n < 2 nfreq} [G + G^H - G0 - G0^H](k, iw_n) + U f(e0) U^H, with G the full
  * n x n lattice Green function (Sigma on the HartrIndex orbitals, its moment tail beyond nfreq), G0 the resolvent
@@ -176,6 +186,19 @@ int dmftgpu_gloc_jvp(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double 
  * FP64.  DMFTGPU_SINGULAR when S is not positive definite or the projected block is rank deficient. */
 int dmftgpu_downfold(dmftgpu_ctx *ctx, int nk, int n, int D, const int *hartr, const double *hk, const double *sk,
                      double *eps, double *hmodel, double *df, double *evec, double *himp, int flags);
+
+/* dmftgpu_downfold with the band window of low_energy_subspace_in_KS_basis (src/downfolding.cpp:130-187, used by
+ * downfolding_ftn, src/downfolding.cpp:20-63): per k the model space is the NBAND[k] bands with
+ * lower < e - mu_dft < upper (strict), FromValToKS[k] their indices (a contiguous ascending range, the band
+ * energies being ascending).  Outputs (host arrays) nband[nk] and from_val_to_ks[nk][n] (entries beyond NBAND[k]:
+ * -1); H_model and DF fill the leading NBAND[k] x NBAND[k] block of their n x n slots, the rest a decoupled padding
+ * (pad_energy on H_model's diagonal, the identity in DF): a padded band couples to no orbital, so every lattice sum of
+ * the padded H_model (G_loc, GwHF, NumMatrix, N(mu) with beta (pad_energy - mu) > 100) equals that of the ragged one.
+ * A k point whose window holds no band or fewer than D bands (where the reference exits) gives DMFTGPU_BADARG. */
+int dmftgpu_downfold_window(dmftgpu_ctx *ctx, int nk, int n, int D, const int *hartr, const double *hk,
+                            const double *sk, double mu_dft, double lower, double upper, double pad_energy,
+                            int *nband, int *from_val_to_ks, double *eps, double *hmodel, double *df, double *evec,
+                            double *himp, int flags);
 
 /* Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119, declared src/TB.h:45-47):
  * delta[nfreq][dim][dim] = (iw+mu) I - himp[orb] - sigma[orb] - (gw[orb])^-1, orb[dim] indexes D. */

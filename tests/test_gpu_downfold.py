@@ -116,3 +116,78 @@ def test_downfold_rejects_bad_input(ctx):
     # the context stays usable
     eps, hm, hi = ctx.downfolding_ftn(H, [0, 1])
     assert np.abs(eps - np.arange(n)[None]).max() < 1e-13
+
+
+def _dp28_overlap(orc, k=3):
+    wl = models.dp28(k=k, nfreq=16, ntau=16, beta=20.0)
+    H = _model_hk(orc, wl)
+    return wl, H, _overlap(np.random.default_rng(7), H.shape[0], wl.n)
+
+
+def test_downfold_band_window_matches_oracle(ctx, orc):
+    """The band window of low_energy_subspace_in_KS_basis (src/downfolding.cpp:130-187) selected on the device:
+    NBAND[k] (8 .. 11 here, ragged) and FromValToKS equal the host selection on the oracle's band energies, and the
+    windowed H_model (padded beyond NBAND[k]) matches the oracle's ragged one on every gauge-free quantity."""
+    from dmftpack_gb300 import window
+    wl, H, S = _dp28_overlap(orc)
+    hartr, mu, lower, upper, epad = list(range(6)), 0.0, -6.0, 3.0, 1e4
+    D = len(hartr)
+    eps_g, hm_g, hi_g, df_g, ev_g, nb_g, fvk_g = ctx.downfolding_ftn(H, hartr, S, with_df=True,
+                                                                     window=(mu, lower, upper), pad_energy=epad)
+    eps_full = orc.downfold(H, S, hartr)[0]
+    nb_o, fvk_o = window.low_energy_subspace_in_KS_basis(eps_full, mu, lower, upper, D)
+    assert np.array_equal(nb_g, nb_o) and all(np.array_equal(a, b) for a, b in zip(fvk_g, fvk_o))
+    assert len(set(nb_o.tolist())) > 1   # ragged
+    eps, Hm, DF, V, himp = orc.downfold_window(H, S, hartr, fvk_o)
+    sc = max(1.0, np.abs(eps_full).max())
+    assert np.abs(eps_g - eps_full).max() < TOL * sc
+    assert np.abs(hi_g - himp).max() < TOL * sc
+    n = wl.n
+    for k in range(H.shape[0]):
+        nb = nb_o[k]
+        blk = hm_g[k][:nb, :nb]
+        assert np.abs(blk[:D, :D] - Hm[k][:D, :D]).max() < TOL * sc
+        assert np.abs(np.linalg.eigvalsh(blk) - eps_full[k][fvk_o[k]]).max() < TOL * sc
+        pl = blk[:D, D:] @ blk[D:, :D]
+        assert np.abs(pl - Hm[k][:D, D:] @ Hm[k][D:, :D]).max() < TOL * sc * sc
+        pad = hm_g[k].copy()
+        pad[:nb, :nb] = 0
+        assert np.abs(pad - np.diag(np.r_[np.zeros(nb), np.full(n - nb, epad)])).max() == 0
+        assert np.abs(df_g[k] @ df_g[k].conj().T - np.eye(n)).max() < 1e-12
+
+
+def test_downfold_band_window_lattice_sum_equals_ragged(ctx, orc):
+    """GreenFtn_w on the padded H_model equals the lattice sum over the ragged NBAND[k] x NBAND[k] matrices (explicit
+    numpy inversion per k), and N(mu) does not depend on the padding energy (the padded bands cancel)."""
+    wl, H, S = _dp28_overlap(orc, k=2)
+    hartr, D = list(range(6)), 6
+    nf, beta, mu = 16, 20.0, 0.3
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    sig = np.zeros((nf, D, D), np.complex128)
+    for d in range(D):
+        sig[:, d, d] = 0.1 - 0.6j / (wn + 0.4)
+    _, hm, _, nb, _ = ctx.downfolding_ftn(H, hartr, S, window=(0.0, -6.0, 3.0), pad_energy=1e4)
+    nk, n = hm.shape[0], hm.shape[1]
+    lat = lib.Lattice(n, nk, nf, beta, 1, D)
+    gw, _, _ = ctx.GreenFtn_w(lat, hm, sig, mu)
+    ref = np.zeros((nf, D, D), np.complex128)
+    for k in range(nk):
+        m = nb[k]
+        for f in range(nf):
+            A = (1j * wn[f] + mu) * np.eye(m) - hm[k][:m, :m]
+            A[:D, :D] -= sig[f]
+            ref[f] += np.linalg.inv(A)[:D, :D]
+    assert rel_err(gw, ref / nk) < 1e-10
+    _, hm2, _, _, _ = ctx.downfolding_ftn(H, hartr, S, window=(0.0, -6.0, 3.0), pad_energy=3e4)
+    N1 = ctx.GiwToNele(lat, hm, sig, mu)
+    N2 = ctx.GiwToNele(lat, hm2, sig, mu)
+    assert abs(N1 - N2) < 1e-11 * abs(N1)
+
+
+def test_downfold_band_window_rejects_too_few_bands(ctx, orc):
+    wl, H, S = _dp28_overlap(orc, k=2)
+    with pytest.raises(lib.DmftGpuError) as e:   # a window narrower than the 6 correlated orbitals at some k
+        ctx.downfolding_ftn(H, list(range(6)), S, window=(0.0, -1.0, 1.0))
+    assert e.value.code == lib.BADARG
+    eps, hm, hi = ctx.downfolding_ftn(H, list(range(6)), S)   # the context stays usable
+    assert np.isfinite(eps).all()

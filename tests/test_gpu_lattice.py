@@ -9,6 +9,7 @@ from dmftpack_gb300 import lib, models
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-10   # relative, plain FP64 path vs FP64 oracle
+TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
 
 
 def _setup(orc, wl):
@@ -105,6 +106,30 @@ def test_greenftn_w_padding_and_hartree_index(ctx, orc, n, D, hartr, explicit):
     assert abs(gN - N) < 1e-11 * max(1, abs(N)) and abs(gdN - dN) < 1e-9 * abs(dN)
 
 
+@pytest.mark.parametrize("n,D,hartr", [(5, 2, [3, 1]), (7, 3, None), (12, 3, None), (16, 5, None), (9, 9, None),
+                                        (28, 10, None)])
+def test_explicit_mixed_matches_oracle(ctx, orc, n, D, hartr):
+    """The reference's own algorithm (an explicit n x n inversion of every (k, iw) matrix, src/GreenFtn.cpp:245-261)
+    in double-float on the FP32 pipe (DMFTGPU_EXPLICIT | DMFTGPU_MIXED): G_loc, GwHF, NumMatrix, N and dN/dmu."""
+    rng = np.random.default_rng(n * 7 + D)
+    nk, nf, beta = 27, 32, 8.0
+    A = rng.normal(size=(nk, n, n)) + 1j * rng.normal(size=(nk, n, n))
+    H = (A + np.conj(np.swapaxes(A, 1, 2))) / 2
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    S = np.zeros((nf, D, D), complex)
+    for d in range(D):
+        S[:, d, d] = 0.2 - 0.7j / (wn + 0.5)
+    S[:, 0, D - 1] = S[:, D - 1, 0] = 0.05 if D > 1 else 0
+    h = np.arange(D) if hartr is None else np.array(hartr)
+    lat = lib.Lattice(n, nk, nf, beta, 1, D, hartr=h)
+    gw, gwhf, num = orc.greenftn_w(H, S, -0.3, beta, 1, D, hartr=h)
+    g_gw, g_gwhf, g_num = ctx.GreenFtn_w(lat, H, S, -0.3, explicit=True, mixed=True)
+    assert rel_err(g_gw, gw) < TOL_MIXED and rel_err(g_gwhf, gwhf) < TOL_MIXED and rel_err(g_num, num) < TOL_MIXED
+    N, dN = orc.nele(H, S, -0.3, beta, 1, D, hartr=h, deriv=True)
+    gN, gdN = ctx.GiwToNele(lat, H, S, -0.3, deriv=True, explicit=True, mixed=True)
+    assert abs(gN - N) < 1e-10 * max(1, abs(N)) and abs(gdN - dN) < 1e-9 * abs(dN)
+
+
 def test_large_orbital_count_schur_only(ctx, orc):
     """n = 56 with a 20-orbital correlated block (beyond the explicit kernels' register budget)."""
     rng = np.random.default_rng(5)
@@ -182,7 +207,6 @@ def test_adjust_mu_reports_singular_inversion(ctx, newton):
     assert e.value.code == lib.SINGULAR
 
 
-TOL_MIXED = 1e-9   # double-float (split-precision) path vs FP64 oracle
 
 
 @pytest.mark.parametrize("n,D,nf", [(12, 4, 40), (16, 6, 33), (20, 8, 48), (28, 10, 64), (19, 9, 40), (40, 10, 24),

@@ -57,3 +57,26 @@ def test_upfold_device_pointers_and_bad_index(ctx, orc):
     with pytest.raises(lib.DmftGpuError) as e:
         ctx.upfolding_density(H, eye, eye, wl.kgrid, bad)
     assert e.value.code == lib.BADARG
+
+
+def test_upfold_band_window_matches_oracle(ctx, orc):
+    """upfolding_density after a windowed downfolding (src/upfolding.cpp:10-35): the Fermi diagonal outside the
+    window, the model-basis block inside it, against the oracle's upfold_window on the same inputs."""
+    wl = models.dp28(k=3, nfreq=16, ntau=16, beta=20.0)
+    H = _hk(orc, wl)
+    rng = np.random.default_rng(9)
+    B = 0.3 * (rng.normal(size=H.shape) + 1j * rng.normal(size=H.shape))
+    S = np.eye(wl.n)[None] + B @ B.conj().transpose(0, 2, 1) / wl.n
+    hartr, D, mu = list(range(6)), 6, 0.1
+    eps, hm, _, df, ev, nb, fvk = ctx.downfolding_ftn(H, hartr, S, with_df=True, window=(0.0, -6.0, 3.0))
+    sig = wl.sigma[:, :D, :D].copy()
+    lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, 1, D)
+    dens = ctx.densityMatDFT(lat, hm, sig, mu)
+    for k in range(wl.nk):   # the padded bands carry no density
+        assert np.abs(dens[k][nb[k]:, :]).max() < 1e-12 and np.abs(dens[k][:, nb[k]:]).max() < 1e-12
+    got = ctx.upfolding_density(dens, df, ev, wl.kgrid, wl.rindex, S, window=(eps, nb, fvk, mu, wl.beta))
+    ref = orc.upfold_window([dens[k][:nb[k], :nb[k]] for k in range(wl.nk)],
+                            [df[k][:nb[k], :nb[k]] for k in range(wl.nk)], ev, S, eps, fvk, mu, wl.beta, wl.kgrid,
+                            wl.rindex)
+    for g, r in zip(got, ref):
+        assert rel_err(g, r) < 1e-12
