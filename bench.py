@@ -537,7 +537,7 @@ def run_dmft(ctx, dev, a):
     tcm = lambda t: t.transpose(-1, -2).contiguous()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)
+    Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev, mixed=mixed)
     torch.cuda.synchronize()
     t_hk = time.perf_counter() - t0
     Hcm = tcm(Hd)
@@ -550,7 +550,7 @@ def run_dmft(ctx, dev, a):
     for it in range(1, a.iters + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev)  # TightBinding rebuilds H(k)
+        Hd = ctx.Construct_Hk(wl.n, wl.rindex, wl.hr, wl.kgrid, device_out=dev, mixed=mixed)  # TightBinding's H(k)
         Hcm = tcm(Hd)
         mu, gi, res = ctx.DMFT_iteration(lat, Hcm, p, it, se, we, nm, gl, mu, mixed=mixed, newton=a.newton)
         torch.cuda.synchronize()
