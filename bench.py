@@ -470,6 +470,7 @@ def run_density(ctx, dev, a):
     out = {"nk": wl.nk, "n": wl.n, "D": wl.D, "nfreq": wl.nfreq, "nnz": len(wl.rindex)}
     eye = torch.eye(wl.n, dtype=torch.complex128, device=dev).expand(wl.nk, wl.n, wl.n).contiguous()
     for name, fn in (("density_dft", lambda: ctx.densityMatDFT(lat, Hd, sig, 0.0)),
+                     ("density_dft_mixed", lambda: ctx.densityMatDFT(lat, Hd, sig, 0.0, mixed=True)),
                      ("greenftn_w_fp64", lambda: ctx.GreenFtn_w(lat, Hd, sig, 0.0)),
                      ("upfolding_density", lambda: ctx.upfolding_density(Hd, eye, eye, wl.kgrid, wl.rindex))):
         fn()

@@ -17,7 +17,8 @@
 //
 // Mapping: one CTA per k point (and frequency split); a lane group of W lanes owns one frequency at a time, lane c
 // holds column c of S and inverts it with gj_inverse (schur.cuh); the group's products and accumulators live in its
-// own shared-memory tiles, reduced over groups in a fixed order at the end.  FP64.
+// own shared-memory tiles, reduced over groups in a fixed order at the end.  FP64 (Ops = OpsD) or double-float on
+// the FP32 pipe (OpsF, DMFTGPU_MIXED), with 16-byte complex elements either way.
 #pragma once
 #include "schur.cuh"
 
@@ -45,10 +46,11 @@ inline size_t dens_smem(int DP, int D, int m, int n, int ng) {
     return ((size_t)m * D + m + (size_t)D * D + n + (size_t)ng * dens_group_elems(DP, D, m, n)) * sizeof(double2);
 }
 
-template <int DP, int W>
+template <class Ops, int DP, int W>
 __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
-    typedef double2 C;
-    extern __shared__ double2 sm[];
+    typedef typename Ops::C C;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
     const int D = g.D, DD = D * D, m = g.m, n = g.n, NG = g.ng;
     const int k = blockIdx.x, split = blockIdx.y, nsplit = gridDim.y;
     const int c = threadIdx.x & (W - 1), grp = threadIdx.x / W;
@@ -56,20 +58,20 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
     C *sB = sm, *sE = sB + (size_t)m * D, *sH = sE + m, *sE0 = sH + DD, *gbase = sE0 + n;
     C *wl = gbase + grp * PG, *tG = wl + m, *Z3 = tG + DP * DP, *Xpq = Z3 + (size_t)m * D, *Yqq = Xpq + (size_t)D * m,
       *sw = Yqq + (size_t)m * m, *sr = sw + m;
-    for (int t = threadIdx.x; t < m * D; t += blockDim.x) sB[t] = g.B[(size_t)k * m * D + t];
-    for (int t = threadIdx.x; t < m; t += blockDim.x) sE[t] = cmk(g.mu - g.epsQ[(size_t)k * m + t], 0.0);
+    for (int t = threadIdx.x; t < m * D; t += blockDim.x) sB[t] = Ops::from(g.B[(size_t)k * m * D + t]);
+    for (int t = threadIdx.x; t < m; t += blockDim.x) sE[t] = Ops::from(cmk(g.mu - g.epsQ[(size_t)k * m + t], 0.0));
     for (int t = threadIdx.x; t < DD; t += blockDim.x)
-        sH[t] = cneg(g.H[(size_t)k * n * n + t % D + (size_t)(t / D) * n]);
-    for (int t = threadIdx.x; t < n; t += blockDim.x) sE0[t] = cmk(g.mu - g.eps0[(size_t)k * n + t], 0.0);
-    for (int q = c; q < D * m; q += W) Xpq[q] = cmk(0, 0);
-    for (int q = c; q < m * m; q += W) Yqq[q] = cmk(0, 0);
-    for (int q = c; q < m; q += W) sw[q] = cmk(0, 0);
-    for (int q = c; q < n; q += W) sr[q] = cmk(0, 0);
+        sH[t] = Ops::from(cneg(g.H[(size_t)k * n * n + t % D + (size_t)(t / D) * n]));
+    for (int t = threadIdx.x; t < n; t += blockDim.x) sE0[t] = Ops::from(cmk(g.mu - g.eps0[(size_t)k * n + t], 0.0));
+    for (int q = c; q < D * m; q += W) Xpq[q] = Ops::zero();
+    for (int q = c; q < m * m; q += W) Yqq[q] = Ops::zero();
+    for (int q = c; q < m; q += W) sw[q] = Ops::zero();
+    for (int q = c; q < n; q += W) sr[q] = Ops::zero();
     __syncthreads();
     const bool col = c < D;
     C accP[DP];
 #pragma unroll
-    for (int a = 0; a < DP; a++) accP[a] = cmk(0, 0);
+    for (int a = 0; a < DP; a++) accP[a] = Ops::zero();
     bool sing = false;
     // every group of the CTA runs the same number of steps (the warp-collective inversion needs converged warps);
     // a step past the last frequency recomputes the last one and accumulates nothing
@@ -79,37 +81,40 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
         const bool valid = f_raw < g.nf2;
         const int f = valid ? f_raw : g.nf2 - 1;
         const double w = DG_PI * (2. * f + 1.) / g.beta;
-        const C iwc = cmk(0.0, w), zc = cmk(g.mu, w);
-        const C *sg = g.sig + (size_t)f * DD;
+        const C iwc = Ops::from(cmk(0.0, w)), zc = Ops::from(cmk(g.mu, w));
+        const double2 *sg = g.sig + (size_t)f * DD;
         __syncwarp();
         for (int l = c; l < m; l += W) {
-            const C x = crcp(cadd(sE[l], iwc));
+            const C x = Ops::rcp(Ops::add(sE[l], iwc));
             wl[l] = x;
-            if (valid) sw[l] = cadd(sw[l], x);
+            if (valid) sw[l] = Ops::add(sw[l], x);
         }
         if (valid)
-            for (int j = c; j < n; j += W) sr[j].x += 2.0 * crcp(cadd(sE0[j], iwc)).x;
+            for (int j = c; j < n; j += W) {
+                const C r = Ops::rcp(Ops::add(sE0[j], iwc));
+                sr[j] = Ops::add(sr[j], Ops::add(r, r));  // 2 Re 1/(z - e0_j): the real part is read
+            }
         __syncwarp();
         // column c of S = z - H_PP - Sigma - sum_l w_l b_l b_l^H (identity padding beyond D), inverted in place
         C s[DP];
 #pragma unroll
         for (int a = 0; a < DP; a++) {
-            if (col && a < D) s[a] = csub(sH[a + c * D], sg[a + (size_t)c * D]);
-            else s[a] = (a == c) ? cmk(1, 0) : cmk(0, 0);
-            if (a == c && col) s[a] = cadd(s[a], zc);
+            if (col && a < D) s[a] = Ops::sub(sH[a + c * D], Ops::from(sg[a + (size_t)c * D]));
+            else s[a] = (a == c) ? Ops::one() : Ops::zero();
+            if (a == c && col) s[a] = Ops::add(s[a], zc);
         }
         if (col)
             for (int l = 0; l < m; l++) {
-                const C q = cmulc(wl[l], sB[l * D + c]);
+                const C q = Ops::mulc(wl[l], sB[l * D + c]);
 #pragma unroll
                 for (int a = 0; a < DP; a++)
-                    if (a < D) s[a] = cfms(sB[l * D + a], q, s[a]);
+                    if (a < D) s[a] = Ops::fms(sB[l * D + a], q, s[a]);
             }
-        const bool sg_ = gj_inverse<OpsD, DP, W>(s, c);
+        const bool sg_ = gj_inverse<Ops, DP, W>(s, c);
         sing |= valid && sg_;
         if (valid) {
 #pragma unroll
-            for (int a = 0; a < DP; a++) accP[a] = cadd(accP[a], s[a]);
+            for (int a = 0; a < DP; a++) accP[a] = Ops::add(accP[a], s[a]);
         }
         if (c < DP) {
 #pragma unroll
@@ -122,15 +127,15 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
             const int a = q % D, l = q / D;
             const C wv = wl[l];
             const C *bl = sB + (size_t)l * D;
-            C z1 = cmk(0, 0), z3 = cmk(0, 0);
+            C z1 = Ops::zero(), z3 = Ops::zero();
             for (int b = 0; b < D; b++) {
-                z1 = cfma(tG[a + b * DP], bl[b], z1);
-                z3 = cfma(cconj(bl[b]), tG[b + a * DP], z3);
+                z1 = Ops::fma(tG[a + b * DP], bl[b], z1);
+                z3 = Ops::fma(Ops::conj(bl[b]), tG[b + a * DP], z3);
             }
-            z1 = cmul(z1, wv);
-            z3 = cmul(z3, wv);
+            z1 = Ops::mul(z1, wv);
+            z3 = Ops::mul(z3, wv);
             Z3[l + (size_t)a * m] = z3;
-            if (valid) Xpq[q] = cadd(Xpq[q], cadd(z1, cconj(z3)));
+            if (valid) Xpq[q] = Ops::add(Xpq[q], Ops::add(z1, Ops::conj(z3)));
         }
         __syncwarp();
         // entries (l, l') spread over the lanes: Y_QQ(l, l') += (Z3 b_l')(l) w_l'
@@ -138,9 +143,9 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
             for (int q = c; q < m * m; q += W) {
                 const int l = q % m, lp = q / m;
                 const C *bl = sB + (size_t)lp * D;
-                C y = cmk(0, 0);
-                for (int b = 0; b < D; b++) y = cfma(Z3[l + (size_t)b * m], bl[b], y);
-                Yqq[q] = cfma(y, wl[lp], Yqq[q]);
+                C y = Ops::zero();
+                for (int b = 0; b < D; b++) y = Ops::fma(Z3[l + (size_t)b * m], bl[b], y);
+                Yqq[q] = Ops::fma(y, wl[lp], Yqq[q]);
             }
     }
     __syncwarp();
@@ -154,15 +159,15 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
     double2 *Yo = g.Y + ((size_t)split * g.nk + k) * n * n;
     for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
         const int i = q % n, j = q / n;
-        C v = cmk(0, 0);
+        double2 v = cmk(0, 0);
         for (int gg = 0; gg < NG; gg++) {
             const C *gb = gbase + gg * PG;
             const C *gG = gb + m, *gX = gG + DP * DP + (size_t)m * D, *gY = gX + (size_t)D * m, *gw = gY + (size_t)m * m;
-            if (i < D && j < D) v = cadd(v, gG[i + j * DP]);
-            else if (i < D) v = cadd(v, gX[i + (size_t)(j - D) * D]);
+            if (i < D && j < D) v = cadd(v, Ops::to(gG[i + j * DP]));
+            else if (i < D) v = cadd(v, Ops::to(gX[i + (size_t)(j - D) * D]));
             else if (j >= D) {
-                v = cadd(v, gY[(i - D) + (size_t)(j - D) * m]);
-                if (i == j) v = cadd(v, gw[i - D]);
+                v = cadd(v, Ops::to(gY[(i - D) + (size_t)(j - D) * m]));
+                if (i == j) v = cadd(v, Ops::to(gw[i - D]));
             }
         }
         Yo[q] = v;
@@ -171,14 +176,14 @@ __global__ void __launch_bounds__(128) k_dens_sum(DensArgs g) {
         double r = 0;
         for (int gg = 0; gg < NG; gg++) {
             const C *gb = gbase + gg * PG;
-            r += (gb + m + DP * DP + 2 * (size_t)m * D + (size_t)m * m + m)[j].x;
+            r += Ops::re((gb + m + DP * DP + 2 * (size_t)m * D + (size_t)m * m + m)[j]);
         }
         g.R[((size_t)split * g.nk + k) * n + j] = r;
     }
 }
 
 typedef void (*DensKernel)(DensArgs);
-#define DG_DENS_DECL(DP) DensKernel dens_kernel_##DP();
+#define DG_DENS_DECL(DP) DensKernel dens_kernel_##DP(bool mixed);
 DG_DENS_DECL(1)
 DG_DENS_DECL(2)
 DG_DENS_DECL(3)
@@ -190,6 +195,6 @@ DG_DENS_DECL(12)
 DG_DENS_DECL(16)
 DG_DENS_DECL(20)
 #define DG_DENS_INST(DP, W) \
-    DensKernel dens_kernel_##DP() { return k_dens_sum<DP, W>; }
+    DensKernel dens_kernel_##DP(bool mixed) { return mixed ? k_dens_sum<OpsF, DP, W> : k_dens_sum<OpsD, DP, W>; }
 
 }  // namespace dg

@@ -82,6 +82,7 @@ struct OpsD {
     static __device__ __forceinline__ C neg(C a) { return cneg(a); }
     static __device__ __forceinline__ C mul(C a, C b) { return cmul(a, b); }
     static __device__ __forceinline__ C mulc(C a, C b) { return cmulc(a, b); }  // a conj(b)
+    static __device__ __forceinline__ C conj(C a) { return cconj(a); }
     static __device__ __forceinline__ C fma(C a, C b, C acc) { return cfma(a, b, acc); }
     static __device__ __forceinline__ C fms(C a, C b, C acc) { return cfms(a, b, acc); }
     static __device__ __forceinline__ C rcp(C a) { return crcp(a); }
@@ -117,6 +118,7 @@ struct OpsF {
     static __device__ __forceinline__ C mul(C a, C b) {
         return {df_fma(df_neg(a.im), b.im, df_mul(a.re, b.re)), df_fma(a.im, b.re, df_mul(a.re, b.im))};
     }
+    static __device__ __forceinline__ C conj(C a) { return {a.re, df_neg(a.im)}; }
     static __device__ __forceinline__ C mulc(C a, C b) {  // a conj(b)
         return {df_fma(a.im, b.im, df_mul(a.re, b.re)), df_fma(df_neg(a.re), b.im, df_mul(a.im, b.re))};
     }

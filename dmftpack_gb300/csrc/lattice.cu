@@ -17,11 +17,13 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 
 #include "gloc.cuh"
 #include "schur.cuh"
 #include "smallmat.cuh"
+#include "smallmat_df.cuh"
 #include "adjoint.cuh"
 #include "density.cuh"
 #include "trace_tc.h"
@@ -200,10 +202,17 @@ __global__ void __launch_bounds__(EIG_THREADS) k_schur_prep_blk(int n, int D, co
     if (st && threadIdx.x == 0) dg_flag(status, DG_NONCONV);
 }
 
-// The same two decompositions with one warp per k point (warp_heig), four k points per CTA: for the matrix sizes
-// up to 32 a block-wide Jacobi spends most of its time in block barriers with idle threads.  Per-warp shared
-// region: three n x n complex matrices, eigenvalues [64], order [64], rotations [33].
+// The same two decompositions with one warp per k point, four k points per CTA: for the matrix sizes up to 32 a
+// block-wide Jacobi spends most of its time in block barriers with idle threads.  Ops = OpsD: warp_heig in FP64;
+// OpsF (the DMFTGPU_MIXED passes): warp_heig_df, every step in double-float on the FP32 pipe.  Per-warp shared
+// region: three n x n complex matrices (16-byte elements either way), eigenvalues [64], order [64], rotations [33].
 constexpr int EIG_WPB = 4;
+template <class Ops>
+__device__ __forceinline__ int warp_heig_ops(int n, const typename Ops::C *A0, typename Ops::C *a,
+                                             typename Ops::C *u, double *w, int *order, DgRot *rot) {
+    if constexpr (std::is_same<Ops, OpsF>::value) return warp_heig_df(n, A0, a, u, w, order, rot, 1e-24f);
+    else return warp_heig(n, A0, a, u, w, order, rot);
+}
 __host__ __device__ inline size_t warp_eig_bytes(int n) {
     const size_t b = (size_t)3 * n * n * sizeof(double2) + EIG_NMAX * sizeof(double) + EIG_NMAX * sizeof(int) + 16 +
                      (EIG_NMAX / 2 + 1) * sizeof(DgRot);
@@ -223,6 +232,7 @@ __device__ inline EigSmem warp_eig_smem(double2 *sm, int n) {
     return e;
 }
 
+template <class Ops>
 __global__ void __launch_bounds__(32 * EIG_WPB) k_static_eig_warp(int nk, int n, int D, int nh, int mask,
                                                                   const double2 *__restrict__ H,
                                                                   const double2 *__restrict__ m0, double *eps,
@@ -232,58 +242,65 @@ __global__ void __launch_bounds__(32 * EIG_WPB) k_static_eig_warp(int nk, int n,
     if (k >= nk) return;  // whole warps only
     const size_t nn = (size_t)n * n;
     EigSmem e = warp_eig_smem(esm, n);
+    typedef typename Ops::C C;
+    C *A0 = reinterpret_cast<C *>(e.A0), *A = reinterpret_cast<C *>(e.A), *U = reinterpret_cast<C *>(e.U);
     const double2 *Hk = H + (size_t)k * nn;
     for (int q = lane; q < (int)nn; q += 32) {
         const int a = q % n, b = q / n;
         double2 v = Hk[q];
         if (a < D && b < D && (!mask || a / nh == b / nh)) v = cadd(v, m0[a + b * D]);
-        e.A0[q] = v;
+        A0[q] = Ops::from(v);
     }
     __syncwarp();
-    const int st = warp_heig(n, e.A0, e.A, e.U, e.w, e.ord, e.rot);
+    const int st = warp_heig_ops<Ops>(n, A0, A, U, e.w, e.ord, e.rot);
     for (int l = lane; l < n; l += 32) eps[(size_t)k * n + l] = e.w[l];
     for (int q = lane; q < n * D; q += 32) {
         const int l = q / D, a = q % D;
-        UP[((size_t)k * n + l) * D + a] = DG_AT(e.U, n, a, l);
+        UP[((size_t)k * n + l) * D + a] = Ops::to(DG_AT(U, n, a, l));
     }
     if (Uf)
-        for (int q = lane; q < (int)nn; q += 32) Uf[(size_t)k * nn + q] = e.U[q];
+        for (int q = lane; q < (int)nn; q += 32) Uf[(size_t)k * nn + q] = Ops::to(U[q]);
     if (st && lane == 0) dg_flag(status, DG_NONCONV);
 }
 
+template <class Ops>
 __global__ void __launch_bounds__(32 * EIG_WPB) k_schur_prep_warp(int nk, int n, int D, const double2 *__restrict__ H,
                                                                   double *epsQ, double2 *B, double2 *Vq, int *status) {
     extern __shared__ double2 esm[];
     const int lane = threadIdx.x & 31, k = blockIdx.x * EIG_WPB + (threadIdx.x >> 5), m = n - D;
     if (k >= nk) return;  // whole warps only
     EigSmem e = warp_eig_smem(esm, m);
+    typedef typename Ops::C C;
+    C *A0 = reinterpret_cast<C *>(e.A0), *A = reinterpret_cast<C *>(e.A), *U = reinterpret_cast<C *>(e.U);
     const double2 *Hk = H + (size_t)k * n * n;
     for (int q = lane; q < m * m; q += 32) {
         const int i = q % m, j = q / m;
-        e.A0[q] = Hk[(D + i) + (size_t)(D + j) * n];
+        A0[q] = Ops::from(Hk[(D + i) + (size_t)(D + j) * n]);
     }
     __syncwarp();
-    const int st = warp_heig(m, e.A0, e.A, e.U, e.w, e.ord, e.rot);
+    const int st = warp_heig_ops<Ops>(m, A0, A, U, e.w, e.ord, e.rot);
     for (int l = lane; l < m; l += 32) epsQ[(size_t)k * m + l] = e.w[l];
+    // b_l = H_PQ V(:, l): in the arithmetic of the decomposition, stored in FP64
     for (int q = lane; q < m * D; q += 32) {
         const int l = q / D, a = q % D;
-        double2 s = cmk(0, 0);
-        for (int j = 0; j < m; j++) s = cfma(Hk[a + (size_t)(D + j) * n], DG_AT(e.U, m, j, l), s);
-        B[((size_t)k * m + l) * D + a] = s;
+        C s = Ops::zero();
+        for (int j = 0; j < m; j++) s = Ops::fma(Ops::from(Hk[a + (size_t)(D + j) * n]), DG_AT(U, m, j, l), s);
+        B[((size_t)k * m + l) * D + a] = Ops::to(s);
     }
     if (Vq)
-        for (int q = lane; q < m * m; q += 32) Vq[(size_t)k * m * m + q] = e.U[q];
+        for (int q = lane; q < m * m; q += 32) Vq[(size_t)k * m * m + q] = Ops::to(U[q]);
     if (st && lane == 0) dg_flag(status, DG_NONCONV);
 }
 
 // the Schur data of every k point (H_QQ = V diag(e) V^H, b_l = H_PQ V(:, l)), by warps for m <= 32
 int launch_schur_prep(dmftgpu_ctx *ctx, cudaStream_t s, int nk, int n, int D, const double2 *H, double *epsQ,
-                      double2 *B, double2 *Vq) {
+                      double2 *B, double2 *Vq, bool df = false) {
     const int m = n - D;
     if (m <= 32) {
         const size_t sm = EIG_WPB * warp_eig_bytes(m);
-        DG_CUDA(cudaFuncSetAttribute(k_schur_prep_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_schur_prep_warp<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, s>>>(nk, n, D, H, epsQ, B, Vq, ctx->d_status);
+        auto kern = df ? k_schur_prep_warp<OpsF> : k_schur_prep_warp<OpsD>;
+        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        kern<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, s>>>(nk, n, D, H, epsQ, B, Vq, ctx->d_status);
         DG_LAUNCH(ctx, "k_schur_prep_warp");
     } else {
         const size_t sm = eig_blk_smem(m);
@@ -488,8 +505,11 @@ int prepare_real(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, 
     return DMFTGPU_OK;
 }
 
+// df (the DMFTGPU_MIXED passes): the per-k eigendecompositions (n <= 32) in double-float on the FP32 pipe, and the
+// static one on the main stream after the Schur data instead of on the side stream (the mixed lattice kernels fill
+// the SMs; an eigendecomposition beside them slows them by more than it takes alone)
 int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const double2 *dS, int mask, Prepared &P,
-            bool vectors = false) {
+            bool vectors = false, bool df = false) {
     P.n = L->n;
     P.nk = L->nk;
     P.Nf = L->nfreq;
@@ -552,20 +572,21 @@ int prepare(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH, const
     // the Schur data (eigen-decomposition of H_QQ) is needed first, by k_schur, on the main stream; the
     // static eigen-decomposition of H + m0 feeds only the Fermi terms, so it runs on the side stream
     // (FP64-pipe work) while the lattice kernel (FP32 pipe in the mixed form) proceeds
-    if (m > 0) DG_TRY(launch_schur_prep(ctx, s, nk, n, D, P.H, P.epsQ, P.B, P.Vq));
+    if (m > 0) DG_TRY(launch_schur_prep(ctx, s, nk, n, D, P.H, P.epsQ, P.B, P.Vq, df));
     DG_CUDA(cudaEventRecord(ctx->ev_fork, s));
     DG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    cudaStream_t es = df ? s : ctx->side;
     if (n <= 32) {
         const size_t sm = EIG_WPB * warp_eig_bytes(n);
-        DG_CUDA(cudaFuncSetAttribute(k_static_eig_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_static_eig_warp<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, ctx->side>>>(nk, n, D, P.nh, mask, P.H, P.m0,
-                                                                                     P.eps, P.UP, P.Uf, ctx->d_status);
+        auto kern = df ? k_static_eig_warp<OpsF> : k_static_eig_warp<OpsD>;
+        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        kern<<<dg_ceil_div(nk, EIG_WPB), 32 * EIG_WPB, sm, es>>>(nk, n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, P.Uf,
+                                                                 ctx->d_status);
         DG_LAUNCH(ctx, "k_static_eig_warp");
     } else {
         const size_t sm = eig_blk_smem(n);
         DG_CUDA(cudaFuncSetAttribute(k_static_eig_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_static_eig_blk<<<nk, EIG_THREADS, sm, ctx->side>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, P.Uf,
-                                                             ctx->d_status);
+        k_static_eig_blk<<<nk, EIG_THREADS, sm, es>>>(n, D, P.nh, mask, P.H, P.m0, P.eps, P.UP, P.Uf, ctx->d_status);
         DG_LAUNCH(ctx, "k_static_eig_blk");
     }
     DG_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
@@ -913,7 +934,7 @@ int greenftn_w_dev(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double2 *dH
     const int D = L->ncl * L->nh, Nf = L->nfreq;
     const size_t DD = (size_t)D * D;
     Prepared P;
-    DG_TRY(prepare(ctx, L, dH, dS, 0, P));
+    DG_TRY(prepare(ctx, L, dH, dS, 0, P, false, (flags & DMFTGPU_MIXED) != 0));
     double2 *blk = (double2 *)dg_buf(ctx, "gloc.blk", 2 * Nf * DD * sizeof(double2));
     double2 *blk0 = (double2 *)dg_buf(ctx, "gloc.blk0", 2 * Nf * DD * sizeof(double2));
     double2 *occ = (double2 *)dg_buf(ctx, "gloc.occ", (size_t)L->nk * DD * sizeof(double2));
@@ -1001,27 +1022,28 @@ __global__ void __launch_bounds__(128) k_dens_finish(int nk, int n, int D, int n
 
 using dg::DensArgs;
 using dg::DensKernel;
-DensKernel pick_dens(int DP) {
+DensKernel pick_dens(int DP, bool mixed) {
     switch (DP) {
-        case 1: return dg::dens_kernel_1();
-        case 2: return dg::dens_kernel_2();
-        case 3: return dg::dens_kernel_3();
-        case 4: return dg::dens_kernel_4();
-        case 6: return dg::dens_kernel_6();
-        case 8: return dg::dens_kernel_8();
-        case 10: return dg::dens_kernel_10();
-        case 12: return dg::dens_kernel_12();
-        case 16: return dg::dens_kernel_16();
-        case 20: return dg::dens_kernel_20();
+        case 1: return dg::dens_kernel_1(mixed);
+        case 2: return dg::dens_kernel_2(mixed);
+        case 3: return dg::dens_kernel_3(mixed);
+        case 4: return dg::dens_kernel_4(mixed);
+        case 6: return dg::dens_kernel_6(mixed);
+        case 8: return dg::dens_kernel_8(mixed);
+        case 10: return dg::dens_kernel_10(mixed);
+        case 12: return dg::dens_kernel_12(mixed);
+        case 16: return dg::dens_kernel_16(mixed);
+        case 20: return dg::dens_kernel_20(mixed);
     }
     return nullptr;
 }
 
-// densityMatDFT for a prepared lattice (prepare(..., vectors = true)): enqueue only
-int run_density(dmftgpu_ctx *ctx, const Prepared &P, double mu, double2 *dens) {
+// densityMatDFT for a prepared lattice (prepare(..., vectors = true)): enqueue only; mixed: the per-(k, iw) work in
+// double-float
+int run_density(dmftgpu_ctx *ctx, const Prepared &P, double mu, double2 *dens, bool mixed) {
     const int n = P.n, D = P.D, m = n - D, nk = P.nk, nf2 = 2 * P.Nf;
     const SInst *si = pick_schur(D);
-    DensKernel kern = si ? pick_dens(si->DP) : nullptr;
+    DensKernel kern = si ? pick_dens(si->DP, mixed) : nullptr;
     if (!kern) return dg_fail(ctx, DMFTGPU_BADARG, "density: unsupported correlated block");
     const int DP = si->DP, W = si->W;
     // groups per CTA: the most resident warps per SM within 227 KB of shared memory per CTA
@@ -1364,7 +1386,7 @@ int dmftgpu_density_dft(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double
     DG_TRY(dg_status_reset(ctx));
     Prepared P;
     DG_TRY(prepare(ctx, L, dH, dS, 0, P, true));
-    DG_TRY(run_density(ctx, P, mu, dD));
+    DG_TRY(run_density(ctx, P, mu, dD, (flags & DMFTGPU_MIXED) != 0));
     DG_TRY(dg_out_done(ctx, dens, dD, nb, flags));
     int code = 0;
     DG_TRY(dg_status_read(ctx, &code));
@@ -1412,7 +1434,7 @@ int dmftgpu_nele(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *hk, c
     if (st) return st;
     DG_TRY(dg_status_reset(ctx));
     Prepared P;
-    DG_TRY(prepare(ctx, L, dH, dS, 1, P));
+    DG_TRY(prepare(ctx, L, dH, dS, 1, P, false, (flags & DMFTGPU_MIXED) != 0));
     DG_TRY(nele_host(ctx, P, mu, dnele != nullptr, nele, dnele, (flags & DMFTGPU_EXPLICIT) != 0,
                      (flags & DMFTGPU_MIXED) != 0));
     int code = 0;
@@ -1435,7 +1457,7 @@ int dmftgpu_adjust_mu(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *
     if (st) return st;
     DG_TRY(dg_status_reset(ctx));
     Prepared P;
-    DG_TRY(prepare(ctx, L, dH, dS, 1, P));
+    DG_TRY(prepare(ctx, L, dH, dS, 1, P, false, (flags & DMFTGPU_MIXED) != 0));
     int evals = 0;
     auto N = [&](double m, double *out, double *dout) {
         evals++;

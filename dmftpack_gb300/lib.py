@@ -342,14 +342,15 @@ class Context:
         self._check("dmftgpu_gloc_real", st)
         return g.result(), tr
 
-    def densityMatDFT(self, lat, H_k, SelfE_w, mu):
-        """GreenFtn_w's per-k density matrix densityMatDFT[nk, n, n] (the full-model-space occupation at each k)."""
+    def densityMatDFT(self, lat, H_k, SelfE_w, mu, mixed=False):
+        """GreenFtn_w's per-k density matrix densityMatDFT[nk, n, n] (the full-model-space occupation at each k);
+        mixed: the per-(k, iw) work in double-float on the FP32 pipe."""
         dev = _is_torch(H_k)
         h, s = _Arr(H_k, dev), _Arr(SelfE_w, dev)
         out = _Arr.empty((lat.nk, lat.n, lat.n), dev, like=h.obj)
         L = lat._c()
         st = self.lib.dmftgpu_density_dft(self.h, C.byref(L), _vp(h.ptr), _vp(s.ptr), float(mu), _vp(out.ptr),
-                                          self._flags(dev))
+                                          self._flags(dev, MIXED if mixed else 0))
         self._check("dmftgpu_density_dft", st)
         return out.result()
 

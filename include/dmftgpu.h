@@ -158,7 +158,8 @@ int dmftgpu_upfold_window(dmftgpu_ctx *ctx, int n, int kx, int ky, int kz, const
  * 311-319): dens[nk][n][n] = (1/beta) sum_{n < 2 nfreq} [G + G^H - G0 - G0^H](k, iw_n) + U f(e0) U^H, with G the full
  * n x n lattice Green function (Sigma on the HartrIndex orbitals, its moment tail beyond nfreq), G0 the resolvent
  * of the static H + m0 = U diag(e0) U^H and f the Fermi factors with the reference's +-100 cut-offs.  Computed
- * from the correlated-block Schur form (no n x n inversion); rows and columns in the caller's orbital order.  FP64. */
+ * from the correlated-block Schur form (no n x n inversion); rows and columns in the caller's orbital order.  FP64,
+ * or double-float on the FP32 pipe with DMFTGPU_MIXED. */
 int dmftgpu_density_dft(dmftgpu_ctx *ctx, const dmftgpu_lattice *lat, const double *hk, const double *sigma, double mu,
                         double *dens, int flags);
 

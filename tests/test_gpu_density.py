@@ -25,16 +25,18 @@ def _hk(orc, wl):
     return orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
 
 
+@pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("case", list(CASES))
-def test_density_dft_matches_oracle(ctx, orc, case):
+def test_density_dft_matches_oracle(ctx, orc, case, mixed):
+    """FP64 at 1e-10 and double-float (DMFTGPU_MIXED) at 1e-9 against the oracle's explicit inversions."""
     make, hartr = CASES[case]
     wl = make()
     H = _hk(orc, wl)
     mu = 0.15
     ref = orc.density_dft(H, wl.sigma, mu, wl.beta, hartr)
     lat = lib.Lattice(wl.n, wl.nk, wl.nfreq, wl.beta, wl.ncl, wl.nh, hartr)
-    got = ctx.densityMatDFT(lat, H, wl.sigma, mu)
-    assert rel_err(got, ref) < TOL
+    got = ctx.densityMatDFT(lat, H, wl.sigma, mu, mixed=mixed)
+    assert rel_err(got, ref) < (1e-9 if mixed else TOL)
 
 
 def test_density_dft_correlated_block_is_nummatrix(ctx, orc):
