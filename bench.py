@@ -13,6 +13,7 @@ Multi-GPU runs are replicas (the k sum of one problem lives on one GPU); value =
 slowest rank's time.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -64,12 +65,14 @@ class Clocks:
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                 "clocks_event_reasons.sw_power_cap,timestamp", "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self):
+    def stop(self, window=None):
+        """Median SM clock, max clock and throttle reasons of the samples taken inside window = (t0, t1) (wall-clock
+        datetimes of the timed region; all samples when none falls inside)."""
         if not self.proc:
             return None
         self.proc.terminate()
@@ -78,23 +81,24 @@ class Clocks:
         except Exception:
             self.proc.kill()
         self.f.close()
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for ln in open(self.path):
             p = [x.strip() for x in ln.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                mx = float(p[2])
+                ts = datetime.datetime.strptime(p[9], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(p[1]), float(p[2]), p[5:9]))
             except ValueError:
                 continue
-            for nm, v in zip(names, p[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        if not sm:
+        inside = [r for r in rows if window and window[0] <= r[0] <= window[1]]
+        use = inside or rows
+        if not use:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        reasons = {nm for r in use for nm, v in zip(names, r[3]) if v.lower().startswith("active")}
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": use[-1][2], "reasons": sorted(reasons),
+                "samples": len(use), "samples_in_timed_region": len(inside)}
 
 
 def fp64_peak_tflops(torch, dev):
@@ -660,6 +664,8 @@ def run_ours(args, rank, world, local_rank):
         ctx._check("dmftgpu_greenftn_w", st)
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.float32, device=dev)  # 1 GiB > L2
+    clocks = Clocks(local_rank, args.clocks_out)
+    clocks.start()  # running through the warm-up; only the samples inside the timed region are summarised
     for _ in range(args.warmup):
         step_dev()
     torch.cuda.synchronize()
@@ -668,11 +674,10 @@ def run_ours(args, rank, world, local_rank):
     assert torch.isfinite(torch.view_as_real(gw)).all()
     if world > 1:
         torch.distributed.barrier()
-    clocks = Clocks(local_rank, args.clocks_out)
-    clocks.start()
     ctx.timing(True)
     launches0 = ctx.launches()
     times = []
+    win0 = datetime.datetime.now()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -687,7 +692,7 @@ def run_ours(args, rank, world, local_rank):
     kname = "k_gloc" if explicit else "k_schur"
     k_ms, k_cnt = ctx.kernel_time(kname)
     ctx.timing(False)
-    clk = clocks.stop()
+    clk = clocks.stop((win0, datetime.datetime.now()))
     inv_per_step = wl.nk * 2 * wl.nfreq
     t_total, value = replica_throughput(sum(times), inv_per_step, args.steps, world, dev)
 
