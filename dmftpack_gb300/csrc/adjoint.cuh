@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(128) k_gloc_ad(AdArgs g) {
                         for (int b = 0; b < DP; b++) y = cfma(tG[a + b * DP], tV[b + c * DP], y);
                         t += cmulc(tX[a + c * DP], y).x;
                     }
-                accmu += group_sum<DP, W>(t);
+                accmu += group_sum<DP, W>(t, 0);
                 __syncwarp();
             }
         }

@@ -449,15 +449,17 @@ const Inst *pick_inst(int n) {
 using dg::SchurArgs;
 using dg::SchurKernel;
 
+// DP: padded correlated-block width; W: lane-group width of the adjoint and density kernels; SW: that of k_schur
+// (10-lane packed groups at DP = 10, three per warp)
 struct SInst {
-    int DP, W;
+    int DP, W, SW;
     SchurKernel (*get)(int, bool);
 };
 const SInst kSInst[] = {
-    {1, 1, dg::schur_kernel_1},    {2, 2, dg::schur_kernel_2},    {3, 4, dg::schur_kernel_3},
-    {4, 4, dg::schur_kernel_4},    {6, 8, dg::schur_kernel_6},    {8, 8, dg::schur_kernel_8},
-    {10, 16, dg::schur_kernel_10}, {12, 16, dg::schur_kernel_12}, {16, 16, dg::schur_kernel_16},
-    {20, 32, dg::schur_kernel_20},
+    {1, 1, 1, dg::schur_kernel_1},      {2, 2, 2, dg::schur_kernel_2},      {3, 4, 4, dg::schur_kernel_3},
+    {4, 4, 4, dg::schur_kernel_4},      {6, 8, 8, dg::schur_kernel_6},      {8, 8, 8, dg::schur_kernel_8},
+    {10, 16, 10, dg::schur_kernel_10},  {12, 16, 16, dg::schur_kernel_12}, {16, 16, 16, dg::schur_kernel_16},
+    {20, 32, 32, dg::schur_kernel_20},
 };
 const SInst *pick_schur(int D) {
     for (const auto &x : kSInst)
@@ -670,10 +672,10 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
     // at most 63 * (3 * 16 + 3 * 8 + 8) + 9 * 16 B = 5.2 KB and the 200 KB check below never rejects a tpi pass.
     const bool tpi = mode == dg::S_BLOCK && P.D <= 3;
     SchurKernel kern = tpi ? dg::schur_tpi_kernel(P.D, mixed) : in->get(mode, mixed);
-    const int m = P.n - P.D, NG = tpi ? 128 : 128 / in->W, DD = P.D * P.D;
+    const int m = P.n - P.D, NG = tpi ? 128 : dg::schur_groups(in->SW), DD = P.D * P.D;
     const int nf2 = (mode & dg::S_REAL) ? P.Nf : 2 * P.Nf;  // the real axis has exactly the caller's points
     auto smem_of = [&](int kc_) {
-        return tpi ? dg::schur_tpi_smem(kc_, P.D, m) : dg::schur_smem(in->DP, in->W, mode, kc_, P.D, m, P.n);
+        return tpi ? dg::schur_tpi_smem(kc_, P.D, m) : dg::schur_smem(in->DP, in->SW, mode, kc_, P.D, m, P.n);
     };
     int kc = 16;
     while (kc > 1 && smem_of(kc) > 96 * 1024) kc /= 2;

@@ -61,10 +61,17 @@ __device__ __forceinline__ bool gj_inverse(typename Ops::C (&a)[DP], int c) {
 }
 
 template <int DP, int W>
-__device__ __forceinline__ double group_sum(double v) {
+__device__ __forceinline__ double group_sum(double v, int base) {
+    if constexpr ((W & (W - 1)) != 0) {  // packed groups: the W lanes from base, in a fixed order
+        double s = 0.0;
 #pragma unroll
-    for (int off = W / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off, W);
-    return v;
+        for (int j = 0; j < W; j++) s += __shfl_sync(0xffffffffu, v, (base + j) & 31, 32);
+        return s;
+    } else {
+#pragma unroll
+        for (int off = W / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off, W);
+        return v;
+    }
 }
 
 // staged per-k data in shared memory (arithmetic type C): B[kc][m][D], e[kc][m] (mu - e_l, real),
@@ -90,11 +97,21 @@ __device__ __forceinline__ void schur_stage(const SchurArgs &g, int k0, int nkc,
     }
 }
 
-// Lane group = one Matsubara frequency; CTA = NG frequencies x one chunk of k points.
+// lane groups per 128-thread CTA: W a power of two, 128 / W; otherwise (W = DP, "packed") 32 / W groups per warp,
+// the warp's remaining lanes idle
+__host__ __device__ constexpr int schur_groups(int W) { return (W & (W - 1)) ? 4 * (32 / W) : 128 / W; }
+
+// Lane group = one Matsubara frequency; CTA = NG frequencies x one chunk of k points.  W a power of two: groups of
+// W lanes, exchanges by shuffles of width W.  W not a power of two (W = DP = 10): 32 / W groups of W lanes per warp
+// (three of ten at D = 10, where 16-lane groups leave six lanes of every group idle), exchanges by full-warp
+// shuffles from absolute source lanes; the two lanes outside the groups compute values that are never written.
 template <class Ops, int DP, int W, int MODE>
 __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     typedef typename Ops::C C;
-    constexpr int NG = 128 / W;
+    constexpr bool PACK = (W & (W - 1)) != 0;
+    static_assert(!PACK || W == DP, "packed groups are one column per lane");
+    constexpr int GPW = PACK ? 32 / W : 1;
+    constexpr int NG = schur_groups(W);
     extern __shared__ double2 sm[];
     const int D = g.D, DD = D * D, m = g.m;
     constexpr bool TR = (MODE & S_TRACE) != 0;
@@ -109,10 +126,13 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
     C *wla = sM0 + DD;                                                   // reciprocals [NG][m]
     C *rla = wla + (size_t)NG * m;                                        // static reciprocals [NG][n] (E0)
     C *tla = rla + (E0 ? (size_t)NG * g.n : 0);                           // DERIV tiles [NG][2][DP][DP]
-    const int c = threadIdx.x & (W - 1);
-    const int grp = threadIdx.x / W;
+    const int lane = threadIdx.x & 31, gw = PACK ? lane / W : 0;
+    const bool active = !PACK || gw < GPW;  // a lane of a group (packed: lanes 30, 31 of each warp are not)
+    const int c = PACK ? lane % W : (threadIdx.x & (W - 1));
+    const int grp = PACK ? (active ? (threadIdx.x >> 5) * GPW + gw : 0) : threadIdx.x / W;
+    const int base = PACK ? gw * W : 0;     // the group's first lane in its warp
     const int f_raw = blockIdx.x * NG + grp;
-    const bool fvalid = f_raw < g.nf2;
+    const bool fvalid = active && f_raw < g.nf2;
     const int f = fvalid ? f_raw : g.nf2 - 1;
     const int chunk = blockIdx.y;
     const int kbeg = chunk * g.kchunk, kend = min(g.nk, kbeg + g.kchunk);
@@ -144,10 +164,12 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
             const C *bs = sB + (size_t)kk * m * D, *es = sE + (size_t)kk * m, *hp = sH + (size_t)kk * DD;
             // w_l = 1/(z - e_l), shared by the group's lanes; TRACE: r_j = 1/(z - e0_j)
             __syncwarp();
-            for (int l = c; l < m; l += W) wl[l] = Ops::rcp(Ops::add(es[l], iwc));
-            if (E0) {
-                const C *e0s = sE0 + (size_t)kk * g.n;
-                for (int j = c; j < g.n; j += W) rl[j] = Ops::rcp(Ops::add(e0s[j], iwc));
+            if (active) {
+                for (int l = c; l < m; l += W) wl[l] = Ops::rcp(Ops::add(es[l], iwc));
+                if (E0) {
+                    const C *e0s = sE0 + (size_t)kk * g.n;
+                    for (int j = c; j < g.n; j += W) rl[j] = Ops::rcp(Ops::add(e0s[j], iwc));
+                }
             }
             __syncwarp();
             C s[DP], s0[DP];  // s0: BLOCK mode only
@@ -183,18 +205,20 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                             if (a < D) sp[a] = Ops::fma(bs[l * D + a], q, sp[a]);
                     }
                 __syncwarp();
-                if (c < DP) {
+                if (active && c < DP) {
 #pragma unroll
                     for (int a = 0; a < DP; a++) tS[a + c * DP] = sp[a];
                 }
             }
-            sing |= gj_inverse<Ops, DP, W>(s, c);
+            if constexpr (PACK) sing |= group_gj_inverse<Ops, DP>(s, c, base) && active;
+            else sing |= gj_inverse<Ops, DP, W>(s, c);
             if (RE && (MODE & S_BLOCK)) {
 #pragma unroll
                 for (int a = 0; a < DP; a++) accG[a] = Ops::add(accG[a], s[a]);
             }
             if ((MODE & S_BLOCK) && !G0E && !RE) {
-                sing |= gj_inverse<Ops, DP, W>(s0, c);
+                if constexpr (PACK) sing |= group_gj_inverse<Ops, DP>(s0, c, base) && active;
+                else sing |= gj_inverse<Ops, DP, W>(s0, c);
 #pragma unroll
                 for (int a = 0; a < DP; a++) {
                     accG[a] = Ops::add(accG[a], s[a]);
@@ -233,7 +257,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                 if (MODE & S_DERIV) {
                     // Y = G S' G, column c: u = S' G(:,c), y = G u
                     __syncwarp();
-                    if (c < DP) {
+                    if (active && c < DP) {
 #pragma unroll
                         for (int a = 0; a < DP; a++) tG[a + c * DP] = s[a];
                     }
@@ -276,9 +300,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
                         }
                     }
                 }
-                acct1 += group_sum<DP, W>(Ops::re(acc1));
-                if (MODE & S_DERIV) acct2 += group_sum<DP, W>(Ops::re(acc2));
-                if (RE) acct2 += group_sum<DP, W>(Ops::im(acc1));  // complex Tr G on the real axis
+                acct1 += group_sum<DP, W>(Ops::re(acc1), base);
+                if (MODE & S_DERIV) acct2 += group_sum<DP, W>(Ops::re(acc2), base);
+                if (RE) acct2 += group_sum<DP, W>(Ops::im(acc1), base);  // complex Tr G on the real axis
             }
         }
     }
@@ -502,7 +526,7 @@ inline size_t schur_tpi_smem(int kc, int D, int m) {
 
 // shared-memory bytes of one k_schur launch
 inline size_t schur_smem(int DP, int W, int mode, int kc, int D, int m, int n) {
-    const int NG = 128 / W;
+    const int NG = schur_groups(W);
     size_t s = (size_t)kc * m * D + (size_t)kc * m + (size_t)kc * D * D + (size_t)D * D + (size_t)NG * m;
     const bool g0e = (mode & S_BLOCK) && DP >= 8 && !(mode & S_REAL);
     if (((mode & S_TRACE) && !(mode & S_REAL)) || g0e) s += (size_t)kc * n + (size_t)NG * n;

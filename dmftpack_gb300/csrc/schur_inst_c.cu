@@ -2,6 +2,6 @@
 #include "schur.cuh"
 
 namespace dg {
-DG_SCHUR_INST(10, 16)
+DG_SCHUR_INST(10, 10)
 DG_SCHUR_INST(12, 16)
 }  // namespace dg
