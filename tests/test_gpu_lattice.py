@@ -284,12 +284,14 @@ def test_hyb_delta_matches_oracle(ctx, orc):
     assert rel_err(d_g, d_o) < TOL
 
 
-@pytest.mark.parametrize("case", ["t2g_p", "soc_small"])
+@pytest.mark.parametrize("case", ["t2g_p", "dp28", "soc_small"])
 @pytest.mark.parametrize("mixed", [False, True])
 def test_retarded_gloc_real_axis(ctx, orc, case, mixed):
     """Real-axis lattice sum (retarded_GreenFtn2 over a qs_spectra energy grid) against explicit inversion."""
     if case == "t2g_p":
         wl = models.t2g_p(k=3, nfreq=8, beta=10.0)
+    elif case == "dp28":   # D = 10: the packed 10-lane groups
+        wl = models.dp28(k=2, nfreq=8, ntau=16, beta=10.0)
     else:
         wl = models.soc56(k=2, nfreq=8, beta=10.0)
     H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
