@@ -261,7 +261,7 @@ def dmft_iteration_timing(ctx, dev, stream, n_iter=4):
     return out
 
 
-def dmft_convergence_cfg1(ctx, dev, max_iter=40):
+def dmft_convergence_hubbard2d(ctx, dev, max_iter=40):
     """DMFT iterations to a self-consistency residual GwRD < 1e-6 (dmft_scf_check's measure, src/dmft_main.cpp:
     902-1014) on the single-band Hubbard workload (64x64 k, beta = 50, N_freq = 2048, N_tau = 8192, U = 2, IPT,
     Sigma seeded U^2/(4 iw)): the plain form (FP64, the reference's bisection mu to |dmu| <= 1e-5 and its
@@ -309,8 +309,8 @@ def dmft_convergence_cfg1(ctx, dev, max_iter=40):
     return out
 
 
-def dmft_iteration_cfg5(ctx, dev, stream, k=16):
-    """The spec comparison on the SC2PT workload (28-orbital d+p model, 729 R vectors, 10 correlated
+def dmft_iteration_sc2pt_dp28(ctx, dev, stream, k=16):
+    """The plain-versus-GB300-form comparison on the SC2PT workload (28-orbital d+p model, 729 R vectors, 10 correlated
     spin-orbitals, Kanamori U = 4, J = 0.7, U' = 2.6, beta = 40, N_freq = 4096, N_tau = 8192) on a k^3 grid: one
     full DMFT iteration (H(k), mu search, G_loc, Delta, SCGF2 to its stopping test, Pulay) in the plain form (FP64
     on the CUDA cores, the reference's bisection) and in the mixed form (double-float, tensor-core H(k) and N(mu)
@@ -759,8 +759,8 @@ def run_ours(args, rank, world, local_rank):
                               "G_loc_vs_fp64": float((gw - gw_ref).abs().max() / gw_ref.abs().max())}
     dmft_iter = None if args.no_variants else dmft_iteration_timing(ctx, dev, stream)
     scgf2 = None if args.no_variants else scgf2_timing(ctx, dev)
-    cfg5 = None if args.no_variants else dmft_iteration_cfg5(ctx, dev, stream, k=args.cfg5_k)
-    conv = None if args.no_variants else dmft_convergence_cfg1(ctx, dev)
+    sc2pt = None if args.no_variants else dmft_iteration_sc2pt_dp28(ctx, dev, stream, k=args.sc2pt_k)
+    conv = None if args.no_variants else dmft_convergence_hubbard2d(ctx, dev)
     if rank != 0:
         return
     # roofline of the dominant kernel.  FP64 forms: the FP64 flops of the algorithm (explicit: 8 n^3 per (k, iw)
@@ -815,7 +815,7 @@ def run_ours(args, rank, world, local_rank):
                           l2="1 GiB buffer written between timed steps", replicas=world),
            "variants": variants, "vs_reference_same_algorithm": same_alg, "peaks": peaks,
            "error_vs_fp64": err, "dmft_iteration": dmft_iter,
-           "scgf2_loop": scgf2, "dmft_iteration_cfg5": cfg5, "dmft_convergence": conv,
+           "scgf2_loop": scgf2, "dmft_iteration_sc2pt_dp28": sc2pt, "dmft_convergence": conv,
            "e2e": {"value": inv_per_step / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
                    "timing": "host clock around the C-ABI call with pinned host buffers, %d steps, the same L2 "
@@ -845,7 +845,7 @@ def main():
     ap.add_argument("--algo", default="schur", choices=["schur", "explicit"],
                     help="schur: exact correlated-block form (default); explicit: full n x n inversion per (k, iw)")
     ap.add_argument("--no-variants", action="store_true", help="skip the side measurement of the other algorithm")
-    ap.add_argument("--cfg5-k", type=int, default=16, help="k grid (k^3) of the SC2PT DMFT-iteration comparison")
+    ap.add_argument("--sc2pt-k", type=int, default=16, help="k grid (k^3) of the SC2PT DMFT-iteration comparison")
     ap.add_argument("--clocks-out", default=None, help="CSV file for the nvidia-smi samples of the timed region")
     ap.add_argument("--case", default=None, choices=["gloc", "scgf2", "dmft", "lattice", "batched", "adjoint",
                                                      "downfold", "density", "hk"],

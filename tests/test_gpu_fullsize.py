@@ -4,7 +4,7 @@ own example input (example/Hubb_model/primitive_Cell_ipt, via tests/golden/hubba
 The toy-size tests elsewhere cover the edge cases; these exercise what only large grids reach: the moment-fit
 window search with Nv = N_freq/20 (src/FourierTransform.cpp:289-316), the positivity fix-ups
 (src/FourierTransform.cpp:145-175, src/SCGF2_fullLoop.cpp:657-688), the SCGF2 stopping test, and the
-lattice sums at N_freq = 2048-4096.  k grids are full where the oracle finishes in seconds (config 1, the
+lattice sums at N_freq = 2048-4096.  k grids are full where the oracle finishes in seconds (the Hubbard lattice, the
 example) and a k subset otherwise (the per-k work is independent of the other k points)."""
 import json
 import os
@@ -105,7 +105,7 @@ def test_reference_example_ipt_iterations(orc):
 
 
 @pytest.fixture(scope="module")
-def config1(orc):
+def hubbard64(orc):
     """Single-band Hubbard, 64 x 64 k, beta = 50, N_freq = 2048, N_tau = 8192 (FFT transforms), U = 2, IPT, Sigma
     seeded U^2/(4 iw): the oracle's initial TightBinding call and one complete DMFT iteration."""
     wl = models.hubbard_2d(kx=64, ky=64, beta=50.0, nfreq=2048, ntau=8192)
@@ -119,9 +119,9 @@ def config1(orc):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-def test_config1_full_size_ipt_iteration(config1, mixed):
+def test_hubbard_64x64_full_size_ipt_iteration(hubbard64, mixed):
     """One complete config-1 DMFT iteration on the device, FP64 and double-float, against the oracle."""
-    wl, H, p, init, ref = config1
+    wl, H, p, init, ref = hubbard64
     _gpu_dmft(H, wl.n, wl.beta, wl.nfreq, p, init, ref, mixed=mixed, tol=TOL_MIXED if mixed else 1e-9,
               mu_tol=1e-10 if mixed else 1e-12)
 
@@ -132,7 +132,7 @@ def _k_subset(orc, wl, nsub, stride):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-def test_config2_k_subset_full_frequencies(ctx, orc, mixed):
+def test_t2g_p_k_subset_full_frequencies(ctx, orc, mixed):
     """t2g + p (12 x 12), 64 k points of the 24^3 grid, beta = 40, N_freq = 4096 (8192 points in the sums):
     GreenFtn_w, N(mu) with dN/dmu, and the mu search (bisection: the reference's mu sequence)."""
     wl = models.t2g_p(k=24, nfreq=4096, beta=40.0)
@@ -159,7 +159,7 @@ def test_config2_k_subset_full_frequencies(ctx, orc, mixed):
     assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, wl.ncl, wl.nh) - target) < 1e-9
 
 
-def test_config3_k_subset_dense_sigma(ctx, orc):
+def test_soc56_k_subset_dense_sigma(ctx, orc):
     """56 x 56 SOC model with a dense 20 x 20 Sigma, 8 k points of the 16^3 grid, beta = 30, N_freq = 2048."""
     wl = models.soc56(k=16, nfreq=2048, beta=30.0)
     H = _k_subset(orc, wl, 8, 512)
@@ -190,7 +190,7 @@ def _kanamori_impurity(d=10, nfreq=4096, beta=40.0, seed=11):
 
 
 @pytest.fixture(scope="module")
-def scgf2_cfg5(orc):
+def scgf2_d10(orc):
     himp, weiss, g0, mu = _kanamori_impurity()
     uidx, ut = orc.gen_uijkl(10, 4.0, 2.6, 0.7)
     ref = orc.scgf2(himp, weiss, g0, uidx, ut, mu, 40.0, 8192, 0.5, max_iter=3, static={"prev": 0.0})
@@ -198,10 +198,10 @@ def scgf2_cfg5(orc):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-def test_config5_impurity_scgf2_loops(scgf2_cfg5, mixed):
+def test_kanamori_d10_impurity_scgf2_loops(scgf2_d10, mixed):
     """SCGF2 on the 10 spin-orbital Kanamori impurity (U = 4, J = 0.7, U' = 2.6, Nu = 180) at N_freq = 4096,
     N_tau = 8192, beta = 40: three loops, FP64 and double-float getStimp."""
-    (himp, weiss, g0, uidx, ut, mu), (se_o, g_o, loops_o) = scgf2_cfg5
+    (himp, weiss, g0, uidx, ut, mu), (se_o, g_o, loops_o) = scgf2_d10
     c2 = lib.Context(0)
     try:
         se, g, loops = c2.SCGF2(himp, weiss, g0, uidx, ut, mu, 40.0, 8192, 0.5, max_iter=3, mixed=mixed)
@@ -213,7 +213,7 @@ def test_config5_impurity_scgf2_loops(scgf2_cfg5, mixed):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-def test_config4_ragged_batch_against_oracle(ctx, orc, mixed):
+def test_ragged_batch_against_oracle(ctx, orc, mixed):
     """The ragged batch's shapes (n in {1,3,5,10,14,28}, N_freq in {512..4096}, beta in [10,100]) through the
     batched entry point, each problem against the oracle on 27 of its k points."""
     import torch
