@@ -96,6 +96,18 @@ def test_dnele_matches_finite_difference(orc):
     assert abs(dN - fd) < 1e-6 * abs(fd)
 
 
+def test_newton_mu_refines_the_bisection_to_the_electron_count(orc):
+    """The oracle's Newton polish after GreenFtn_w_adjust_mu's bisection (the mu the library's DMFTGPU_NEWTON search
+    converges to): |N(mu) - target| below 1e-12, within the bisection's 1e-5 resolution of its mu."""
+    wl = _small_t2g()
+    H = orc.hk(wl.n, wl.rindex, wl.hr, orc.kmesh(*wl.kgrid))
+    target = 7.3
+    mu_b, _ = orc.adjust_mu(H, wl.sigma, 0.0, wl.beta, wl.ncl, wl.nh, target)
+    mu_n = orc.newton_mu(H, wl.sigma, mu_b, wl.beta, wl.D, target)
+    assert abs(orc.nele(H, wl.sigma, mu_n, wl.beta, wl.ncl, wl.nh) - target) < 1e-12
+    assert abs(mu_n - mu_b) < 2e-5
+
+
 def test_free_electron_known_answers(orc):
     """Sigma = 0, diagonal H(k): G_loc = (1/Nk) sum_k 1/(iw+mu-e_k)."""
     wl = models.hubbard_2d(kx=6, ky=6, nfreq=40, beta=8.0)
