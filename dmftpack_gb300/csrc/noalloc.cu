@@ -10,8 +10,8 @@
 // Limits and sharing: nfreq * dim * dim <= DG_NOALLOC_HYB_MAX complex numbers (8 MiB) and dim <= 32;
 // larger requests are rejected with DMFTGPU_BADARG.  All calls share the one array, so calls that overlap
 // on the GPU (different streams, or several host threads at once) race on it; serialise them.  The first
-// call on each device resolves the device address of the array (cudaGetSymbolAddress); make that first
-// call before any stream capture.  The arrays belong to the device that is current when the call is made,
+// call on each device resolves the device address of the array (cudaGetSymbolAddress).  No call may be made
+// on a stream under capture: each one reads its status back and waits for the stream.  The arrays belong to the device that is current when the call is made,
 // and cuda_stream must belong to that device too (else DMFTGPU_BADARG).  Every call is synchronous: it
 // reads the status word back and waits for cuda_stream to finish before it returns.
 #include <mutex>

@@ -324,6 +324,9 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 
 // In-place inverse of a D x D matrix held by one thread (D <= 3): Gauss-Jordan with partial pivoting whose row
 // swaps are predicated moves between compile-time indices (no local memory), undone as column swaps at the end.
+// Each step stores the pivot's reciprocal in place and updates only the other columns: row j becomes
+// a_jc / a_jj, row r becomes a_rc - a_rj a_jc for c != j, and column j becomes -a_rj / a_jj (no products with the
+// known 1 and 0 entries).
 template <class Ops, int N>
 __device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
     typedef typename Ops::C C;
@@ -355,16 +358,18 @@ __device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
         }
         sing |= !(best > M(0));
         const C piv = Ops::rcp(a[j][j]);
-        a[j][j] = Ops::one();
+        a[j][j] = piv;
 #pragma unroll
-        for (int c = 0; c < N; c++) a[j][c] = Ops::mul(a[j][c], piv);
+        for (int c = 0; c < N; c++)
+            if (c != j) a[j][c] = Ops::mul(a[j][c], piv);
 #pragma unroll
         for (int r = 0; r < N; r++)
             if (r != j) {
                 const C t = a[r][j];
-                a[r][j] = Ops::zero();
 #pragma unroll
-                for (int c = 0; c < N; c++) a[r][c] = Ops::fms(t, a[j][c], a[r][c]);
+                for (int c = 0; c < N; c++)
+                    if (c != j) a[r][c] = Ops::fms(t, a[j][c], a[r][c]);
+                a[r][j] = Ops::mul(Ops::neg(t), piv);
             }
     }
 #pragma unroll
@@ -454,25 +459,42 @@ __global__ void __launch_bounds__(128) k_schur_tpi(SchurArgs g) {
             for (int a = 0; a < D; a++) Ad[a] = Bd[a] = Ops::rzero();
 #pragma unroll
             for (int q = 0; q < NP; q++) Ar[q] = Ai[q] = Br[q] = Bi[q] = Ops::rzero();
+            // the pole sums are lazy double-float sums, renormalised after every 16 poles and at the end
+            auto renorm = [&]() {
+#pragma unroll
+                for (int a = 0; a < D; a++) {
+                    Ad[a] = Ops::rnorm(Ad[a]);
+                    Bd[a] = Ops::rnorm(Bd[a]);
+                }
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Ar[q] = Ops::rnorm(Ar[q]);
+                    Ai[q] = Ops::rnorm(Ai[q]);
+                    Br[q] = Ops::rnorm(Br[q]);
+                    Bi[q] = Ops::rnorm(Bi[q]);
+                }
+            };
             for (int l = 0; l < m; l++) {
+                if (l > 0 && (l & 15) == 0) renorm();
                 const R x = es[l];
                 const R r = Ops::rrcp(Ops::rfma(x, x, w2));
                 const R re = Ops::rmul(x, r), im = Ops::rneg(Ops::rmul(wr, r));  // w_l
 #pragma unroll
                 for (int a = 0; a < D; a++) {
                     const R p = pd[(size_t)l * D + a];
-                    Ad[a] = Ops::rfma(re, p, Ad[a]);
-                    Bd[a] = Ops::rfma(im, p, Bd[a]);
+                    Ad[a] = Ops::racc(re, p, Ad[a]);
+                    Bd[a] = Ops::racc(im, p, Bd[a]);
                 }
 #pragma unroll
                 for (int q = 0; q < NP; q++) {
                     const C p = po[(size_t)l * NP + q];
-                    Ar[q] = Ops::rfma(re, Ops::cre(p), Ar[q]);
-                    Ai[q] = Ops::rfma(re, Ops::cim(p), Ai[q]);
-                    Br[q] = Ops::rfma(im, Ops::cre(p), Br[q]);
-                    Bi[q] = Ops::rfma(im, Ops::cim(p), Bi[q]);
+                    Ar[q] = Ops::racc(re, Ops::cre(p), Ar[q]);
+                    Ai[q] = Ops::racc(re, Ops::cim(p), Ai[q]);
+                    Br[q] = Ops::racc(im, Ops::cre(p), Br[q]);
+                    Bi[q] = Ops::racc(im, Ops::cim(p), Bi[q]);
                 }
             }
+            renorm();
             C s0[D][D];
 #pragma unroll
             for (int a = 0; a < D; a++) {

@@ -372,8 +372,8 @@ int dmftgpu_imgfreq_read(const char *path, int nfreq, int norbit, double beta, d
  * to the current device (else DMFTGPU_BADARG).  The call is synchronous: it waits for cuda_stream to finish
  * and returns the status its kernel raised.  Scratch is a static device array of 2^19 complex numbers
  * (8 MiB) per GPU that loads the library, so nfreq*dim*dim must not exceed 524288 (else DMFTGPU_BADARG).
- * The first call on a device resolves the array's device address and should precede any stream capture;
- * calls that overlap on the GPU share the array and race. */
+ * Being synchronous, the call must not be made on a stream under capture (the read-back and the wait would
+ * invalidate the capture).  Calls that overlap on the GPU share the array and race. */
 int dmftgpu_hyb_delta_noalloc(int dim, const int *orb, int nfreq, double beta, int D, const double *sigma,
                               const double *gw, const double *himp, double mu, double *delta, void *cuda_stream);
 
