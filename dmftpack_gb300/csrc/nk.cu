@@ -31,8 +31,8 @@ __global__ void k_vdot(long long n, const double2 *__restrict__ a, const double2
     if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-// y = a x + b y
-__global__ void k_vaxpby(long long n, double a, const double2 *__restrict__ x, double b, double2 *__restrict__ y) {
+// y = a x + b y (x may be y: the scaling of a vector in place)
+__global__ void k_vaxpby(long long n, double a, const double2 *x, double b, double2 *y) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) y[t] = cadd(cscale(x[t], a), cscale(y[t], b));
 }

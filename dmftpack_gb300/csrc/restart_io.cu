@@ -4,6 +4,7 @@
 // slots) of column-major norbit x norbit complex matrices, element (m, n) of slot w at 2 (w N^2 + m + n N).
 #include <cmath>
 #include <cstdio>
+#include <new>
 #include <vector>
 
 #include "dmftgpu.h"
@@ -11,6 +12,7 @@
 namespace {
 
 constexpr double TOL = 1e-7;  // dataOut_full writes |F| > tol only (src/ImgTimeFtn.cpp:10)
+constexpr int W_MAX = 1 << 24;  // frequency indices at or above this mark a damaged file (DMFTGPU_BADARG)
 
 struct Row {
     int w, m, n;
@@ -22,13 +24,21 @@ int read_rows(const char *path, std::vector<Row> &rows) {
     FILE *f = std::fopen(path, "r");
     if (!f) return DMFTGPU_IO;
     char line[512];
-    while (std::fgets(line, sizeof line, f)) {
-        Row r;
-        if (std::sscanf(line, "%d %d %d %lf %lf", &r.w, &r.m, &r.n, &r.re, &r.im) == 5) rows.push_back(r);
+    int st = DMFTGPU_OK;
+    try {
+        while (std::fgets(line, sizeof line, f)) {
+            Row r;
+            if (std::sscanf(line, "%d %d %d %lf %lf", &r.w, &r.m, &r.n, &r.re, &r.im) == 5) {
+                if (r.w >= W_MAX) st = DMFTGPU_BADARG;
+                rows.push_back(r);
+            }
+        }
+    } catch (const std::bad_alloc &) {
+        st = DMFTGPU_NOMEM;
     }
-    const bool err = std::ferror(f) != 0;
+    if (std::ferror(f) != 0 && st == DMFTGPU_OK) st = DMFTGPU_IO;
     std::fclose(f);
-    return err ? DMFTGPU_IO : DMFTGPU_OK;
+    return st;
 }
 
 }  // namespace
@@ -88,7 +98,13 @@ extern "C" int dmftgpu_imgfreq_read(const char *path, int nfreq, int norbit, dou
     if (wmax < 2) return DMFTGPU_BADARG;  // the extrapolation below the grid needs two points
     const size_t NN = (size_t)norbit * norbit;
     // the file's points; as in the reference, a frequency with no line (every element <= 1e-7) keeps grid point 0
-    std::vector<double> S(2 * (size_t)wmax * NN, 0.0), mats(wmax, 0.0);
+    std::vector<double> S, mats;
+    try {
+        S.assign(2 * (size_t)wmax * NN, 0.0);
+        mats.assign(wmax, 0.0);
+    } catch (const std::bad_alloc &) {
+        return DMFTGPU_NOMEM;
+    }
     for (const Row &r : rows)
         if (r.w >= 0) {
             mats[r.w] = (2 * r.w + 1) * M_PI / beta_prev;

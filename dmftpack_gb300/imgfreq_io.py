@@ -8,6 +8,7 @@ ImgFreqFtn slot layout (src/ImgTimeFtn.h:32-98).
 import numpy as np
 
 TOL = 1e-7  # src/ImgTimeFtn.cpp:10
+W_MAX = 1 << 24  # frequency indices at or above this mark a damaged file
 
 
 def write_full(path, F):
@@ -39,6 +40,8 @@ def _rows(path):
             if len(p) < 5:
                 continue
             out.append((int(p[0]), int(p[1]), int(p[2]), float(p[3]), float(p[4])))
+            if out[-1][0] >= W_MAX:
+                raise ValueError("%s: frequency index %d out of range" % (path, out[-1][0]))
     return out
 
 

@@ -100,3 +100,11 @@ def test_c_abi_errors(tmp_path):
     assert e.value.code == lib.BADARG
     with pytest.raises(ValueError):
         io.update_full(p, 8, 2)
+    # a damaged frequency index is refused before anything is sized by it
+    p.write_text("0 0 0 +1.00000000 +0.00000000\n99999999 0 0 +1.00000000 +0.00000000\n")
+    for call in (lambda: lib.imgfreq_update(p, 8, 2), lambda: lib.imgfreq_read(p, 8, 2, 10.0, 10.0)):
+        with pytest.raises(lib.DmftGpuError) as e:
+            call()
+        assert e.value.code == lib.BADARG
+    with pytest.raises(ValueError):
+        io.read_full(p, 8, 2, 10.0, 10.0)
