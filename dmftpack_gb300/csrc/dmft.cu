@@ -307,6 +307,8 @@ int dmft_newton_step(dmftgpu_ctx *ctx, const dmftgpu_lattice *L, const double *h
     DG_CUDA(cudaMemcpyAsync(b, x, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     DG_TRY(dg_vaxpby(ctx, n, -1.0, seout0, 1.0, b));
     double N0 = 0, dNdmu = 0, dummy = 0, xx = 0;
+    // N0 from the same pass as the perturbed N(mu) below (the derivative pass may take another kernel path, whose
+    // rounding would then enter the directional difference)
     DG_TRY(dmftgpu_nele(ctx, L, hk, (const double *)x, mu, &N0, nullptr, lflags));
     DG_TRY(dmftgpu_nele(ctx, L, hk, (const double *)x, mu, &dummy, &dNdmu, lflags));
     if (!(dNdmu > 0)) return dg_fail(ctx, DMFTGPU_NONCONVERGED, "dmft_iteration: dN/dmu <= 0 at the Newton point");
