@@ -66,7 +66,7 @@ def test_gen_uijkl_matches_oracle(orc, nso, dd):
     assert np.array_equal(ui, oi) and np.array_equal(ut, ot)
 
 
-def test_new_entry_points_reject_a_null_context_without_a_device():
+def test_entry_points_reject_a_null_context_without_a_device():
     # argument validation happens before any CUDA call, so these run on a machine without a GPU
     from dmftpack_gb300 import lib
     L = lib.load()
@@ -79,6 +79,20 @@ def test_new_entry_points_reject_a_null_context_without_a_device():
     assert L.dmftgpu_density_dft(None, ctypes.byref(lat), p, p, 0.0, p, 0) == lib.BADARG
     assert L.dmftgpu_upfold(None, 2, 1, 1, 1, p, p, p, None, 1, rindex, p, p, p, 0) == lib.BADARG
     assert L.dmftgpu_gloc_real(None, ctypes.byref(lat), p, p, 1, 0.0, 0.1, 0.05, 0.0, p, p, 0) == lib.BADARG
+    ip = (ctypes.c_int * 4)()
+    dp = (ctypes.c_double * 4)()
+    assert L.dmftgpu_downfold_window(None, 1, 2, 1, hartr, p, None, 0.0, -1.0, 1.0, 1e4, ip, ip, p, p, p, p, p,
+                                     0) == lib.BADARG
+    assert L.dmftgpu_upfold_window(None, 2, 1, 1, 1, p, p, p, None, p, ip, ip, 0.0, 10.0, 1, rindex, p, p, p,
+                                   0) == lib.BADARG
+    assert L.dmftgpu_moments(None, 2, 16, 10.0, p, 1, p, 0) == lib.BADARG
+    assert L.dmftgpu_ipt(None, 2, 16, 64, 10.0, 1.0, 0.0, p, p, p, 0, None, None, p, p, p, 0) == lib.BADARG
+    assert L.dmftgpu_scgf2(None, 2, 16, 64, 10.0, 0.0, 0.5, p, p, p, 0, None, None, 10, p, ip, 0) == lib.BADARG
+    assert L.dmftgpu_weak_solver(None, 0, 2, 16, 64, 10.0, p, p, 0, None, None, p, 0) == lib.BADARG
+    params = lib.DmftParams()
+    assert L.dmftgpu_dmft_iteration(None, ctypes.byref(lat), p, ctypes.byref(params), 1, p, p, p, dp, p, p, dp,
+                                    0) == lib.BADARG
+    assert L.dmftgpu_mixer_stats(None, ip, dp, dp) == lib.BADARG
 
 
 def test_density_hwr_round_trip(orc):
