@@ -122,6 +122,11 @@ int dmftgpu_create(dmftgpu_ctx **out, int device) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         int code = dg_set_cuda_error(ctx, e, "dmftgpu_create");
+        // release whatever was created before the failing call
+        if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->d_status) cudaFree(ctx->d_status);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return code;

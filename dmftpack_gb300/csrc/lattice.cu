@@ -742,28 +742,34 @@ int run_schur(dmftgpu_ctx *ctx, const Prepared &P, int mode, double mu, int wgri
         nchunk = chunks(tuned->second, &kchunk);
         g.kchunk = kchunk;
     } else if (ctx->autotune && !ctx->capturing) {
-        cudaEvent_t e0, e1;
-        DG_CUDA(cudaEventCreate(&e0));
-        DG_CUDA(cudaEventCreate(&e1));
+        // the two timing events are released on every exit, an error return included
+        struct EventPair {
+            cudaEvent_t a = nullptr, b = nullptr;
+            ~EventPair() {
+                if (a) cudaEventDestroy(a);
+                if (b) cudaEventDestroy(b);
+            }
+        } ev;
+        DG_CUDA(cudaEventCreate(&ev.a));
+        DG_CUDA(cudaEventCreate(&ev.b));
         float best = 1e30f;
         int best_cps = 8;
         for (int cps : {4, 8, 16}) {
             int kch;
             const int nc = chunks(cps, &kch);
             g.kchunk = kch;
-            DG_CUDA(cudaEventRecord(e0, ctx->stream));
+            DG_CUDA(cudaEventRecord(ev.a, ctx->stream));
             kern<<<dim3(fblocks, nc), 128, smem, ctx->stream>>>(g);
-            DG_CUDA(cudaEventRecord(e1, ctx->stream));
-            DG_CUDA(cudaEventSynchronize(e1));
+            DG_LAUNCH(ctx, "k_schur (autotune)");
+            DG_CUDA(cudaEventRecord(ev.b, ctx->stream));
+            DG_CUDA(cudaEventSynchronize(ev.b));
             float ms = 0;
-            DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            DG_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
             if (ms < best) {
                 best = ms;
                 best_cps = cps;
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         ctx->tuned[key] = best_cps;
         nchunk = chunks(best_cps, &kchunk);
         g.kchunk = kchunk;

@@ -95,6 +95,18 @@ def test_entry_points_reject_a_null_context_without_a_device():
     assert L.dmftgpu_mixer_stats(None, ip, dp, dp) == lib.BADARG
 
 
+def test_create_without_a_device_fails_cleanly():
+    # on a machine without a usable GPU the context constructor returns the CUDA error and no handle
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from dmftpack_gb300 import lib
+    L = lib.load()
+    h = ctypes.c_void_p()
+    assert L.dmftgpu_create(ctypes.byref(h), 0) == lib.CUDA_ERROR
+    assert not h.value
+
+
 def test_density_hwr_round_trip(orc):
     # the upfolded density of H(k) itself (DF = V = I) is the hopping table; written and read back at %e precision
     from dmftpack_gb300 import hwr, models
