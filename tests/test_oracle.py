@@ -163,6 +163,65 @@ def test_sigma2_vanishes_without_interaction(orc):
     assert np.all(np.abs(st[1:-1]) <= 1e-10)
 
 
+def test_sigma2_matches_a_dense_tensor_contraction(orc):
+    """getStimp (src/SCGF2_fullLoop.cpp:603-690) restated independently: the U list scattered into a dense
+    U_{iqmk} and the second-order diagram as one einsum over G(tau) and G(beta - tau),
+    Sigma_ij(tau) = U_{iqmk} U_{lnpj} [G_kl G_mn - G_kn G_ml](tau) G_pq(beta - tau), against the oracle's loop over
+    pairs of list entries.  G(tau) of a non-interacting 4-orbital model is negative definite, so the positivity
+    fix-up does not fire."""
+    rng = np.random.default_rng(7)
+    d, ntau, beta = 4, 32, 6.0
+    A = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    eps, V = np.linalg.eigh(0.4 * (A + A.conj().T))
+    tau = np.arange(ntau + 1) * beta / ntau
+    occ = np.exp(-np.outer(tau, eps)) / (1 + np.exp(-beta * eps))[None]
+    gt = -np.einsum("ia,ta,ja->tij", V, occ, V.conj())
+    uidx, ut = orc.gen_uijkl(d, 3.0, 1.9, 0.55)
+    U = np.zeros((d,) * 4, complex)
+    for (i, q, m, k), u in zip(uidx, ut):
+        U[i, q, m, k] += u
+    gm = gt[::-1]
+    want = (np.einsum("iqmk,lnpj,tkl,tmn,tpq->tij", U, U, gt, gt, gm, optimize=True)
+            - np.einsum("iqmk,lnpj,tkn,tml,tpq->tij", U, U, gt, gt, gm, optimize=True))
+    got, fix, status = orc.sigma2_tau(gt, uidx, ut, beta)
+    assert fix == 0
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_hyb_delta_fock_and_dyson_match_dense_restatements(orc):
+    """Construct_hyb_delta (src/Construct_hyb_delta.cpp:47-119) on a projected orbital subset, getFockOperator
+    (src/SCGF2_fullLoop.cpp:583-597) as two einsums over a dense U, and getGwimp (src/SCGF2_fullLoop.cpp:551-578)
+    as a batched inverse, each restated with numpy and compared with the oracle."""
+    rng = np.random.default_rng(11)
+    D, nf, beta, mu = 3, 24, 7.0, 0.3
+    wn = np.pi * (2 * np.arange(nf) + 1) / beta
+    A = rng.normal(size=(D, D)) + 1j * rng.normal(size=(D, D))
+    himp = (A + A.conj().T) / 4
+    sig = 0.2 * (rng.normal(size=(nf, D, D)) + 1j * rng.normal(size=(nf, D, D)))
+    gw = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(D)[None] - himp[None] - sig - 0.5j * np.eye(D)[None])
+    orb = np.array([2, 0])
+    P = np.ix_(orb, orb)
+    want = ((1j * wn[:, None, None] + mu) * np.eye(2)[None] - himp[P][None] - sig[(slice(None),) + P]
+            - np.linalg.inv(gw[(slice(None),) + P]))
+    assert np.abs(orc.hyb_delta(orb, sig, gw, himp, mu, beta) - want).max() <= 1e-12 * np.abs(want).max()
+    d = 4
+    uidx, ut = orc.gen_uijkl(d, 3.0, 1.9, 0.55)
+    U = np.zeros((d,) * 4, complex)
+    for (a, b_, c, e), u in zip(uidx, ut):
+        U[a, b_, c, e] += u
+    B = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    occ = B @ B.conj().T / (2 * d)
+    want_f = np.einsum("abcd,ca->bd", U, occ) - np.einsum("abcd,da->bc", U, occ)
+    fk = orc.fock(occ, uidx, ut)
+    assert np.abs(fk - want_f).max() <= 1e-12 * np.abs(want_f).max()
+    delta = 0.3 * np.eye(d)[None] / (1j * wn[:, None, None] - 0.2)
+    s2 = 0.1 * (rng.normal(size=(nf, d, d)) + 1j * rng.normal(size=(nf, d, d)))
+    h4 = np.diag([0.1, -0.2, 0.3, 0.0]).astype(complex)
+    want_g = np.linalg.inv((1j * wn[:, None, None] + mu) * np.eye(d)[None] - h4[None] - delta - fk[None] - s2)
+    got_g, _ = orc.dyson(h4, delta, fk, s2, mu, beta)
+    assert np.abs(got_g[:nf] - want_g).max() <= 1e-12 * np.abs(want_g).max()
+
+
 def test_gen_uijkl_counts(orc):
     uidx, ut = orc.gen_uijkl(10, 4.0, 2.6, 0.7)
     assert len(ut) == 180
