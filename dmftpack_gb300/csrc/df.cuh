@@ -10,7 +10,57 @@
 // Ops policies used by the templated lattice kernels:
 //   OpsD: complex FP64 (double2)       OpsF: complex double-float (cdf)
 #pragma once
+#include <cmath>
+
 #include "common.cuh"
+
+#define DG_HD __host__ __device__ __forceinline__
+
+// IEEE single-precision operations rounded to nearest: the device intrinsics (never contracted into FMAs), and the
+// same operations on the host, so that the double-float arithmetic below can be checked on a CPU (host code that
+// includes this header is built with -ffp-contract=off)
+DG_HD float f_add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+DG_HD float f_sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+DG_HD float f_mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+DG_HD float f_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+DG_HD float f_rcp(float a) {
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(a);
+#else
+    return 1.0f / a;
+#endif
+}
+DG_HD float f_from_double(double x) {
+#ifdef __CUDA_ARCH__
+    return __double2float_rn(x);
+#else
+    return (float)x;
+#endif
+}
 
 struct dfl {
     float h, l;
@@ -19,84 +69,84 @@ struct cdf {
     dfl re, im;
 };
 
-__device__ __forceinline__ dfl df_make(double x) {
-    const float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};
+DG_HD dfl df_make(double x) {
+    const float h = f_from_double(x);
+    return {h, f_from_double(x - (double)h)};
 }
-__device__ __forceinline__ double df_val(dfl a) { return (double)a.h + (double)a.l; }
-__device__ __forceinline__ dfl fast_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+DG_HD double df_val(dfl a) { return (double)a.h + (double)a.l; }
+DG_HD dfl fast_two_sum(float a, float b) {
+    const float s = f_add(a, b);
+    return {s, f_sub(b, f_sub(s, a))};
 }
-__device__ __forceinline__ dfl two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+DG_HD dfl two_sum(float a, float b) {
+    const float s = f_add(a, b);
+    const float bb = f_sub(s, a);
+    return {s, f_add(f_sub(a, f_sub(s, bb)), f_sub(b, bb))};
 }
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+DG_HD dfl df_add(dfl a, dfl b) {
     dfl s = two_sum(a.h, b.h);
-    const float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+    const float e = f_add(s.l, f_add(a.l, b.l));
     return fast_two_sum(s.h, e);
 }
-__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
-__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
+DG_HD dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+DG_HD dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+DG_HD dfl df_mul(dfl a, dfl b) {
+    const float p = f_mul(a.h, b.h);
+    float e = f_fma(a.h, b.h, -p);
+    e = f_fma(a.h, b.l, e);
+    e = f_fma(a.l, b.h, e);
     return fast_two_sum(p, e);
 }
 // c + a*b with one rounding of the product's error term
-__device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
+DG_HD dfl df_fma(dfl a, dfl b, dfl c) {
+    const float p = f_mul(a.h, b.h);
+    float e = f_fma(a.h, b.h, -p);
+    e = f_fma(a.h, b.l, e);
+    e = f_fma(a.l, b.h, e);
     dfl s = two_sum(c.h, p);
-    const float t = __fadd_rn(s.l, __fadd_rn(c.l, e));
+    const float t = f_add(s.l, f_add(c.l, e));
     return fast_two_sum(s.h, t);
 }
 // the product a*b as hi p plus the FP32 sum e of its error terms (p + e = a*b to ~2^-48 relative)
-__device__ __forceinline__ float df_prod(dfl a, dfl b, float &e) {
-    const float p = __fmul_rn(a.h, b.h);
-    e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
+DG_HD float df_prod(dfl a, dfl b, float &e) {
+    const float p = f_mul(a.h, b.h);
+    e = f_fma(a.h, b.h, -p);
+    e = f_fma(a.h, b.l, e);
+    e = f_fma(a.l, b.h, e);
     return p;
 }
 // a*b + c*d with one renormalisation (the real or imaginary part of a complex product): the two hi products
 // are added exactly (two-sum), the error terms in FP32, so the result is as accurate as two chained
 // df_fma and takes 19 FP32 operations instead of 22
-__device__ __forceinline__ dfl df_dot2(dfl a, dfl b, dfl c, dfl d) {
+DG_HD dfl df_dot2(dfl a, dfl b, dfl c, dfl d) {
     float e1, e2;
     const float p1 = df_prod(a, b, e1), p2 = df_prod(c, d, e2);
     const dfl s = two_sum(p1, p2);
-    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(e1, e2)));
+    return fast_two_sum(s.h, f_add(s.l, f_add(e1, e2)));
 }
 // acc + a*b + c*d with one renormalisation (27 FP32 operations instead of 30 for two chained df_fma)
-__device__ __forceinline__ dfl df_fma2(dfl a, dfl b, dfl c, dfl d, dfl acc) {
+DG_HD dfl df_fma2(dfl a, dfl b, dfl c, dfl d, dfl acc) {
     float e1, e2;
     const float p1 = df_prod(a, b, e1), p2 = df_prod(c, d, e2);
     const dfl s1 = two_sum(acc.h, p1);
     const dfl s2 = two_sum(s1.h, p2);
-    const float t = __fadd_rn(__fadd_rn(s1.l, s2.l), __fadd_rn(acc.l, __fadd_rn(e1, e2)));
+    const float t = f_add(f_add(s1.l, s2.l), f_add(acc.l, f_add(e1, e2)));
     return fast_two_sum(s2.h, t);
 }
 // Lazy accumulation for a running sum of products: acc + a*b with the hi parts added exactly (two-sum) and the
 // low parts summed unnormalised in FP32 (12 FP32 operations instead of 15).  The low part of a lazy sum of n
 // terms grows to ~n ulp of the hi part and its own rounding with it, so lazy sums are for short runs (the poles of
 // one k point, n <= ~64) and pass through df_renorm before any other double-float operation reads them.
-__device__ __forceinline__ dfl df_fma_lazy(dfl a, dfl b, dfl acc) {
+DG_HD dfl df_fma_lazy(dfl a, dfl b, dfl acc) {
     float e;
     const float p = df_prod(a, b, e);
     const dfl s = two_sum(acc.h, p);
-    return {s.h, __fadd_rn(__fadd_rn(acc.l, e), s.l)};
+    return {s.h, f_add(f_add(acc.l, e), s.l)};
 }
-__device__ __forceinline__ dfl df_renorm(dfl a) { return fast_two_sum(a.h, a.l); }
+DG_HD dfl df_renorm(dfl a) { return fast_two_sum(a.h, a.l); }
 // 1/a: FP32 reciprocal refined by one Newton step in double-float (24 -> ~48 bits)
-__device__ __forceinline__ dfl df_rcp(dfl a) {
-    const float r = __frcp_rn(a.h);
+DG_HD dfl df_rcp(dfl a) {
+    const float r = f_rcp(a.h);
     // e = 1 - a*r in double-float
     dfl ar = df_mul(a, {r, 0.0f});
     dfl e = df_sub({1.0f, 0.0f}, ar);
@@ -104,95 +154,95 @@ __device__ __forceinline__ dfl df_rcp(dfl a) {
     return df_fma({r, 0.0f}, e, {r, 0.0f});
 }
 
-__device__ __forceinline__ cdf cdf_make(double2 z) { return {df_make(z.x), df_make(z.y)}; }
-__device__ __forceinline__ double2 cdf_val(cdf z) { return make_double2(df_val(z.re), df_val(z.im)); }
+DG_HD cdf cdf_make(double2 z) { return {df_make(z.x), df_make(z.y)}; }
+DG_HD double2 cdf_val(cdf z) { return make_double2(df_val(z.re), df_val(z.im)); }
 
 struct OpsD {
     typedef double2 C;
     typedef double M;  // pivot magnitude type
-    static __device__ __forceinline__ C zero() { return cmk(0, 0); }
-    static __device__ __forceinline__ C one() { return cmk(1, 0); }
-    static __device__ __forceinline__ C from(double2 z) { return z; }
-    static __device__ __forceinline__ double2 to(C z) { return z; }
-    static __device__ __forceinline__ C add(C a, C b) { return cadd(a, b); }
-    static __device__ __forceinline__ C sub(C a, C b) { return csub(a, b); }
-    static __device__ __forceinline__ C neg(C a) { return cneg(a); }
-    static __device__ __forceinline__ C mul(C a, C b) { return cmul(a, b); }
-    static __device__ __forceinline__ C mulc(C a, C b) { return cmulc(a, b); }  // a conj(b)
-    static __device__ __forceinline__ C conj(C a) { return cconj(a); }
-    static __device__ __forceinline__ C fma(C a, C b, C acc) { return cfma(a, b, acc); }
-    static __device__ __forceinline__ C fms(C a, C b, C acc) { return cfms(a, b, acc); }
-    static __device__ __forceinline__ C rcp(C a) { return crcp(a); }
-    static __device__ __forceinline__ double re(C a) { return a.x; }
-    static __device__ __forceinline__ double im(C a) { return a.y; }
-    static __device__ __forceinline__ double mag2(C a) { return cabs2(a); }
+    static DG_HD C zero() { return cmk(0, 0); }
+    static DG_HD C one() { return cmk(1, 0); }
+    static DG_HD C from(double2 z) { return z; }
+    static DG_HD double2 to(C z) { return z; }
+    static DG_HD C add(C a, C b) { return cadd(a, b); }
+    static DG_HD C sub(C a, C b) { return csub(a, b); }
+    static DG_HD C neg(C a) { return cneg(a); }
+    static DG_HD C mul(C a, C b) { return cmul(a, b); }
+    static DG_HD C mulc(C a, C b) { return cmulc(a, b); }  // a conj(b)
+    static DG_HD C conj(C a) { return cconj(a); }
+    static DG_HD C fma(C a, C b, C acc) { return cfma(a, b, acc); }
+    static DG_HD C fms(C a, C b, C acc) { return cfms(a, b, acc); }
+    static DG_HD C rcp(C a) { return crcp(a); }
+    static DG_HD double re(C a) { return a.x; }
+    static DG_HD double im(C a) { return a.y; }
+    static DG_HD double mag2(C a) { return cabs2(a); }
     static __device__ __forceinline__ C shfl(C v, int src, int w) { return shfl2(v, src, w); }
     // real parts (R) for the Hermitian split of the pole sums
     typedef double R;
-    static __device__ __forceinline__ R rzero() { return 0.0; }
-    static __device__ __forceinline__ R rfrom(double x) { return x; }
-    static __device__ __forceinline__ R rfma(R a, R b, R acc) { return ::fma(a, b, acc); }
-    static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
-    static __device__ __forceinline__ R radd(R a, R b) { return a + b; }
-    static __device__ __forceinline__ R rsub(R a, R b) { return a - b; }
-    static __device__ __forceinline__ R rneg(R a) { return -a; }
-    static __device__ __forceinline__ R rrcp(R a) { return 1.0 / a; }
+    static DG_HD R rzero() { return 0.0; }
+    static DG_HD R rfrom(double x) { return x; }
+    static DG_HD R rfma(R a, R b, R acc) { return ::fma(a, b, acc); }
+    static DG_HD R rmul(R a, R b) { return a * b; }
+    static DG_HD R radd(R a, R b) { return a + b; }
+    static DG_HD R rsub(R a, R b) { return a - b; }
+    static DG_HD R rneg(R a) { return -a; }
+    static DG_HD R rrcp(R a) { return 1.0 / a; }
     // lazy running sums of a few terms (double-float: unnormalised low parts, read through rnorm)
-    static __device__ __forceinline__ R racc(R a, R b, R acc) { return ::fma(a, b, acc); }
-    static __device__ __forceinline__ R rnorm(R a) { return a; }
-    static __device__ __forceinline__ C mk(R re, R im) { return cmk(re, im); }
-    static __device__ __forceinline__ R cre(C a) { return a.x; }
-    static __device__ __forceinline__ R cim(C a) { return a.y; }
+    static DG_HD R racc(R a, R b, R acc) { return ::fma(a, b, acc); }
+    static DG_HD R rnorm(R a) { return a; }
+    static DG_HD C mk(R re, R im) { return cmk(re, im); }
+    static DG_HD R cre(C a) { return a.x; }
+    static DG_HD R cim(C a) { return a.y; }
 };
 
 struct OpsF {
     typedef cdf C;
     typedef float M;
-    static __device__ __forceinline__ C zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
-    static __device__ __forceinline__ C one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
-    static __device__ __forceinline__ C from(double2 z) { return cdf_make(z); }
-    static __device__ __forceinline__ double2 to(C z) { return cdf_val(z); }
-    static __device__ __forceinline__ C add(C a, C b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
-    static __device__ __forceinline__ C sub(C a, C b) { return {df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
-    static __device__ __forceinline__ C neg(C a) { return {df_neg(a.re), df_neg(a.im)}; }
-    static __device__ __forceinline__ C mul(C a, C b) {
+    static DG_HD C zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+    static DG_HD C one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
+    static DG_HD C from(double2 z) { return cdf_make(z); }
+    static DG_HD double2 to(C z) { return cdf_val(z); }
+    static DG_HD C add(C a, C b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+    static DG_HD C sub(C a, C b) { return {df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+    static DG_HD C neg(C a) { return {df_neg(a.re), df_neg(a.im)}; }
+    static DG_HD C mul(C a, C b) {
         return {df_dot2(a.re, b.re, df_neg(a.im), b.im), df_dot2(a.re, b.im, a.im, b.re)};
     }
-    static __device__ __forceinline__ C conj(C a) { return {a.re, df_neg(a.im)}; }
-    static __device__ __forceinline__ C mulc(C a, C b) {  // a conj(b)
+    static DG_HD C conj(C a) { return {a.re, df_neg(a.im)}; }
+    static DG_HD C mulc(C a, C b) {  // a conj(b)
         return {df_dot2(a.re, b.re, a.im, b.im), df_dot2(a.im, b.re, df_neg(a.re), b.im)};
     }
-    static __device__ __forceinline__ C fma(C a, C b, C acc) {
+    static DG_HD C fma(C a, C b, C acc) {
         return {df_fma2(a.re, b.re, df_neg(a.im), b.im, acc.re), df_fma2(a.re, b.im, a.im, b.re, acc.im)};
     }
-    static __device__ __forceinline__ C fms(C a, C b, C acc) {
+    static DG_HD C fms(C a, C b, C acc) {
         return {df_fma2(df_neg(a.re), b.re, a.im, b.im, acc.re),
                 df_fma2(df_neg(a.re), b.im, df_neg(a.im), b.re, acc.im)};
     }
-    static __device__ __forceinline__ C rcp(C a) {  // conj(a)/|a|^2
+    static DG_HD C rcp(C a) {  // conj(a)/|a|^2
         const dfl n = df_dot2(a.re, a.re, a.im, a.im);
         const dfl r = df_rcp(n);
         return {df_mul(a.re, r), df_neg(df_mul(a.im, r))};
     }
-    static __device__ __forceinline__ double re(C a) { return df_val(a.re); }
-    static __device__ __forceinline__ double im(C a) { return df_val(a.im); }
-    static __device__ __forceinline__ float mag2(C a) {  // pivot choice only: FP32 magnitude suffices
-        return __fmaf_rn(a.re.h, a.re.h, __fmul_rn(a.im.h, a.im.h));
+    static DG_HD double re(C a) { return df_val(a.re); }
+    static DG_HD double im(C a) { return df_val(a.im); }
+    static DG_HD float mag2(C a) {  // pivot choice only: FP32 magnitude suffices
+        return f_fma(a.re.h, a.re.h, f_mul(a.im.h, a.im.h));
     }
     typedef dfl R;
-    static __device__ __forceinline__ R rzero() { return {0.f, 0.f}; }
-    static __device__ __forceinline__ R rfrom(double x) { return df_make(x); }
-    static __device__ __forceinline__ R rfma(R a, R b, R acc) { return df_fma(a, b, acc); }
-    static __device__ __forceinline__ R rmul(R a, R b) { return df_mul(a, b); }
-    static __device__ __forceinline__ R radd(R a, R b) { return df_add(a, b); }
-    static __device__ __forceinline__ R rsub(R a, R b) { return df_sub(a, b); }
-    static __device__ __forceinline__ R rneg(R a) { return df_neg(a); }
-    static __device__ __forceinline__ R rrcp(R a) { return df_rcp(a); }
-    static __device__ __forceinline__ R racc(R a, R b, R acc) { return df_fma_lazy(a, b, acc); }
-    static __device__ __forceinline__ R rnorm(R a) { return df_renorm(a); }
-    static __device__ __forceinline__ C mk(R re, R im) { return {re, im}; }
-    static __device__ __forceinline__ R cre(C a) { return a.re; }
-    static __device__ __forceinline__ R cim(C a) { return a.im; }
+    static DG_HD R rzero() { return {0.f, 0.f}; }
+    static DG_HD R rfrom(double x) { return df_make(x); }
+    static DG_HD R rfma(R a, R b, R acc) { return df_fma(a, b, acc); }
+    static DG_HD R rmul(R a, R b) { return df_mul(a, b); }
+    static DG_HD R radd(R a, R b) { return df_add(a, b); }
+    static DG_HD R rsub(R a, R b) { return df_sub(a, b); }
+    static DG_HD R rneg(R a) { return df_neg(a); }
+    static DG_HD R rrcp(R a) { return df_rcp(a); }
+    static DG_HD R racc(R a, R b, R acc) { return df_fma_lazy(a, b, acc); }
+    static DG_HD R rnorm(R a) { return df_renorm(a); }
+    static DG_HD C mk(R re, R im) { return {re, im}; }
+    static DG_HD R cre(C a) { return a.re; }
+    static DG_HD R cim(C a) { return a.im; }
     static __device__ __forceinline__ C shfl(C v, int src, int w) {
         C o;
         o.re.h = __shfl_sync(0xffffffffu, v.re.h, src, w);

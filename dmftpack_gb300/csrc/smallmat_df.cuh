@@ -13,14 +13,14 @@
 #include "smallmat.cuh"
 
 // sqrt(a), a >= 0: the FP32 root refined by one Newton step in double-float
-__device__ __forceinline__ dfl df_sqrt(dfl a) {
+DG_HD dfl df_sqrt(dfl a) {
     if (!(a.h > 0.f)) return {0.f, 0.f};
     const float s = sqrtf(a.h);
     const dfl e = df_sub(a, df_mul({s, 0.f}, {s, 0.f}));  // a - s^2
     return fast_two_sum(s, e.h / (2.f * s));
 }
 // a / b: the FP32 quotient corrected by the double-float remainder
-__device__ __forceinline__ dfl df_div(dfl a, dfl b) {
+DG_HD dfl df_div(dfl a, dfl b) {
     const float q1 = a.h / b.h;
     const dfl r = df_sub(a, df_mul(b, {q1, 0.f}));
     const float q2 = r.h / b.h;

@@ -1,0 +1,73 @@
+// df_arith_check.cu -- runs the double-float arithmetic of the lattice kernels (dmftpack_gb300/csrc/df.cuh and the
+// square root / division of smallmat_df.cuh) on the host, so that tests/test_df_arith.py can hold it to exact
+// rational arithmetic without a GPU.  Built by nvcc with -ffp-contract=off: every single-precision operation is
+// then the IEEE round-to-nearest operation its device intrinsic performs.
+//
+// stdin: one case per line, "<op> <x1> <x2> ..." with every float in C99 hex notation (%a); stdout: the result
+// floats of each case on one line, in the same notation.  A double-float value is two floats (hi lo), a complex one
+// four (re.hi re.lo im.hi im.lo).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "df.cuh"
+#include "smallmat_df.cuh"
+
+namespace {
+
+bool read_floats(const char *s, std::vector<float> &v) {
+    while (*s) {
+        while (*s == ' ' || *s == '\t') s++;
+        if (!*s || *s == '\n') break;
+        char *end = nullptr;
+        const float x = std::strtof(s, &end);
+        if (end == s) return false;
+        v.push_back(x);
+        s = end;
+    }
+    return true;
+}
+dfl d_at(const std::vector<float> &v, int i) { return {v[2 * i], v[2 * i + 1]}; }
+cdf c_at(const std::vector<float> &v, int i) { return {{v[4 * i], v[4 * i + 1]}, {v[4 * i + 2], v[4 * i + 3]}}; }
+void put(dfl a) { std::printf("%a %a", a.h, a.l); }
+void put(cdf a) {
+    put(a.re);
+    std::printf(" ");
+    put(a.im);
+}
+
+}  // namespace
+
+int main() {
+    char line[4096];
+    while (std::fgets(line, sizeof line, stdin)) {
+        char op[32];
+        int off = 0;
+        if (std::sscanf(line, "%31s%n", op, &off) != 1) continue;
+        std::vector<float> v;
+        if (!read_floats(line + off, v)) return 2;
+        const std::string o(op);
+        if (o == "two_sum") put(two_sum(v[0], v[1]));
+        else if (o == "add") put(df_add(d_at(v, 0), d_at(v, 1)));
+        else if (o == "mul") put(df_mul(d_at(v, 0), d_at(v, 1)));
+        else if (o == "fma") put(df_fma(d_at(v, 0), d_at(v, 1), d_at(v, 2)));
+        else if (o == "dot2") put(df_dot2(d_at(v, 0), d_at(v, 1), d_at(v, 2), d_at(v, 3)));
+        else if (o == "fma2") put(df_fma2(d_at(v, 0), d_at(v, 1), d_at(v, 2), d_at(v, 3), d_at(v, 4)));
+        else if (o == "lazy") {  // a lazy sum of the products of the pairs that follow, renormalised at the end
+            dfl acc = {0.f, 0.f};
+            for (size_t i = 0; i + 3 < v.size(); i += 4) acc = df_fma_lazy(d_at(v, i / 2), d_at(v, i / 2 + 1), acc);
+            put(df_renorm(acc));
+        } else if (o == "rcp") put(df_rcp(d_at(v, 0)));
+        else if (o == "sqrt") put(df_sqrt(d_at(v, 0)));
+        else if (o == "div") put(df_div(d_at(v, 0), d_at(v, 1)));
+        else if (o == "cmul") put(OpsF::mul(c_at(v, 0), c_at(v, 1)));
+        else if (o == "cmulc") put(OpsF::mulc(c_at(v, 0), c_at(v, 1)));
+        else if (o == "cfma") put(OpsF::fma(c_at(v, 0), c_at(v, 1), c_at(v, 2)));
+        else if (o == "cfms") put(OpsF::fms(c_at(v, 0), c_at(v, 1), c_at(v, 2)));
+        else if (o == "crcp") put(OpsF::rcp(c_at(v, 0)));
+        else return 3;
+        std::printf("\n");
+    }
+    return 0;
+}

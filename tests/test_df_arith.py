@@ -1,0 +1,145 @@
+"""The double-float arithmetic of the mixed-precision kernels (dmftpack_gb300/csrc/df.cuh, smallmat_df.cuh) held to
+exact rational arithmetic.  The header's own functions are compiled for the host (tests/cxx/df_arith_check.cu, nvcc
+with -ffp-contract=off, where each single-precision operation is the IEEE round-to-nearest operation of its device
+intrinsic) and run on seeded inputs; every result is compared with the exact value of the operation on the same
+double-float inputs.  Bounds are in units of the inputs' magnitudes, as the error analysis of each operation gives
+them (~2^-47 per operation; 2^-44 leaves room for the few roundings a composite operation chains)."""
+import os
+import shutil
+import subprocess
+import zlib
+from fractions import Fraction as Q
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+SRC = os.path.join(ROOT, "tests", "cxx", "df_arith_check.cu")
+EPS = Q(1, 2 ** 44)
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+    if nvcc is None:
+        pytest.skip("no nvcc")
+    exe = str(tmp_path_factory.mktemp("df") / "df_arith_check")
+    csrc = os.path.join(ROOT, "dmftpack_gb300", "csrc")
+    cmd = [nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-ffp-contract=off",
+           "-I", os.path.join(ROOT, "include"), "-I", csrc, SRC, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+    def run(lines):
+        out = subprocess.run([exe], input="".join(lines), capture_output=True, text=True, timeout=120)
+        assert out.returncode == 0, out.stderr
+        return [[float.fromhex(t) for t in ln.split()] for ln in out.stdout.splitlines()]
+    return run
+
+
+def _df(rng, lo=-8.0, hi=8.0, positive=False):
+    """A double-float (hi, lo) split of a random double of random sign and magnitude."""
+    x = float(np.exp(rng.uniform(lo, hi))) * (1 if positive or rng.random() < 0.5 else -1)
+    h = float(np.float32(x))
+    return h, float(np.float32(x - h))
+
+
+def _v(d):
+    return Q(d[0]) + Q(d[1])
+
+
+def _hex(*ds):
+    return " ".join(float(t).hex() for d in ds for t in d)
+
+
+def _close(got, want, scale):
+    return abs(got - want) <= EPS * scale
+
+
+def test_two_sum_is_exact(harness):
+    rng = np.random.default_rng(1)
+    cases = [(float(np.float32(rng.normal() * 10 ** rng.uniform(-6, 6))), float(np.float32(rng.normal())))
+             for _ in range(400)]
+    out = harness(["two_sum %s %s\n" % (a.hex(), b.hex()) for a, b in cases])
+    for (a, b), (s, e) in zip(cases, out):
+        assert Q(s) + Q(e) == Q(a) + Q(b)
+
+
+@pytest.mark.parametrize("op", ["add", "mul", "fma", "dot2", "fma2", "rcp", "sqrt", "div"])
+def test_real_operations(harness, op):
+    rng = np.random.default_rng(zlib.crc32(op.encode()))
+    nargs = {"add": 2, "mul": 2, "fma": 3, "dot2": 4, "fma2": 5, "rcp": 1, "sqrt": 1, "div": 2}[op]
+    cases = [[_df(rng, positive=(op == "sqrt")) for _ in range(nargs)] for _ in range(300)]
+    out = harness(["%s %s\n" % (op, _hex(*c)) for c in cases])
+    for c, r in zip(cases, out):
+        x = [_v(d) for d in c]
+        got = Q(r[0]) + Q(r[1])
+        if op == "add":
+            want, scale = x[0] + x[1], abs(x[0]) + abs(x[1])
+        elif op == "mul":
+            want = x[0] * x[1]
+            scale = abs(want)
+        elif op == "fma":
+            want, scale = x[2] + x[0] * x[1], abs(x[0] * x[1]) + abs(x[2])
+        elif op == "dot2":
+            want, scale = x[0] * x[1] + x[2] * x[3], abs(x[0] * x[1]) + abs(x[2] * x[3])
+        elif op == "fma2":
+            want = x[4] + x[0] * x[1] + x[2] * x[3]
+            scale = abs(x[0] * x[1]) + abs(x[2] * x[3]) + abs(x[4])
+        elif op == "rcp":
+            want = 1 / x[0]
+            scale = abs(want)
+        elif op == "div":
+            want = x[0] / x[1]
+            scale = abs(want)
+        else:  # sqrt: compare squares (exact rational square root is not available)
+            want, got, scale = x[0], got * got, abs(x[0])
+        assert _close(got, want, scale), (op, c, r)
+
+
+def test_lazy_sum_of_products(harness):
+    rng = np.random.default_rng(5)
+    cases = [[_df(rng, -3, 3) for _ in range(2 * n)] for n in (1, 2, 5, 9, 16) for _ in range(40)]
+    out = harness(["lazy %s\n" % _hex(*c) for c in cases])
+    for c, r in zip(cases, out):
+        x = [_v(d) for d in c]
+        want = sum((x[2 * i] * x[2 * i + 1] for i in range(len(c) // 2)), Q(0))
+        scale = sum((abs(x[2 * i] * x[2 * i + 1]) for i in range(len(c) // 2)), Q(0))
+        assert _close(Q(r[0]) + Q(r[1]), want, 4 * scale)
+
+
+@pytest.mark.parametrize("op", ["cmul", "cmulc", "cfma", "cfms", "crcp"])
+def test_complex_operations(harness, op):
+    rng = np.random.default_rng(zlib.crc32(op.encode()))
+    nargs = {"cmul": 2, "cmulc": 2, "cfma": 3, "cfms": 3, "crcp": 1}[op]
+    cases = [[(_df(rng, -4, 4), _df(rng, -4, 4)) for _ in range(nargs)] for _ in range(200)]
+    out = harness(["%s %s\n" % (op, _hex(*[d for z in c for d in z])) for c in cases])
+
+    def cv(z):
+        return _v(z[0]), _v(z[1])
+
+    def mag(a):
+        return abs(a[0]) + abs(a[1])
+
+    for c, r in zip(cases, out):
+        z = [cv(t) for t in c]
+        got = (Q(r[0]) + Q(r[1]), Q(r[2]) + Q(r[3]))
+        a = z[0]
+        if op in ("cmul", "cmulc", "cfma", "cfms"):
+            b = (z[1][0], -z[1][1]) if op == "cmulc" else z[1]
+            p = (a[0] * b[0] - a[1] * b[1], a[0] * b[1] + a[1] * b[0])
+            scale = mag(a) * mag(b)
+            if op == "cfma":
+                want = (z[2][0] + p[0], z[2][1] + p[1])
+                scale += mag(z[2])
+            elif op == "cfms":
+                want = (z[2][0] - p[0], z[2][1] - p[1])
+                scale += mag(z[2])
+            else:
+                want = p
+        else:
+            n = a[0] * a[0] + a[1] * a[1]
+            want = (a[0] / n, -a[1] / n)
+            scale = 4 * mag(want)
+        assert _close(got[0], want[0], scale) and _close(got[1], want[1], scale), (op, c, r)
