@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(128) k_schur(SchurArgs g) {
 // a_jc / a_jj, row r becomes a_rc - a_rj a_jc for c != j, and column j becomes -a_rj / a_jj (no products with the
 // known 1 and 0 entries).
 template <class Ops, int N>
-__device__ __forceinline__ bool thread_inverse(typename Ops::C (&a)[N][N]) {
+DG_HD bool thread_inverse(typename Ops::C (&a)[N][N]) {
     typedef typename Ops::C C;
     typedef typename Ops::M M;
     bool sing = false;

@@ -1,7 +1,8 @@
-// df_arith_check.cu -- runs the double-float arithmetic of the lattice kernels (dmftpack_gb300/csrc/df.cuh and the
-// square root / division of smallmat_df.cuh) on the host, so that tests/test_df_arith.py can hold it to exact
-// rational arithmetic without a GPU.  Built by nvcc with -ffp-contract=off: every single-precision operation is
-// then the IEEE round-to-nearest operation its device intrinsic performs.
+// df_arith_check.cu -- runs the double-float arithmetic of the lattice kernels (dmftpack_gb300/csrc/df.cuh, the
+// square root / division of smallmat_df.cuh and the in-register 3 x 3 inverse of schur.cuh) on the host, so that
+// tests/test_df_arith.py can hold it to exact rational arithmetic without a GPU.  Built by nvcc with
+// -ffp-contract=off: every single-precision operation is then the IEEE round-to-nearest operation its device
+// intrinsic performs.
 //
 // stdin: one case per line, "<op> <x1> <x2> ..." with every float in C99 hex notation (%a); stdout: the result
 // floats of each case on one line, in the same notation.  A double-float value is two floats (hi lo), a complex one
@@ -12,6 +13,7 @@
 #include <vector>
 
 #include "df.cuh"
+#include "schur.cuh"
 #include "smallmat_df.cuh"
 
 namespace {
@@ -66,7 +68,34 @@ int main() {
         else if (o == "cfma") put(OpsF::fma(c_at(v, 0), c_at(v, 1), c_at(v, 2)));
         else if (o == "cfms") put(OpsF::fms(c_at(v, 0), c_at(v, 1), c_at(v, 2)));
         else if (o == "crcp") put(OpsF::rcp(c_at(v, 0)));
-        else return 3;
+        else if (o == "inv3" || o == "inv3d") {
+            // the in-register Gauss-Jordan inverse of the thread-per-frequency Schur kernel, row-major input;
+            // output: the singular flag, then the inverse row-major (double-float, or FP64 as hi 0 pairs)
+            bool sing;
+            if (o == "inv3") {
+                cdf a[3][3];
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) a[r][c] = c_at(v, 3 * r + c);
+                sing = dg::thread_inverse<OpsF, 3>(a);
+                std::printf("%d", (int)sing);
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) {
+                        std::printf(" ");
+                        put(a[r][c]);
+                    }
+            } else {
+                double2 a[3][3];
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) {
+                        const cdf z = c_at(v, 3 * r + c);
+                        a[r][c] = make_double2((double)z.re.h + (double)z.re.l, (double)z.im.h + (double)z.im.l);
+                    }
+                sing = dg::thread_inverse<OpsD, 3>(a);
+                std::printf("%d", (int)sing);
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) std::printf(" %a 0x0p+0 %a 0x0p+0", a[r][c].x, a[r][c].y);
+            }
+        } else return 3;
         std::printf("\n");
     }
     return 0;

@@ -143,3 +143,79 @@ def test_complex_operations(harness, op):
             want = (a[0] / n, -a[1] / n)
             scale = 4 * mag(want)
         assert _close(got[0], want[0], scale) and _close(got[1], want[1], scale), (op, c, r)
+
+
+def _cmul(a, b):
+    return a[0] * b[0] - a[1] * b[1], a[0] * b[1] + a[1] * b[0]
+
+
+def _csub(a, b):
+    return a[0] - b[0], a[1] - b[1]
+
+
+def _exact_inverse3(A):
+    """The inverse of a 3 x 3 complex rational matrix (pairs of Fractions) by its adjugate."""
+    def cof(r, c):
+        rs = [i for i in range(3) if i != r]
+        cs = [j for j in range(3) if j != c]
+        m = _csub(_cmul(A[rs[0]][cs[0]], A[rs[1]][cs[1]]), _cmul(A[rs[0]][cs[1]], A[rs[1]][cs[0]]))
+        return m if (r + c) % 2 == 0 else (-m[0], -m[1])
+    C = [[cof(r, c) for c in range(3)] for r in range(3)]
+    det = (Q(0), Q(0))
+    for c in range(3):
+        t = _cmul(A[0][c], C[0][c])
+        det = (det[0] + t[0], det[1] + t[1])
+    n = det[0] * det[0] + det[1] * det[1]
+    idet = (det[0] / n, -det[1] / n)
+    return [[_cmul(C[c][r], idet) for c in range(3)] for r in range(3)]
+
+
+@pytest.mark.parametrize("form", ["inv3", "inv3d"])
+def test_in_register_inverse(harness, form):
+    """The thread-per-frequency Schur kernel's pivoted in-register Gauss-Jordan (schur.cuh thread_inverse) in
+    double-float and FP64 against the exact inverse: matrices of the kernel's form (mu + i w) I - H with H Hermitian,
+    and row-permuted ones whose leading entries are small, so that every pivot choice is taken."""
+    rng = np.random.default_rng(17)
+    cases = []
+    for t in range(120):
+        Hm = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+        Hm = (Hm + Hm.conj().T) / 2
+        w = float(np.exp(rng.uniform(np.log(0.05), np.log(5.0))))
+        M = (0.3 + 1j * w) * np.eye(3) - Hm
+        if t % 3 == 1:
+            M = M[[1, 2, 0]]
+        elif t % 3 == 2:
+            M = M[[2, 0, 1]]
+            M[0, 0] *= 1e-3
+        cases.append(M)
+
+    def split(x):
+        h = float(np.float32(x))
+        return h, float(np.float32(x - h))
+
+    lines = []
+    for M in cases:
+        lines.append("%s %s\n" % (form, _hex(*[d for z in M.ravel() for d in (split(z.real), split(z.imag))])))
+    out = harness(lines)
+    for M, r in zip(cases, out):
+        A = [[(_v(split(M[i, j].real)), _v(split(M[i, j].imag))) for j in range(3)] for i in range(3)]
+        X = _exact_inverse3(A)
+        assert r[0] == 0
+        vals = r[1:]
+        kappa = np.linalg.cond(M)
+        scale = max(abs(X[i][j][0]) + abs(X[i][j][1]) for i in range(3) for j in range(3))
+        tol = (Q(1, 2 ** 44) if form == "inv3" else Q(1, 2 ** 48)) * Q(float(kappa)) * scale
+        for k in range(9):
+            i, j = divmod(k, 3)
+            got = (Q(vals[4 * k]) + Q(vals[4 * k + 1]), Q(vals[4 * k + 2]) + Q(vals[4 * k + 3]))
+            assert abs(got[0] - X[i][j][0]) <= tol and abs(got[1] - X[i][j][1]) <= tol, (form, M, k)
+
+
+def test_in_register_inverse_flags_a_singular_matrix(harness):
+    z = "0x0p+0 " * 4
+    one = "0x1p+0 0x0p+0 0x0p+0 0x0p+0 "
+    # rows 1 and 2 equal: singular
+    row = one + one + z
+    out = harness(["inv3 %s\n" % (one + z + z + row + row)])
+    assert out[0][0] == 1
+
