@@ -75,7 +75,7 @@ __device__ __forceinline__ bool warp_gj_inverse(double2 (&a)[N], const int c) {
 // ---------------------------------------------------------------------------------------------------
 #define DG_AT(A, n, i, j) (A)[(i) + (size_t)(j) * (n)]
 
-__device__ inline int thread_gj_inverse(int n, double2 *a, int *perm) {
+__host__ __device__ inline int thread_gj_inverse(int n, double2 *a, int *perm) {
     int st = DG_OK;
     for (int j = 0; j < n; j++) {
         int p = j;
@@ -117,7 +117,7 @@ __device__ inline int thread_gj_inverse(int n, double2 *a, int *perm) {
 }
 
 // C = A * B   (all n x n, distinct buffers)
-__device__ inline void thread_matmul(int n, const double2 *A, const double2 *B, double2 *C) {
+__host__ __device__ inline void thread_matmul(int n, const double2 *A, const double2 *B, double2 *C) {
     for (int j = 0; j < n; j++)
         for (int i = 0; i < n; i++) {
             double2 s = cmk(0, 0);
@@ -129,7 +129,7 @@ __device__ inline void thread_matmul(int n, const double2 *A, const double2 *B, 
 // Hermitian eigen-decomposition from the lower triangle of A0 (A0 untouched).  a, u: n x n scratch;
 // w: n eigenvalues ascending; if u == nullptr only eigenvalues are produced (a still needed).
 // Cyclic Jacobi: the rotation G = [[c, s], [-s conj(u), c conj(u)]] zeroes the (p,q) element of G^H A G.
-__device__ inline int thread_heig(int n, const double2 *A0, double2 *a, double2 *u, double *w, int *order) {
+__host__ __device__ inline int thread_heig(int n, const double2 *A0, double2 *a, double2 *u, double *w, int *order) {
     for (int j = 0; j < n; j++)
         for (int i = 0; i < n; i++) {
             double2 v;

@@ -319,7 +319,7 @@ __device__ inline void block_matmul(int n, const double2 *A, const double2 *B, d
 // t[idx] = tri[(idx) * stride] (stride = threads sharing the interleaved shared array).  Destroys t.
 // strict: positive definite; else positive semidefinite (an exactly zero pivot with an exactly zero
 // remaining column is skipped).
-__device__ inline bool posdef_tri(int n, double2 *t, int stride, bool strict) {
+__host__ __device__ inline bool posdef_tri(int n, double2 *t, int stride, bool strict) {
 #define DG_TRI(i, j) t[(size_t)(((i) * ((i) + 1)) / 2 + (j)) * stride]
     for (int j = 0; j < n; j++) {
         const double p = DG_TRI(j, j).x;

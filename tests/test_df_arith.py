@@ -219,3 +219,67 @@ def test_in_register_inverse_flags_a_singular_matrix(harness):
     out = harness(["inv3 %s\n" % (one + z + z + row + row)])
     assert out[0][0] == 1
 
+
+def _fp64_lines(op, mats):
+    lines = []
+    for A in mats:
+        n = A.shape[0]
+        flat = A.ravel(order="F")
+        lines.append("%s %s %s\n" % (op, float(n).hex(), " ".join("%s %s" % (z.real.hex(), z.imag.hex())
+                                                                   for z in flat)))
+    return lines
+
+
+def test_fp64_gauss_jordan_inverse(harness):
+    """linalg.cuh thread_gj_inverse (the impurity and moment kernels' per-thread inverse) against LAPACK."""
+    rng = np.random.default_rng(21)
+    mats = []
+    for n in (1, 2, 3, 5, 8, 10):
+        for _ in range(10):
+            A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)) + 1j * np.eye(n)
+            mats.append(A[rng.permutation(n)])
+    out = harness(_fp64_lines("gj", mats))
+    for A, r in zip(mats, out):
+        n = A.shape[0]
+        assert r[0] == 0
+        X = (np.array(r[1::2]) + 1j * np.array(r[2::2])).reshape(n, n, order="F")
+        want = np.linalg.inv(A)
+        assert np.abs(X - want).max() <= 1e-14 * np.linalg.cond(A) * np.abs(want).max()
+
+
+def test_fp64_jacobi_eigensolver(harness):
+    """linalg.cuh thread_heig (reads the lower triangle) against LAPACK eigenvalues, with A U = U diag(w)."""
+    rng = np.random.default_rng(23)
+    mats = []
+    for n in (1, 2, 4, 7, 10):
+        for _ in range(8):
+            B = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+            mats.append((B + B.conj().T) / 2)
+    out = harness(_fp64_lines("heig", mats))
+    for A, r in zip(mats, out):
+        n = A.shape[0]
+        assert r[0] == 0
+        w = np.array(r[1:1 + n])
+        U = (np.array(r[1 + n::2]) + 1j * np.array(r[2 + n::2])).reshape(n, n, order="F")
+        scale = np.abs(A).max()
+        assert np.abs(w - np.linalg.eigvalsh(A)).max() <= 1e-13 * scale
+        assert np.abs(A @ U - U * w[None]).max() <= 1e-12 * scale
+        assert np.abs(U.conj().T @ U - np.eye(n)).max() <= 1e-13
+
+
+def test_cholesky_sign_tests(harness):
+    """smallmat.cuh posdef_tri: the strict and semidefinite tests the positivity fix-up and causality checks ask."""
+    def line(A, strict):
+        n = A.shape[0]
+        tri = [A[i, j] for i in range(n) for j in range(i + 1)]
+        return "posdef %s %s %s\n" % (float(strict).hex(), float(n).hex(),
+                                       " ".join("%s %s" % (z.real.hex(), z.imag.hex()) for z in tri))
+    rng = np.random.default_rng(29)
+    B = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    pd = B @ B.conj().T + 0.1 * np.eye(4)
+    indef = pd - (np.linalg.eigvalsh(pd)[0] + 0.5) * np.eye(4)
+    psd = np.diag([1.0, 0.0, 2.0]).astype(complex)
+    cases = [(pd, 1, 1), (pd, 0, 1), (indef, 1, 0), (indef, 0, 0), (psd, 1, 0), (psd, 0, 1), (-pd, 0, 0)]
+    out = harness([line(A, s) for A, s, _ in cases])
+    assert [int(r[0]) for r in out] == [want for _, _, want in cases]
+
